@@ -1,0 +1,451 @@
+"""cloudgb -- host-side mirror of the reference's cloud-rendering classes over
+the libcloudgb C ABI (include/cloudgb.h).
+
+Class and field names follow the reference (jaafersheriff/Cloud-Renderer):
+CloudVolume (src/CloudVolume.hpp:12-55), Sun (src/Sun.hpp:10-44), Camera
+(src/Camera.hpp:12-46), VoxelizeShader (src/Shaders/VoxelizeShader.hpp:10-35)
+and ConeTraceShader (src/Shaders/ConeTraceShader.hpp:8-44).  Every call runs on
+the GPU through libcloudgb.so; errors raise CloudError with the library's
+message.
+"""
+import ctypes
+import math
+
+import numpy as np
+
+from . import _lib
+from ._lib import (CONE_REFERENCE, CONE_TRANSMITTANCE, FORMAT_BF16_FP16, FORMAT_RGBA32F,
+                   CloudError, check, load)
+
+__all__ = ["Context", "CloudVolume", "Sun", "Camera", "VoxelizeShader", "ConeTraceShader",
+           "CloudError", "FORMAT_RGBA32F", "FORMAT_BF16_FP16", "CONE_TRANSMITTANCE",
+           "CONE_REFERENCE", "default_context", "HostBuffer", "DeviceBuffer"]
+
+
+def _fptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+class Context:
+    """One device and its stream (the GL context of Window::init, Window.cpp:54-106)."""
+
+    def __init__(self, device=0):
+        self._lib = load()
+        h = ctypes.c_void_p()
+        check(self._lib.cg_context_create(device, ctypes.byref(h)), "cg_context_create")
+        self.handle = h
+        self.device = device
+
+    def synchronize(self):
+        check(self._lib.cg_context_synchronize(self.handle), "cg_context_synchronize")
+
+    @property
+    def launch_count(self):
+        return int(self._lib.cg_context_launch_count(self.handle))
+
+    def close(self):
+        if self.handle:
+            self._lib.cg_context_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx = None
+
+
+def default_context():
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+class HostBuffer:
+    """Pinned host memory from cg_host_alloc, viewed as a numpy array."""
+
+    def __init__(self, shape, dtype=np.float32):
+        self._lib = load()
+        self.nbytes = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        p = ctypes.c_void_p()
+        check(self._lib.cg_host_alloc(self.nbytes, ctypes.byref(p)), "cg_host_alloc")
+        self.ptr = p
+        buf = (ctypes.c_char * self.nbytes).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=dtype).reshape(shape)
+
+    def free(self):
+        if self.ptr:
+            self.array = None
+            self._lib.cg_host_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class DeviceBuffer:
+    """Device memory from cg_device_alloc."""
+
+    def __init__(self, nbytes):
+        self._lib = load()
+        self.nbytes = int(nbytes)
+        p = ctypes.c_void_p()
+        check(self._lib.cg_device_alloc(self.nbytes, ctypes.byref(p)), "cg_device_alloc")
+        self.ptr = p
+
+    def upload(self, arr):
+        arr = np.ascontiguousarray(arr)
+        assert arr.nbytes <= self.nbytes
+        check(self._lib.cg_memcpy(self.ptr, arr.ctypes.data_as(ctypes.c_void_p), arr.nbytes,
+                                  _lib.MEMCPY_H2D), "cg_memcpy")
+
+    def download(self, shape, dtype=np.float32):
+        out = np.empty(shape, dtype)
+        check(self._lib.cg_memcpy(out.ctypes.data_as(ctypes.c_void_p), self.ptr, out.nbytes,
+                                  _lib.MEMCPY_D2H), "cg_memcpy")
+        return out
+
+    def free(self):
+        if self.ptr:
+            self._lib.cg_device_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Sun:
+    """Directional sun (Sun.hpp:10-44).  `direction` points toward the sun;
+    the sun-view position map is map_width x map_height texels (the reference
+    sizes it to the window, 1280x720, main.cpp:25-26)."""
+
+    def __init__(self, direction=(0.3, 1.0, 0.2), map_width=1280, map_height=720):
+        d = np.asarray(direction, np.float64)
+        self.direction = tuple(float(x) for x in (d / np.sqrt((d * d).sum())))
+        self.map_width = int(map_width)
+        self.map_height = int(map_height)
+
+    def _c(self):
+        s = _lib.cg_sun()
+        s.direction[:] = [float(x) for x in self.direction]
+        s.map_width = self.map_width
+        s.map_height = self.map_height
+        return s
+
+
+class Camera:
+    """Pinhole camera (Camera::getP/getV, Camera.cpp:59-60)."""
+
+    def __init__(self, eye, target, up=(0.0, 1.0, 0.0), fov_y_degrees=60.0, width=256,
+                 height=256):
+        self.eye = tuple(float(x) for x in eye)
+        self.target = tuple(float(x) for x in target)
+        self.up = tuple(float(x) for x in up)
+        self.fov_y_degrees = float(fov_y_degrees)
+        self.width = int(width)
+        self.height = int(height)
+
+    def _c(self):
+        c = _lib.cg_camera()
+        c.eye[:] = list(self.eye)
+        c.target[:] = list(self.target)
+        c.up[:] = list(self.up)
+        c.fov_y_degrees = self.fov_y_degrees
+        c.width = self.width
+        c.height = self.height
+        return c
+
+    def getPosition(self):
+        return self.eye
+
+
+class CloudVolume:
+    """CloudVolume(int dim, vec2 bounds, vec3 position, int mips) (CloudVolume.cpp:7-55).
+
+    The world box is position + [bounds[0], bounds[1]]^3.  Billboards hold
+    positions relative to `position`, radii (`scales`) and per-board
+    densities; `fluffiness` multiplies the radii at upload."""
+
+    def __init__(self, dim, bounds, position, mips, fmt=FORMAT_RGBA32F, ctx=None):
+        self.ctx = ctx or default_context()
+        self._lib = self.ctx._lib
+        self.dimension = int(dim)
+        self.position = tuple(float(x) for x in position)
+        self.xBounds = self.yBounds = self.zBounds = (float(bounds[0]), float(bounds[1]))
+        self.levels = int(mips)
+        self.format = int(fmt)
+        r = self.xBounds[1] - self.xBounds[0]
+        self.range = (r, r, r)
+        self.voxelSize = tuple(x / self.dimension for x in self.range)
+        self.fluffiness = 1.0
+        self.positions = np.zeros((0, 3), np.float32)
+        self.scales = np.zeros((0,), np.float32)
+        self.densities = np.zeros((0,), np.float32)
+        self._regen = None
+        pos = (ctypes.c_float * 3)(*self.position)
+        h = ctypes.c_void_p()
+        check(self._lib.cg_volume_create(self.ctx.handle, self.dimension, self.xBounds[0],
+                                         self.xBounds[1], pos, self.levels, self.format,
+                                         ctypes.byref(h)), "cg_volume_create")
+        self.handle = h
+
+    # -- billboards (CloudVolume.cpp:58-62, 120-164) --
+    @property
+    def count(self):
+        return int(self.positions.shape[0])
+
+    def set_billboards(self, positions, scales, densities=None):
+        self.positions = np.ascontiguousarray(positions, np.float32).reshape(-1, 3)
+        self.scales = np.ascontiguousarray(scales, np.float32).reshape(-1)
+        if densities is None:
+            densities = np.ones(self.scales.shape, np.float32)
+        self.densities = np.ascontiguousarray(densities, np.float32).reshape(-1)
+
+    def addCloudBoard(self, pos, scale, density=1.0):
+        self.positions = np.concatenate([self.positions, np.asarray([pos], np.float32)])
+        self.scales = np.concatenate([self.scales, np.asarray([scale], np.float32)])
+        self.densities = np.concatenate([self.densities, np.asarray([density], np.float32)])
+
+    def regenerateBillboards(self, count, minOffset, maxOffset, minScale, maxScale, seed=0):
+        """Uniform offsets in [minOffset, maxOffset] and scales in
+        [minScale, maxScale] (CloudVolume.cpp:120-133), from a seeded stream."""
+        from .scene import SplitMix64
+        rng = SplitMix64(seed)
+        lo = np.asarray(minOffset, np.float64) * np.ones(3)
+        hi = np.asarray(maxOffset, np.float64) * np.ones(3)
+        u = rng.uniform(3 * count).reshape(count, 3)
+        pos = (lo + (hi - lo) * u).astype(np.float32)
+        sc = rng.uniform_range(count, minScale, maxScale).astype(np.float32)
+        self._regen = (count, minOffset, maxOffset, minScale, maxScale, seed)
+        self.set_billboards(pos, sc)
+
+    def resetBillboards(self):
+        if self._regen:
+            self.regenerateBillboards(*self._regen)
+
+    def sortBoards(self, point):
+        """Far-to-near order by distance to `point` (CloudVolume.cpp:65-82).
+        The renderer composites front to back per pixel and does not need it;
+        it only changes which board wins a sun-map depth tie."""
+        c = np.asarray(self.position, np.float32) + self.positions
+        d = np.sqrt(((c - np.asarray(point, np.float32)) ** 2).sum(axis=1))
+        order = np.argsort(-d, kind="stable")
+        self.set_billboards(self.positions[order], self.scales[order], self.densities[order])
+
+    def update(self):
+        """Upload the billboard list (CloudVolume::update, CloudVolume.cpp:84-93)."""
+        self.uploadBillboards()
+
+    def uploadBillboards(self):
+        n = self.count
+        check(self._lib.cg_volume_set_billboards(self.handle, _fptr(self.positions),
+                                                 _fptr(self.scales), _fptr(self.densities), n,
+                                                 float(self.fluffiness)),
+              "cg_volume_set_billboards")
+
+    def clearGPU(self):
+        """The volume is cleared by every voxelize (CloudVolume.cpp:96-100)."""
+
+    # -- index helpers (CloudVolume.cpp:103-118) --
+    def get3DIndices(self, index):
+        line = self.dimension
+        sl = self.dimension * line
+        z = index // sl
+        y = (index - z * sl) // line
+        x = index - z * sl - y * line
+        return (x, y, z)
+
+    def reverseVoxelIndex(self, idx):
+        return tuple(float(idx[a]) * self.range[a] / self.dimension + self.xBounds[0]
+                     for a in range(3))
+
+    # -- readback (VoxelShader::updateVoxelData, VoxelShader.cpp:102-133) --
+    def info(self):
+        inf = _lib.cg_volume_info()
+        check(self._lib.cg_volume_get_info(self.handle, ctypes.byref(inf)), "cg_volume_get_info")
+        return inf
+
+    def read_level(self, level):
+        n = max(1, self.dimension >> level)
+        if self.format == FORMAT_RGBA32F:
+            out = np.empty((n, n, n, 4), np.float32)
+        else:
+            out = np.empty((n, n, n), np.uint32)
+        check(self._lib.cg_volume_read_level(self.handle, level,
+                                             out.ctypes.data_as(ctypes.c_void_p), out.nbytes),
+              "cg_volume_read_level")
+        return out
+
+    def read_coverage(self):
+        D = self.dimension
+        cnt = np.empty((D, D, D), np.uint32)
+        dq = np.empty((D, D, D), np.uint32)
+        check(self._lib.cg_volume_read_coverage(
+            self.handle, cnt.ctypes.data_as(_lib.U32P), dq.ctypes.data_as(_lib.U32P)),
+            "cg_volume_read_coverage")
+        return cnt, dq
+
+    def read_sun_map(self, sun):
+        keys = np.empty((sun.map_height, sun.map_width), np.uint64)
+        pos = np.empty((sun.map_height, sun.map_width, 4), np.float32)
+        check(self._lib.cg_volume_read_sun_map(self.handle, keys.ctypes.data_as(_lib.U64P),
+                                               _fptr(pos)), "cg_volume_read_sun_map")
+        return keys, pos
+
+    def read_highlight(self):
+        D = self.dimension
+        m = np.empty((D, D, D), np.uint8)
+        check(self._lib.cg_volume_read_highlight(self.handle, m.ctypes.data_as(_lib.U8P)),
+              "cg_volume_read_highlight")
+        return m
+
+    def activeVoxels(self):
+        v = ctypes.c_uint64()
+        check(self._lib.cg_volume_active_voxels(self.handle, ctypes.byref(v)),
+              "cg_volume_active_voxels")
+        return int(v.value)
+
+    def close(self):
+        if self.handle:
+            self._lib.cg_volume_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class VoxelizeShader:
+    """VoxelizeShader::voxelize(CloudVolume*) (VoxelizeShader.cpp:18-31)."""
+
+    def voxelize(self, volume, sun, stream=None):
+        s = sun._c()
+        check(self._lib().cg_voxelize(volume.handle, ctypes.byref(s), stream), "cg_voxelize")
+
+    @staticmethod
+    def _lib():
+        return load()
+
+
+class ConeTraceShader:
+    """ConeTraceShader::coneTrace(CloudVolume*) (ConeTraceShader.cpp:15-82).
+
+    Field names follow ConeTraceShader.hpp:15-32.  vctConeAngle is the full
+    cone aperture as in the reference (its half is the cone half-angle);
+    freqStep / persStep are the fBm lacunarity / gain."""
+
+    def __init__(self, **kw):
+        p = _lib.cg_render_params()
+        load().cg_render_params_default(ctypes.byref(p))
+        self.viewSteps = p.view_steps
+        self.vctSteps = p.sun_steps
+        self.vctConeAngle = 2.0 * p.cone_half_angle
+        self.vctConeInitialHeight = p.cone_initial_height
+        self.vctConeMinRadius = p.cone_min_radius
+        self.vctLodOffset = p.lod_offset
+        self.vctDownScaling = p.down_scaling
+        self.densityScale = p.density_scale
+        self.ambient = p.ambient
+        self.sunColor = tuple(p.sun_color)
+        self.transmittanceCutoff = p.transmittance_cutoff
+        self.coneMode = p.cone_mode
+        self.noiseSeed = p.noise.seed
+        self.numOctaves = p.noise.octaves
+        self.noiseFrequency = p.noise.frequency
+        self.freqStep = p.noise.lacunarity
+        self.persStep = p.noise.gain
+        self.useMlp = False
+        self.mlp = None
+        for k, v in kw.items():
+            if not hasattr(self, k):
+                raise AttributeError(f"ConeTraceShader has no parameter {k!r}")
+            setattr(self, k, v)
+
+    def params(self):
+        p = _lib.cg_render_params()
+        p.view_steps = int(self.viewSteps)
+        p.sun_steps = int(self.vctSteps)
+        p.cone_half_angle = float(self.vctConeAngle) / 2.0
+        p.cone_initial_height = float(self.vctConeInitialHeight)
+        p.cone_min_radius = float(self.vctConeMinRadius)
+        p.lod_offset = float(self.vctLodOffset)
+        p.down_scaling = float(self.vctDownScaling)
+        p.density_scale = float(self.densityScale)
+        p.ambient = float(self.ambient)
+        p.sun_color[:] = [float(x) for x in self.sunColor]
+        p.transmittance_cutoff = float(self.transmittanceCutoff)
+        p.cone_mode = int(self.coneMode)
+        p.noise.seed = int(self.noiseSeed) & 0xFFFFFFFF
+        p.noise.octaves = int(self.numOctaves)
+        p.noise.frequency = float(self.noiseFrequency)
+        p.noise.lacunarity = float(self.freqStep)
+        p.noise.gain = float(self.persStep)
+        p.use_mlp = 1 if self.useMlp else 0
+        p.mlp = self.mlp.handle if (self.useMlp and self.mlp is not None) else None
+        return p
+
+    def coneTrace(self, volume, camera, out=None, stream=None):
+        """Render `camera`'s view of `volume`; returns an H x W x 4 float32 image
+        (row 0 = top).  `out` may be a numpy array, a HostBuffer (pinned) or a
+        DeviceBuffer (result left on the device)."""
+        p = self.params()
+        c = camera._c()
+        lib = load()
+        if isinstance(out, DeviceBuffer):
+            check(lib.cg_render(volume.ctx.handle, volume.handle, ctypes.byref(c), ctypes.byref(p),
+                                out.ptr, 1, stream), "cg_render")
+            return out
+        if isinstance(out, HostBuffer):
+            arr = out.array
+        elif out is None:
+            arr = np.empty((camera.height, camera.width, 4), np.float32)
+        else:
+            arr = out
+        assert arr.dtype == np.float32 and arr.flags["C_CONTIGUOUS"]
+        assert arr.size >= camera.width * camera.height * 4
+        check(lib.cg_render(volume.ctx.handle, volume.handle, ctypes.byref(c), ctypes.byref(p),
+                            arr.ctypes.data_as(ctypes.c_void_p), 0, stream), "cg_render")
+        return arr
+
+    def renderStats(self, volume, camera):
+        """Executed-work counters of one render: view samples, sun cones,
+        sun-cone samples, pixels whose ray met the box."""
+        p = self.params()
+        c = camera._c()
+        out = (ctypes.c_uint64 * 4)()
+        check(load().cg_render_stats(volume.ctx.handle, volume.handle, ctypes.byref(c),
+                                     ctypes.byref(p), out), "cg_render_stats")
+        return dict(view_samples=int(out[0]), sun_cones=int(out[1]), sun_samples=int(out[2]),
+                    hit_pixels=int(out[3]))
+
+    def traceCone(self, volume, positions, direction):
+        """traceCone at level-0 voxel-space positions (conetrace_frag.glsl:64-79)."""
+        pos = np.ascontiguousarray(positions, np.float32).reshape(-1, 3)
+        out = np.empty((pos.shape[0],), np.float32)
+        d = (ctypes.c_float * 3)(*[float(x) for x in direction])
+        p = self.params()
+        check(load().cg_trace_cones(volume.handle, pos.ctypes.data_as(ctypes.c_void_p),
+                                    pos.shape[0], d, ctypes.byref(p),
+                                    out.ctypes.data_as(ctypes.c_void_p), 0, None),
+              "cg_trace_cones")
+        return out
+
+    @staticmethod
+    def half_angle_to_cone_angle(half):
+        return 2.0 * half
+
+
+def deg(x):
+    return math.degrees(x)

@@ -1,0 +1,132 @@
+"""ctypes binding of include/cloudgb.h (libcloudgb.so, built for sm_103a).
+
+Loading fails loudly when the library is missing: there is no CPU fallback.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libcloudgb.so")
+
+CG_OK = 0
+STATUS_NAMES = {
+    0: "CG_OK", 1: "CG_ERR_INVALID_ARGUMENT", 2: "CG_ERR_OUT_OF_RANGE",
+    3: "CG_ERR_OUT_OF_MEMORY", 4: "CG_ERR_CUDA", 5: "CG_ERR_NOT_READY",
+    6: "CG_ERR_DEVICE_FAULT", 7: "CG_ERR_IO", 8: "CG_ERR_BAD_CHECKPOINT",
+    9: "CG_ERR_UNSUPPORTED",
+}
+FORMAT_RGBA32F = 0
+FORMAT_BF16_FP16 = 1
+CONE_TRANSMITTANCE = 0
+CONE_REFERENCE = 1
+MEMCPY_H2D, MEMCPY_D2H, MEMCPY_D2D = 1, 2, 3
+
+
+class CloudError(RuntimeError):
+    """A libcloudgb call returned a non-OK cg_status."""
+
+    def __init__(self, status, message):
+        self.status = status
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+
+
+class cg_sun(ctypes.Structure):
+    _fields_ = [("direction", ctypes.c_float * 3), ("map_width", ctypes.c_int),
+                ("map_height", ctypes.c_int)]
+
+
+class cg_camera(ctypes.Structure):
+    _fields_ = [("eye", ctypes.c_float * 3), ("target", ctypes.c_float * 3),
+                ("up", ctypes.c_float * 3), ("fov_y_degrees", ctypes.c_float),
+                ("width", ctypes.c_int), ("height", ctypes.c_int)]
+
+
+class cg_noise(ctypes.Structure):
+    _fields_ = [("seed", ctypes.c_uint32), ("octaves", ctypes.c_int),
+                ("frequency", ctypes.c_float), ("lacunarity", ctypes.c_float),
+                ("gain", ctypes.c_float)]
+
+
+class cg_render_params(ctypes.Structure):
+    _fields_ = [("view_steps", ctypes.c_int), ("sun_steps", ctypes.c_int),
+                ("cone_half_angle", ctypes.c_float), ("cone_initial_height", ctypes.c_float),
+                ("cone_min_radius", ctypes.c_float), ("lod_offset", ctypes.c_float),
+                ("down_scaling", ctypes.c_float), ("density_scale", ctypes.c_float),
+                ("ambient", ctypes.c_float), ("sun_color", ctypes.c_float * 3),
+                ("transmittance_cutoff", ctypes.c_float), ("cone_mode", ctypes.c_int),
+                ("noise", cg_noise), ("use_mlp", ctypes.c_int), ("mlp", ctypes.c_void_p)]
+
+
+class cg_volume_info(ctypes.Structure):
+    _fields_ = [("dimension", ctypes.c_int), ("mips", ctypes.c_int), ("format", ctypes.c_int),
+                ("board_count", ctypes.c_int), ("world_min", ctypes.c_float * 3),
+                ("world_max", ctypes.c_float * 3), ("level_dim", ctypes.c_int * 16),
+                ("level_offset", ctypes.c_size_t * 16), ("bytes_per_voxel", ctypes.c_size_t),
+                ("pyramid_bytes", ctypes.c_size_t)]
+
+
+P = ctypes.c_void_p
+PP = ctypes.POINTER(ctypes.c_void_p)
+I = ctypes.c_int
+F = ctypes.c_float
+FP = ctypes.POINTER(ctypes.c_float)
+U32P = ctypes.POINTER(ctypes.c_uint32)
+U64P = ctypes.POINTER(ctypes.c_uint64)
+U8P = ctypes.POINTER(ctypes.c_uint8)
+SZ = ctypes.c_size_t
+
+# (name, restype, argtypes) for every function declared in include/cloudgb.h
+SIGNATURES = [
+    ("cg_status_string", ctypes.c_char_p, [I]),
+    ("cg_last_error", ctypes.c_char_p, []),
+    ("cg_abi_version", I, []),
+    ("cg_context_create", I, [I, PP]),
+    ("cg_context_destroy", None, [P]),
+    ("cg_context_synchronize", I, [P]),
+    ("cg_context_launch_count", ctypes.c_uint64, [P]),
+    ("cg_render_params_default", None, [ctypes.POINTER(cg_render_params)]),
+    ("cg_host_alloc", I, [SZ, PP]),
+    ("cg_host_free", None, [P]),
+    ("cg_device_alloc", I, [SZ, PP]),
+    ("cg_device_free", None, [P]),
+    ("cg_memcpy", I, [P, P, SZ, I]),
+    ("cg_volume_create", I, [P, I, F, F, FP, I, I, PP]),
+    ("cg_volume_destroy", None, [P]),
+    ("cg_volume_set_billboards", I, [P, FP, FP, FP, I, F]),
+    ("cg_voxelize", I, [P, ctypes.POINTER(cg_sun), P]),
+    ("cg_render", I, [P, P, ctypes.POINTER(cg_camera), ctypes.POINTER(cg_render_params), P, I, P]),
+    ("cg_render_stats", I, [P, P, ctypes.POINTER(cg_camera), ctypes.POINTER(cg_render_params),
+                            U64P]),
+    ("cg_trace_cones", I, [P, P, I, FP, ctypes.POINTER(cg_render_params), P, I, P]),
+    ("cg_volume_get_info", I, [P, ctypes.POINTER(cg_volume_info)]),
+    ("cg_volume_read_level", I, [P, I, P, SZ]),
+    ("cg_volume_read_coverage", I, [P, U32P, U32P]),
+    ("cg_volume_read_sun_map", I, [P, U64P, FP]),
+    ("cg_volume_read_highlight", I, [P, U8P]),
+    ("cg_volume_active_voxels", I, [P, U64P]),
+]
+
+_lib = None
+
+
+def load():
+    """Load libcloudgb.so and bind every declared entry point."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(
+            f"{LIB_PATH} is missing: build it with `python -c \"import __graft_entry__ as g; g.build()\"`")
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status, what=""):
+    if status != CG_OK:
+        msg = load().cg_last_error().decode(errors="replace")
+        raise CloudError(status, f"{what}: {msg}" if what else msg)

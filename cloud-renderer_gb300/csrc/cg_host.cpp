@@ -1,0 +1,896 @@
+// cg_host.cpp -- the C ABI (include/cloudgb.h): contexts, volumes, board
+// quantization, pass orchestration and readback.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "cg_internal.h"
+#include "cloudgb.h"
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+static thread_local std::string g_last_error;
+
+static cg_status fail(cg_status s, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return s;
+}
+
+#define CG_CUDA(call)                                                                      \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess)                                                             \
+            return fail(e_ == cudaErrorMemoryAllocation ? CG_ERR_OUT_OF_MEMORY : CG_ERR_CUDA, \
+                        "%s: %s", #call, cudaGetErrorString(e_));                          \
+    } while (0)
+
+#define CG_CHECK(cond, status, ...)                  \
+    do {                                             \
+        if (!(cond)) return fail(status, __VA_ARGS__); \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// device buffers
+// ---------------------------------------------------------------------------
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t want) {
+        if (want <= bytes && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, want ? want : 16);
+        if (e == cudaSuccess) bytes = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <class T>
+    T* as() const {
+        return reinterpret_cast<T*>(p);
+    }
+};
+
+struct HostBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t want) {
+        if (want <= bytes && p) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMallocHost(&p, want ? want : 16);
+        if (e == cudaSuccess) bytes = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+    }
+};
+
+struct cg_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint64_t launches = 0;
+    DevBuf image;  // render target when the caller passes a host pointer
+};
+
+struct cg_volume {
+    cg_context* ctx = nullptr;
+    int D = 0, L = 0, fmt = 0;
+    float pos[3] = {0, 0, 0}, b0 = 0, b1 = 0;
+    float wmin[3], wmax[3], range[3];
+    int dims[CG_MAX_LEVELS];
+    size_t offs[CG_MAX_LEVELS];
+    size_t total = 0;
+    DevBuf pyr, count, dq, mask;
+    // boards
+    int n = 0;
+    size_t pairs = 0;
+    DevBuf cwr, q, thr, dqb, culled;
+    HostBuf h_stage;
+    Bins bins{};
+    DevBuf bcount, boff, bcursor, blist;
+    // sun map
+    int mapW = 0, mapH = 0;
+    DevBuf keys, posmap;
+    bool voxelized = false;
+    SunFrame frame{};
+    float sun_dir[3] = {0, 1, 0};
+    DevBuf scratch;  // small scalars (active voxel count)
+};
+
+// ---------------------------------------------------------------------------
+// library
+// ---------------------------------------------------------------------------
+extern "C" const char* cg_status_string(cg_status s) {
+    switch (s) {
+        case CG_OK: return "ok";
+        case CG_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case CG_ERR_OUT_OF_RANGE: return "out of range";
+        case CG_ERR_OUT_OF_MEMORY: return "out of memory";
+        case CG_ERR_CUDA: return "CUDA error";
+        case CG_ERR_NOT_READY: return "not ready";
+        case CG_ERR_DEVICE_FAULT: return "device fault";
+        case CG_ERR_IO: return "I/O error";
+        case CG_ERR_BAD_CHECKPOINT: return "bad checkpoint";
+        case CG_ERR_UNSUPPORTED: return "unsupported";
+    }
+    return "unknown status";
+}
+
+extern "C" const char* cg_last_error(void) { return g_last_error.c_str(); }
+extern "C" int cg_abi_version(void) { return CLOUDGB_ABI_VERSION; }
+
+extern "C" cg_status cg_context_create(int device, cg_context** out) {
+    CG_CHECK(out, CG_ERR_INVALID_ARGUMENT, "cg_context_create: out is NULL");
+    *out = nullptr;
+    int ndev = 0;
+    CG_CUDA(cudaGetDeviceCount(&ndev));
+    CG_CHECK(device >= 0 && device < ndev, CG_ERR_OUT_OF_RANGE,
+             "cg_context_create: device %d not in [0, %d)", device, ndev);
+    CG_CUDA(cudaSetDevice(device));
+    cg_context* c = new cg_context();
+    c->device = device;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return fail(CG_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+    }
+    *out = c;
+    return CG_OK;
+}
+
+extern "C" void cg_context_destroy(cg_context* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    ctx->image.release();
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+static cudaStream_t pick(cg_context* ctx, void* stream) {
+    return stream ? reinterpret_cast<cudaStream_t>(stream) : ctx->stream;
+}
+
+extern "C" cg_status cg_context_synchronize(cg_context* ctx) {
+    CG_CHECK(ctx, CG_ERR_INVALID_ARGUMENT, "cg_context_synchronize: ctx is NULL");
+    CG_CUDA(cudaSetDevice(ctx->device));
+    CG_CUDA(cudaDeviceSynchronize());
+    return CG_OK;
+}
+
+extern "C" uint64_t cg_context_launch_count(const cg_context* ctx) {
+    return ctx ? ctx->launches : 0;
+}
+
+extern "C" void cg_render_params_default(cg_render_params* p) {
+    if (!p) return;
+    memset(p, 0, sizeof(*p));
+    p->view_steps = 64;
+    p->sun_steps = 24;
+    p->cone_half_angle = 0.03f;
+    p->cone_initial_height = 1.0f;
+    p->cone_min_radius = 2.0f;
+    p->lod_offset = 0.0f;
+    p->down_scaling = 1.0f;
+    p->density_scale = 4.0f;
+    p->ambient = 0.3f;
+    p->sun_color[0] = p->sun_color[1] = p->sun_color[2] = 1.0f;
+    p->transmittance_cutoff = 1e-5f;
+    p->cone_mode = CG_CONE_TRANSMITTANCE;
+    p->noise.seed = 1;
+    p->noise.octaves = 0;
+    p->noise.frequency = 4.0f;
+    p->noise.lacunarity = 2.0f;
+    p->noise.gain = 0.5f;
+    p->use_mlp = 0;
+    p->mlp = nullptr;
+}
+
+extern "C" cg_status cg_host_alloc(size_t bytes, void** out) {
+    CG_CHECK(out, CG_ERR_INVALID_ARGUMENT, "cg_host_alloc: out is NULL");
+    CG_CUDA(cudaMallocHost(out, bytes ? bytes : 16));
+    return CG_OK;
+}
+extern "C" void cg_host_free(void* p) {
+    if (p) cudaFreeHost(p);
+}
+extern "C" cg_status cg_device_alloc(size_t bytes, void** out) {
+    CG_CHECK(out, CG_ERR_INVALID_ARGUMENT, "cg_device_alloc: out is NULL");
+    CG_CUDA(cudaMalloc(out, bytes ? bytes : 16));
+    return CG_OK;
+}
+extern "C" void cg_device_free(void* p) {
+    if (p) cudaFree(p);
+}
+extern "C" cg_status cg_memcpy(void* dst, const void* src, size_t bytes, int kind) {
+    CG_CHECK(dst && src, CG_ERR_INVALID_ARGUMENT, "cg_memcpy: null pointer");
+    CG_CUDA(cudaMemcpy(dst, src, bytes, (cudaMemcpyKind)kind));
+    return CG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// CloudVolume
+// ---------------------------------------------------------------------------
+extern "C" cg_status cg_volume_create(cg_context* ctx, int dimension, float bound_min,
+                                      float bound_max, const float position[3], int mips,
+                                      int format, cg_volume** out) {
+    CG_CHECK(ctx && position && out, CG_ERR_INVALID_ARGUMENT, "cg_volume_create: null pointer");
+    *out = nullptr;
+    CG_CHECK(dimension >= 2 && dimension <= 512, CG_ERR_OUT_OF_RANGE,
+             "cg_volume_create: dimension %d not in [2, 512]", dimension);
+    int maxl = 1;
+    while ((dimension >> maxl) >= 1 && maxl < CG_MAX_LEVELS) maxl++;
+    CG_CHECK(mips >= 1 && mips <= maxl, CG_ERR_OUT_OF_RANGE,
+             "cg_volume_create: mips %d not in [1, %d]", mips, maxl);
+    CG_CHECK(format == CG_FORMAT_RGBA32F || format == CG_FORMAT_BF16_FP16,
+             CG_ERR_INVALID_ARGUMENT, "cg_volume_create: unknown format %d", format);
+    CG_CHECK(std::isfinite(bound_min) && std::isfinite(bound_max) && bound_max > bound_min,
+             CG_ERR_INVALID_ARGUMENT, "cg_volume_create: bounds must be finite, min < max");
+    for (int a = 0; a < 3; ++a)
+        CG_CHECK(std::isfinite(position[a]), CG_ERR_INVALID_ARGUMENT,
+                 "cg_volume_create: non-finite position");
+    CG_CUDA(cudaSetDevice(ctx->device));
+    cg_volume* v = new cg_volume();
+    v->ctx = ctx;
+    v->D = dimension;
+    v->L = mips;
+    v->fmt = format;
+    v->b0 = bound_min;
+    v->b1 = bound_max;
+    for (int a = 0; a < 3; ++a) {
+        v->pos[a] = position[a];
+        v->wmin[a] = position[a] + bound_min;
+        v->wmax[a] = position[a] + bound_max;
+        v->range[a] = v->wmax[a] - v->wmin[a];
+    }
+    size_t off = 0;
+    for (int l = 0; l < mips; ++l) {
+        int n = dimension >> l;
+        if (n < 1) n = 1;
+        v->dims[l] = n;
+        v->offs[l] = off;
+        off += (size_t)n * n * n;
+    }
+    for (int l = mips; l < CG_MAX_LEVELS; ++l) {
+        v->dims[l] = 0;
+        v->offs[l] = off;
+    }
+    v->total = off;
+    const size_t n0 = (size_t)dimension * dimension * dimension;
+    const size_t bpv = format == CG_FORMAT_RGBA32F ? 16 : 4;
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = v->pyr.ensure(off * bpv);
+    if (e == cudaSuccess) e = v->count.ensure(n0 * 4);
+    if (e == cudaSuccess) e = v->dq.ensure(n0 * 4);
+    if (e == cudaSuccess) e = v->mask.ensure(n0);
+    if (e == cudaSuccess) e = v->scratch.ensure(64);
+    const int nb = (dimension + CG_BRICK - 1) / CG_BRICK;
+    v->bins.nbx = v->bins.nby = v->bins.nbz = nb;
+    v->bins.nbricks = nb * nb * nb;
+    if (e == cudaSuccess) e = v->bcount.ensure((size_t)v->bins.nbricks * 4);
+    if (e == cudaSuccess) e = v->boff.ensure(((size_t)v->bins.nbricks + 1) * 4);
+    if (e == cudaSuccess) e = v->bcursor.ensure((size_t)v->bins.nbricks * 4);
+    if (e != cudaSuccess) {
+        cg_volume_destroy(v);
+        return fail(e == cudaErrorMemoryAllocation ? CG_ERR_OUT_OF_MEMORY : CG_ERR_CUDA,
+                    "cg_volume_create: %s", cudaGetErrorString(e));
+    }
+    *out = v;
+    return CG_OK;
+}
+
+extern "C" void cg_volume_destroy(cg_volume* v) {
+    if (!v) return;
+    cudaSetDevice(v->ctx->device);
+    cudaStreamSynchronize(v->ctx->stream);
+    DevBuf* bufs[] = {&v->pyr, &v->count, &v->dq, &v->mask, &v->cwr, &v->q, &v->thr,
+                      &v->dqb, &v->culled, &v->bcount, &v->boff, &v->bcursor, &v->blist,
+                      &v->keys, &v->posmap, &v->scratch};
+    for (DevBuf* b : bufs) b->release();
+    v->h_stage.release();
+    delete v;
+}
+
+static long long floor_div_ll(long long a, long long b) {
+    long long q = a / b;
+    if ((a % b != 0) && ((a < 0) != (b < 0))) q--;
+    return q;
+}
+
+static bool axis_range_host(long long q, long long rq, int D, int& lo, int& hi) {
+    long long l = floor_div_ll(q - rq - CG_HALF_Q20 + CG_Q20 - 1, CG_Q20);
+    long long h = floor_div_ll(q + rq - CG_HALF_Q20, CG_Q20);
+    if (l < 0) l = 0;
+    if (h > D - 1) h = D - 1;
+    if (l > h) return false;
+    lo = (int)l;
+    hi = (int)h;
+    return true;
+}
+
+// Board quantization to the Q20 voxel grid (FP64, round to nearest even):
+//   v = (cw - wmin) / range * D per axis, q = rint(v * 2^20), culled from
+//   coverage when v is outside [-D, 2D];  rq = rint(r / range_x * D * 2^20),
+//   error when r > range_x;  thr = floor(rq^2 * 9999 / 10000) (the 0.01
+//   profile discard of first_voxelize.glsl:46);  dq = rint(density * 2^16).
+extern "C" cg_status cg_volume_set_billboards(cg_volume* v, const float* positions,
+                                              const float* scales, const float* densities,
+                                              int count, float fluffiness) {
+    CG_CHECK(v, CG_ERR_INVALID_ARGUMENT, "cg_volume_set_billboards: volume is NULL");
+    CG_CHECK(count >= 0 && count <= (1 << 24), CG_ERR_OUT_OF_RANGE,
+             "cg_volume_set_billboards: count %d not in [0, 2^24]", count);
+    CG_CHECK(count == 0 || (positions && scales), CG_ERR_INVALID_ARGUMENT,
+             "cg_volume_set_billboards: null positions/scales");
+    CG_CHECK(std::isfinite(fluffiness) && fluffiness >= 0.f, CG_ERR_INVALID_ARGUMENT,
+             "cg_volume_set_billboards: fluffiness must be finite and >= 0");
+    CG_CUDA(cudaSetDevice(v->ctx->device));
+    const size_t n = (size_t)count;
+    const size_t bytes_cwr = n * 16, bytes_q = n * 16, bytes_thr = n * 8, bytes_dq = n * 4,
+                 bytes_cul = n;
+    const size_t o_cwr = 0, o_q = o_cwr + bytes_cwr, o_thr = o_q + bytes_q,
+                 o_dq = o_thr + bytes_thr, o_cul = o_dq + bytes_dq;
+    const size_t total = o_cul + bytes_cul;
+    CG_CUDA(cudaStreamSynchronize(v->ctx->stream));  // staging buffer reuse
+    CG_CUDA(v->h_stage.ensure(total + 16));
+    char* st = reinterpret_cast<char*>(v->h_stage.p);
+    float* cwr = reinterpret_cast<float*>(st + o_cwr);
+    int* qv = reinterpret_cast<int*>(st + o_q);
+    uint64_t* thr = reinterpret_cast<uint64_t*>(st + o_thr);
+    uint32_t* dqv = reinterpret_cast<uint32_t*>(st + o_dq);
+    uint8_t* cul = reinterpret_cast<uint8_t*>(st + o_cul);
+    const int D = v->D;
+    size_t pairs = 0;
+    for (size_t b = 0; b < n; ++b) {
+        float r = scales[b] * fluffiness;
+        float d = densities ? densities[b] : 1.0f;
+        CG_CHECK(std::isfinite(r) && r >= 0.f, CG_ERR_INVALID_ARGUMENT,
+                 "billboard %zu: radius must be finite and >= 0", b);
+        CG_CHECK(std::isfinite(d) && d >= 0.f && d < 32768.f, CG_ERR_INVALID_ARGUMENT,
+                 "billboard %zu: density must be in [0, 32768)", b);
+        bool cull = false;
+        long long q[3];
+        for (int a = 0; a < 3; ++a) {
+            float c = v->pos[a] + positions[3 * b + a];
+            CG_CHECK(std::isfinite(c), CG_ERR_INVALID_ARGUMENT,
+                     "billboard %zu: non-finite position", b);
+            cwr[4 * b + a] = c;
+            double vv = ((double)c - (double)v->wmin[a]) / (double)v->range[a] * (double)D;
+            if (!(vv >= -(double)D && vv <= 2.0 * (double)D)) {
+                cull = true;
+                q[a] = 0;
+            } else {
+                q[a] = llrint(vv * (double)CG_Q20);
+            }
+        }
+        cwr[4 * b + 3] = r;
+        double rv = (double)r / (double)v->range[0] * (double)D;
+        CG_CHECK(rv <= (double)D, CG_ERR_OUT_OF_RANGE,
+                 "billboard %zu: radius %g exceeds the volume extent", b, (double)r);
+        long long rq = llrint(rv * (double)CG_Q20);
+        unsigned __int128 r2 = (unsigned __int128)(uint64_t)rq * (uint64_t)rq;
+        thr[b] = (uint64_t)((r2 * 9999u) / 10000u);
+        dqv[b] = (uint32_t)llrint((double)d * 65536.0);
+        for (int a = 0; a < 3; ++a) qv[4 * b + a] = (int)q[a];
+        qv[4 * b + 3] = (int)rq;
+        int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+        if (!cull)
+            for (int a = 0; a < 3; ++a)
+                if (!axis_range_host(q[a], rq, D, lo[a], hi[a])) cull = true;
+        cul[b] = cull ? 1 : 0;
+        if (!cull) {
+            size_t nbz = (size_t)(hi[2] / CG_BRICK - lo[2] / CG_BRICK + 1);
+            size_t nby = (size_t)(hi[1] / CG_BRICK - lo[1] / CG_BRICK + 1);
+            size_t nbx = (size_t)(hi[0] / CG_BRICK - lo[0] / CG_BRICK + 1);
+            pairs += nbx * nby * nbz;
+        }
+    }
+    CG_CHECK(pairs < (size_t)0xFFFFFFFFu, CG_ERR_OUT_OF_RANGE,
+             "cg_volume_set_billboards: %zu board-brick pairs exceed 2^32", pairs);
+    CG_CUDA(v->cwr.ensure(bytes_cwr));
+    CG_CUDA(v->q.ensure(bytes_q));
+    CG_CUDA(v->thr.ensure(bytes_thr));
+    CG_CUDA(v->dqb.ensure(bytes_dq));
+    CG_CUDA(v->culled.ensure(bytes_cul));
+    CG_CUDA(v->blist.ensure(pairs * 4));
+    cudaStream_t s = v->ctx->stream;
+    if (n) {
+        CG_CUDA(cudaMemcpyAsync(v->cwr.p, cwr, bytes_cwr, cudaMemcpyHostToDevice, s));
+        CG_CUDA(cudaMemcpyAsync(v->q.p, qv, bytes_q, cudaMemcpyHostToDevice, s));
+        CG_CUDA(cudaMemcpyAsync(v->thr.p, thr, bytes_thr, cudaMemcpyHostToDevice, s));
+        CG_CUDA(cudaMemcpyAsync(v->dqb.p, dqv, bytes_dq, cudaMemcpyHostToDevice, s));
+        CG_CUDA(cudaMemcpyAsync(v->culled.p, cul, bytes_cul, cudaMemcpyHostToDevice, s));
+    }
+    v->n = count;
+    v->pairs = pairs;
+    v->voxelized = false;
+    return CG_OK;
+}
+
+static BoardsDev boards_of(const cg_volume* v) {
+    BoardsDev b;
+    b.n = v->n;
+    b.cwr = v->cwr.as<const float4>();
+    b.q = v->q.as<const int4>();
+    b.thr = v->thr.as<const uint64_t>();
+    b.dq = v->dqb.as<const uint32_t>();
+    b.culled = v->culled.as<const uint8_t>();
+    return b;
+}
+
+static VolDesc desc_of(const cg_volume* v) {
+    VolDesc d;
+    d.D = v->D;
+    d.L = v->L;
+    d.fmt = v->fmt;
+    for (int l = 0; l < CG_MAX_LEVELS; ++l) {
+        d.dims[l] = v->dims[l];
+        d.offs[l] = (long long)v->offs[l];
+    }
+    for (int a = 0; a < 3; ++a) {
+        d.wmin[a] = v->wmin[a];
+        d.range[a] = v->range[a];
+    }
+    d.pyr = v->pyr.p;
+    return d;
+}
+
+// FP32 vector helpers in GLM's operation order; this translation unit is
+// compiled with -ffp-contract=off so that the frame is bit-identical to the
+// oracle's.
+struct V3 {
+    float x, y, z;
+};
+static float dot3(V3 a, V3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+static V3 cross3(V3 a, V3 b) {
+    return {a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y};
+}
+static V3 normalize3(V3 v) {
+    float inv = 1.0f / std::sqrt(dot3(v, v));
+    return {v.x * inv, v.y * inv, v.z * inv};
+}
+
+// Sun::update (Sun.hpp:26-43) for a directional sun: lookDir = -s, lookPos =
+// position - lookDir * max(|min|, |max|), V = lookAt(lookPos, position, +y),
+// ortho box [2 minComp, 2 maxComp]^2, near 0.01.
+static bool make_sun_frame(const cg_volume* v, const float dir[3], int W, int H, SunFrame& fr) {
+    V3 pos{v->pos[0], v->pos[1], v->pos[2]};
+    V3 lookDir = normalize3({-dir[0], -dir[1], -dir[2]});
+    V3 mn{v->b0, v->b0, v->b0}, mx{v->b1, v->b1, v->b1};
+    float minLen = std::sqrt(dot3(mn, mn)), maxLen = std::sqrt(dot3(mx, mx));
+    float dist = minLen > maxLen ? minLen : maxLen;
+    V3 lookPos{pos.x - lookDir.x * dist, pos.y - lookDir.y * dist, pos.z - lookDir.z * dist};
+    V3 f = normalize3({pos.x - lookPos.x, pos.y - lookPos.y, pos.z - lookPos.z});
+    V3 c = cross3(f, {0.0f, 1.0f, 0.0f});
+    float cl = dot3(c, c);
+    if (!(cl > 1e-12f)) return false;
+    V3 r = normalize3(c);
+    V3 u = cross3(r, f);
+    fr.eye[0] = lookPos.x; fr.eye[1] = lookPos.y; fr.eye[2] = lookPos.z;
+    fr.right[0] = r.x; fr.right[1] = r.y; fr.right[2] = r.z;
+    fr.up[0] = u.x; fr.up[1] = u.y; fr.up[2] = u.z;
+    fr.fwd[0] = f.x; fr.fwd[1] = f.y; fr.fwd[2] = f.z;
+    fr.t[0] = -dot3(r, lookPos);
+    fr.t[1] = -dot3(u, lookPos);
+    fr.t[2] = dot3(f, lookPos);
+    fr.lo = 2.0f * v->b0;
+    fr.hi = 2.0f * v->b1;
+    fr.near_z = 0.01f;
+    V3 np{lookPos.x + lookDir.x * 0.01f, lookPos.y + lookDir.y * 0.01f,
+          lookPos.z + lookDir.z * 0.01f};
+    float two_d = 2.0f * dist;
+    V3 fp{lookPos.x + lookDir.x * two_d, lookPos.y + lookDir.y * two_d,
+          lookPos.z + lookDir.z * two_d};
+    V3 dd{np.x - fp.x, np.y - fp.y, np.z - fp.z};
+    fr.clip = std::sqrt(dot3(dd, dd));
+    fr.W = W;
+    fr.H = H;
+    return true;
+}
+
+// stepSize = min(voxelSize) (VoxelizeShader.cpp:128); offset along each axis
+// of stepSize * normalize(+-1,+-1,+-1) (second_voxelize.glsl:42-49).
+static float highlight_offset(const cg_volume* v) {
+    float vs0 = v->range[0] / (float)v->D, vs1 = v->range[1] / (float)v->D,
+          vs2 = v->range[2] / (float)v->D;
+    float step = vs0 < vs1 ? vs0 : vs1;
+    step = step < vs2 ? step : vs2;
+    return step * 0.57735026f;
+}
+
+#define CG_LAUNCH(ctx, expr)                                                          \
+    do {                                                                              \
+        cudaError_t e_ = (expr);                                                      \
+        if (e_ != cudaSuccess)                                                        \
+            return fail(CG_ERR_CUDA, "%s: %s", #expr, cudaGetErrorString(e_));        \
+        (ctx)->launches++;                                                            \
+    } while (0)
+
+extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) {
+    CG_CHECK(v && sun, CG_ERR_INVALID_ARGUMENT, "cg_voxelize: null pointer");
+    CG_CHECK(sun->map_width >= 1 && sun->map_height >= 1 && sun->map_width <= 16384 &&
+                 sun->map_height <= 16384,
+             CG_ERR_OUT_OF_RANGE, "cg_voxelize: sun map %dx%d not in [1, 16384]^2",
+             sun->map_width, sun->map_height);
+    for (int a = 0; a < 3; ++a)
+        CG_CHECK(std::isfinite(sun->direction[a]), CG_ERR_INVALID_ARGUMENT,
+                 "cg_voxelize: non-finite sun direction");
+    SunFrame fr;
+    CG_CHECK(make_sun_frame(v, sun->direction, sun->map_width, sun->map_height, fr),
+             CG_ERR_INVALID_ARGUMENT,
+             "cg_voxelize: sun direction is zero or parallel to the up axis (0,1,0)");
+    cg_context* ctx = v->ctx;
+    CG_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = pick(ctx, stream);
+    const size_t texels = (size_t)sun->map_width * sun->map_height;
+    if (v->mapW != sun->map_width || v->mapH != sun->map_height) {
+        CG_CUDA(cudaStreamSynchronize(s));
+        CG_CUDA(v->keys.ensure(texels * 8));
+        CG_CUDA(v->posmap.ensure(texels * 16));
+        v->mapW = sun->map_width;
+        v->mapH = sun->map_height;
+    }
+    v->frame = fr;
+    for (int a = 0; a < 3; ++a) v->sun_dir[a] = sun->direction[a];
+    const size_t n0 = (size_t)v->D * v->D * v->D;
+    BoardsDev b = boards_of(v);
+    Bins bins = v->bins;
+    bins.count = v->bcount.as<uint32_t>();
+    bins.offset = v->boff.as<uint32_t>();
+    bins.cursor = v->bcursor.as<uint32_t>();
+    bins.list = v->blist.as<uint32_t>();
+    VolDesc vd = desc_of(v);
+    // clearGPU (CloudVolume.cpp:96-100) + clearPositionMap (VoxelizeShader.cpp:185-187)
+    CG_CUDA(cudaMemsetAsync(v->keys.p, 0xFF, texels * 8, s));
+    CG_CUDA(cudaMemsetAsync(v->mask.p, 0, n0, s));
+    CG_CUDA(cudaMemsetAsync(bins.count, 0, (size_t)bins.nbricks * 4, s));
+    // brick bins
+    if (b.n) CG_LAUNCH(ctx, launch_bin_count(b, v->D, bins, s));
+    CG_LAUNCH(ctx, launch_bin_scan(bins, s));
+    if (b.n) CG_LAUNCH(ctx, launch_bin_fill(b, v->D, bins, s));
+    // pass 1: sun-view nearest-surface map
+    if (b.n) CG_LAUNCH(ctx, launch_sunmap(b, fr, v->keys.as<uint64_t>(), s));
+    // pass 2: highlight stores
+    CG_LAUNCH(ctx, launch_highlight(b, fr, v->keys.as<uint64_t>(), v->posmap.as<float4>(), v->D,
+                                    v->wmin, v->range, highlight_offset(v),
+                                    v->mask.as<uint8_t>(), s));
+    // coverage splat + level 0 + fused mips
+    int fused = (v->D % CG_BRICK == 0) ? std::min(CG_FUSED_MIPS, v->L - 1) : 0;
+    CG_LAUNCH(ctx, launch_splat(b, bins, v->mask.as<uint8_t>(), vd, v->pyr.p,
+                                v->count.as<uint32_t>(), v->dq.as<uint32_t>(), fused, s));
+    // remaining mips (glGenerateMipmap, VoxelizeShader.cpp:105)
+    for (int l = fused; l + 1 < v->L; ++l) CG_LAUNCH(ctx, launch_mip_level(vd, v->pyr.p, l, s));
+    v->voxelized = true;
+    return CG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// render
+// ---------------------------------------------------------------------------
+static cg_status check_params(const cg_render_params* p) {
+    CG_CHECK(p->view_steps >= 1 && p->view_steps <= 4096, CG_ERR_OUT_OF_RANGE,
+             "render params: view_steps %d not in [1, 4096]", p->view_steps);
+    CG_CHECK(p->sun_steps >= 0 && p->sun_steps <= 64, CG_ERR_OUT_OF_RANGE,
+             "render params: sun_steps %d not in [0, 64]", p->sun_steps);
+    CG_CHECK(std::isfinite(p->cone_half_angle) && p->cone_half_angle >= 0.f &&
+                 p->cone_half_angle < 1.5f,
+             CG_ERR_OUT_OF_RANGE, "render params: cone_half_angle not in [0, 1.5)");
+    CG_CHECK(std::isfinite(p->cone_initial_height) && p->cone_initial_height >= 0.f,
+             CG_ERR_INVALID_ARGUMENT, "render params: cone_initial_height must be >= 0");
+    CG_CHECK(std::isfinite(p->cone_min_radius) && p->cone_min_radius >= 0.f,
+             CG_ERR_INVALID_ARGUMENT, "render params: cone_min_radius must be >= 0");
+    CG_CHECK(std::isfinite(p->lod_offset), CG_ERR_INVALID_ARGUMENT,
+             "render params: lod_offset must be finite");
+    CG_CHECK(std::isfinite(p->down_scaling) && p->down_scaling > 0.f, CG_ERR_INVALID_ARGUMENT,
+             "render params: down_scaling must be > 0");
+    CG_CHECK(std::isfinite(p->density_scale) && p->density_scale >= 0.f,
+             CG_ERR_INVALID_ARGUMENT, "render params: density_scale must be >= 0");
+    CG_CHECK(std::isfinite(p->ambient) && p->ambient >= 0.f && p->ambient <= 1.f,
+             CG_ERR_OUT_OF_RANGE, "render params: ambient not in [0, 1]");
+    CG_CHECK(std::isfinite(p->transmittance_cutoff) && p->transmittance_cutoff >= 0.f &&
+                 p->transmittance_cutoff < 1.f,
+             CG_ERR_OUT_OF_RANGE, "render params: transmittance_cutoff not in [0, 1)");
+    CG_CHECK(p->cone_mode == CG_CONE_TRANSMITTANCE || p->cone_mode == CG_CONE_REFERENCE,
+             CG_ERR_INVALID_ARGUMENT, "render params: unknown cone_mode %d", p->cone_mode);
+    CG_CHECK(p->noise.octaves >= 0 && p->noise.octaves <= 16, CG_ERR_OUT_OF_RANGE,
+             "render params: noise octaves %d not in [0, 16]", p->noise.octaves);
+    CG_CHECK(std::isfinite(p->noise.frequency) && std::isfinite(p->noise.lacunarity) &&
+                 std::isfinite(p->noise.gain) && p->noise.gain > 0.f,
+             CG_ERR_INVALID_ARGUMENT, "render params: noise values must be finite, gain > 0");
+    for (int a = 0; a < 3; ++a)
+        CG_CHECK(std::isfinite(p->sun_color[a]), CG_ERR_INVALID_ARGUMENT,
+                 "render params: non-finite sun colour");
+    return CG_OK;
+}
+
+static TraceParams trace_params_of(const cg_render_params* p, const float sun_dir[3]) {
+    TraceParams tp;
+    tp.view_steps = p->view_steps;
+    tp.sun_steps = p->sun_steps;
+    tp.cone_mode = p->cone_mode;
+    tp.tan_half = (float)std::tan((double)p->cone_half_angle);
+    tp.h0 = p->cone_initial_height;
+    tp.rmin = p->cone_min_radius;
+    tp.lod_offset = p->lod_offset;
+    tp.down_scaling = p->down_scaling;
+    tp.sigma = p->density_scale;
+    tp.ambient = p->ambient;
+    tp.cutoff = p->transmittance_cutoff;
+    for (int a = 0; a < 3; ++a) tp.sun_color[a] = p->sun_color[a];
+    double sx = sun_dir[0], sy = sun_dir[1], sz = sun_dir[2];
+    double sn = std::sqrt(sx * sx + sy * sy + sz * sz);
+    tp.sun[0] = (float)(sx / sn);
+    tp.sun[1] = (float)(sy / sn);
+    tp.sun[2] = (float)(sz / sn);
+    tp.noise_seed = p->noise.seed;
+    tp.noise_octaves = p->noise.octaves;
+    tp.noise_freq = p->noise.frequency;
+    tp.noise_lac = p->noise.lacunarity;
+    tp.noise_gain = p->noise.gain;
+    double norm = 0.0, amp = 1.0;
+    for (int k = 0; k < p->noise.octaves; ++k) {
+        norm += amp;
+        amp *= (double)p->noise.gain;
+    }
+    tp.noise_inv_norm = norm > 0.0 ? (float)(1.0 / norm) : 1.0f;
+    return tp;
+}
+
+static cg_status camera_of(const cg_camera* c, CamDesc& cam) {
+    for (int a = 0; a < 3; ++a)
+        CG_CHECK(std::isfinite(c->eye[a]) && std::isfinite(c->target[a]) &&
+                     std::isfinite(c->up[a]),
+                 CG_ERR_INVALID_ARGUMENT, "camera: non-finite vector");
+    CG_CHECK(c->width >= 1 && c->height >= 1 && c->width <= 16384 && c->height <= 16384,
+             CG_ERR_OUT_OF_RANGE, "camera: image %dx%d not in [1, 16384]^2", c->width,
+             c->height);
+    CG_CHECK(std::isfinite(c->fov_y_degrees) && c->fov_y_degrees > 0.f &&
+                 c->fov_y_degrees < 180.f,
+             CG_ERR_OUT_OF_RANGE, "camera: fov_y_degrees not in (0, 180)");
+    double f[3], s[3], u[3];
+    for (int a = 0; a < 3; ++a) f[a] = (double)c->target[a] - (double)c->eye[a];
+    double fn = std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+    CG_CHECK(fn > 0.0, CG_ERR_INVALID_ARGUMENT, "camera: eye equals target");
+    for (double& x : f) x /= fn;
+    double up[3] = {c->up[0], c->up[1], c->up[2]};
+    s[0] = f[1] * up[2] - up[1] * f[2];
+    s[1] = f[2] * up[0] - up[2] * f[0];
+    s[2] = f[0] * up[1] - up[0] * f[1];
+    double sn = std::sqrt(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
+    CG_CHECK(sn > 1e-12, CG_ERR_INVALID_ARGUMENT, "camera: up is parallel to the view direction");
+    for (double& x : s) x /= sn;
+    u[0] = s[1] * f[2] - f[1] * s[2];
+    u[1] = s[2] * f[0] - f[2] * s[0];
+    u[2] = s[0] * f[1] - f[0] * s[1];
+    for (int a = 0; a < 3; ++a) {
+        cam.eye[a] = c->eye[a];
+        cam.f[a] = (float)f[a];
+        cam.s[a] = (float)s[a];
+        cam.u[a] = (float)u[a];
+    }
+    cam.tanh = (float)std::tan((double)c->fov_y_degrees * 3.14159265358979323846 / 360.0);
+    cam.aspect = (float)c->width / (float)c->height;
+    cam.W = c->width;
+    cam.H = c->height;
+    return CG_OK;
+}
+
+extern "C" cg_status cg_render(cg_context* ctx, const cg_volume* v, const cg_camera* cam,
+                               const cg_render_params* params, float* rgba_out,
+                               int out_on_device, void* stream) {
+    CG_CHECK(ctx && v && cam && params && rgba_out, CG_ERR_INVALID_ARGUMENT,
+             "cg_render: null pointer");
+    CG_CHECK(v->ctx == ctx, CG_ERR_INVALID_ARGUMENT, "cg_render: volume of another context");
+    CG_CHECK(v->voxelized, CG_ERR_NOT_READY, "cg_render: volume has not been voxelized");
+    cg_status st = check_params(params);
+    if (st != CG_OK) return st;
+    CG_CHECK(!params->use_mlp, CG_ERR_UNSUPPORTED, "cg_render: MLP surrogate not loaded");
+    CamDesc cd;
+    st = camera_of(cam, cd);
+    if (st != CG_OK) return st;
+    CG_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = pick(ctx, stream);
+    const size_t pixels = (size_t)cam->width * cam->height;
+    float4* out = reinterpret_cast<float4*>(rgba_out);
+    if (!out_on_device) {
+        CG_CUDA(ctx->image.ensure(pixels * 16));
+        out = ctx->image.as<float4>();
+    }
+    TraceParams tp = trace_params_of(params, v->sun_dir);
+    CG_LAUNCH(ctx, launch_trace_fused(desc_of(v), cd, tp, out, nullptr, s));
+    if (!out_on_device) {
+        CG_CUDA(cudaMemcpyAsync(rgba_out, out, pixels * 16, cudaMemcpyDeviceToHost, s));
+        CG_CUDA(cudaStreamSynchronize(s));
+    }
+    return CG_OK;
+}
+
+extern "C" cg_status cg_render_stats(cg_context* ctx, const cg_volume* v, const cg_camera* cam,
+                                     const cg_render_params* params, uint64_t counts[4]) {
+    CG_CHECK(ctx && v && cam && params && counts, CG_ERR_INVALID_ARGUMENT,
+             "cg_render_stats: null pointer");
+    CG_CHECK(v->ctx == ctx, CG_ERR_INVALID_ARGUMENT, "cg_render_stats: volume of another context");
+    CG_CHECK(v->voxelized, CG_ERR_NOT_READY, "cg_render_stats: volume has not been voxelized");
+    cg_status st = check_params(params);
+    if (st != CG_OK) return st;
+    CG_CHECK(!params->use_mlp, CG_ERR_UNSUPPORTED, "cg_render_stats: MLP surrogate not loaded");
+    CamDesc cd;
+    st = camera_of(cam, cd);
+    if (st != CG_OK) return st;
+    CG_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    const size_t pixels = (size_t)cam->width * cam->height;
+    CG_CUDA(ctx->image.ensure(pixels * 16));
+    DevBuf cnt;
+    CG_CUDA(cnt.ensure(64));
+    cudaError_t e = cudaMemsetAsync(cnt.p, 0, 64, s);
+    TraceParams tp = trace_params_of(params, v->sun_dir);
+    if (e == cudaSuccess)
+        e = launch_trace_fused(desc_of(v), cd, tp, ctx->image.as<float4>(),
+                               cnt.as<unsigned long long>(), s);
+    unsigned long long h[4] = {0, 0, 0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, cnt.p, 32, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cnt.release();
+    if (e != cudaSuccess) return fail(CG_ERR_CUDA, "cg_render_stats: %s", cudaGetErrorString(e));
+    ctx->launches++;
+    for (int i = 0; i < 4; ++i) counts[i] = h[i];
+    return CG_OK;
+}
+
+extern "C" cg_status cg_trace_cones(const cg_volume* v, const float* positions, int n,
+                                    const float direction[3], const cg_render_params* params,
+                                    float* out, int on_device, void* stream) {
+    CG_CHECK(v && direction && params && (n == 0 || (positions && out)),
+             CG_ERR_INVALID_ARGUMENT, "cg_trace_cones: null pointer");
+    CG_CHECK(n >= 0, CG_ERR_OUT_OF_RANGE, "cg_trace_cones: n < 0");
+    CG_CHECK(v->voxelized, CG_ERR_NOT_READY, "cg_trace_cones: volume has not been voxelized");
+    cg_status st = check_params(params);
+    if (st != CG_OK) return st;
+    double dn = std::sqrt((double)direction[0] * direction[0] + (double)direction[1] * direction[1] +
+                          (double)direction[2] * direction[2]);
+    CG_CHECK(std::isfinite(dn) && dn > 0.0, CG_ERR_INVALID_ARGUMENT,
+             "cg_trace_cones: direction must be finite and non-zero");
+    if (n == 0) return CG_OK;
+    cg_context* ctx = v->ctx;
+    CG_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = pick(ctx, stream);
+    TraceParams tp = trace_params_of(params, direction);
+    const float* dpos = positions;
+    float* dout = out;
+    DevBuf tmp;
+    if (!on_device) {
+        CG_CUDA(tmp.ensure((size_t)n * 16));
+        float* base = tmp.as<float>();
+        CG_CUDA(cudaMemcpyAsync(base, positions, (size_t)n * 12, cudaMemcpyHostToDevice, s));
+        dpos = base;
+        dout = base + (size_t)n * 3;
+    }
+    cudaError_t e = launch_trace_cones(desc_of(v), tp, dpos, n, dout, s);
+    if (e != cudaSuccess) {
+        tmp.release();
+        return fail(CG_ERR_CUDA, "launch_trace_cones: %s", cudaGetErrorString(e));
+    }
+    ctx->launches++;
+    if (!on_device) {
+        e = cudaMemcpyAsync(out, dout, (size_t)n * 4, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        tmp.release();
+        if (e != cudaSuccess) return fail(CG_ERR_CUDA, "cg_trace_cones: %s", cudaGetErrorString(e));
+    }
+    return CG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// readback
+// ---------------------------------------------------------------------------
+extern "C" cg_status cg_volume_get_info(const cg_volume* v, cg_volume_info* info) {
+    CG_CHECK(v && info, CG_ERR_INVALID_ARGUMENT, "cg_volume_get_info: null pointer");
+    memset(info, 0, sizeof(*info));
+    info->dimension = v->D;
+    info->mips = v->L;
+    info->format = v->fmt;
+    info->board_count = v->n;
+    for (int a = 0; a < 3; ++a) {
+        info->world_min[a] = v->wmin[a];
+        info->world_max[a] = v->wmax[a];
+    }
+    for (int l = 0; l < 16; ++l) {
+        info->level_dim[l] = l < v->L ? v->dims[l] : 0;
+        info->level_offset[l] = v->offs[l];
+    }
+    info->bytes_per_voxel = v->fmt == CG_FORMAT_RGBA32F ? 16 : 4;
+    info->pyramid_bytes = v->total * info->bytes_per_voxel;
+    return CG_OK;
+}
+
+static cg_status sync_volume(const cg_volume* v) {
+    CG_CUDA(cudaSetDevice(v->ctx->device));
+    CG_CUDA(cudaStreamSynchronize(v->ctx->stream));
+    return CG_OK;
+}
+
+extern "C" cg_status cg_volume_read_level(const cg_volume* v, int level, void* dst,
+                                          size_t dst_bytes) {
+    CG_CHECK(v && dst, CG_ERR_INVALID_ARGUMENT, "cg_volume_read_level: null pointer");
+    CG_CHECK(level >= 0 && level < v->L, CG_ERR_OUT_OF_RANGE,
+             "cg_volume_read_level: level %d not in [0, %d)", level, v->L);
+    const size_t bpv = v->fmt == CG_FORMAT_RGBA32F ? 16 : 4;
+    const size_t n = (size_t)v->dims[level] * v->dims[level] * v->dims[level];
+    CG_CHECK(dst_bytes >= n * bpv, CG_ERR_OUT_OF_RANGE,
+             "cg_volume_read_level: buffer %zu B < %zu B", dst_bytes, n * bpv);
+    cg_status st = sync_volume(v);
+    if (st != CG_OK) return st;
+    CG_CUDA(cudaMemcpy(dst, reinterpret_cast<const char*>(v->pyr.p) + v->offs[level] * bpv,
+                       n * bpv, cudaMemcpyDeviceToHost));
+    return CG_OK;
+}
+
+extern "C" cg_status cg_volume_read_coverage(const cg_volume* v, uint32_t* count,
+                                             uint32_t* density_q16) {
+    CG_CHECK(v && count && density_q16, CG_ERR_INVALID_ARGUMENT,
+             "cg_volume_read_coverage: null pointer");
+    CG_CHECK(v->voxelized, CG_ERR_NOT_READY, "cg_volume_read_coverage: not voxelized");
+    cg_status st = sync_volume(v);
+    if (st != CG_OK) return st;
+    const size_t n0 = (size_t)v->D * v->D * v->D;
+    CG_CUDA(cudaMemcpy(count, v->count.p, n0 * 4, cudaMemcpyDeviceToHost));
+    CG_CUDA(cudaMemcpy(density_q16, v->dq.p, n0 * 4, cudaMemcpyDeviceToHost));
+    return CG_OK;
+}
+
+extern "C" cg_status cg_volume_read_sun_map(const cg_volume* v, uint64_t* keys, float* positions) {
+    CG_CHECK(v && keys && positions, CG_ERR_INVALID_ARGUMENT,
+             "cg_volume_read_sun_map: null pointer");
+    CG_CHECK(v->voxelized, CG_ERR_NOT_READY, "cg_volume_read_sun_map: not voxelized");
+    cg_status st = sync_volume(v);
+    if (st != CG_OK) return st;
+    const size_t t = (size_t)v->mapW * v->mapH;
+    CG_CUDA(cudaMemcpy(keys, v->keys.p, t * 8, cudaMemcpyDeviceToHost));
+    CG_CUDA(cudaMemcpy(positions, v->posmap.p, t * 16, cudaMemcpyDeviceToHost));
+    return CG_OK;
+}
+
+extern "C" cg_status cg_volume_read_highlight(const cg_volume* v, uint8_t* mask) {
+    CG_CHECK(v && mask, CG_ERR_INVALID_ARGUMENT, "cg_volume_read_highlight: null pointer");
+    CG_CHECK(v->voxelized, CG_ERR_NOT_READY, "cg_volume_read_highlight: not voxelized");
+    cg_status st = sync_volume(v);
+    if (st != CG_OK) return st;
+    CG_CUDA(cudaMemcpy(mask, v->mask.p, (size_t)v->D * v->D * v->D, cudaMemcpyDeviceToHost));
+    return CG_OK;
+}
+
+extern "C" cg_status cg_volume_active_voxels(const cg_volume* v, uint64_t* active) {
+    CG_CHECK(v && active, CG_ERR_INVALID_ARGUMENT, "cg_volume_active_voxels: null pointer");
+    CG_CHECK(v->voxelized, CG_ERR_NOT_READY, "cg_volume_active_voxels: not voxelized");
+    CG_CUDA(cudaSetDevice(v->ctx->device));
+    cudaStream_t s = v->ctx->stream;
+    unsigned long long* d = const_cast<cg_volume*>(v)->scratch.as<unsigned long long>();
+    CG_CUDA(cudaMemsetAsync(d, 0, 8, s));
+    CG_LAUNCH(v->ctx, launch_count_active(v->count.as<uint32_t>(), v->mask.as<uint8_t>(),
+                                          (size_t)v->D * v->D * v->D, d, s));
+    unsigned long long h = 0;
+    CG_CUDA(cudaMemcpyAsync(&h, d, 8, cudaMemcpyDeviceToHost, s));
+    CG_CUDA(cudaStreamSynchronize(s));
+    *active = h;
+    return CG_OK;
+}

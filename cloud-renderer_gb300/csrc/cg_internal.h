@@ -1,0 +1,88 @@
+// cg_internal.h -- structures shared by the host library and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define CG_MAX_LEVELS 16
+#define CG_Q20 1048576LL
+#define CG_HALF_Q20 524288LL
+#define CG_KEY_EMPTY 0xFFFFFFFFFFFFFFFFULL
+#define CG_BRICK 8           // splat brick edge (voxels)
+#define CG_FUSED_MIPS 3      // levels produced inside the splat kernel
+#define CG_SPLAT_CHUNK 256   // boards staged in shared memory per pass
+
+// Sun-view frame: lookAt basis + ortho window (Sun::update, Sun.hpp:26-43).
+struct SunFrame {
+    float eye[3], right[3], up[3], fwd[3], t[3];
+    float lo, hi, near_z, clip;
+    int W, H;
+};
+
+// Pyramid description passed by value to kernels.
+struct VolDesc {
+    int D, L, fmt;
+    int dims[CG_MAX_LEVELS];
+    long long offs[CG_MAX_LEVELS];  // voxels
+    float wmin[3], range[3];
+    const void* pyr;                // float4* (RGBA32F) or uint32_t* (BF16_FP16)
+};
+
+// Camera in FP32 for the trace kernels.
+struct CamDesc {
+    float eye[3], f[3], s[3], u[3];
+    float tanh, aspect;
+    int W, H;
+};
+
+// Render parameters resolved for the device.
+struct TraceParams {
+    int view_steps, sun_steps, cone_mode;
+    float tan_half, h0, rmin, lod_offset, down_scaling;
+    float sigma, ambient, cutoff;
+    float sun_color[3];
+    float sun[3];   // unit direction toward the sun
+    uint32_t noise_seed;
+    int noise_octaves;
+    float noise_freq, noise_lac, noise_gain, noise_inv_norm;
+};
+
+// Per-board device arrays (SoA).
+struct BoardsDev {
+    int n;
+    const float4* cwr;      // world centre xyz, radius w
+    const int4* q;          // Q20 voxel-space centre xyz, radius w (coverage)
+    const uint64_t* thr;    // squared-radius threshold, Q40
+    const uint32_t* dq;     // Q16.16 density
+    const uint8_t* culled;  // 1 = no coverage contribution
+};
+
+struct Bins {
+    int nbx, nby, nbz, nbricks;
+    uint32_t* count;   // nbricks
+    uint32_t* offset;  // nbricks + 1
+    uint32_t* cursor;  // nbricks
+    uint32_t* list;    // pairs
+};
+
+// ---- launchers (return cudaGetLastError of the launch) -------------------
+cudaError_t launch_bin_count(const BoardsDev& b, int D, Bins bins, cudaStream_t st);
+cudaError_t launch_bin_scan(Bins bins, cudaStream_t st);
+cudaError_t launch_bin_fill(const BoardsDev& b, int D, Bins bins, cudaStream_t st);
+cudaError_t launch_sunmap(const BoardsDev& b, const SunFrame& fr, uint64_t* keys,
+                          cudaStream_t st);
+cudaError_t launch_highlight(const BoardsDev& b, const SunFrame& fr, const uint64_t* keys,
+                             float4* posmap, int D, const float wmin[3],
+                             const float range[3], float offset, uint8_t* mask,
+                             cudaStream_t st);
+cudaError_t launch_splat(const BoardsDev& b, Bins bins, const uint8_t* mask, VolDesc vd,
+                         void* pyr, uint32_t* count, uint32_t* dq, int fused_levels,
+                         cudaStream_t st);
+cudaError_t launch_mip_level(VolDesc vd, void* pyr, int l, cudaStream_t st);
+cudaError_t launch_count_active(const uint32_t* count, const uint8_t* mask, size_t n,
+                                unsigned long long* out, cudaStream_t st);
+
+cudaError_t launch_trace_fused(VolDesc vd, CamDesc cam, TraceParams tp, float4* out,
+                               unsigned long long* stats, cudaStream_t st);
+cudaError_t launch_trace_cones(VolDesc vd, TraceParams tp, const float* pos, int n,
+                               float* out, cudaStream_t st);

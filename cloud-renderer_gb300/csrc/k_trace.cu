@@ -1,0 +1,179 @@
+// k_trace.cu -- per-pixel view march with the exact sun cone (one thread per
+// pixel), and the traceCone evaluator.
+#include "cg_internal.h"
+#include "cg_sample.cuh"
+
+namespace {
+
+// 16x16 pixel tile per 256-thread CTA; each warp owns an 8x4 sub-tile so that
+// its rays stay spatially coherent.
+__device__ __forceinline__ void tile_pixel(int& px, int& py) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    px = blockIdx.x * 16 + (w & 1) * 8 + (lane & 7);
+    py = blockIdx.y * 16 + (w >> 1) * 4 + (lane >> 3);
+}
+
+// Ray through the pixel centre and its slab interval against the world box.
+__device__ __forceinline__ bool pixel_ray(const CamDesc& cam, const VolDesc& vd, int px, int py,
+                                          float3& d, float& tin, float& tout) {
+    float ndx = (2.f * ((float)px + 0.5f) / (float)cam.W - 1.f) * cam.tanh * cam.aspect;
+    float ndy = (1.f - 2.f * ((float)py + 0.5f) / (float)cam.H) * cam.tanh;
+    float dx = cam.f[0] + ndx * cam.s[0] + ndy * cam.u[0];
+    float dy = cam.f[1] + ndx * cam.s[1] + ndy * cam.u[1];
+    float dz = cam.f[2] + ndx * cam.s[2] + ndy * cam.u[2];
+    float inv = rsqrtf(dx * dx + dy * dy + dz * dz);
+    d = make_float3(dx * inv, dy * inv, dz * inv);
+    float dd[3] = {d.x, d.y, d.z};
+    float tmin = -1e30f, tmax = 1e30f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float lo = vd.wmin[a], hi = vd.wmin[a] + vd.range[a];
+        if (dd[a] == 0.f) {
+            if (cam.eye[a] < lo || cam.eye[a] > hi) return false;
+            continue;
+        }
+        float iv = 1.f / dd[a];
+        float t0 = (lo - cam.eye[a]) * iv, t1 = (hi - cam.eye[a]) * iv;
+        tmin = fmaxf(tmin, fminf(t0, t1));
+        tmax = fminf(tmax, fmaxf(t0, t1));
+    }
+    tin = fmaxf(tmin, 0.f);
+    tout = tmax;
+    return tout > tin;
+}
+
+// Counts (STATS only): [0] view samples evaluated, [1] sun cones, [2] sun-cone
+// samples, [3] pixels whose ray met the box.  The counting variant is used
+// once, untimed, to derive the algorithmic bytes of a frame.
+template <bool STATS>
+__device__ __forceinline__ void bump(unsigned long long* stats, int i, unsigned v) {
+    if (STATS && v) atomicAdd(stats + i, (unsigned long long)v);
+}
+
+template <int FMT, bool STATS>
+__global__ void __launch_bounds__(256) k_trace_fused(VolDesc vd, CamDesc cam, TraceParams tp,
+                                                     ConeSchedule cs, float4* out,
+                                                     unsigned long long* stats) {
+    int px, py;
+    tile_pixel(px, py);
+    if (px >= cam.W || py >= cam.H) return;
+    float3 d;
+    float tin, tout;
+    float4 res = make_float4(0.f, 0.f, 0.f, 0.f);
+    unsigned n_view = 0, n_cone = 0, n_sun = 0, n_hit = 0;
+    if (pixel_ray(cam, vd, px, py, d, tin, tout)) {
+        n_hit = 1;
+        const int Nv = tp.view_steps;
+        const float dt = (tout - tin) / (float)Nv;
+        const float D = (float)vd.D;
+        const float vsx = D / vd.range[0], vsy = D / vd.range[1], vsz = D / vd.range[2];
+        const float pixk = cam.tanh / (float)cam.H * vsx;
+        float T = 1.f, C = 0.f, Cc = 0.f;
+        for (int k = 0; k < Nv; ++k) {
+            float t = tin + ((float)k + 0.5f) * dt;
+            float p0 = cam.eye[0] + t * d.x, p1 = cam.eye[1] + t * d.y, p2 = cam.eye[2] + t * d.z;
+            float v0 = (p0 - vd.wmin[0]) * vsx, v1 = (p1 - vd.wmin[1]) * vsy,
+                  v2 = (p2 - vd.wmin[2]) * vsz;
+            float lod = log2f(fmaxf(1.f, 2.f * t * pixk));
+            float2 rg = cgs::quad<FMT, true, true>(vd, v0, v1, v2, lod);
+            n_view++;
+            if (!(rg.x > 0.f)) continue;
+            float rho = rg.x * cgs::fbm(tp, p0, p1, p2);
+            if (!(rho > 0.f)) continue;
+            float alpha = 1.f - expf(-tp.sigma * rho * dt);
+            float tau = cgs::sun_cone<FMT>(vd, cs, v0, v1, v2, tp.sun[0], tp.sun[1], tp.sun[2]);
+            if (STATS) {
+                n_cone++;
+                n_sun += cgs::cone_samples(vd, cs, v0, v1, v2, tp.sun[0], tp.sun[1], tp.sun[2]);
+            }
+            float Ts = expf(-tp.sigma * tau);
+            float L = Ts * (tp.ambient + (1.f - tp.ambient) * rg.y);
+            cgs::neumaier(C, Cc, T * alpha * L);
+            T *= 1.f - alpha;
+            if (T < tp.cutoff) break;
+        }
+        C += Cc;
+        res = make_float4(C * tp.sun_color[0], C * tp.sun_color[1], C * tp.sun_color[2], 1.f - T);
+    }
+    out[(size_t)py * cam.W + px] = res;
+    bump<STATS>(stats, 0, n_view);
+    bump<STATS>(stats, 1, n_cone);
+    bump<STATS>(stats, 2, n_sun);
+    bump<STATS>(stats, 3, n_hit);
+}
+
+template <int FMT>
+__global__ void k_trace_cones(VolDesc vd, TraceParams tp, ConeSchedule cs, const float* pos,
+                              int n, float* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = cgs::sun_cone<FMT>(vd, cs, pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], tp.sun[0],
+                                tp.sun[1], tp.sun[2]);
+}
+
+}  // namespace
+
+// Cone schedule in FP64 on the host (see ConeSchedule).
+static ConeSchedule make_schedule(const VolDesc& vd, const TraceParams& tp) {
+    ConeSchedule cs;
+    cs.steps = tp.sun_steps;
+    cs.mode = tp.cone_mode;
+    cs.edge = (float)vd.D / (float)vd.dims[vd.L - 1];
+    const double vw = (double)vd.range[0] / (double)vd.D;
+    double h = tp.h0;
+    const double maxl = (double)(vd.L - 1);
+    for (int i = 0; i < tp.sun_steps && i < CG_MAX_SUN_STEPS; ++i) {
+        double r, lod, w;
+        if (tp.cone_mode == 1) {
+            r = h * (double)tp.tan_half;
+            double rr = 2.0 * r > 1.0 ? 2.0 * r : 1.0;
+            lod = log2(rr) + (double)tp.lod_offset;
+            w = (double)(i + 1) / ((double)tp.sun_steps * (double)tp.down_scaling);
+        } else {
+            r = h * (double)tp.tan_half;
+            if (r < (double)tp.rmin) r = (double)tp.rmin;
+            double rr = 2.0 * r > 1.0 ? 2.0 * r : 1.0;
+            lod = log2(rr) + (double)tp.lod_offset;
+            w = r * vw;
+        }
+        if (!(lod > 0.0)) lod = 0.0;
+        if (lod > maxl) lod = maxl;
+        int l0 = (int)floor(lod);
+        cs.h[i] = (float)h;
+        cs.w[i] = (float)w;
+        cs.l0[i] = (unsigned char)l0;
+        cs.frac[i] = (float)(lod - (double)l0);
+        h += r;
+    }
+    return cs;
+}
+
+cudaError_t launch_trace_fused(VolDesc vd, CamDesc cam, TraceParams tp, float4* out,
+                               unsigned long long* stats, cudaStream_t st) {
+    ConeSchedule cs = make_schedule(vd, tp);
+    dim3 grd((cam.W + 15) / 16, (cam.H + 15) / 16);
+    if (stats) {
+        if (vd.fmt == 0)
+            k_trace_fused<0, true><<<grd, 256, 0, st>>>(vd, cam, tp, cs, out, stats);
+        else
+            k_trace_fused<1, true><<<grd, 256, 0, st>>>(vd, cam, tp, cs, out, stats);
+    } else {
+        if (vd.fmt == 0)
+            k_trace_fused<0, false><<<grd, 256, 0, st>>>(vd, cam, tp, cs, out, nullptr);
+        else
+            k_trace_fused<1, false><<<grd, 256, 0, st>>>(vd, cam, tp, cs, out, nullptr);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace_cones(VolDesc vd, TraceParams tp, const float* pos, int n, float* out,
+                               cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    ConeSchedule cs = make_schedule(vd, tp);
+    int blocks = (n + 127) / 128;
+    if (vd.fmt == 0)
+        k_trace_cones<0><<<blocks, 128, 0, st>>>(vd, tp, cs, pos, n, out);
+    else
+        k_trace_cones<1><<<blocks, 128, 0, st>>>(vd, tp, cs, pos, n, out);
+    return cudaGetLastError();
+}

@@ -1,0 +1,487 @@
+// k_voxelize.cu -- sun-view map, highlight stores, brick-binned coverage splat
+// and the mip pyramid.  Compiled with -fmad=false: every FP32 operation that
+// decides an index (sun-view depth keys, highlight voxel indices) is written
+// with explicitly rounded intrinsics in the same order as the CPU oracle, so
+// winners, indices and integer coverage match it bit for bit.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "cg_internal.h"
+
+namespace {
+
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float fsqrt(float a) { return __fsqrt_rn(a); }
+
+__device__ __forceinline__ long long floor_div(long long a, long long b) {
+    long long q = a / b;
+    if ((a % b != 0) && ((a < 0) != (b < 0))) q--;
+    return q;
+}
+
+// Voxels whose centre (2i+1)*2^19 lies in [q-rq, q+rq], clamped to [0, D-1].
+__device__ __forceinline__ bool axis_range(int q, int rq, int D, int& lo, int& hi) {
+    long long l = floor_div((long long)q - rq - CG_HALF_Q20 + CG_Q20 - 1, CG_Q20);
+    long long h = floor_div((long long)q + rq - CG_HALF_Q20, CG_Q20);
+    if (l < 0) l = 0;
+    if (h > D - 1) h = D - 1;
+    if (l > h) return false;
+    lo = (int)l;
+    hi = (int)h;
+    return true;
+}
+
+// ---- brick binning ---------------------------------------------------------
+
+__global__ void k_bin_count(BoardsDev b, int D, Bins bins) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.n || b.culled[i]) return;
+    int4 q = b.q[i];
+    int xl, xh, yl, yh, zl, zh;
+    if (!axis_range(q.x, q.w, D, xl, xh) || !axis_range(q.y, q.w, D, yl, yh) ||
+        !axis_range(q.z, q.w, D, zl, zh))
+        return;
+    for (int bz = zl / CG_BRICK; bz <= zh / CG_BRICK; ++bz)
+        for (int by = yl / CG_BRICK; by <= yh / CG_BRICK; ++by)
+            for (int bx = xl / CG_BRICK; bx <= xh / CG_BRICK; ++bx)
+                atomicAdd(&bins.count[(bz * bins.nby + by) * bins.nbx + bx], 1u);
+}
+
+// Exclusive scan of the brick counts in one CTA (1024 threads, each owning a
+// contiguous chunk).  Also seeds the fill cursors.
+__global__ void __launch_bounds__(1024) k_bin_scan(Bins bins) {
+    __shared__ uint32_t warp_sums[32];
+    const int n = bins.nbricks;
+    const int tid = threadIdx.x;
+    const int per = (n + 1023) / 1024;
+    const int beg = min(n, tid * per), end = min(n, beg + per);
+    uint32_t s = 0;
+    for (int i = beg; i < end; ++i) s += bins.count[i];
+    // block exclusive scan of s
+    const int lane = tid & 31, wid = tid >> 5;
+    uint32_t x = s;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t w = warp_sums[lane];
+        uint32_t z = w;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, z, o);
+            if (lane >= o) z += y;
+        }
+        warp_sums[lane] = z - w;
+    }
+    __syncthreads();
+    uint32_t run = warp_sums[wid] + x - s;
+    for (int i = beg; i < end; ++i) {
+        bins.offset[i] = run;
+        bins.cursor[i] = run;
+        run += bins.count[i];
+    }
+    if (tid == 1023) bins.offset[n] = warp_sums[wid] + x;
+}
+
+__global__ void k_bin_fill(BoardsDev b, int D, Bins bins) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.n || b.culled[i]) return;
+    int4 q = b.q[i];
+    int xl, xh, yl, yh, zl, zh;
+    if (!axis_range(q.x, q.w, D, xl, xh) || !axis_range(q.y, q.w, D, yl, yh) ||
+        !axis_range(q.z, q.w, D, zl, zh))
+        return;
+    for (int bz = zl / CG_BRICK; bz <= zh / CG_BRICK; ++bz)
+        for (int by = yl / CG_BRICK; by <= yh / CG_BRICK; ++by)
+            for (int bx = xl / CG_BRICK; bx <= xh / CG_BRICK; ++bx) {
+                uint32_t slot = atomicAdd(&bins.cursor[(bz * bins.nby + by) * bins.nbx + bx], 1u);
+                bins.list[slot] = (uint32_t)i;
+            }
+}
+
+// ---- sun-view nearest-surface map (first_voxelize.glsl:39-64) --------------
+
+__device__ __forceinline__ float dot3(const float a[3], float x, float y, float z) {
+    return fadd(fadd(fmul(a[0], x), fmul(a[1], y)), fmul(a[2], z));
+}
+
+// Board centre in sun view space: lookAt rows s, u, -f plus translation.
+__device__ __forceinline__ float3 sun_view_of(const SunFrame& fr, float4 c) {
+    float nf[3] = {-fr.fwd[0], -fr.fwd[1], -fr.fwd[2]};
+    return make_float3(fadd(dot3(fr.right, c.x, c.y, c.z), fr.t[0]),
+                       fadd(dot3(fr.up, c.x, c.y, c.z), fr.t[1]),
+                       fadd(dot3(nf, c.x, c.y, c.z), fr.t[2]));
+}
+
+__device__ __forceinline__ float texel_coord(float lo, float hi, int i, int n) {
+    float a = fadd(__int2float_rn(i), 0.5f);
+    float b = fdiv(a, __int2float_rn(n));
+    return fadd(lo, fmul(b, fsub(hi, lo)));
+}
+
+// Spherical profile, discard below 0.01, surface point pushed toward the sun,
+// depth from the near-plane point (first_voxelize.glsl:43-63).
+__device__ __forceinline__ bool sun_fragment(float xv, float yv, float3 cv, float r,
+                                             float near_z, float& zs, float& depth) {
+    float dx = fsub(xv, cv.x);
+    float dy = fsub(yv, cv.y);
+    float d2 = fadd(fmul(dx, dx), fmul(dy, dy));
+    float dist = fsqrt(d2);
+    float q = fdiv(dist, r);
+    float t = fsub(1.0f, fmul(q, q));
+    float prof = fsqrt(t > 0.0f ? t : 0.0f);
+    if (!(prof >= 0.01f)) return false;
+    zs = fadd(cv.z, fmul(r, prof));
+    float dz = fadd(zs, near_z);
+    float dep2 = fadd(fadd(fmul(xv, xv), fmul(yv, yv)), fmul(dz, dz));
+    depth = fsqrt(dep2);
+    return true;
+}
+
+__device__ __forceinline__ void texel_range(float lo, float hi, float c, float r, int n,
+                                            int& a, int& b) {
+    float span = hi - lo;
+    float l = (c - r - lo) / span * (float)n - 0.5f;
+    float h = (c + r - lo) / span * (float)n - 0.5f;
+    // conservative: one texel of margin each side; NaN/huge values clamp
+    float fa = floorf(l) - 1.0f, fb = ceilf(h) + 1.0f;
+    fa = fmaxf(fa, 0.0f);
+    fb = fminf(fb, (float)(n - 1));
+    if (!(fa <= fb)) { a = 1; b = 0; return; }
+    a = (int)fa;
+    b = (int)fb;
+}
+
+// One CTA per board; threads sweep the board's texel box.
+__global__ void __launch_bounds__(256) k_sunmap(BoardsDev b, SunFrame fr,
+                                                unsigned long long* keys) {
+    const int i = blockIdx.x;
+    if (i >= b.n) return;
+    float4 c = b.cwr[i];
+    float3 cv = sun_view_of(fr, c);
+    float r = c.w;
+    int ia, ib, ja, jb;
+    texel_range(fr.lo, fr.hi, cv.x, r, fr.W, ia, ib);
+    texel_range(fr.lo, fr.hi, cv.y, r, fr.H, ja, jb);
+    if (ia > ib || ja > jb) return;
+    const int nx = ib - ia + 1, ny = jb - ja + 1;
+    const int total = nx * ny;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        int ti = ia + t % nx, tj = ja + t / nx;
+        float xv = texel_coord(fr.lo, fr.hi, ti, fr.W);
+        float yv = texel_coord(fr.lo, fr.hi, tj, fr.H);
+        float zs, depth;
+        if (!sun_fragment(xv, yv, cv, r, fr.near_z, zs, depth)) continue;
+        unsigned long long key =
+            ((unsigned long long)__float_as_uint(depth) << 32) | (unsigned)i;
+        unsigned long long* k = keys + (size_t)tj * fr.W + ti;
+        // values only decrease, so a stale read can only make this test pass
+        if (key < *(volatile unsigned long long*)k) atomicMin(k, key);
+    }
+}
+
+// ---- highlight stores (second_voxelize.glsl:34-51) -------------------------
+
+struct HiParams {
+    float wmin[3], range[3];
+    float fD, offset;
+    int D;
+};
+
+__device__ __forceinline__ bool voxel_index(const HiParams& hp, float x, float y, float z,
+                                            int& o) {
+    float c[3] = {x, y, z};
+    int id[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float t = fdiv(fsub(c[a], hp.wmin[a]), hp.range[a]);
+        float v = fmul(hp.fD, t);
+        if (!(v > -1.0f && v < hp.fD)) return false;
+        id[a] = __float2int_rz(v);  // ivec3(): truncation toward zero
+    }
+    o = (id[2] * hp.D + id[1]) * hp.D + id[0];
+    return true;
+}
+
+__global__ void k_highlight(BoardsDev b, SunFrame fr, const unsigned long long* keys,
+                            float4* posmap, HiParams hp, uint8_t* mask) {
+    const int ti = blockIdx.x * blockDim.x + threadIdx.x;
+    const int tj = blockIdx.y * blockDim.y + threadIdx.y;
+    if (ti >= fr.W || tj >= fr.H) return;
+    const size_t idx = (size_t)tj * fr.W + ti;
+    unsigned long long key = keys[idx];
+    if (key == CG_KEY_EMPTY) {
+        posmap[idx] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    int bi = (int)(key & 0xFFFFFFFFull);
+    float4 c = b.cwr[bi];
+    float3 cv = sun_view_of(fr, c);
+    float xv = texel_coord(fr.lo, fr.hi, ti, fr.W);
+    float yv = texel_coord(fr.lo, fr.hi, tj, fr.H);
+    float zs = 0.f, depth = 0.f;
+    sun_fragment(xv, yv, cv, c.w, fr.near_z, zs, depth);
+    float p[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        p[a] = fadd(fadd(fadd(fmul(xv, fr.right[a]), fmul(yv, fr.up[a])), fmul(zs, -fr.fwd[a])),
+                    fr.eye[a]);
+    posmap[idx] = make_float4(p[0], p[1], p[2], 1.0f);
+    const float o = hp.offset;
+    int vi;
+    if (voxel_index(hp, p[0], p[1], p[2], vi)) mask[vi] = 1;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        float x = (k & 4) ? fsub(p[0], o) : fadd(p[0], o);
+        float y = (k & 2) ? fsub(p[1], o) : fadd(p[1], o);
+        float z = (k & 1) ? fsub(p[2], o) : fadd(p[2], o);
+        if (voxel_index(hp, x, y, z, vi)) mask[vi] = 1;
+    }
+}
+
+// ---- coverage splat + level 0 + fused mips ---------------------------------
+
+__device__ __forceinline__ uint32_t pack_bf16_fp16(float r, float g) {
+    __nv_bfloat16 rb = __float2bfloat16_rn(r);
+    __half gh = __float2half_rn(g);
+    return (uint32_t)__bfloat16_as_ushort(rb) | ((uint32_t)__half_as_ushort(gh) << 16);
+}
+
+__device__ __forceinline__ float4 unpack_bf16_fp16(uint32_t v) {
+    float r = __bfloat162float(__ushort_as_bfloat16((unsigned short)(v & 0xFFFFu)));
+    float g = __half2float(__ushort_as_half((unsigned short)(v >> 16)));
+    return make_float4(r, g, 0.f, 0.f);
+}
+
+__device__ __forceinline__ void store_voxel(const VolDesc& vd, void* pyr, int l, int x, int y,
+                                            int z, float4 v) {
+    const int N = vd.dims[l];
+    size_t idx = (size_t)vd.offs[l] + ((size_t)z * N + y) * N + x;
+    if (vd.fmt == 0)
+        reinterpret_cast<float4*>(pyr)[idx] = v;
+    else
+        reinterpret_cast<uint32_t*>(pyr)[idx] = pack_bf16_fp16(v.x, v.y);
+}
+
+__device__ __forceinline__ float4 load_voxel(const VolDesc& vd, const void* pyr, int l, int x,
+                                             int y, int z) {
+    const int N = vd.dims[l];
+    size_t idx = (size_t)vd.offs[l] + ((size_t)z * N + y) * N + x;
+    if (vd.fmt == 0) return reinterpret_cast<const float4*>(pyr)[idx];
+    return unpack_bf16_fp16(reinterpret_cast<const uint32_t*>(pyr)[idx]);
+}
+
+__device__ __forceinline__ float4 f4add(float4 a, float4 b) {
+    return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+}
+// 2x2x2 box mean in the oracle's order: ((c000+c100)+(c010+c110)) + ((c001+c101)+(c011+c111))
+__device__ __forceinline__ float4 box8(float4 c000, float4 c100, float4 c010, float4 c110,
+                                       float4 c001, float4 c101, float4 c011, float4 c111) {
+    float4 s = f4add(f4add(f4add(c000, c100), f4add(c010, c110)),
+                     f4add(f4add(c001, c101), f4add(c011, c111)));
+    return make_float4(s.x * 0.125f, s.y * 0.125f, s.z * 0.125f, s.w * 0.125f);
+}
+
+// One CTA per 8^3 brick, one thread per voxel.  Boards of the brick's bin are
+// staged through shared memory; each voxel tests its centre against each
+// board's ball on the Q20 grid (int64 squared distance) and sums count and
+// Q16.16 density.  Level 0 is assembled in registers and the next
+// `fused_levels` mip levels are reduced in shared memory.
+__global__ void __launch_bounds__(512) k_splat(BoardsDev b, Bins bins, const uint8_t* mask,
+                                               VolDesc vd, void* pyr, uint32_t* count,
+                                               uint32_t* dqout, int fused_levels) {
+    __shared__ int4 sq[CG_SPLAT_CHUNK];
+    __shared__ unsigned long long sthr[CG_SPLAT_CHUNK];
+    __shared__ uint32_t sdq[CG_SPLAT_CHUNK];
+    __shared__ float4 tile[CG_BRICK * CG_BRICK * CG_BRICK];
+    __shared__ float4 tile1[64];
+    __shared__ float4 tile2[8];
+
+    const int brick = blockIdx.x;
+    const int bx = brick % bins.nbx;
+    const int by = (brick / bins.nbx) % bins.nby;
+    const int bz = brick / (bins.nbx * bins.nby);
+    const int tid = threadIdx.x;
+    const int lx = tid & 7, ly = (tid >> 3) & 7, lz = tid >> 6;
+    const int D = vd.D;
+    const int x = bx * CG_BRICK + lx, y = by * CG_BRICK + ly, z = bz * CG_BRICK + lz;
+    const bool inside = (x < D && y < D && z < D);
+    const int vx = (2 * x + 1) * (int)CG_HALF_Q20;
+    const int vy = (2 * y + 1) * (int)CG_HALF_Q20;
+    const int vz = (2 * z + 1) * (int)CG_HALF_Q20;
+
+    const uint32_t beg = bins.offset[brick];
+    const uint32_t n = bins.offset[brick + 1] - beg;
+    uint32_t cnt = 0, dsum = 0;
+    for (uint32_t base = 0; base < n; base += CG_SPLAT_CHUNK) {
+        const uint32_t m = min((uint32_t)CG_SPLAT_CHUNK, n - base);
+        __syncthreads();
+        for (uint32_t t = tid; t < m; t += blockDim.x) {
+            uint32_t bi = bins.list[beg + base + t];
+            sq[t] = b.q[bi];
+            sthr[t] = b.thr[bi];
+            sdq[t] = b.dq[bi];
+        }
+        __syncthreads();
+        for (uint32_t k = 0; k < m; ++k) {
+            int4 q = sq[k];
+            int dx = vx - q.x, dy = vy - q.y, dz = vz - q.z;
+            unsigned long long d2 = (unsigned long long)((long long)dx * dx) +
+                                    (unsigned long long)((long long)dy * dy) +
+                                    (unsigned long long)((long long)dz * dz);
+            if (d2 <= sthr[k]) {
+                cnt += 1u;
+                dsum += sdq[k];
+            }
+        }
+    }
+    float4 v0 = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (inside) {
+        size_t i = ((size_t)z * D + y) * D + x;
+        uint8_t mk = mask[i];
+        count[i] = cnt;
+        dqout[i] = dsum;
+        v0.x = __uint2float_rn(dsum) * (1.0f / 65536.0f);
+        v0.y = mk ? 1.0f : 0.0f;
+        v0.z = __uint2float_rn(cnt);
+        v0.w = (cnt > 0u || mk) ? 1.0f : 0.0f;
+        store_voxel(vd, pyr, 0, x, y, z, v0);
+    }
+    if (fused_levels <= 0) return;
+    tile[tid] = v0;
+    __syncthreads();
+    // level 1: 4^3 parents
+    if (tid < 64) {
+        int px = tid & 3, py = (tid >> 2) & 3, pz = tid >> 4;
+#define T8(a, b2, c) tile[((2 * pz + (c)) * 8 + (2 * py + (b2))) * 8 + (2 * px + (a))]
+        float4 m1 = box8(T8(0, 0, 0), T8(1, 0, 0), T8(0, 1, 0), T8(1, 1, 0), T8(0, 0, 1),
+                         T8(1, 0, 1), T8(0, 1, 1), T8(1, 1, 1));
+#undef T8
+        int gx = bx * 4 + px, gy = by * 4 + py, gz = bz * 4 + pz;
+        if (gx < vd.dims[1] && gy < vd.dims[1] && gz < vd.dims[1])
+            store_voxel(vd, pyr, 1, gx, gy, gz, m1);
+        tile1[tid] = m1;
+    }
+    __syncthreads();
+    if (fused_levels < 2) return;
+    if (tid < 8) {
+        int px = tid & 1, py = (tid >> 1) & 1, pz = tid >> 2;
+#define T4(a, b2, c) tile1[((2 * pz + (c)) * 4 + (2 * py + (b2))) * 4 + (2 * px + (a))]
+        float4 m2 = box8(T4(0, 0, 0), T4(1, 0, 0), T4(0, 1, 0), T4(1, 1, 0), T4(0, 0, 1),
+                         T4(1, 0, 1), T4(0, 1, 1), T4(1, 1, 1));
+#undef T4
+        int gx = bx * 2 + px, gy = by * 2 + py, gz = bz * 2 + pz;
+        if (gx < vd.dims[2] && gy < vd.dims[2] && gz < vd.dims[2])
+            store_voxel(vd, pyr, 2, gx, gy, gz, m2);
+        tile2[tid] = m2;
+    }
+    __syncthreads();
+    if (fused_levels < 3) return;
+    if (tid == 0) {
+        float4 m3 = box8(tile2[0], tile2[1], tile2[2], tile2[3], tile2[4], tile2[5], tile2[6],
+                         tile2[7]);
+        if (bx < vd.dims[3] && by < vd.dims[3] && bz < vd.dims[3])
+            store_voxel(vd, pyr, 3, bx, by, bz, m3);
+    }
+}
+
+// Generic 2x2x2 reduction from level l to l+1 (one thread per parent).
+__global__ void k_mip_level(VolDesc vd, void* pyr, int l) {
+    const int Nc = vd.dims[l], Np = vd.dims[l + 1];
+    const long long total = (long long)Np * Np * Np;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    int x = (int)(i % Np), y = (int)((i / Np) % Np), z = (int)(i / ((long long)Np * Np));
+    int cx0 = min(2 * x, Nc - 1), cx1 = min(2 * x + 1, Nc - 1);
+    int cy0 = min(2 * y, Nc - 1), cy1 = min(2 * y + 1, Nc - 1);
+    int cz0 = min(2 * z, Nc - 1), cz1 = min(2 * z + 1, Nc - 1);
+    float4 m = box8(load_voxel(vd, pyr, l, cx0, cy0, cz0), load_voxel(vd, pyr, l, cx1, cy0, cz0),
+                    load_voxel(vd, pyr, l, cx0, cy1, cz0), load_voxel(vd, pyr, l, cx1, cy1, cz0),
+                    load_voxel(vd, pyr, l, cx0, cy0, cz1), load_voxel(vd, pyr, l, cx1, cy0, cz1),
+                    load_voxel(vd, pyr, l, cx0, cy1, cz1), load_voxel(vd, pyr, l, cx1, cy1, cz1));
+    store_voxel(vd, pyr, l + 1, x, y, z, m);
+}
+
+__global__ void k_count_active(const uint32_t* count, const uint8_t* mask, size_t n,
+                               unsigned long long* out) {
+    unsigned long long local = 0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        local += (count[i] > 0u || mask[i]) ? 1ull : 0ull;
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0 && local) atomicAdd(out, local);
+}
+
+}  // namespace
+
+cudaError_t launch_bin_count(const BoardsDev& b, int D, Bins bins, cudaStream_t st) {
+    if (b.n == 0) return cudaSuccess;
+    k_bin_count<<<(b.n + 127) / 128, 128, 0, st>>>(b, D, bins);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bin_scan(Bins bins, cudaStream_t st) {
+    k_bin_scan<<<1, 1024, 0, st>>>(bins);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bin_fill(const BoardsDev& b, int D, Bins bins, cudaStream_t st) {
+    if (b.n == 0) return cudaSuccess;
+    k_bin_fill<<<(b.n + 127) / 128, 128, 0, st>>>(b, D, bins);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sunmap(const BoardsDev& b, const SunFrame& fr, uint64_t* keys,
+                          cudaStream_t st) {
+    if (b.n == 0) return cudaSuccess;
+    k_sunmap<<<b.n, 256, 0, st>>>(b, fr, reinterpret_cast<unsigned long long*>(keys));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_highlight(const BoardsDev& b, const SunFrame& fr, const uint64_t* keys,
+                             float4* posmap, int D, const float wmin[3],
+                             const float range[3], float offset, uint8_t* mask,
+                             cudaStream_t st) {
+    HiParams hp;
+    for (int a = 0; a < 3; ++a) {
+        hp.wmin[a] = wmin[a];
+        hp.range[a] = range[a];
+    }
+    hp.fD = (float)D;
+    hp.offset = offset;
+    hp.D = D;
+    dim3 blk(32, 8);
+    dim3 grd((fr.W + 31) / 32, (fr.H + 7) / 8);
+    k_highlight<<<grd, blk, 0, st>>>(b, fr, reinterpret_cast<const unsigned long long*>(keys),
+                                     posmap, hp, mask);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_splat(const BoardsDev& b, Bins bins, const uint8_t* mask, VolDesc vd,
+                         void* pyr, uint32_t* count, uint32_t* dq, int fused_levels,
+                         cudaStream_t st) {
+    k_splat<<<bins.nbricks, 512, 0, st>>>(b, bins, mask, vd, pyr, count, dq, fused_levels);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mip_level(VolDesc vd, void* pyr, int l, cudaStream_t st) {
+    long long np = (long long)vd.dims[l + 1];
+    long long total = np * np * np;
+    int blocks = (int)((total + 255) / 256);
+    k_mip_level<<<blocks, 256, 0, st>>>(vd, pyr, l);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_count_active(const uint32_t* count, const uint8_t* mask, size_t n,
+                                unsigned long long* out, cudaStream_t st) {
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks < 1) blocks = 1;
+    k_count_active<<<blocks, 256, 0, st>>>(count, mask, n, out);
+    return cudaGetLastError();
+}

@@ -1,0 +1,225 @@
+/*
+ * cloudgb.h -- C ABI of the GB300-native volumetric cloud path.
+ *
+ * The path: spherical billboards -> sun-view nearest-surface map -> highlight
+ * stores -> integer coverage/density volume -> 3D mip pyramid -> per-pixel
+ * view march with a sun cone (exact, or an MLP surrogate).
+ *
+ * Every entry point replaces one piece of the reference's C++/GLSL surface
+ * (jaafersheriff/Cloud-Renderer); the citation is given beside it.  The
+ * reference had no FFI: its boundary was the OpenGL API (glBufferData,
+ * glDrawArraysInstanced, glGenerateMipmap, glGetTexImage).  Here the boundary is
+ * this header: plain pointers and sizes, opaque handles, status codes, no CUDA
+ * or C++ types.  A `void* stream` argument is a cudaStream_t (NULL = the
+ * context's own stream).
+ *
+ * Error behaviour: every call returns a cg_status and never aborts; the
+ * message of the last failure on the calling thread is cg_last_error().
+ * (Reference: GL errors were only printed, GLSL.hpp:40-44, and shader
+ * failures called exit(), Shader.cpp:35-36.)
+ *
+ * Threading: a context and its volumes are used from one thread at a time.
+ */
+#ifndef CLOUDGB_H
+#define CLOUDGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CLOUDGB_ABI_VERSION 1
+
+typedef enum cg_status {
+    CG_OK = 0,
+    CG_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad enum, non-finite value */
+    CG_ERR_OUT_OF_RANGE = 2,     /* size or value beyond a documented limit */
+    CG_ERR_OUT_OF_MEMORY = 3,    /* device or host allocation failed */
+    CG_ERR_CUDA = 4,             /* a CUDA runtime call failed */
+    CG_ERR_NOT_READY = 5,        /* call order: e.g. render before voxelize */
+    CG_ERR_DEVICE_FAULT = 6,     /* a kernel raised its error flag */
+    CG_ERR_IO = 7,               /* file open/read/write failed */
+    CG_ERR_BAD_CHECKPOINT = 8,   /* wrong magic/version/shape/CRC */
+    CG_ERR_UNSUPPORTED = 9       /* feature not available in this build */
+} cg_status;
+
+/* Volume storage format of the mip pyramid. */
+typedef enum cg_format {
+    CG_FORMAT_RGBA32F = 0,  /* 16 B/voxel: R density, G light, B count, A occupancy */
+    CG_FORMAT_BF16_FP16 = 1 /* 4 B/voxel: bf16 density (low half), fp16 light (high half) */
+} cg_format;
+
+/* Sun-cone accumulation rule. */
+typedef enum cg_cone_mode {
+    CG_CONE_TRANSMITTANCE = 0, /* optical depth sum(R * dh), T = exp(-sigma tau) */
+    CG_CONE_REFERENCE = 1      /* traceCone's sum(r * i / (steps*downScaling)) over the
+                                  light channel, clamp-to-edge (conetrace_frag.glsl:64-79) */
+} cg_cone_mode;
+
+typedef struct cg_context cg_context;
+typedef struct cg_volume cg_volume;
+typedef struct cg_mlp cg_mlp;
+
+/* Directional sun (reference: Sun::position + Sun::update, Sun.hpp:26-43).
+ * direction points from the volume toward the sun.  The sun-view map is the
+ * reference's position FBO (VoxelizeShader.cpp:136-167), window-sized there
+ * (1280x720 by default, main.cpp:25-26). */
+typedef struct cg_sun {
+    float direction[3];
+    int map_width;
+    int map_height;
+} cg_sun;
+
+/* Pinhole camera (reference: Camera::getP/getV, Camera.cpp:59-60).
+ * Image row 0 is the top row; RGBA32F output, row-major. */
+typedef struct cg_camera {
+    float eye[3];
+    float target[3];
+    float up[3];
+    float fov_y_degrees;
+    int width;
+    int height;
+} cg_camera;
+
+/* Hash value-noise fBm that replaces the reference's 32^3 noise texture
+ * (ConeTraceShader.cpp:127-159, noise3D conetrace_frag.glsl:103-120). */
+typedef struct cg_noise {
+    uint32_t seed;
+    int octaves;      /* 0 = no noise (density not modulated) */
+    float frequency;  /* base lattice frequency over world units */
+    float lacunarity; /* reference freqStep */
+    float gain;       /* reference persStep */
+} cg_noise;
+
+/* Render parameters (reference: ConeTraceShader public fields,
+ * ConeTraceShader.hpp:15-32). */
+typedef struct cg_render_params {
+    int view_steps;            /* uniform view-march samples over the AABB chord */
+    int sun_steps;             /* vctSteps */
+    float cone_half_angle;     /* radians; the reference's vctConeAngle is 2x this */
+    float cone_initial_height; /* vctConeInitialHeight, level-0 voxels */
+    float cone_min_radius;     /* floor of the cone radius, level-0 voxels */
+    float lod_offset;          /* vctLodOffset */
+    float down_scaling;        /* vctDownScaling (CG_CONE_REFERENCE only) */
+    float density_scale;       /* extinction sigma per unit density per world unit */
+    float ambient;             /* light floor in [0,1] */
+    float sun_color[3];
+    float transmittance_cutoff;/* early ray termination threshold */
+    int cone_mode;             /* cg_cone_mode */
+    cg_noise noise;
+    int use_mlp;               /* 1: sun cone replaced by the MLP surrogate */
+    const cg_mlp* mlp;         /* required when use_mlp != 0 */
+} cg_render_params;
+
+/* Snapshot of a volume's layout, for readback. */
+typedef struct cg_volume_info {
+    int dimension;
+    int mips;
+    int format;
+    int board_count;
+    float world_min[3];
+    float world_max[3];
+    int level_dim[16];
+    size_t level_offset[16]; /* in voxels from the start of the pyramid */
+    size_t bytes_per_voxel;
+    size_t pyramid_bytes;
+} cg_volume_info;
+
+/* ---- library / context ------------------------------------------------- */
+
+const char* cg_status_string(cg_status s);
+/* Message of the last failing call on this thread ("" if none). */
+const char* cg_last_error(void);
+int cg_abi_version(void);
+
+/* One context per device and host thread.  (Reference: the GL context made
+ * by Window::init, Window.cpp:54-106.) */
+cg_status cg_context_create(int device, cg_context** out);
+void cg_context_destroy(cg_context* ctx);
+cg_status cg_context_synchronize(cg_context* ctx);
+/* Number of this library's kernels launched on the context so far. */
+uint64_t cg_context_launch_count(const cg_context* ctx);
+/* Fill p with the documented defaults. */
+void cg_render_params_default(cg_render_params* p);
+
+/* Memory helpers so that callers without a CUDA binding can pass pinned host
+ * or device buffers (the reference's VBO/texture storage, CloudVolume.cpp:27-48).
+ * kind of cg_memcpy: 1 host->device, 2 device->host, 3 device->device. */
+cg_status cg_host_alloc(size_t bytes, void** out);
+void cg_host_free(void* p);
+cg_status cg_device_alloc(size_t bytes, void** out);
+void cg_device_free(void* p);
+cg_status cg_memcpy(void* dst, const void* src, size_t bytes, int kind);
+
+/* ---- CloudVolume ------------------------------------------------------- */
+
+/* CloudVolume(int dim, vec2 bounds, vec3 position, int mips)
+ * (CloudVolume.cpp:7-55).  World box = position + [bound_min, bound_max]^3.
+ * mips <= floor(log2(dimension)) + 1; dimension in [2, 512]. */
+cg_status cg_volume_create(cg_context* ctx, int dimension, float bound_min,
+                           float bound_max, const float position[3], int mips,
+                           int format, cg_volume** out);
+void cg_volume_destroy(cg_volume* vol);
+
+/* Billboard list upload (CloudVolume::uploadBillboards, CloudVolume.cpp:139-164,
+ * with fluffiness multiplying the radii, :153-160).  positions: count*3 floats
+ * relative to the volume position; scales: radii; densities: per-board density
+ * (>= 0, < 32768; NULL = all 1).  Host pointers; copied before return. */
+cg_status cg_volume_set_billboards(cg_volume* vol, const float* positions,
+                                   const float* scales, const float* densities,
+                                   int count, float fluffiness);
+/* VoxelizeShader::voxelize(CloudVolume*) (VoxelizeShader.cpp:18-31): clear,
+ * sun-view nearest-surface map (first_voxelize.glsl), highlight stores
+ * (second_voxelize.glsl), coverage/density splat, and the mip pyramid
+ * (glGenerateMipmap, VoxelizeShader.cpp:105). Asynchronous on stream. */
+cg_status cg_voxelize(cg_volume* vol, const cg_sun* sun, void* stream);
+
+/* ConeTraceShader::coneTrace(CloudVolume*) (ConeTraceShader.cpp:15-82):
+ * per-pixel view march + sun cone.  rgba_out holds width*height*4 floats; it
+ * is a host pointer (copied back, call is synchronous) unless out_on_device. */
+cg_status cg_render(cg_context* ctx, const cg_volume* vol, const cg_camera* cam,
+                    const cg_render_params* params, float* rgba_out,
+                    int out_on_device, void* stream);
+
+/* Render once with counting on (untimed measurement aid, cf. the reference's
+ * Stats pane, main.cpp:144-155): counts[0] view samples evaluated, [1] sun
+ * cones traced, [2] sun-cone samples taken, [3] pixels whose ray met the box. */
+cg_status cg_render_stats(cg_context* ctx, const cg_volume* vol, const cg_camera* cam,
+                          const cg_render_params* params, uint64_t counts[4]);
+
+/* traceCone(sampler3D, position, direction, steps, angle, height)
+ * (conetrace_frag.glsl:64-79) evaluated at n level-0 voxel-space positions
+ * (n*3 floats) toward direction.  out[i] = optical depth (CG_CONE_TRANSMITTANCE)
+ * or the reference's weighted sum (CG_CONE_REFERENCE).  Host pointers unless
+ * on_device. */
+cg_status cg_trace_cones(const cg_volume* vol, const float* positions, int n,
+                         const float direction[3], const cg_render_params* params,
+                         float* out, int on_device, void* stream);
+
+/* ---- readback (reference: VoxelShader::updateVoxelData's glGetTexImage,
+ * VoxelShader.cpp:102-133) -- synchronous, host destinations ------------- */
+
+cg_status cg_volume_get_info(const cg_volume* vol, cg_volume_info* info);
+/* Raw level contents in the volume's format (level_dim^3 voxels). */
+cg_status cg_volume_read_level(const cg_volume* vol, int level, void* dst,
+                               size_t dst_bytes);
+/* Level-0 integer coverage: per voxel board count and Q16.16 density sum. */
+cg_status cg_volume_read_coverage(const cg_volume* vol, uint32_t* count,
+                                  uint32_t* density_q16);
+/* Sun-view map of the last voxelize: keys (depth bits << 32 | board, or
+ * ~0 = empty) and world positions (x, y, z, valid) per texel, row 0 = bottom. */
+cg_status cg_volume_read_sun_map(const cg_volume* vol, uint64_t* keys,
+                                 float* positions);
+/* Level-0 highlight mask (second_voxelize.glsl stores), one byte per voxel. */
+cg_status cg_volume_read_highlight(const cg_volume* vol, uint8_t* mask);
+/* activeVoxels statistic (VoxelShader.cpp:110-119): voxels with count > 0 or
+ * a highlight mark, counted on the device. */
+cg_status cg_volume_active_voxels(const cg_volume* vol, uint64_t* active);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CLOUDGB_H */

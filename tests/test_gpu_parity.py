@@ -1,0 +1,216 @@
+"""GPU parity through the C ABI against the CPU oracle.
+
+Bit-exact: quantized boards, coverage counts, Q16.16 density sums, sun-view
+depth keys (winner boards), position map, highlight mask, level-0 texels.
+Tolerance: mips (FP32 vs FP64, 1e-6 relative), traceCone (1e-5 relative),
+and the FP32 image vs the FP64 oracle: max-abs <= 1e-4 per RGBA channel.
+"""
+import numpy as np
+import pytest
+
+import cloudgb
+from cloudgb import configs, workload
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+IMAGE_TOL = 1e-4
+
+
+def make_pair(ctx, dim, mips, positions, scales, densities, sun_dir, sun_map, fmt=0,
+              fluffiness=1.0):
+    vol = cloudgb.CloudVolume(dim, configs.VOLUME_BOUNDS, configs.VOLUME_POSITION, mips, fmt=fmt,
+                              ctx=ctx)
+    vol.set_billboards(positions, scales, densities)
+    vol.fluffiness = fluffiness
+    vol.update()
+    sun = cloudgb.Sun(sun_dir, *sun_map)
+    cloudgb.VoxelizeShader().voxelize(vol, sun)
+    ov = O.OracleVolume(dim, configs.VOLUME_BOUNDS, configs.VOLUME_POSITION, mips)
+    assert ov.set_boards(positions, scales, densities, fluffiness) == 0
+    assert ov.voxelize(sun.direction, *sun_map) == 0
+    return vol, sun, ov
+
+
+def random_scene(seed, n, spread=0.3, rmin=0.02, rmax=0.12):
+    rng = np.random.default_rng(seed)
+    pos = rng.uniform(-spread, spread, (n, 3)).astype(np.float32)
+    rad = rng.uniform(rmin, rmax, n).astype(np.float32)
+    den = rng.uniform(0.5, 1.0, n).astype(np.float32)
+    return pos, rad, den
+
+
+def assert_voxelize_exact(vol, sun, ov):
+    cnt, dq = vol.read_coverage()
+    ocnt, odq = ov.coverage()
+    assert np.array_equal(cnt, ocnt), f"count mismatch at {np.argwhere(cnt != ocnt)[:5]}"
+    assert np.array_equal(dq, odq), "density mismatch"
+    keys, pos = vol.read_sun_map(sun)
+    okeys, opos = ov.sun_map()
+    assert np.array_equal(keys, okeys), f"{int((keys != okeys).sum())} sun-map keys differ"
+    assert np.array_equal(pos, opos), "position map differs"
+    assert np.array_equal(vol.read_highlight(), ov.mask()), "highlight mask differs"
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2, 3])
+def test_voxelize_random_scenes_bit_exact(ctx, seed):
+    pos, rad, den = random_scene(seed, 48)
+    vol, sun, ov = make_pair(ctx, 64, 7, pos, rad, den, (0.3, 1.0, 0.2), (320, 180))
+    assert_voxelize_exact(vol, sun, ov)
+
+
+def test_voxelize_small_config_bit_exact(ctx):
+    cfg = configs.SMALL_64
+    wl = workload.build(cfg)
+    vol, sun, ov = make_pair(ctx, cfg["dim"], cfg["mips"], wl.positions, wl.scales, wl.densities,
+                             wl.sun_direction, wl.sun_map)
+    assert_voxelize_exact(vol, sun, ov)
+    lv0 = vol.read_level(0)
+    olv = ov.pyramid()
+    assert np.array_equal(lv0, olv[0].astype(np.float32)), "level-0 texels differ"
+    for l in range(1, cfg["mips"]):
+        g = vol.read_level(l).astype(np.float64)
+        np.testing.assert_allclose(g, olv[l], rtol=1e-6, atol=1e-7)
+    assert vol.activeVoxels() == int(((ov.coverage()[0] > 0) | (ov.mask() > 0)).sum())
+
+
+def test_voxelize_full_1080p_scene_bit_exact(ctx):
+    cfg = configs.PLAIN_1080P
+    wl = workload.build(cfg)
+    vol, sun, ov = make_pair(ctx, cfg["dim"], cfg["mips"], wl.positions, wl.scales, wl.densities,
+                             wl.sun_direction, wl.sun_map)
+    assert_voxelize_exact(vol, sun, ov)
+
+
+@pytest.mark.parametrize("dim,mips", [(2, 2), (20, 3), (96, 7), (128, 8)])
+def test_voxelize_odd_sizes(ctx, dim, mips):
+    pos, rad, den = random_scene(dim, 30, rmin=0.05, rmax=0.2)
+    vol, sun, ov = make_pair(ctx, dim, mips, pos, rad, den, (-0.4, 0.8, 0.5), (97, 61))
+    assert_voxelize_exact(vol, sun, ov)
+    olv = ov.pyramid()
+    for l in range(mips):
+        np.testing.assert_allclose(vol.read_level(l).astype(np.float64), olv[l], rtol=1e-6,
+                                   atol=1e-7)
+
+
+def test_voxelize_edge_cases(ctx):
+    # boards outside the box (culled from coverage but present in the sun
+    # map), zero radius, a board touching the box face, fluffiness
+    pos = np.array([[5.0, 5.0, 5.0], [0.0, 0.0, 0.0], [0.49, 0.0, 0.0], [-0.7, 0.1, 0.0],
+                    [0.0, 0.3, 0.0]], np.float32)
+    rad = np.array([0.3, 0.0, 0.1, 0.25, 0.05], np.float32)
+    den = np.array([1.0, 1.0, 0.75, 0.5, 2.0], np.float32)
+    vol, sun, ov = make_pair(ctx, 32, 6, pos, rad, den, (0.2, 0.9, -0.3), (128, 72),
+                             fluffiness=1.5)
+    assert_voxelize_exact(vol, sun, ov)
+
+
+def test_empty_volume(ctx):
+    z = np.zeros((0, 3), np.float32)
+    vol, sun, ov = make_pair(ctx, 32, 6, z, np.zeros(0, np.float32), np.zeros(0, np.float32),
+                             (0.3, 1, 0.2), (64, 64))
+    cnt, dq = vol.read_coverage()
+    assert cnt.sum() == 0 and dq.sum() == 0
+    cam = cloudgb.Camera((0.5, 0.5, -1.5), (0.5, 0.5, 0.5), width=32, height=32)
+    img = cloudgb.ConeTraceShader().coneTrace(vol, cam)
+    assert np.all(img == 0)
+
+
+def test_error_paths(ctx):
+    vol = cloudgb.CloudVolume(16, configs.VOLUME_BOUNDS, configs.VOLUME_POSITION, 5, ctx=ctx)
+    cam = cloudgb.Camera((0.5, 0.5, -1.5), (0.5, 0.5, 0.5), width=8, height=8)
+    with pytest.raises(cloudgb.CloudError) as e:
+        cloudgb.ConeTraceShader().coneTrace(vol, cam)
+    assert e.value.status == 5  # not voxelized
+    with pytest.raises(cloudgb.CloudError) as e:
+        vol.set_billboards([[0, 0, np.nan]], [0.1])
+        vol.update()
+    assert e.value.status == 1
+    with pytest.raises(cloudgb.CloudError) as e:
+        vol.set_billboards([[0, 0, 0]], [2.0])  # radius beyond the box extent
+        vol.update()
+    assert e.value.status == 2
+    vol.set_billboards([[0, 0, 0]], [0.2])
+    vol.update()
+    with pytest.raises(cloudgb.CloudError):
+        cloudgb.VoxelizeShader().voxelize(vol, cloudgb.Sun((0, 1, 0), 16, 16))
+    with pytest.raises(cloudgb.CloudError):
+        cloudgb.CloudVolume(1024, configs.VOLUME_BOUNDS, configs.VOLUME_POSITION, 5, ctx=ctx)
+    with pytest.raises(cloudgb.CloudError):
+        cloudgb.CloudVolume(16, configs.VOLUME_BOUNDS, configs.VOLUME_POSITION, 9, ctx=ctx)
+    cloudgb.VoxelizeShader().voxelize(vol, cloudgb.Sun((0.3, 1, 0.2), 16, 16))
+    with pytest.raises(cloudgb.CloudError):
+        cloudgb.ConeTraceShader(viewSteps=0).coneTrace(vol, cam)
+    with pytest.raises(cloudgb.CloudError):
+        cloudgb.ConeTraceShader(vctSteps=65).coneTrace(vol, cam)
+
+
+def _oracle_image(ov, shader, cam, sun_dir, rect=None):
+    return ov.render(cam, O.params_from_shader(shader), sun_dir, rect=rect)
+
+
+def test_render_small_config_full_image(ctx):
+    cfg = configs.SMALL_64
+    wl = workload.build(cfg)
+    vol, sun, ov = make_pair(ctx, cfg["dim"], cfg["mips"], wl.positions, wl.scales, wl.densities,
+                             wl.sun_direction, wl.sun_map)
+    shader = cloudgb.ConeTraceShader(**wl.shader_kwargs())
+    cam = workload.make_camera(wl.cameras[0])
+    img = shader.coneTrace(vol, cam).astype(np.float64)
+    ref = _oracle_image(ov, shader, cam, sun.direction)
+    err = np.abs(img - ref).max(axis=(0, 1))
+    assert np.all(err <= IMAGE_TOL), f"max-abs per channel {err}"
+    assert ref[..., 3].max() > 0.5  # the cloud is in view
+
+
+@pytest.mark.parametrize("view", [0, 5, 11])
+def test_render_1080p_scene_sampled_tiles(ctx, view):
+    """Plain FP32 path on the 256^3 / 4096-board / noise scene; the oracle
+    checks 32x32 tiles of the 1920x1080 image."""
+    cfg = configs.PLAIN_1080P
+    wl = workload.build(cfg)
+    vol, sun, ov = make_pair(ctx, cfg["dim"], cfg["mips"], wl.positions, wl.scales, wl.densities,
+                             wl.sun_direction, wl.sun_map)
+    shader = cloudgb.ConeTraceShader(**wl.shader_kwargs())
+    cam = workload.make_camera(wl.cameras[view])
+    img = shader.coneTrace(vol, cam).astype(np.float64)
+    alpha = img[..., 3]
+    ys, xs = np.nonzero(alpha > 0.2)
+    rng = np.random.default_rng(view)
+    picks = [(960 - 16, 540 - 16)]
+    for k in rng.choice(len(xs), size=min(3, len(xs)), replace=False):
+        picks.append((int(min(max(xs[k] - 16, 0), 1920 - 32)), int(min(max(ys[k] - 16, 0), 1080 - 32))))
+    for (x0, y0) in picks:
+        ref = _oracle_image(ov, shader, cam, sun.direction, rect=(x0, y0, 32, 32))
+        got = img[y0:y0 + 32, x0:x0 + 32]
+        err = np.abs(got - ref).max(axis=(0, 1))
+        assert np.all(err <= IMAGE_TOL), f"tile {x0},{y0}: max-abs {err}"
+
+
+def test_trace_cones_match_oracle(ctx):
+    cfg = configs.SMALL_64
+    wl = workload.build(cfg)
+    vol, sun, ov = make_pair(ctx, cfg["dim"], cfg["mips"], wl.positions, wl.scales, wl.densities,
+                             wl.sun_direction, wl.sun_map)
+    rng = np.random.default_rng(5)
+    pts = rng.uniform(8, 56, (500, 3)).astype(np.float32)
+    for mode, kw in [(0, dict(vctSteps=16, vctConeAngle=0.1)),
+                     (1, dict(vctSteps=16, vctConeAngle=0.9, vctConeInitialHeight=0.1,
+                              vctDownScaling=1.0))]:
+        shader = cloudgb.ConeTraceShader(coneMode=mode, **kw)
+        got = shader.traceCone(vol, pts, sun.direction).astype(np.float64)
+        ref = ov.trace_cones(pts.astype(np.float64), sun.direction, O.params_from_shader(shader))
+        np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-6)
+        assert ref.max() > 0
+
+
+def test_render_is_deterministic(ctx):
+    cfg = configs.SMALL_64
+    wl = workload.build(cfg, width=96, height=64)
+    vol, sun, _ = make_pair(ctx, cfg["dim"], cfg["mips"], wl.positions, wl.scales, wl.densities,
+                            wl.sun_direction, wl.sun_map)
+    shader = cloudgb.ConeTraceShader(**wl.shader_kwargs())
+    cam = workload.make_camera(wl.cameras[0])
+    a = shader.coneTrace(vol, cam)
+    b = shader.coneTrace(vol, cam)
+    assert np.array_equal(a, b)
