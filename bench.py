@@ -32,8 +32,8 @@ UNIT = "Mpix/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=32)
-    ap.add_argument("--warmup", type=int, default=4)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--fmt", choices=["rgba32f", "bf16_fp16"], default="rgba32f")
     ap.add_argument("--no-cpu-baseline", action="store_true")
