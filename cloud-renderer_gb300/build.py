@@ -24,6 +24,7 @@ SOURCES = [
     ("cg_host.cpp", ["-Xcompiler", "-ffp-contract=off"]),
     ("k_voxelize.cu", ["-fmad=false"]),
     ("k_trace.cu", []),
+    ("k_noalloc.cu", []),
 ]
 
 

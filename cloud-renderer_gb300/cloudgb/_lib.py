@@ -104,7 +104,9 @@ SIGNATURES = [
     ("cg_volume_read_sun_map", I, [P, U64P, FP]),
     ("cg_volume_read_highlight", I, [P, U8P]),
     ("cg_volume_active_voxels", I, [P, U64P]),
+    ("cg_sun_map_noalloc", I, [I, F, F, FP, P, I, ctypes.POINTER(cg_sun), P, P, P]),
 ]
+NOALLOC_MAX_TEXELS = 1 << 20
 
 _lib = None
 

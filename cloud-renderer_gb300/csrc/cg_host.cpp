@@ -137,6 +137,8 @@ extern "C" const char* cg_status_string(cg_status s) {
 }
 
 extern "C" const char* cg_last_error(void) { return g_last_error.c_str(); }
+
+void set_last_error(const char* msg) { g_last_error = msg; }
 extern "C" int cg_abi_version(void) { return CLOUDGB_ABI_VERSION; }
 
 extern "C" cg_status cg_context_create(int device, cg_context** out) {
@@ -472,10 +474,11 @@ static V3 normalize3(V3 v) {
 // Sun::update (Sun.hpp:26-43) for a directional sun: lookDir = -s, lookPos =
 // position - lookDir * max(|min|, |max|), V = lookAt(lookPos, position, +y),
 // ortho box [2 minComp, 2 maxComp]^2, near 0.01.
-static bool make_sun_frame(const cg_volume* v, const float dir[3], int W, int H, SunFrame& fr) {
-    V3 pos{v->pos[0], v->pos[1], v->pos[2]};
+bool sun_frame_for_box(const float position[3], float b0, float b1, const float dir[3], int W,
+                       int H, SunFrame& fr) {
+    V3 pos{position[0], position[1], position[2]};
     V3 lookDir = normalize3({-dir[0], -dir[1], -dir[2]});
-    V3 mn{v->b0, v->b0, v->b0}, mx{v->b1, v->b1, v->b1};
+    V3 mn{b0, b0, b0}, mx{b1, b1, b1};
     float minLen = std::sqrt(dot3(mn, mn)), maxLen = std::sqrt(dot3(mx, mx));
     float dist = minLen > maxLen ? minLen : maxLen;
     V3 lookPos{pos.x - lookDir.x * dist, pos.y - lookDir.y * dist, pos.z - lookDir.z * dist};
@@ -492,8 +495,8 @@ static bool make_sun_frame(const cg_volume* v, const float dir[3], int W, int H,
     fr.t[0] = -dot3(r, lookPos);
     fr.t[1] = -dot3(u, lookPos);
     fr.t[2] = dot3(f, lookPos);
-    fr.lo = 2.0f * v->b0;
-    fr.hi = 2.0f * v->b1;
+    fr.lo = 2.0f * b0;
+    fr.hi = 2.0f * b1;
     fr.near_z = 0.01f;
     V3 np{lookPos.x + lookDir.x * 0.01f, lookPos.y + lookDir.y * 0.01f,
           lookPos.z + lookDir.z * 0.01f};
@@ -505,6 +508,10 @@ static bool make_sun_frame(const cg_volume* v, const float dir[3], int W, int H,
     fr.W = W;
     fr.H = H;
     return true;
+}
+
+static bool make_sun_frame(const cg_volume* v, const float dir[3], int W, int H, SunFrame& fr) {
+    return sun_frame_for_box(v->pos, v->b0, v->b1, dir, W, H, fr);
 }
 
 // stepSize = min(voxelSize) (VoxelizeShader.cpp:128); offset along each axis

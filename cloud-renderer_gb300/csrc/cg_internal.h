@@ -65,6 +65,14 @@ struct Bins {
     uint32_t* list;    // pairs
 };
 
+// Message returned by cg_last_error() on this thread (cg_host.cpp).
+void set_last_error(const char* msg);
+
+// Sun::update's frame for the box position + [b0, b1]^3 (FP32, fixed order;
+// cg_host.cpp).  False when the sun is parallel to the up axis.
+bool sun_frame_for_box(const float position[3], float b0, float b1, const float dir[3], int W,
+                       int H, SunFrame& fr);
+
 // ---- launchers (return cudaGetLastError of the launch) -------------------
 cudaError_t launch_bin_count(const BoardsDev& b, int D, Bins bins, cudaStream_t st);
 cudaError_t launch_bin_scan(Bins bins, cudaStream_t st);

@@ -218,6 +218,31 @@ cg_status cg_volume_read_highlight(const cg_volume* vol, uint8_t* mask);
  * a highlight mark, counted on the device. */
 cg_status cg_volume_active_voxels(const cg_volume* vol, uint64_t* active);
 
+/* ---- allocation-free variant ------------------------------------------- */
+
+/* No counterpart in the reference.  The sun-view nearest-surface map and its
+ * highlight stores (the first two passes of cg_voxelize) for callers that
+ * cannot allocate device memory: hosts that own all device memory through
+ * their own fixed budget, and real-time threads that cannot take cudaMalloc's
+ * implicit synchronisation.  The call allocates nothing.  The caller passes
+ * d_boards (count * 4 floats in device memory: world-space centre xyz =
+ * volume position + board position, and radius = scale * fluffiness) and
+ * the two outputs in device memory: d_positions (map_width * map_height * 4
+ * floats, cg_volume_read_sun_map's layout) and d_mask (dimension^3 bytes,
+ * cleared by the call, cg_volume_read_highlight's layout).  The per-texel depth
+ * keys live in a fixed array inside the library of CG_NOALLOC_MAX_TEXELS keys
+ * (8 MiB), held by every GPU that loads the library until the process exits;
+ * larger sun maps are rejected with CG_ERR_OUT_OF_RANGE.  The first call on a
+ * device looks up that array's device address (make it before any stream
+ * capture).  All calls share the array: calls that overlap on the GPU race,
+ * so serialise them.  Asynchronous on stream (NULL = the legacy default
+ * stream); results match cg_voxelize's sun map and highlight mask bit for bit. */
+#define CG_NOALLOC_MAX_TEXELS (1 << 20)
+cg_status cg_sun_map_noalloc(int dimension, float bound_min, float bound_max,
+                             const float position[3], const float* d_boards, int count,
+                             const cg_sun* sun, float* d_positions, uint8_t* d_mask,
+                             void* stream);
+
 #ifdef __cplusplus
 }
 #endif
