@@ -90,6 +90,13 @@ struct cg_context {
     cudaStream_t stream = nullptr;
     uint64_t launches = 0;
     DevBuf image;  // render target when the caller passes a host pointer
+    // hash-noise lattice tables of the last (noise parameters, world box)
+    DevBuf noise;
+    bool noise_valid = false;
+    uint32_t noise_seed = 0;
+    int noise_octaves = 0;
+    float noise_freq = 0, noise_lac = 0, noise_box[6] = {0, 0, 0, 0, 0, 0};
+    NoiseTab noise_tab{};
 };
 
 struct cg_volume {
@@ -115,6 +122,10 @@ struct cg_volume {
     SunFrame frame{};
     float sun_dir[3] = {0, 1, 0};
     DevBuf scratch;  // small scalars (active voxel count)
+    DevBuf occ;      // occupancy grids (see VolDesc)
+    int occ_nb[CG_MAX_LEVELS];
+    int occ_off[CG_MAX_LEVELS];
+    int occ_total = 0;
 };
 
 // ---------------------------------------------------------------------------
@@ -165,6 +176,7 @@ extern "C" void cg_context_destroy(cg_context* ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     ctx->image.release();
+    ctx->noise.release();
     cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -286,6 +298,16 @@ extern "C" cg_status cg_volume_create(cg_context* ctx, int dimension, float boun
     if (e == cudaSuccess) e = v->dq.ensure(n0 * 4);
     if (e == cudaSuccess) e = v->mask.ensure(n0);
     if (e == cudaSuccess) e = v->scratch.ensure(64);
+    int occ_total = 0;
+    for (int l = 0; l < CG_MAX_LEVELS; ++l) {
+        int nbl = l < mips ? (v->dims[l] + 7) / 8 : 0;
+        v->occ_nb[l] = nbl;
+        v->occ_off[l] = occ_total;
+        occ_total += nbl * nbl * nbl;
+    }
+    v->occ_total = occ_total;
+    // raw grids (written by the splat) followed by the dilated grids
+    if (e == cudaSuccess) e = v->occ.ensure(2 * (size_t)occ_total);
     const int nb = (dimension + CG_BRICK - 1) / CG_BRICK;
     v->bins.nbx = v->bins.nby = v->bins.nbz = nb;
     v->bins.nbricks = nb * nb * nb;
@@ -307,7 +329,7 @@ extern "C" void cg_volume_destroy(cg_volume* v) {
     cudaStreamSynchronize(v->ctx->stream);
     DevBuf* bufs[] = {&v->pyr, &v->count, &v->dq, &v->mask, &v->cwr, &v->q, &v->thr,
                       &v->dqb, &v->culled, &v->bcount, &v->boff, &v->bcursor, &v->blist,
-                      &v->keys, &v->posmap, &v->scratch};
+                      &v->keys, &v->posmap, &v->scratch, &v->occ};
     for (DevBuf* b : bufs) b->release();
     v->h_stage.release();
     delete v;
@@ -453,6 +475,11 @@ static VolDesc desc_of(const cg_volume* v) {
         d.range[a] = v->range[a];
     }
     d.pyr = v->pyr.p;
+    d.occ = v->occ.as<const uint8_t>() + v->occ_total;
+    for (int l = 0; l < CG_MAX_LEVELS; ++l) {
+        d.occ_nb[l] = v->occ_nb[l];
+        d.occ_off[l] = v->occ_off[l];
+    }
     return d;
 }
 
@@ -570,6 +597,7 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
     CG_CUDA(cudaMemsetAsync(v->keys.p, 0xFF, texels * 8, s));
     CG_CUDA(cudaMemsetAsync(v->mask.p, 0, n0, s));
     CG_CUDA(cudaMemsetAsync(bins.count, 0, (size_t)bins.nbricks * 4, s));
+    CG_CUDA(cudaMemsetAsync(v->occ.p, 0, (size_t)v->occ_total, s));
     // brick bins
     if (b.n) CG_LAUNCH(ctx, launch_bin_count(b, v->D, bins, s));
     CG_LAUNCH(ctx, launch_bin_scan(bins, s));
@@ -583,7 +611,10 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
     // coverage splat + level 0 + fused mips
     int fused = (v->D % CG_BRICK == 0) ? std::min(CG_FUSED_MIPS, v->L - 1) : 0;
     CG_LAUNCH(ctx, launch_splat(b, bins, v->mask.as<uint8_t>(), vd, v->pyr.p,
-                                v->count.as<uint32_t>(), v->dq.as<uint32_t>(), fused, s));
+                                v->count.as<uint32_t>(), v->dq.as<uint32_t>(), fused,
+                                v->occ.as<uint8_t>(), s));
+    CG_LAUNCH(ctx, launch_occ_dilate(vd, v->occ.as<uint8_t>(), v->occ.as<uint8_t>() + v->occ_total,
+                                     v->occ_total, s));
     // remaining mips (glGenerateMipmap, VoxelizeShader.cpp:105)
     for (int l = fused; l + 1 < v->L; ++l) CG_LAUNCH(ctx, launch_mip_level(vd, v->pyr.p, l, s));
     v->voxelized = true;
@@ -659,6 +690,7 @@ static TraceParams trace_params_of(const cg_render_params* p, const float sun_di
         amp *= (double)p->noise.gain;
     }
     tp.noise_inv_norm = norm > 0.0 ? (float)(1.0 / norm) : 1.0f;
+    memset(&tp.nt, 0, sizeof(tp.nt));
     return tp;
 }
 
@@ -701,6 +733,64 @@ static cg_status camera_of(const cg_camera* c, CamDesc& cam) {
     return CG_OK;
 }
 
+// Lattice tables for the render's noise parameters over the volume's box,
+// rebuilt only when those change.  Each octave covers floor(wmin*f) - 1 ..
+// floor(wmax*f) + 2 per axis, f = frequency * lacunarity^o in FP32 as the
+// kernel computes it; samples outside fall back to hashing.
+static cg_status ensure_noise(cg_context* ctx, const cg_volume* v, TraceParams& tp,
+                              cudaStream_t s) {
+    if (tp.noise_octaves <= 0) return CG_OK;
+    float box[6] = {v->wmin[0], v->wmin[1], v->wmin[2], v->wmax[0], v->wmax[1], v->wmax[2]};
+    bool same = ctx->noise_valid && ctx->noise_seed == tp.noise_seed &&
+                ctx->noise_octaves == tp.noise_octaves && ctx->noise_freq == tp.noise_freq &&
+                ctx->noise_lac == tp.noise_lac && memcmp(ctx->noise_box, box, sizeof(box)) == 0;
+    if (!same) {
+        NoiseTab nt{};
+        long long total = 0;
+        float f = tp.noise_freq;
+        for (int o = 0; o < tp.noise_octaves; ++o) {
+            nt.off[o] = (int)total;
+            long long n = 1;
+            for (int a = 0; a < 3; ++a) {
+                double lo = std::floor((double)box[a] * (double)f) - 1.0;
+                double hi = std::floor((double)box[3 + a] * (double)f) + 2.0;
+                if (!(hi - lo < 4096.0) || !(lo > -1e9) || !(hi < 1e9)) {
+                    n = -1;
+                    break;
+                }
+                nt.lo[o][a] = (int)lo;
+                nt.dim[o][a] = (int)(hi - lo) + 1;
+                n *= nt.dim[o][a];
+            }
+            if (n < 0 || total + n > (64ll << 20)) {  // too large: hash on the fly
+                total = -1;
+                break;
+            }
+            total += n;
+            f *= tp.noise_lac;
+        }
+        ctx->noise_valid = false;
+        if (total > 0) {
+            CG_CUDA(cudaStreamSynchronize(s));
+            CG_CUDA(ctx->noise.ensure((size_t)total * 4));
+            nt.tab = ctx->noise.as<const float>();
+            tp.nt = nt;
+            CG_LAUNCH(ctx, launch_noise_table(tp, ctx->noise.as<float>(), (int)total, s));
+            ctx->noise_tab = nt;
+            ctx->noise_valid = true;
+            ctx->noise_seed = tp.noise_seed;
+            ctx->noise_octaves = tp.noise_octaves;
+            ctx->noise_freq = tp.noise_freq;
+            ctx->noise_lac = tp.noise_lac;
+            memcpy(ctx->noise_box, box, sizeof(box));
+        } else {
+            memset(&ctx->noise_tab, 0, sizeof(ctx->noise_tab));
+        }
+    }
+    tp.nt = ctx->noise_valid ? ctx->noise_tab : NoiseTab{};
+    return CG_OK;
+}
+
 extern "C" cg_status cg_render(cg_context* ctx, const cg_volume* v, const cg_camera* cam,
                                const cg_render_params* params, float* rgba_out,
                                int out_on_device, void* stream) {
@@ -723,6 +813,8 @@ extern "C" cg_status cg_render(cg_context* ctx, const cg_volume* v, const cg_cam
         out = ctx->image.as<float4>();
     }
     TraceParams tp = trace_params_of(params, v->sun_dir);
+    st = ensure_noise(ctx, v, tp, s);
+    if (st != CG_OK) return st;
     CG_LAUNCH(ctx, launch_trace_fused(desc_of(v), cd, tp, out, nullptr, s));
     if (!out_on_device) {
         CG_CUDA(cudaMemcpyAsync(rgba_out, out, pixels * 16, cudaMemcpyDeviceToHost, s));
@@ -749,8 +841,10 @@ extern "C" cg_status cg_render_stats(cg_context* ctx, const cg_volume* v, const 
     CG_CUDA(ctx->image.ensure(pixels * 16));
     DevBuf cnt;
     CG_CUDA(cnt.ensure(64));
-    cudaError_t e = cudaMemsetAsync(cnt.p, 0, 64, s);
     TraceParams tp = trace_params_of(params, v->sun_dir);
+    st = ensure_noise(ctx, v, tp, s);
+    if (st != CG_OK) return st;
+    cudaError_t e = cudaMemsetAsync(cnt.p, 0, 64, s);
     if (e == cudaSuccess)
         e = launch_trace_fused(desc_of(v), cd, tp, ctx->image.as<float4>(),
                                cnt.as<unsigned long long>(), s);

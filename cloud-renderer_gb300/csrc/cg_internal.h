@@ -20,12 +20,32 @@ struct SunFrame {
 };
 
 // Pyramid description passed by value to kernels.
+//
+// Occupancy: for every level l a grid of occ_nb[l]^3 bytes, one per brick of
+// 8^3 level-l texels (level-0 bricks map to level-l bricks by b >> l).  A byte
+// is 1 when the brick or one of its 26 neighbours holds a voxel with density
+// R > 0.  Because the mips are means of non-negative values, a trilinear
+// footprint whose brick reads 0 has R = 0 exactly, so samplers may skip it.
 struct VolDesc {
     int D, L, fmt;
     int dims[CG_MAX_LEVELS];
     long long offs[CG_MAX_LEVELS];  // voxels
     float wmin[3], range[3];
     const void* pyr;                // float4* (RGBA32F) or uint32_t* (BF16_FP16)
+    const uint8_t* occ;             // occupancy grids, concatenated by level
+    int occ_nb[CG_MAX_LEVELS];
+    int occ_off[CG_MAX_LEVELS];
+};
+
+// Hash-noise lattice values tabulated per octave over the world box: octave
+// k covers lattice points lo[k] + [0, dim[k]) per axis, row-major x fastest,
+// starting at off[k] in the table.  Values equal the on-the-fly hash bit for
+// bit; points outside a table fall back to hashing.
+struct NoiseTab {
+    const float* tab;
+    int off[CG_MAX_LEVELS];
+    int lo[CG_MAX_LEVELS][3];
+    int dim[CG_MAX_LEVELS][3];
 };
 
 // Camera in FP32 for the trace kernels.
@@ -45,6 +65,7 @@ struct TraceParams {
     uint32_t noise_seed;
     int noise_octaves;
     float noise_freq, noise_lac, noise_gain, noise_inv_norm;
+    NoiseTab nt;
 };
 
 // Per-board device arrays (SoA).
@@ -85,12 +106,15 @@ cudaError_t launch_highlight(const BoardsDev& b, const SunFrame& fr, const uint6
                              cudaStream_t st);
 cudaError_t launch_splat(const BoardsDev& b, Bins bins, const uint8_t* mask, VolDesc vd,
                          void* pyr, uint32_t* count, uint32_t* dq, int fused_levels,
-                         cudaStream_t st);
+                         uint8_t* occ, cudaStream_t st);
 cudaError_t launch_mip_level(VolDesc vd, void* pyr, int l, cudaStream_t st);
+cudaError_t launch_occ_dilate(VolDesc vd, const uint8_t* raw, uint8_t* occ, int total,
+                              cudaStream_t st);
 cudaError_t launch_count_active(const uint32_t* count, const uint8_t* mask, size_t n,
                                 unsigned long long* out, cudaStream_t st);
 
 cudaError_t launch_trace_fused(VolDesc vd, CamDesc cam, TraceParams tp, float4* out,
                                unsigned long long* stats, cudaStream_t st);
+cudaError_t launch_noise_table(TraceParams tp, float* tab, int total, cudaStream_t st);
 cudaError_t launch_trace_cones(VolDesc vd, TraceParams tp, const float* pos, int n,
                                float* out, cudaStream_t st);

@@ -30,10 +30,44 @@ __device__ __forceinline__ float fp16_hi(uint32_t v) {
     return __half2float(__ushort_as_half((unsigned short)(v >> 16)));
 }
 
+// One voxel's (R, G) at flat index idx.
+template <int FMT, bool WANT_G>
+__device__ __forceinline__ float2 fetch(const void* pyr, int idx) {
+    if (FMT == 0) {
+        const float4* p4 = reinterpret_cast<const float4*>(pyr);
+        if (WANT_G) return __ldg(reinterpret_cast<const float2*>(p4 + idx));
+        return make_float2(__ldg(reinterpret_cast<const float*>(p4 + idx)), 0.f);
+    }
+    uint32_t t = __ldg(reinterpret_cast<const uint32_t*>(pyr) + idx);
+    return make_float2(bf16_lo(t), WANT_G ? fp16_hi(t) : 0.f);
+}
+
+__device__ __forceinline__ float lerp3(const float c[8], float wx, float wy, float wz) {
+    float x00 = c[0] + wx * (c[1] - c[0]);
+    float x10 = c[2] + wx * (c[3] - c[2]);
+    float x01 = c[4] + wx * (c[5] - c[4]);
+    float x11 = c[6] + wx * (c[7] - c[6]);
+    float y0 = x00 + wy * (x10 - x00);
+    float y1 = x01 + wy * (x11 - x01);
+    return y0 + wz * (y1 - y0);
+}
+
+// Occupancy of the level-l brick holding texel (ix, iy, iz) (see VolDesc).
+__device__ __forceinline__ bool occupied(const VolDesc& vd, int l, int ix, int iy, int iz) {
+    const int nb = vd.occ_nb[l];
+    int bx = min(max(ix >> 3, 0), nb - 1);
+    int by = min(max(iy >> 3, 0), nb - 1);
+    int bz = min(max(iz >> 3, 0), nb - 1);
+    return __ldg(vd.occ + vd.occ_off[l] + (bz * nb + by) * nb + bx) != 0;
+}
+
 // Trilinear at level l of channel R (and G when WANT_G), level-0 voxel-space
 // position (px,py,pz).  BORDER: taps outside the level read 0; otherwise
-// clamp to edge.  Texel coordinates x = p * N_l / D - 0.5.
-template <int FMT, bool WANT_G, bool BORDER>
+// clamp to edge.  Texel coordinates x = p * N_l / D - 0.5.  SKIP_EMPTY: when
+// the footprint's brick is unoccupied the result is exactly (0, 0) for R and
+// is returned without touching the volume (callers that use G only where
+// R > 0).
+template <int FMT, bool WANT_G, bool BORDER, bool SKIP_EMPTY>
 __device__ __forceinline__ float2 tri(const VolDesc& vd, int l, float px, float py, float pz) {
     const int N = vd.dims[l];
     const float sc = (float)N / (float)vd.D;
@@ -41,96 +75,69 @@ __device__ __forceinline__ float2 tri(const VolDesc& vd, int l, float px, float 
     float fx = floorf(x), fy = floorf(y), fz = floorf(z);
     float wx = x - fx, wy = y - fy, wz = z - fz;
     int ix = (int)fx, iy = (int)fy, iz = (int)fz;
-    int xs[2] = {ix, ix + 1}, ys[2] = {iy, iy + 1}, zs[2] = {iz, iz + 1};
-    bool vx[2], vy[2], vz[2];
+    if (SKIP_EMPTY && !occupied(vd, l, ix, iy, iz)) return make_float2(0.f, 0.f);
+    float r[8], g[8];
+    const int base = (int)vd.offs[l];
+    if (ix >= 0 && iy >= 0 && iz >= 0 && ix + 1 < N && iy + 1 < N && iz + 1 < N) {
+        // interior: one base index, fixed offsets
+        const int i0 = base + (iz * N + iy) * N + ix;
+        const int NN = N * N;
+        const int o[8] = {0, 1, N, N + 1, NN, NN + 1, NN + N, NN + N + 1};
 #pragma unroll
-    for (int a = 0; a < 2; ++a) {
-        vx[a] = (xs[a] >= 0 && xs[a] < N);
-        vy[a] = (ys[a] >= 0 && ys[a] < N);
-        vz[a] = (zs[a] >= 0 && zs[a] < N);
-        xs[a] = min(max(xs[a], 0), N - 1);
-        ys[a] = min(max(ys[a], 0), N - 1);
-        zs[a] = min(max(zs[a], 0), N - 1);
-    }
-    float r[2][2][2], g[2][2][2];
-    const long long base = vd.offs[l];
+        for (int k = 0; k < 8; ++k) {
+            float2 t = fetch<FMT, WANT_G>(vd.pyr, i0 + o[k]);
+            r[k] = t.x;
+            g[k] = t.y;
+        }
+    } else {
+        int xs[2] = {ix, ix + 1}, ys[2] = {iy, iy + 1}, zs[2] = {iz, iz + 1};
+        bool vx[2], vy[2], vz[2];
 #pragma unroll
-    for (int c = 0; c < 2; ++c)
+        for (int a = 0; a < 2; ++a) {
+            vx[a] = (xs[a] >= 0 && xs[a] < N);
+            vy[a] = (ys[a] >= 0 && ys[a] < N);
+            vz[a] = (zs[a] >= 0 && zs[a] < N);
+            xs[a] = min(max(xs[a], 0), N - 1);
+            ys[a] = min(max(ys[a], 0), N - 1);
+            zs[a] = min(max(zs[a], 0), N - 1);
+        }
 #pragma unroll
-        for (int b = 0; b < 2; ++b)
+        for (int c = 0; c < 2; ++c)
 #pragma unroll
-            for (int a = 0; a < 2; ++a) {
-                const long long idx = base + ((long long)zs[c] * N + ys[b]) * N + xs[a];
-                const bool ok = !BORDER || (vx[a] && vy[b] && vz[c]);
-                float rv = 0.f, gv = 0.f;
-                if (FMT == 0) {
-                    const float4* p4 = reinterpret_cast<const float4*>(vd.pyr);
-                    if (WANT_G) {
-                        float2 t = __ldg(reinterpret_cast<const float2*>(p4 + idx));
-                        rv = t.x;
-                        gv = t.y;
-                    } else {
-                        rv = __ldg(reinterpret_cast<const float*>(p4 + idx));
-                    }
-                } else {
-                    uint32_t t = __ldg(reinterpret_cast<const uint32_t*>(vd.pyr) + idx);
-                    rv = bf16_lo(t);
-                    if (WANT_G) gv = fp16_hi(t);
+            for (int b = 0; b < 2; ++b)
+#pragma unroll
+                for (int a = 0; a < 2; ++a) {
+                    const int k = c * 4 + b * 2 + a;
+                    const bool ok = !BORDER || (vx[a] && vy[b] && vz[c]);
+                    float2 t = fetch<FMT, WANT_G>(vd.pyr, base + (zs[c] * N + ys[b]) * N + xs[a]);
+                    r[k] = ok ? t.x : 0.f;
+                    g[k] = ok ? t.y : 0.f;
                 }
-                r[c][b][a] = ok ? rv : 0.f;
-                g[c][b][a] = ok ? gv : 0.f;
-            }
-    float2 out;
-    {
-        float x00 = r[0][0][0] + wx * (r[0][0][1] - r[0][0][0]);
-        float x10 = r[0][1][0] + wx * (r[0][1][1] - r[0][1][0]);
-        float x01 = r[1][0][0] + wx * (r[1][0][1] - r[1][0][0]);
-        float x11 = r[1][1][0] + wx * (r[1][1][1] - r[1][1][0]);
-        float y0 = x00 + wy * (x10 - x00);
-        float y1 = x01 + wy * (x11 - x01);
-        out.x = y0 + wz * (y1 - y0);
     }
-    out.y = 0.f;
-    if (WANT_G) {
-        float x00 = g[0][0][0] + wx * (g[0][0][1] - g[0][0][0]);
-        float x10 = g[0][1][0] + wx * (g[0][1][1] - g[0][1][0]);
-        float x01 = g[1][0][0] + wx * (g[1][0][1] - g[1][0][0]);
-        float x11 = g[1][1][0] + wx * (g[1][1][1] - g[1][1][0]);
-        float y0 = x00 + wy * (x10 - x00);
-        float y1 = x01 + wy * (x11 - x01);
-        out.y = y0 + wz * (y1 - y0);
+    return make_float2(lerp3(r, wx, wy, wz), WANT_G ? lerp3(g, wx, wy, wz) : 0.f);
+}
+
+// Quadrilinear with a precomputed (l0, frac) split.
+template <int FMT, bool WANT_G, bool BORDER, bool SKIP_EMPTY>
+__device__ __forceinline__ float2 quad_split(const VolDesc& vd, float px, float py, float pz,
+                                             int l0, float fr) {
+    float2 a = tri<FMT, WANT_G, BORDER, SKIP_EMPTY>(vd, l0, px, py, pz);
+    if (fr > 0.f && l0 + 1 < vd.L) {
+        float2 b = tri<FMT, WANT_G, BORDER, SKIP_EMPTY>(vd, l0 + 1, px, py, pz);
+        a.x = a.x + fr * (b.x - a.x);
+        a.y = a.y + fr * (b.y - a.y);
     }
-    return out;
+    return a;
 }
 
 // Quadrilinear (GL_LINEAR_MIPMAP_LINEAR): lod clamped to [0, L-1].
-template <int FMT, bool WANT_G, bool BORDER>
+template <int FMT, bool WANT_G, bool BORDER, bool SKIP_EMPTY>
 __device__ __forceinline__ float2 quad(const VolDesc& vd, float px, float py, float pz,
                                        float lod) {
     const float maxl = (float)(vd.L - 1);
     lod = fminf(fmaxf(lod, 0.f), maxl);
     const int l0 = (int)floorf(lod);
-    const float fr = lod - (float)l0;
-    float2 a = tri<FMT, WANT_G, BORDER>(vd, l0, px, py, pz);
-    if (fr > 0.f && l0 + 1 < vd.L) {
-        float2 b = tri<FMT, WANT_G, BORDER>(vd, l0 + 1, px, py, pz);
-        a.x = a.x + fr * (b.x - a.x);
-        a.y = a.y + fr * (b.y - a.y);
-    }
-    return a;
-}
-
-// Same with a precomputed (l0, frac) split.
-template <int FMT, bool WANT_G, bool BORDER>
-__device__ __forceinline__ float2 quad_split(const VolDesc& vd, float px, float py, float pz,
-                                             int l0, float fr) {
-    float2 a = tri<FMT, WANT_G, BORDER>(vd, l0, px, py, pz);
-    if (fr > 0.f && l0 + 1 < vd.L) {
-        float2 b = tri<FMT, WANT_G, BORDER>(vd, l0 + 1, px, py, pz);
-        a.x = a.x + fr * (b.x - a.x);
-        a.y = a.y + fr * (b.y - a.y);
-    }
-    return a;
+    return quad_split<FMT, WANT_G, BORDER, SKIP_EMPTY>(vd, px, py, pz, l0, lod - (float)l0);
 }
 
 // Neumaier compensated accumulation.
@@ -153,8 +160,8 @@ __device__ __forceinline__ float sun_cone(const VolDesc& vd, const ConeSchedule&
         float acc = 0.f;
         for (int i = 0; i < cs.steps; ++i) {
             float h = cs.h[i];
-            float2 c = quad_split<FMT, true, false>(vd, vx + h * sx, vy + h * sy, vz + h * sz,
-                                                    cs.l0[i], cs.frac[i]);
+            float2 c = quad_split<FMT, true, false, false>(vd, vx + h * sx, vy + h * sy,
+                                                           vz + h * sz, cs.l0[i], cs.frac[i]);
             acc += c.y * cs.w[i];
         }
         return acc;
@@ -165,7 +172,7 @@ __device__ __forceinline__ float sun_cone(const VolDesc& vd, const ConeSchedule&
         float h = cs.h[i];
         float x = vx + h * sx, y = vy + h * sy, z = vz + h * sz;
         if (x < -E || y < -E || z < -E || x > D + E || y > D + E || z > D + E) break;
-        float2 c = quad_split<FMT, false, true>(vd, x, y, z, cs.l0[i], cs.frac[i]);
+        float2 c = quad_split<FMT, false, true, true>(vd, x, y, z, cs.l0[i], cs.frac[i]);
         neumaier(tau, comp, c.x * cs.w[i]);
     }
     return tau + comp;
@@ -207,39 +214,61 @@ __device__ __forceinline__ uint3 pcg3d(uint3 v) {
     return v;
 }
 
+__device__ __forceinline__ uint32_t octave_key(uint32_t seed, int o) {
+    return seed * 0x9E3779B9u + (uint32_t)o * 0x85EBCA6Bu + 1u;
+}
+
 __device__ __forceinline__ float lattice(int ix, int iy, int iz, uint32_t k) {
     uint3 h = pcg3d(make_uint3((uint32_t)ix + k, (uint32_t)iy + (k ^ 0x68E31DA4u),
                                (uint32_t)iz + (k ^ 0xB5297A4Du)));
     return (float)(h.x >> 8) * (1.0f / 16777216.0f);
 }
 
-__device__ __forceinline__ float value_noise(float x, float y, float z, uint32_t k) {
+// Value noise of octave o at lattice coordinates (x, y, z): trilinear over
+// the lattice with smoothstep weights.  Corner values come from the octave's
+// table when the 2x2x2 corner block lies inside it, else from the hash.
+__device__ __forceinline__ float value_noise(const TraceParams& tp, int o, float x, float y,
+                                             float z) {
     float fx = floorf(x), fy = floorf(y), fz = floorf(z);
     int ix = (int)fx, iy = (int)fy, iz = (int)fz;
     float ux = x - fx, uy = y - fy, uz = z - fz;
     float wx = ux * ux * (3.f - 2.f * ux);
     float wy = uy * uy * (3.f - 2.f * uy);
     float wz = uz * uz * (3.f - 2.f * uz);
-    float c000 = lattice(ix, iy, iz, k), c100 = lattice(ix + 1, iy, iz, k);
-    float c010 = lattice(ix, iy + 1, iz, k), c110 = lattice(ix + 1, iy + 1, iz, k);
-    float c001 = lattice(ix, iy, iz + 1, k), c101 = lattice(ix + 1, iy, iz + 1, k);
-    float c011 = lattice(ix, iy + 1, iz + 1, k), c111 = lattice(ix + 1, iy + 1, iz + 1, k);
-    float x00 = c000 + wx * (c100 - c000);
-    float x10 = c010 + wx * (c110 - c010);
-    float x01 = c001 + wx * (c101 - c001);
-    float x11 = c011 + wx * (c111 - c011);
-    float y0 = x00 + wy * (x10 - x00);
-    float y1 = x01 + wy * (x11 - x01);
-    return y0 + wz * (y1 - y0);
+    float c[8];
+    const int tx = ix - tp.nt.lo[o][0], ty = iy - tp.nt.lo[o][1], tz = iz - tp.nt.lo[o][2];
+    const int dx = tp.nt.dim[o][0], dy = tp.nt.dim[o][1], dz = tp.nt.dim[o][2];
+    if (tp.nt.tab && tx >= 0 && ty >= 0 && tz >= 0 && tx + 1 < dx && ty + 1 < dy && tz + 1 < dz) {
+        const float* t = tp.nt.tab + tp.nt.off[o] + (tz * dy + ty) * dx + tx;
+        const int sy = dx, sz = dx * dy;
+        c[0] = __ldg(t);
+        c[1] = __ldg(t + 1);
+        c[2] = __ldg(t + sy);
+        c[3] = __ldg(t + sy + 1);
+        c[4] = __ldg(t + sz);
+        c[5] = __ldg(t + sz + 1);
+        c[6] = __ldg(t + sz + sy);
+        c[7] = __ldg(t + sz + sy + 1);
+    } else {
+        const uint32_t k = octave_key(tp.noise_seed, o);
+        c[0] = lattice(ix, iy, iz, k);
+        c[1] = lattice(ix + 1, iy, iz, k);
+        c[2] = lattice(ix, iy + 1, iz, k);
+        c[3] = lattice(ix + 1, iy + 1, iz, k);
+        c[4] = lattice(ix, iy, iz + 1, k);
+        c[5] = lattice(ix + 1, iy, iz + 1, k);
+        c[6] = lattice(ix, iy + 1, iz + 1, k);
+        c[7] = lattice(ix + 1, iy + 1, iz + 1, k);
+    }
+    return lerp3(c, wx, wy, wz);
 }
 
-// fBm over world position p; octave key k = seed*0x9E3779B9 + o*0x85EBCA6B + 1.
+// fBm = sum_o gain^o noise_o(p * freq * lac^o) / sum_o gain^o; 1 without octaves.
 __device__ __forceinline__ float fbm(const TraceParams& tp, float px, float py, float pz) {
     if (tp.noise_octaves <= 0) return 1.f;
     float amp = 1.f, sum = 0.f, f = tp.noise_freq;
     for (int o = 0; o < tp.noise_octaves; ++o) {
-        uint32_t k = tp.noise_seed * 0x9E3779B9u + (uint32_t)o * 0x85EBCA6Bu + 1u;
-        sum += amp * value_noise(px * f, py * f, pz * f, k);
+        sum += amp * value_noise(tp, o, px * f, py * f, pz * f);
         amp *= tp.noise_gain;
         f *= tp.noise_lac;
     }

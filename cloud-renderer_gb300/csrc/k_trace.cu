@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(256) k_trace_fused(VolDesc vd, CamDesc cam, Tr
             float v0 = (p0 - vd.wmin[0]) * vsx, v1 = (p1 - vd.wmin[1]) * vsy,
                   v2 = (p2 - vd.wmin[2]) * vsz;
             float lod = log2f(fmaxf(1.f, 2.f * t * pixk));
-            float2 rg = cgs::quad<FMT, true, true>(vd, v0, v1, v2, lod);
+            float2 rg = cgs::quad<FMT, true, true, true>(vd, v0, v1, v2, lod);
             n_view++;
             if (!(rg.x > 0.f)) continue;
             float rho = rg.x * cgs::fbm(tp, p0, p1, p2);
@@ -163,6 +163,27 @@ cudaError_t launch_trace_fused(VolDesc vd, CamDesc cam, TraceParams tp, float4* 
         else
             k_trace_fused<1, false><<<grd, 256, 0, st>>>(vd, cam, tp, cs, out, nullptr);
     }
+    return cudaGetLastError();
+}
+
+namespace {
+// Lattice values of every tabulated octave (one thread per entry).
+__global__ void k_noise_table(TraceParams tp, float* tab, int total) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    int o = 0;
+    while (o + 1 < tp.noise_octaves && i >= tp.nt.off[o + 1]) ++o;
+    int r = i - tp.nt.off[o];
+    const int dx = tp.nt.dim[o][0], dy = tp.nt.dim[o][1];
+    int tx = r % dx, ty = (r / dx) % dy, tz = r / (dx * dy);
+    tab[i] = cgs::lattice(tp.nt.lo[o][0] + tx, tp.nt.lo[o][1] + ty, tp.nt.lo[o][2] + tz,
+                          cgs::octave_key(tp.noise_seed, o));
+}
+}  // namespace
+
+cudaError_t launch_noise_table(TraceParams tp, float* tab, int total, cudaStream_t st) {
+    if (total <= 0) return cudaSuccess;
+    k_noise_table<<<(total + 255) / 256, 256, 0, st>>>(tp, tab, total);
     return cudaGetLastError();
 }
 

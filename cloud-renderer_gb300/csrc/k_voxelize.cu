@@ -36,72 +36,100 @@ __device__ __forceinline__ bool axis_range(int q, int rq, int D, int& lo, int& h
 
 // ---- brick binning ---------------------------------------------------------
 
-__global__ void k_bin_count(BoardsDev b, int D, Bins bins) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+// Distance term along one axis from the board centre q to the nearest voxel
+// centre of the voxel range [lo, hi] (Q20).
+__device__ __forceinline__ long long axis_gap(int q, int lo, int hi) {
+    long long c0 = (2ll * lo + 1) * CG_HALF_Q20, c1 = (2ll * hi + 1) * CG_HALF_Q20;
+    long long c = q < c0 ? c0 : (q > c1 ? c1 : (long long)q);
+    return (long long)q - c;
+}
+
+// Board bin walk shared by the count and fill passes: one warp per board,
+// lanes over the bricks of its voxel box; a brick is kept only when its
+// nearest voxel centre passes the board's ball test, so no brick without an
+// inside voxel enters the bins (the per-voxel test in k_splat stays exact).
+template <bool FILL>
+__device__ __forceinline__ void bin_walk(const BoardsDev& b, int D, Bins& bins) {
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (i >= b.n || b.culled[i]) return;
-    int4 q = b.q[i];
+    const int4 q = b.q[i];
+    const unsigned long long thr = b.thr[i];
     int xl, xh, yl, yh, zl, zh;
     if (!axis_range(q.x, q.w, D, xl, xh) || !axis_range(q.y, q.w, D, yl, yh) ||
         !axis_range(q.z, q.w, D, zl, zh))
         return;
-    for (int bz = zl / CG_BRICK; bz <= zh / CG_BRICK; ++bz)
-        for (int by = yl / CG_BRICK; by <= yh / CG_BRICK; ++by)
-            for (int bx = xl / CG_BRICK; bx <= xh / CG_BRICK; ++bx)
-                atomicAdd(&bins.count[(bz * bins.nby + by) * bins.nbx + bx], 1u);
+    const int bx0 = xl / CG_BRICK, by0 = yl / CG_BRICK, bz0 = zl / CG_BRICK;
+    const int nx = xh / CG_BRICK - bx0 + 1, ny = yh / CG_BRICK - by0 + 1,
+              nz = zh / CG_BRICK - bz0 + 1;
+    const int total = nx * ny * nz;
+    for (int t = lane; t < total; t += 32) {
+        const int bx = bx0 + t % nx, by = by0 + (t / nx) % ny, bz = bz0 + t / (nx * ny);
+        long long gx = axis_gap(q.x, max(bx * CG_BRICK, xl), min(bx * CG_BRICK + 7, xh));
+        long long gy = axis_gap(q.y, max(by * CG_BRICK, yl), min(by * CG_BRICK + 7, yh));
+        long long gz = axis_gap(q.z, max(bz * CG_BRICK, zl), min(bz * CG_BRICK + 7, zh));
+        unsigned long long d2 = (unsigned long long)(gx * gx) + (unsigned long long)(gy * gy) +
+                                (unsigned long long)(gz * gz);
+        if (d2 > thr) continue;
+        const int brick = (bz * bins.nby + by) * bins.nbx + bx;
+        if (FILL) {
+            uint32_t slot = atomicAdd(&bins.cursor[brick], 1u);
+            bins.list[slot] = (uint32_t)i;
+        } else {
+            atomicAdd(&bins.count[brick], 1u);
+        }
+    }
 }
 
-// Exclusive scan of the brick counts in one CTA (1024 threads, each owning a
-// contiguous chunk).  Also seeds the fill cursors.
+__global__ void k_bin_count(BoardsDev b, int D, Bins bins) { bin_walk<false>(b, D, bins); }
+__global__ void k_bin_fill(BoardsDev b, int D, Bins bins) { bin_walk<true>(b, D, bins); }
+
+// Exclusive scan of the brick counts in one CTA: tiles of 4096 counts, four
+// per thread, block scan per tile with a running carry.  Seeds the cursors.
 __global__ void __launch_bounds__(1024) k_bin_scan(Bins bins) {
     __shared__ uint32_t warp_sums[32];
+    __shared__ uint32_t carry_s;
     const int n = bins.nbricks;
-    const int tid = threadIdx.x;
-    const int per = (n + 1023) / 1024;
-    const int beg = min(n, tid * per), end = min(n, beg + per);
-    uint32_t s = 0;
-    for (int i = beg; i < end; ++i) s += bins.count[i];
-    // block exclusive scan of s
-    const int lane = tid & 31, wid = tid >> 5;
-    uint32_t x = s;
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) warp_sums[wid] = x;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (tid == 0) carry_s = 0;
     __syncthreads();
-    if (wid == 0) {
-        uint32_t w = warp_sums[lane];
-        uint32_t z = w;
+    for (int base = 0; base < n; base += 4096) {
+        const int i0 = base + tid * 4;
+        uint32_t c[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) c[k] = (i0 + k < n) ? bins.count[i0 + k] : 0u;
+        const uint32_t s = c[0] + c[1] + c[2] + c[3];
+        uint32_t x = s;
         for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(0xffffffffu, z, o);
-            if (lane >= o) z += y;
+            uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
         }
-        warp_sums[lane] = z - w;
-    }
-    __syncthreads();
-    uint32_t run = warp_sums[wid] + x - s;
-    for (int i = beg; i < end; ++i) {
-        bins.offset[i] = run;
-        bins.cursor[i] = run;
-        run += bins.count[i];
-    }
-    if (tid == 1023) bins.offset[n] = warp_sums[wid] + x;
-}
-
-__global__ void k_bin_fill(BoardsDev b, int D, Bins bins) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= b.n || b.culled[i]) return;
-    int4 q = b.q[i];
-    int xl, xh, yl, yh, zl, zh;
-    if (!axis_range(q.x, q.w, D, xl, xh) || !axis_range(q.y, q.w, D, yl, yh) ||
-        !axis_range(q.z, q.w, D, zl, zh))
-        return;
-    for (int bz = zl / CG_BRICK; bz <= zh / CG_BRICK; ++bz)
-        for (int by = yl / CG_BRICK; by <= yh / CG_BRICK; ++by)
-            for (int bx = xl / CG_BRICK; bx <= xh / CG_BRICK; ++bx) {
-                uint32_t slot = atomicAdd(&bins.cursor[(bz * bins.nby + by) * bins.nbx + bx], 1u);
-                bins.list[slot] = (uint32_t)i;
+        if (lane == 31) warp_sums[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            uint32_t w = warp_sums[lane], z = w;
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t y = __shfl_up_sync(0xffffffffu, z, o);
+                if (lane >= o) z += y;
             }
+            warp_sums[lane] = z - w;
+        }
+        __syncthreads();
+        const uint32_t carry = carry_s;
+        uint32_t run = carry + warp_sums[wid] + x - s;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (i0 + k < n) {
+                bins.offset[i0 + k] = run;
+                bins.cursor[i0 + k] = run;
+            }
+            run += c[k];
+        }
+        __syncthreads();
+        if (tid == 1023) carry_s = carry + warp_sums[wid] + x;
+        __syncthreads();
+    }
+    if (tid == 0) bins.offset[n] = carry_s;
 }
 
 // ---- sun-view nearest-surface map (first_voxelize.glsl:39-64) --------------
@@ -294,7 +322,8 @@ __device__ __forceinline__ float4 box8(float4 c000, float4 c100, float4 c010, fl
 // `fused_levels` mip levels are reduced in shared memory.
 __global__ void __launch_bounds__(512) k_splat(BoardsDev b, Bins bins, const uint8_t* mask,
                                                VolDesc vd, void* pyr, uint32_t* count,
-                                               uint32_t* dqout, int fused_levels) {
+                                               uint32_t* dqout, int fused_levels,
+                                               uint8_t* occ_raw) {
     __shared__ int4 sq[CG_SPLAT_CHUNK];
     __shared__ unsigned long long sthr[CG_SPLAT_CHUNK];
     __shared__ uint32_t sdq[CG_SPLAT_CHUNK];
@@ -352,6 +381,15 @@ __global__ void __launch_bounds__(512) k_splat(BoardsDev b, Bins bins, const uin
         v0.w = (cnt > 0u || mk) ? 1.0f : 0.0f;
         store_voxel(vd, pyr, 0, x, y, z, v0);
     }
+    // Raw occupancy: a brick with any R > 0 flags the brick holding it at
+    // every level, one level per thread (idempotent byte stores into grids
+    // cleared before the launch; k_occ_dilate spreads them to neighbours).
+    if (__syncthreads_or(inside && v0.x > 0.f) && tid < vd.L) {
+        const int l = tid, nb = vd.occ_nb[l];
+        const int cx = min(bx >> l, nb - 1), cy = min(by >> l, nb - 1), cz = min(bz >> l, nb - 1);
+        uint8_t* p = occ_raw + vd.occ_off[l] + (cz * nb + cy) * nb + cx;
+        if (!*(volatile uint8_t*)p) *p = 1;
+    }
     if (fused_levels <= 0) return;
     tile[tid] = v0;
     __syncthreads();
@@ -390,6 +428,24 @@ __global__ void __launch_bounds__(512) k_splat(BoardsDev b, Bins bins, const uin
     }
 }
 
+// Dilated occupancy: occ[l][c] = OR of raw[l] over c's 3x3x3 neighbourhood,
+// one thread per brick of every level.
+__global__ void k_occ_dilate(VolDesc vd, const uint8_t* raw, uint8_t* occ, int total) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    int l = 0;
+    while (l + 1 < vd.L && i >= vd.occ_off[l + 1]) ++l;
+    const int nb = vd.occ_nb[l], r = i - vd.occ_off[l];
+    const int cx = r % nb, cy = (r / nb) % nb, cz = r / (nb * nb);
+    const uint8_t* g = raw + vd.occ_off[l];
+    uint8_t any = 0;
+    for (int z = max(cz - 1, 0); z <= min(cz + 1, nb - 1); ++z)
+        for (int y = max(cy - 1, 0); y <= min(cy + 1, nb - 1); ++y)
+            for (int x = max(cx - 1, 0); x <= min(cx + 1, nb - 1); ++x)
+                any |= g[(z * nb + y) * nb + x];
+    occ[i] = any ? 1 : 0;
+}
+
 // Generic 2x2x2 reduction from level l to l+1 (one thread per parent).
 __global__ void k_mip_level(VolDesc vd, void* pyr, int l) {
     const int Nc = vd.dims[l], Np = vd.dims[l + 1];
@@ -421,7 +477,7 @@ __global__ void k_count_active(const uint32_t* count, const uint8_t* mask, size_
 
 cudaError_t launch_bin_count(const BoardsDev& b, int D, Bins bins, cudaStream_t st) {
     if (b.n == 0) return cudaSuccess;
-    k_bin_count<<<(b.n + 127) / 128, 128, 0, st>>>(b, D, bins);
+    k_bin_count<<<(b.n + 3) / 4, 128, 0, st>>>(b, D, bins);  // one warp per board
     return cudaGetLastError();
 }
 
@@ -432,7 +488,7 @@ cudaError_t launch_bin_scan(Bins bins, cudaStream_t st) {
 
 cudaError_t launch_bin_fill(const BoardsDev& b, int D, Bins bins, cudaStream_t st) {
     if (b.n == 0) return cudaSuccess;
-    k_bin_fill<<<(b.n + 127) / 128, 128, 0, st>>>(b, D, bins);
+    k_bin_fill<<<(b.n + 3) / 4, 128, 0, st>>>(b, D, bins);
     return cudaGetLastError();
 }
 
@@ -464,8 +520,14 @@ cudaError_t launch_highlight(const BoardsDev& b, const SunFrame& fr, const uint6
 
 cudaError_t launch_splat(const BoardsDev& b, Bins bins, const uint8_t* mask, VolDesc vd,
                          void* pyr, uint32_t* count, uint32_t* dq, int fused_levels,
-                         cudaStream_t st) {
-    k_splat<<<bins.nbricks, 512, 0, st>>>(b, bins, mask, vd, pyr, count, dq, fused_levels);
+                         uint8_t* occ, cudaStream_t st) {
+    k_splat<<<bins.nbricks, 512, 0, st>>>(b, bins, mask, vd, pyr, count, dq, fused_levels, occ);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_occ_dilate(VolDesc vd, const uint8_t* raw, uint8_t* occ, int total,
+                              cudaStream_t st) {
+    k_occ_dilate<<<(total + 255) / 256, 256, 0, st>>>(vd, raw, occ, total);
     return cudaGetLastError();
 }
 

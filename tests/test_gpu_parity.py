@@ -204,6 +204,57 @@ def test_trace_cones_match_oracle(ctx):
         assert ref.max() > 0
 
 
+def _unpack_bf16_fp16(packed):
+    r = (packed.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+    g = (packed >> 16).astype(np.uint16).view(np.float16).astype(np.float64)
+    return r, g
+
+
+def test_bf16_volume_sampling_and_rmse(ctx):
+    """BF16 density + FP16 light storage: (a) the GPU image equals the oracle
+    rendering the same quantized pyramid within the FP32 tolerance; (b) the
+    image RMSE against the full-precision FP64 oracle stays within 1e-2."""
+    cfg = configs.SMALL_64
+    wl = workload.build(cfg)
+    vol, sun, ov = make_pair(ctx, cfg["dim"], cfg["mips"], wl.positions, wl.scales, wl.densities,
+                             wl.sun_direction, wl.sun_map, fmt=cloudgb.FORMAT_BF16_FP16)
+    shader = cloudgb.ConeTraceShader(**wl.shader_kwargs())
+    cam = workload.make_camera(wl.cameras[0])
+    img = shader.coneTrace(vol, cam).astype(np.float64)
+    full = _oracle_image(ov, shader, cam, sun.direction)
+    rmse = float(np.sqrt(((img - full) ** 2).mean()))
+    assert rmse <= 1e-2, f"RMSE vs FP64 oracle {rmse}"
+    # feed the oracle the GPU's quantized pyramid
+    levels = ov.pyramid()
+    for l in range(cfg["mips"]):
+        r, g = _unpack_bf16_fp16(vol.read_level(l))
+        levels[l][..., 0] = r
+        levels[l][..., 1] = g
+        # the FP32 mips of levels <= 3 were rounded once from FP32 values
+        np.testing.assert_allclose(r, ov.pyramid()[l][..., 0], rtol=2 ** -7, atol=1e-6)
+    ov.set_pyramid(levels)
+    ref = _oracle_image(ov, shader, cam, sun.direction)
+    err = np.abs(img - ref).max(axis=(0, 1))
+    assert np.all(err <= IMAGE_TOL), f"max-abs per channel {err}"
+
+
+def test_noise_scene_small_image_full_parity(ctx):
+    """Noise path (table-driven on the GPU, hashed in the oracle) on a full
+    image of the 256^3 scene at reduced resolution."""
+    cfg = configs.PLAIN_1080P
+    wl = workload.build(cfg, width=160, height=90)
+    vol, sun, ov = make_pair(ctx, cfg["dim"], cfg["mips"], wl.positions, wl.scales, wl.densities,
+                             wl.sun_direction, wl.sun_map)
+    shader = cloudgb.ConeTraceShader(**wl.shader_kwargs())
+    for view in (1, 7):
+        cam = workload.make_camera(wl.cameras[view])
+        img = shader.coneTrace(vol, cam).astype(np.float64)
+        ref = _oracle_image(ov, shader, cam, sun.direction)
+        err = np.abs(img - ref).max(axis=(0, 1))
+        assert np.all(err <= IMAGE_TOL), f"view {view}: max-abs per channel {err}"
+        assert ref[..., 3].max() > 0.5
+
+
 def test_render_is_deterministic(ctx):
     cfg = configs.SMALL_64
     wl = workload.build(cfg, width=96, height=64)
