@@ -25,6 +25,10 @@ SOURCES = [
     ("k_voxelize.cu", ["-fmad=false"]),
     ("k_trace.cu", []),
     ("k_noalloc.cu", []),
+    ("k_deferred.cu", []),
+    ("k_mlp.cu", []),
+    ("k_textures.cu", []),
+    ("cg_mlp.cpp", ["-Xcompiler", "-ffp-contract=off"]),
 ]
 
 

@@ -43,6 +43,25 @@ class Context:
     def launch_count(self):
         return int(self._lib.cg_context_launch_count(self.handle))
 
+    def set_timing(self, on=True):
+        check(self._lib.cg_context_set_timing(self.handle, 1 if on else 0), "cg_context_set_timing")
+
+    def stage_times(self):
+        """{stage: ms} of the last voxelize/render call made with timing on."""
+        ms = (ctypes.c_float * 32)()
+        n = ctypes.c_int()
+        names = ctypes.create_string_buffer(1024)
+        check(self._lib.cg_context_stage_times(self.handle, ms, 32, ctypes.byref(n), names, 1024),
+              "cg_context_stage_times")
+        keys = names.value.decode().split(";") if n.value else []
+        return {k: float(ms[i]) for i, k in enumerate(keys)}
+
+    def mlp_fallbacks(self):
+        v = ctypes.c_uint64()
+        check(self._lib.cg_context_mlp_fallbacks(self.handle, ctypes.byref(v)),
+              "cg_context_mlp_fallbacks")
+        return int(v.value)
+
     def close(self):
         if self.handle:
             self._lib.cg_context_destroy(self.handle)
@@ -368,6 +387,7 @@ class ConeTraceShader:
         self.persStep = p.noise.gain
         self.useMlp = False
         self.mlp = None
+        self.pipeline = p.pipeline
         for k, v in kw.items():
             if not hasattr(self, k):
                 raise AttributeError(f"ConeTraceShader has no parameter {k!r}")
@@ -394,6 +414,7 @@ class ConeTraceShader:
         p.noise.gain = float(self.persStep)
         p.use_mlp = 1 if self.useMlp else 0
         p.mlp = self.mlp.handle if (self.useMlp and self.mlp is not None) else None
+        p.pipeline = int(self.pipeline)
         return p
 
     def coneTrace(self, volume, camera, out=None, stream=None):

@@ -54,7 +54,30 @@ class cg_render_params(ctypes.Structure):
                 ("down_scaling", ctypes.c_float), ("density_scale", ctypes.c_float),
                 ("ambient", ctypes.c_float), ("sun_color", ctypes.c_float * 3),
                 ("transmittance_cutoff", ctypes.c_float), ("cone_mode", ctypes.c_int),
-                ("noise", cg_noise), ("use_mlp", ctypes.c_int), ("mlp", ctypes.c_void_p)]
+                ("noise", cg_noise), ("use_mlp", ctypes.c_int), ("mlp", ctypes.c_void_p),
+                ("pipeline", ctypes.c_int)]
+
+
+PIPELINE_FUSED = 0
+PIPELINE_DEFERRED = 1
+MLP_FEATURES = 16
+MLP_PARAMS = 9473
+
+
+class cg_mlp_config(ctypes.Structure):
+    _fields_ = [("base_level", ctypes.c_int), ("initial_height", ctypes.c_float),
+                ("dimension", ctypes.c_int), ("sun_steps", ctypes.c_int),
+                ("cone_half_angle", ctypes.c_float), ("cone_initial_height", ctypes.c_float),
+                ("cone_min_radius", ctypes.c_float), ("lod_offset", ctypes.c_float),
+                ("mean", ctypes.c_float * 16), ("stddev", ctypes.c_float * 16),
+                ("feature_min", ctypes.c_float * 16), ("feature_max", ctypes.c_float * 16),
+                ("tau_scale", ctypes.c_float)]
+
+
+class cg_train_params(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_int), ("batch", ctypes.c_int), ("lr", ctypes.c_float),
+                ("beta1", ctypes.c_float), ("beta2", ctypes.c_float), ("eps", ctypes.c_float),
+                ("sigma", ctypes.c_float), ("seed", ctypes.c_uint64)]
 
 
 class cg_volume_info(ctypes.Structure):
@@ -85,6 +108,8 @@ SIGNATURES = [
     ("cg_context_synchronize", I, [P]),
     ("cg_context_launch_count", ctypes.c_uint64, [P]),
     ("cg_render_params_default", None, [ctypes.POINTER(cg_render_params)]),
+    ("cg_context_set_timing", I, [P, I]),
+    ("cg_context_stage_times", I, [P, FP, I, ctypes.POINTER(ctypes.c_int), ctypes.c_char_p, SZ]),
     ("cg_host_alloc", I, [SZ, PP]),
     ("cg_host_free", None, [P]),
     ("cg_device_alloc", I, [SZ, PP]),
@@ -105,6 +130,25 @@ SIGNATURES = [
     ("cg_volume_read_highlight", I, [P, U8P]),
     ("cg_volume_active_voxels", I, [P, U64P]),
     ("cg_sun_map_noalloc", I, [I, F, F, FP, P, I, ctypes.POINTER(cg_sun), P, P, P]),
+    ("cg_march_samples", I, [P, P, ctypes.POINTER(cg_camera), ctypes.POINTER(cg_render_params),
+                             FP, FP, I, ctypes.POINTER(ctypes.c_int)]),
+    ("cg_mlp_config_default", None, [ctypes.POINTER(cg_mlp_config)]),
+    ("cg_train_params_default", None, [ctypes.POINTER(cg_train_params)]),
+    ("cg_mlp_param_count", I, []),
+    ("cg_mlp_create", I, [P, ctypes.c_uint64, PP]),
+    ("cg_mlp_destroy", None, [P]),
+    ("cg_mlp_configure", I, [P, ctypes.POINTER(cg_mlp_config)]),
+    ("cg_mlp_get_config", I, [P, ctypes.POINTER(cg_mlp_config)]),
+    ("cg_mlp_features", I, [P, P, P, I, FP, P, I, P]),
+    ("cg_mlp_infer", I, [P, P, I, P, I, P]),
+    ("cg_mlp_gradient", I, [P, P, P, I, F, FP, FP, I]),
+    ("cg_mlp_train", I, [P, P, P, ctypes.c_longlong, ctypes.POINTER(cg_train_params), FP]),
+    ("cg_mlp_get_params", I, [P, FP, FP, FP, ctypes.POINTER(ctypes.c_int)]),
+    ("cg_mlp_set_params", I, [P, FP, FP, FP, I]),
+    ("cg_mlp_save", I, [P, ctypes.c_char_p]),
+    ("cg_mlp_load", I, [P, ctypes.c_char_p, PP]),
+    ("cg_context_mlp_fallbacks", I, [P, U64P]),
+    ("cg_context_last_samples", I, [P, U64P]),
 ]
 NOALLOC_MAX_TEXELS = 1 << 20
 

@@ -9,15 +9,14 @@
 #include <string>
 #include <vector>
 
-#include "cg_internal.h"
-#include "cloudgb.h"
+#include "cg_host_util.h"
 
 // ---------------------------------------------------------------------------
 // errors
 // ---------------------------------------------------------------------------
 static thread_local std::string g_last_error;
 
-static cg_status fail(cg_status s, const char* fmt, ...) {
+cg_status fail(cg_status s, const char* fmt, ...) {
     char buf[512];
     va_list ap;
     va_start(ap, fmt);
@@ -26,107 +25,6 @@ static cg_status fail(cg_status s, const char* fmt, ...) {
     g_last_error = buf;
     return s;
 }
-
-#define CG_CUDA(call)                                                                      \
-    do {                                                                                   \
-        cudaError_t e_ = (call);                                                           \
-        if (e_ != cudaSuccess)                                                             \
-            return fail(e_ == cudaErrorMemoryAllocation ? CG_ERR_OUT_OF_MEMORY : CG_ERR_CUDA, \
-                        "%s: %s", #call, cudaGetErrorString(e_));                          \
-    } while (0)
-
-#define CG_CHECK(cond, status, ...)                  \
-    do {                                             \
-        if (!(cond)) return fail(status, __VA_ARGS__); \
-    } while (0)
-
-// ---------------------------------------------------------------------------
-// device buffers
-// ---------------------------------------------------------------------------
-struct DevBuf {
-    void* p = nullptr;
-    size_t bytes = 0;
-    cudaError_t ensure(size_t want) {
-        if (want <= bytes && p) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        bytes = 0;
-        cudaError_t e = cudaMalloc(&p, want ? want : 16);
-        if (e == cudaSuccess) bytes = want;
-        return e;
-    }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        bytes = 0;
-    }
-    template <class T>
-    T* as() const {
-        return reinterpret_cast<T*>(p);
-    }
-};
-
-struct HostBuf {
-    void* p = nullptr;
-    size_t bytes = 0;
-    cudaError_t ensure(size_t want) {
-        if (want <= bytes && p) return cudaSuccess;
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        bytes = 0;
-        cudaError_t e = cudaMallocHost(&p, want ? want : 16);
-        if (e == cudaSuccess) bytes = want;
-        return e;
-    }
-    void release() {
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        bytes = 0;
-    }
-};
-
-struct cg_context {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    uint64_t launches = 0;
-    DevBuf image;  // render target when the caller passes a host pointer
-    // hash-noise lattice tables of the last (noise parameters, world box)
-    DevBuf noise;
-    bool noise_valid = false;
-    uint32_t noise_seed = 0;
-    int noise_octaves = 0;
-    float noise_freq = 0, noise_lac = 0, noise_box[6] = {0, 0, 0, 0, 0, 0};
-    NoiseTab noise_tab{};
-};
-
-struct cg_volume {
-    cg_context* ctx = nullptr;
-    int D = 0, L = 0, fmt = 0;
-    float pos[3] = {0, 0, 0}, b0 = 0, b1 = 0;
-    float wmin[3], wmax[3], range[3];
-    int dims[CG_MAX_LEVELS];
-    size_t offs[CG_MAX_LEVELS];
-    size_t total = 0;
-    DevBuf pyr, count, dq, mask;
-    // boards
-    int n = 0;
-    size_t pairs = 0;
-    DevBuf cwr, q, thr, dqb, culled;
-    HostBuf h_stage;
-    Bins bins{};
-    DevBuf bcount, boff, bcursor, blist;
-    // sun map
-    int mapW = 0, mapH = 0;
-    DevBuf keys, posmap;
-    bool voxelized = false;
-    SunFrame frame{};
-    float sun_dir[3] = {0, 1, 0};
-    DevBuf scratch;  // small scalars (active voxel count)
-    DevBuf occ;      // occupancy grids (see VolDesc)
-    int occ_nb[CG_MAX_LEVELS];
-    int occ_off[CG_MAX_LEVELS];
-    int occ_total = 0;
-};
 
 // ---------------------------------------------------------------------------
 // library
@@ -171,17 +69,170 @@ extern "C" cg_status cg_context_create(int device, cg_context** out) {
     return CG_OK;
 }
 
-extern "C" void cg_context_destroy(cg_context* ctx) {
-    if (!ctx) return;
+void stage_begin(cg_context* ctx, cudaStream_t s) {
+    if (!ctx->timing) return;
+    ctx->n_marks = 0;
+    stage_mark(ctx, s, "begin");
+}
+
+void stage_mark(cg_context* ctx, cudaStream_t s, const char* name) {
+    if (!ctx->timing || ctx->n_marks >= 32) return;
+    const int i = ctx->n_marks;
+    if (!ctx->marks[i] && cudaEventCreate(&ctx->marks[i]) != cudaSuccess) return;
+    if (cudaEventRecord(ctx->marks[i], s) != cudaSuccess) return;
+    snprintf(ctx->mark_names[i], sizeof(ctx->mark_names[i]), "%s", name);
+    ctx->n_marks = i + 1;
+}
+
+extern "C" cg_status cg_context_last_samples(cg_context* ctx, uint64_t* samples) {
+    CG_CHECK(ctx && samples, CG_ERR_INVALID_ARGUMENT, "cg_context_last_samples: null pointer");
+    *samples = 0;
+    if (!ctx->samples_cnt.p || ctx->last_regions <= 0) return CG_OK;
+    CG_CUDA(cudaSetDevice(ctx->device));
+    CG_CUDA(cudaStreamSynchronize(ctx->stream));
+    unsigned total = 0;
+    CG_CUDA(cudaMemcpy(&total, ctx->samples_cnt.as<unsigned>() + 2 * ctx->last_regions, 4,
+                       cudaMemcpyDeviceToHost));
+    *samples = total;
+    return CG_OK;
+}
+
+extern "C" cg_status cg_context_set_timing(cg_context* ctx, int enable) {
+    CG_CHECK(ctx, CG_ERR_INVALID_ARGUMENT, "cg_context_set_timing: ctx is NULL");
+    ctx->timing = enable != 0;
+    ctx->n_marks = 0;
+    return CG_OK;
+}
+
+extern "C" cg_status cg_context_stage_times(cg_context* ctx, float* ms, int max_stages,
+                                            int* count, char* names, size_t names_len) {
+    CG_CHECK(ctx && ms && count, CG_ERR_INVALID_ARGUMENT, "cg_context_stage_times: null pointer");
+    CG_CUDA(cudaSetDevice(ctx->device));
+    *count = 0;
+    if (names && names_len) names[0] = '\0';
+    size_t used = 0;
+    for (int i = 1; i < ctx->n_marks && *count < max_stages; ++i) {
+        CG_CUDA(cudaEventSynchronize(ctx->marks[i]));
+        float t = 0.f;
+        CG_CUDA(cudaEventElapsedTime(&t, ctx->marks[i - 1], ctx->marks[i]));
+        ms[(*count)++] = t;
+        if (names && used + 1 < names_len) {
+            int w = snprintf(names + used, names_len - used, "%s%s", i > 1 ? ";" : "",
+                             ctx->mark_names[i]);
+            if (w > 0) used += (size_t)w;
+        }
+    }
+    return CG_OK;
+}
+
+void release_noise_textures(cg_context* ctx) {
+    for (int o = 0; o < CG_MAX_LEVELS; ++o) {
+        if (ctx->noise_tex[o]) cudaDestroyTextureObject(ctx->noise_tex[o]);
+        if (ctx->noise_arr[o]) cudaFreeArray(ctx->noise_arr[o]);
+        ctx->noise_tex[o] = 0;
+        ctx->noise_arr[o] = nullptr;
+    }
+    if (ctx->fbm_tex) cudaDestroyTextureObject(ctx->fbm_tex);
+    if (ctx->fbm_surf) cudaDestroySurfaceObject(ctx->fbm_surf);
+    if (ctx->fbm_arr) cudaFreeArray(ctx->fbm_arr);
+    ctx->fbm_tex = 0;
+    ctx->fbm_surf = 0;
+    ctx->fbm_arr = nullptr;
+    ctx->fbm_res = 0;
+    ctx->fbm_valid = false;
+}
+
+// The fBm of the current noise tables sampled at R^3 texel centres over the
+// volume's box (R = 8 texels per finest lattice cell, at most 512), as a
+// half-precision 3D texture: one fetch per view sample in the surrogate path.
+cg_status ensure_fbm_volume(cg_context* ctx, const cg_volume* v, TraceParams& tp, cudaStream_t s) {
+    if (tp.noise_octaves <= 0 || !ctx->noise_valid) return CG_OK;
+    if (!ctx->fbm_valid) {
+        double fmax = (double)tp.noise_freq;
+        for (int o = 1; o < tp.noise_octaves; ++o) fmax *= (double)tp.noise_lac;
+        double rmax = std::max((double)v->range[0], std::max((double)v->range[1], (double)v->range[2]));
+        double cells = std::ceil(std::fabs(fmax) * rmax);
+        int R = (int)std::min(512.0, std::max(8.0, 8.0 * cells));
+        cudaChannelFormatDesc fd = cudaCreateChannelDescHalf();
+        CG_CUDA(cudaMalloc3DArray(&ctx->fbm_arr, &fd, make_cudaExtent(R, R, R),
+                                  cudaArraySurfaceLoadStore));
+        cudaResourceDesc rd = {};
+        rd.resType = cudaResourceTypeArray;
+        rd.res.array.array = ctx->fbm_arr;
+        CG_CUDA(cudaCreateSurfaceObject(&ctx->fbm_surf, &rd));
+        cudaTextureDesc td = {};
+        td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeClamp;
+        td.filterMode = cudaFilterModeLinear;
+        td.readMode = cudaReadModeElementType;
+        td.normalizedCoords = 0;
+        CG_CUDA(cudaCreateTextureObject(&ctx->fbm_tex, &rd, &td, nullptr));
+        CG_LAUNCH(ctx, launch_fbm_volume(tp, v->wmin, v->range, R, ctx->fbm_surf, s));
+        ctx->fbm_res = R;
+        ctx->fbm_valid = true;
+        ctx->noise_tab.fbm_tex = ctx->fbm_tex;
+        ctx->noise_tab.fbm_res = R;
+    }
+    tp.nt.fbm_tex = ctx->fbm_tex;
+    tp.nt.fbm_res = ctx->fbm_res;
+    return CG_OK;
+}
+
+// Half2 (density, light) texture copies of every level for the surrogate
+// renderer: arrays created on first use, refreshed after each voxelize.
+cg_status ensure_textures(cg_volume* v, cudaStream_t s) {
+    if (!v->tex_arr[0]) {
+        for (int l = 0; l < v->L; ++l) {
+            cudaChannelFormatDesc fd = cudaCreateChannelDescHalf2();
+            cudaExtent ext = make_cudaExtent(v->dims[l], v->dims[l], v->dims[l]);
+            CG_CUDA(cudaMalloc3DArray(&v->tex_arr[l], &fd, ext, cudaArraySurfaceLoadStore));
+            cudaResourceDesc rd = {};
+            rd.resType = cudaResourceTypeArray;
+            rd.res.array.array = v->tex_arr[l];
+            CG_CUDA(cudaCreateSurfaceObject(&v->tex_surf[l], &rd));
+            cudaTextureDesc td = {};
+            td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeBorder;
+            td.filterMode = cudaFilterModeLinear;
+            td.readMode = cudaReadModeElementType;
+            td.normalizedCoords = 0;
+            CG_CUDA(cudaCreateTextureObject(&v->tex_obj[l], &rd, &td, nullptr));
+        }
+    }
+    if (v->tex_gen != v->gen) {
+        const VolDesc vd = desc_of(v);
+        for (int l = 0; l < v->L; ++l)
+            CG_LAUNCH(v->ctx, launch_pack_level(vd, l, v->tex_surf[l], s));
+        v->tex_gen = v->gen;
+    }
+    return CG_OK;
+}
+
+// Volumes and models hold a reference on their context, so the context's
+// resources outlive every object created on it whatever the destroy order.
+void context_retain(cg_context* ctx) { ctx->refs++; }
+
+void context_release(cg_context* ctx) {
+    if (--ctx->refs > 0) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     ctx->image.release();
     ctx->noise.release();
+    ctx->samples_pw.release();
+    ctx->samples_gl.release();
+    ctx->samples_cnt.release();
+    ctx->fallbacks.release();
+    release_noise_textures(ctx);
+    for (cudaEvent_t e : ctx->marks)
+        if (e) cudaEventDestroy(e);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
 
-static cudaStream_t pick(cg_context* ctx, void* stream) {
+extern "C" void cg_context_destroy(cg_context* ctx) {
+    if (!ctx) return;
+    context_release(ctx);
+}
+
+cudaStream_t pick_stream(cg_context* ctx, void* stream) {
     return stream ? reinterpret_cast<cudaStream_t>(stream) : ctx->stream;
 }
 
@@ -266,6 +317,7 @@ extern "C" cg_status cg_volume_create(cg_context* ctx, int dimension, float boun
     CG_CUDA(cudaSetDevice(ctx->device));
     cg_volume* v = new cg_volume();
     v->ctx = ctx;
+    context_retain(ctx);
     v->D = dimension;
     v->L = mips;
     v->fmt = format;
@@ -332,7 +384,14 @@ extern "C" void cg_volume_destroy(cg_volume* v) {
                       &v->keys, &v->posmap, &v->scratch, &v->occ};
     for (DevBuf* b : bufs) b->release();
     v->h_stage.release();
+    for (int l = 0; l < CG_MAX_LEVELS; ++l) {
+        if (v->tex_obj[l]) cudaDestroyTextureObject(v->tex_obj[l]);
+        if (v->tex_surf[l]) cudaDestroySurfaceObject(v->tex_surf[l]);
+        if (v->tex_arr[l]) cudaFreeArray(v->tex_arr[l]);
+    }
+    cg_context* ctx = v->ctx;
     delete v;
+    context_release(ctx);
 }
 
 static long long floor_div_ll(long long a, long long b) {
@@ -450,7 +509,7 @@ extern "C" cg_status cg_volume_set_billboards(cg_volume* v, const float* positio
     return CG_OK;
 }
 
-static BoardsDev boards_of(const cg_volume* v) {
+BoardsDev boards_of(const cg_volume* v) {
     BoardsDev b;
     b.n = v->n;
     b.cwr = v->cwr.as<const float4>();
@@ -461,7 +520,7 @@ static BoardsDev boards_of(const cg_volume* v) {
     return b;
 }
 
-static VolDesc desc_of(const cg_volume* v) {
+VolDesc desc_of(const cg_volume* v) {
     VolDesc d;
     d.D = v->D;
     d.L = v->L;
@@ -476,6 +535,7 @@ static VolDesc desc_of(const cg_volume* v) {
     }
     d.pyr = v->pyr.p;
     d.occ = v->occ.as<const uint8_t>() + v->occ_total;
+    for (int l = 0; l < CG_MAX_LEVELS; ++l) d.tex[l] = v->tex_obj[l];
     for (int l = 0; l < CG_MAX_LEVELS; ++l) {
         d.occ_nb[l] = v->occ_nb[l];
         d.occ_off[l] = v->occ_off[l];
@@ -551,13 +611,6 @@ static float highlight_offset(const cg_volume* v) {
     return step * 0.57735026f;
 }
 
-#define CG_LAUNCH(ctx, expr)                                                          \
-    do {                                                                              \
-        cudaError_t e_ = (expr);                                                      \
-        if (e_ != cudaSuccess)                                                        \
-            return fail(CG_ERR_CUDA, "%s: %s", #expr, cudaGetErrorString(e_));        \
-        (ctx)->launches++;                                                            \
-    } while (0)
 
 extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) {
     CG_CHECK(v && sun, CG_ERR_INVALID_ARGUMENT, "cg_voxelize: null pointer");
@@ -574,7 +627,7 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
              "cg_voxelize: sun direction is zero or parallel to the up axis (0,1,0)");
     cg_context* ctx = v->ctx;
     CG_CUDA(cudaSetDevice(ctx->device));
-    cudaStream_t s = pick(ctx, stream);
+    cudaStream_t s = pick_stream(ctx, stream);
     const size_t texels = (size_t)sun->map_width * sun->map_height;
     if (v->mapW != sun->map_width || v->mapH != sun->map_height) {
         CG_CUDA(cudaStreamSynchronize(s));
@@ -593,6 +646,7 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
     bins.cursor = v->bcursor.as<uint32_t>();
     bins.list = v->blist.as<uint32_t>();
     VolDesc vd = desc_of(v);
+    stage_begin(ctx, s);
     // clearGPU (CloudVolume.cpp:96-100) + clearPositionMap (VoxelizeShader.cpp:185-187)
     CG_CUDA(cudaMemsetAsync(v->keys.p, 0xFF, texels * 8, s));
     CG_CUDA(cudaMemsetAsync(v->mask.p, 0, n0, s));
@@ -602,29 +656,35 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
     if (b.n) CG_LAUNCH(ctx, launch_bin_count(b, v->D, bins, s));
     CG_LAUNCH(ctx, launch_bin_scan(bins, s));
     if (b.n) CG_LAUNCH(ctx, launch_bin_fill(b, v->D, bins, s));
+    stage_mark(ctx, s, "bins");
     // pass 1: sun-view nearest-surface map
     if (b.n) CG_LAUNCH(ctx, launch_sunmap(b, fr, v->keys.as<uint64_t>(), s));
+    stage_mark(ctx, s, "sunmap");
     // pass 2: highlight stores
     CG_LAUNCH(ctx, launch_highlight(b, fr, v->keys.as<uint64_t>(), v->posmap.as<float4>(), v->D,
                                     v->wmin, v->range, highlight_offset(v),
                                     v->mask.as<uint8_t>(), s));
+    stage_mark(ctx, s, "highlight");
     // coverage splat + level 0 + fused mips
     int fused = (v->D % CG_BRICK == 0) ? std::min(CG_FUSED_MIPS, v->L - 1) : 0;
     CG_LAUNCH(ctx, launch_splat(b, bins, v->mask.as<uint8_t>(), vd, v->pyr.p,
                                 v->count.as<uint32_t>(), v->dq.as<uint32_t>(), fused,
                                 v->occ.as<uint8_t>(), s));
+    stage_mark(ctx, s, "splat");
     CG_LAUNCH(ctx, launch_occ_dilate(vd, v->occ.as<uint8_t>(), v->occ.as<uint8_t>() + v->occ_total,
                                      v->occ_total, s));
     // remaining mips (glGenerateMipmap, VoxelizeShader.cpp:105)
     for (int l = fused; l + 1 < v->L; ++l) CG_LAUNCH(ctx, launch_mip_level(vd, v->pyr.p, l, s));
+    stage_mark(ctx, s, "mips");
     v->voxelized = true;
+    v->gen++;
     return CG_OK;
 }
 
 // ---------------------------------------------------------------------------
 // render
 // ---------------------------------------------------------------------------
-static cg_status check_params(const cg_render_params* p) {
+cg_status check_params(const cg_render_params* p) {
     CG_CHECK(p->view_steps >= 1 && p->view_steps <= 4096, CG_ERR_OUT_OF_RANGE,
              "render params: view_steps %d not in [1, 4096]", p->view_steps);
     CG_CHECK(p->sun_steps >= 0 && p->sun_steps <= 64, CG_ERR_OUT_OF_RANGE,
@@ -660,7 +720,7 @@ static cg_status check_params(const cg_render_params* p) {
     return CG_OK;
 }
 
-static TraceParams trace_params_of(const cg_render_params* p, const float sun_dir[3]) {
+TraceParams trace_params_of(const cg_render_params* p, const float sun_dir[3]) {
     TraceParams tp;
     tp.view_steps = p->view_steps;
     tp.sun_steps = p->sun_steps;
@@ -694,7 +754,7 @@ static TraceParams trace_params_of(const cg_render_params* p, const float sun_di
     return tp;
 }
 
-static cg_status camera_of(const cg_camera* c, CamDesc& cam) {
+cg_status camera_of(const cg_camera* c, CamDesc& cam) {
     for (int a = 0; a < 3; ++a)
         CG_CHECK(std::isfinite(c->eye[a]) && std::isfinite(c->target[a]) &&
                      std::isfinite(c->up[a]),
@@ -737,7 +797,7 @@ static cg_status camera_of(const cg_camera* c, CamDesc& cam) {
 // rebuilt only when those change.  Each octave covers floor(wmin*f) - 1 ..
 // floor(wmax*f) + 2 per axis, f = frequency * lacunarity^o in FP32 as the
 // kernel computes it; samples outside fall back to hashing.
-static cg_status ensure_noise(cg_context* ctx, const cg_volume* v, TraceParams& tp,
+cg_status ensure_noise(cg_context* ctx, const cg_volume* v, TraceParams& tp,
                               cudaStream_t s) {
     if (tp.noise_octaves <= 0) return CG_OK;
     float box[6] = {v->wmin[0], v->wmin[1], v->wmin[2], v->wmax[0], v->wmax[1], v->wmax[2]};
@@ -776,6 +836,31 @@ static cg_status ensure_noise(cg_context* ctx, const cg_volume* v, TraceParams& 
             nt.tab = ctx->noise.as<const float>();
             tp.nt = nt;
             CG_LAUNCH(ctx, launch_noise_table(tp, ctx->noise.as<float>(), (int)total, s));
+            // the same tables as 3D float textures (linear filter, unnormalised)
+            release_noise_textures(ctx);
+            for (int o = 0; o < tp.noise_octaves; ++o) {
+                cudaChannelFormatDesc fd = cudaCreateChannelDesc<float>();
+                cudaExtent ext = make_cudaExtent(nt.dim[o][0], nt.dim[o][1], nt.dim[o][2]);
+                CG_CUDA(cudaMalloc3DArray(&ctx->noise_arr[o], &fd, ext));
+                cudaMemcpy3DParms cp = {};
+                cp.srcPtr = make_cudaPitchedPtr(ctx->noise.as<float>() + nt.off[o],
+                                                (size_t)nt.dim[o][0] * 4, nt.dim[o][0],
+                                                nt.dim[o][1]);
+                cp.dstArray = ctx->noise_arr[o];
+                cp.extent = ext;
+                cp.kind = cudaMemcpyDeviceToDevice;
+                CG_CUDA(cudaMemcpy3DAsync(&cp, s));
+                cudaResourceDesc rd = {};
+                rd.resType = cudaResourceTypeArray;
+                rd.res.array.array = ctx->noise_arr[o];
+                cudaTextureDesc td = {};
+                td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeClamp;
+                td.filterMode = cudaFilterModeLinear;
+                td.readMode = cudaReadModeElementType;
+                td.normalizedCoords = 0;
+                CG_CUDA(cudaCreateTextureObject(&ctx->noise_tex[o], &rd, &td, nullptr));
+                nt.tex[o] = ctx->noise_tex[o];
+            }
             ctx->noise_tab = nt;
             ctx->noise_valid = true;
             ctx->noise_seed = tp.noise_seed;
@@ -800,12 +885,16 @@ extern "C" cg_status cg_render(cg_context* ctx, const cg_volume* v, const cg_cam
     CG_CHECK(v->voxelized, CG_ERR_NOT_READY, "cg_render: volume has not been voxelized");
     cg_status st = check_params(params);
     if (st != CG_OK) return st;
-    CG_CHECK(!params->use_mlp, CG_ERR_UNSUPPORTED, "cg_render: MLP surrogate not loaded");
     CamDesc cd;
     st = camera_of(cam, cd);
     if (st != CG_OK) return st;
+    MlpDev md;
+    if (params->use_mlp) {
+        st = mlp_device_for_render(params->mlp, v, params, md);
+        if (st != CG_OK) return st;
+    }
     CG_CUDA(cudaSetDevice(ctx->device));
-    cudaStream_t s = pick(ctx, stream);
+    cudaStream_t s = pick_stream(ctx, stream);
     const size_t pixels = (size_t)cam->width * cam->height;
     float4* out = reinterpret_cast<float4*>(rgba_out);
     if (!out_on_device) {
@@ -813,9 +902,42 @@ extern "C" cg_status cg_render(cg_context* ctx, const cg_volume* v, const cg_cam
         out = ctx->image.as<float4>();
     }
     TraceParams tp = trace_params_of(params, v->sun_dir);
+    stage_begin(ctx, s);
     st = ensure_noise(ctx, v, tp, s);
     if (st != CG_OK) return st;
-    CG_LAUNCH(ctx, launch_trace_fused(desc_of(v), cd, tp, out, nullptr, s));
+    if (params->use_mlp) {
+        st = ensure_textures(const_cast<cg_volume*>(v), s);
+        if (st == CG_OK) st = ensure_fbm_volume(ctx, v, tp, s);
+        if (st != CG_OK) return st;
+        stage_mark(ctx, s, "textures");
+    }
+    const VolDesc vd = desc_of(v);
+    if (params->use_mlp || params->pipeline == CG_PIPELINE_DEFERRED) {
+        // deferred: march records the contributing samples, shading resolves them
+        SampleBuf sb;
+        st = ensure_samples(ctx, cam->width, cam->height, params->view_steps, sb);
+        if (st != CG_OK) return st;
+        CG_LAUNCH(ctx, launch_march(vd, cd, tp, sb, out, params->use_mlp != 0, s));
+        stage_mark(ctx, s, "march");
+        if (params->use_mlp) {
+            CG_CUDA(cudaMemsetAsync(ctx->fallbacks.p, 0, 8, s));
+            CG_LAUNCH(ctx, launch_region_scan(cd, sb, sb.offset, s));
+            ctx->launches++;  // the scan and the chunk-table fill
+            ctx->last_regions = ((cam->width + 15) / 16) * ((cam->height + 15) / 16) * 8;
+            stage_mark(ctx, s, "scan");
+            CG_LAUNCH(ctx, launch_shade_mlp(vd, cd, tp, md, sb, sb.offset,
+                                            ctx->fallbacks.as<unsigned long long>(), s));
+            stage_mark(ctx, s, "shade_mlp");
+            CG_LAUNCH(ctx, launch_accumulate(cd, tp, sb, out, s));
+            stage_mark(ctx, s, "accumulate");
+        } else {
+            CG_LAUNCH(ctx, launch_shade_exact(vd, cd, tp, sb, out, s));
+            stage_mark(ctx, s, "shade_exact");
+        }
+    } else {
+        CG_LAUNCH(ctx, launch_trace_fused(vd, cd, tp, out, nullptr, s));
+        stage_mark(ctx, s, "trace");
+    }
     if (!out_on_device) {
         CG_CUDA(cudaMemcpyAsync(rgba_out, out, pixels * 16, cudaMemcpyDeviceToHost, s));
         CG_CUDA(cudaStreamSynchronize(s));
@@ -858,6 +980,53 @@ extern "C" cg_status cg_render_stats(cg_context* ctx, const cg_volume* v, const 
     return CG_OK;
 }
 
+extern "C" cg_status cg_march_samples(cg_context* ctx, const cg_volume* v, const cg_camera* cam,
+                                      const cg_render_params* params, float* positions,
+                                      float* weights, int capacity, int* count) {
+    CG_CHECK(ctx && v && cam && params && count && (capacity == 0 || (positions && weights)),
+             CG_ERR_INVALID_ARGUMENT, "cg_march_samples: null pointer");
+    CG_CHECK(capacity >= 0, CG_ERR_OUT_OF_RANGE, "cg_march_samples: capacity < 0");
+    CG_CHECK(v->ctx == ctx, CG_ERR_INVALID_ARGUMENT, "cg_march_samples: volume of another context");
+    CG_CHECK(v->voxelized, CG_ERR_NOT_READY, "cg_march_samples: volume has not been voxelized");
+    cg_status st = check_params(params);
+    if (st != CG_OK) return st;
+    CamDesc cd;
+    st = camera_of(cam, cd);
+    if (st != CG_OK) return st;
+    CG_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    const size_t pixels = (size_t)cam->width * cam->height;
+    CG_CUDA(ctx->image.ensure(pixels * 16));
+    TraceParams tp = trace_params_of(params, v->sun_dir);
+    st = ensure_noise(ctx, v, tp, s);
+    if (st != CG_OK) return st;
+    SampleBuf sb;
+    st = ensure_samples(ctx, cam->width, cam->height, params->view_steps, sb);
+    if (st != CG_OK) return st;
+    CG_LAUNCH(ctx, launch_march(desc_of(v), cd, tp, sb, ctx->image.as<float4>(), false, s));
+    const size_t regions = (size_t)((cam->width + 15) / 16) * ((cam->height + 15) / 16) * 8;
+    std::vector<unsigned> cnt(regions);
+    CG_CUDA(cudaMemcpyAsync(cnt.data(), sb.count, regions * 4, cudaMemcpyDeviceToHost, s));
+    CG_CUDA(cudaStreamSynchronize(s));
+    size_t total = 0;
+    std::vector<float4> tmp;
+    for (size_t r = 0; r < regions; ++r) {
+        if (!cnt[r]) continue;
+        tmp.resize(cnt[r]);
+        CG_CUDA(cudaMemcpy(tmp.data(), sb.pos_w + r * (size_t)sb.capacity, cnt[r] * 16,
+                           cudaMemcpyDeviceToHost));
+        for (unsigned i = 0; i < cnt[r]; ++i, ++total) {
+            if (total >= (size_t)capacity) continue;
+            positions[3 * total] = tmp[i].x;
+            positions[3 * total + 1] = tmp[i].y;
+            positions[3 * total + 2] = tmp[i].z;
+            weights[total] = tmp[i].w;
+        }
+    }
+    *count = (int)std::min(total, (size_t)0x7FFFFFFF);
+    return CG_OK;
+}
+
 extern "C" cg_status cg_trace_cones(const cg_volume* v, const float* positions, int n,
                                     const float direction[3], const cg_render_params* params,
                                     float* out, int on_device, void* stream) {
@@ -874,7 +1043,7 @@ extern "C" cg_status cg_trace_cones(const cg_volume* v, const float* positions, 
     if (n == 0) return CG_OK;
     cg_context* ctx = v->ctx;
     CG_CUDA(cudaSetDevice(ctx->device));
-    cudaStream_t s = pick(ctx, stream);
+    cudaStream_t s = pick_stream(ctx, stream);
     TraceParams tp = trace_params_of(params, direction);
     const float* dpos = positions;
     float* dout = out;

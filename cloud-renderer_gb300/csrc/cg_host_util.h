@@ -1,0 +1,179 @@
+// cg_host_util.h -- host-side internals shared by the C-ABI translation units:
+// error reporting, device/host buffers and the context and volume objects.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "cg_internal.h"
+#include "cloudgb.h"
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+cg_status fail(cg_status s, const char* fmt, ...);
+
+#define CG_CUDA(call)                                                                      \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess)                                                             \
+            return fail(e_ == cudaErrorMemoryAllocation ? CG_ERR_OUT_OF_MEMORY : CG_ERR_CUDA, \
+                        "%s: %s", #call, cudaGetErrorString(e_));                          \
+    } while (0)
+
+#define CG_CHECK(cond, status, ...)                  \
+    do {                                             \
+        if (!(cond)) return fail(status, __VA_ARGS__); \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// device buffers
+// ---------------------------------------------------------------------------
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t want) {
+        if (want <= bytes && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, want ? want : 16);
+        if (e == cudaSuccess) bytes = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <class T>
+    T* as() const {
+        return reinterpret_cast<T*>(p);
+    }
+};
+
+struct HostBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t want) {
+        if (want <= bytes && p) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMallocHost(&p, want ? want : 16);
+        if (e == cudaSuccess) bytes = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+    }
+};
+
+struct cg_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint64_t launches = 0;
+    int refs = 1;  // the caller's handle + one per volume / model created on it
+    int last_regions = 0;  // regions of the last surrogate render (sample total lookup)
+    // optional per-stage CUDA-event timing of voxelize/render calls
+    bool timing = false;
+    int n_marks = 0;
+    cudaEvent_t marks[32] = {};
+    char mark_names[32][24] = {};
+    DevBuf image;  // render target when the caller passes a host pointer
+    // hash-noise lattice tables of the last (noise parameters, world box)
+    DevBuf noise;
+    bool noise_valid = false;
+    uint32_t noise_seed = 0;
+    int noise_octaves = 0;
+    float noise_freq = 0, noise_lac = 0, noise_box[6] = {0, 0, 0, 0, 0, 0};
+    NoiseTab noise_tab{};
+    // deferred renderer: recorded view samples and the MLP fallback counter
+    DevBuf samples_pw, samples_gl, samples_cnt;
+    DevBuf fallbacks;
+    // noise lattice tables as 3D float textures (surrogate renderer)
+    cudaArray_t noise_arr[CG_MAX_LEVELS] = {};
+    cudaTextureObject_t noise_tex[CG_MAX_LEVELS] = {};
+    // the fBm sampled on a grid (surrogate renderer), valid for the current tables
+    cudaArray_t fbm_arr = nullptr;
+    cudaSurfaceObject_t fbm_surf = 0;
+    cudaTextureObject_t fbm_tex = 0;
+    int fbm_res = 0;
+    bool fbm_valid = false;
+};
+
+void release_noise_textures(cg_context* ctx);
+cg_status ensure_fbm_volume(cg_context* ctx, const cg_volume* v, TraceParams& tp, cudaStream_t s);
+
+struct cg_volume {
+    cg_context* ctx = nullptr;
+    int D = 0, L = 0, fmt = 0;
+    float pos[3] = {0, 0, 0}, b0 = 0, b1 = 0;
+    float wmin[3], wmax[3], range[3];
+    int dims[CG_MAX_LEVELS];
+    size_t offs[CG_MAX_LEVELS];
+    size_t total = 0;
+    DevBuf pyr, count, dq, mask;
+    // boards
+    int n = 0;
+    size_t pairs = 0;
+    DevBuf cwr, q, thr, dqb, culled;
+    HostBuf h_stage;
+    Bins bins{};
+    DevBuf bcount, boff, bcursor, blist;
+    // sun map
+    int mapW = 0, mapH = 0;
+    DevBuf keys, posmap;
+    bool voxelized = false;
+    SunFrame frame{};
+    float sun_dir[3] = {0, 1, 0};
+    DevBuf scratch;  // small scalars (active voxel count)
+    DevBuf occ;      // occupancy grids (see VolDesc)
+    int occ_nb[CG_MAX_LEVELS];
+    int occ_off[CG_MAX_LEVELS];
+    int occ_total = 0;
+    // half2 texture copies of the levels for the surrogate renderer, rebuilt
+    // lazily after each voxelize (gen counts voxelizations)
+    cudaArray_t tex_arr[CG_MAX_LEVELS] = {};
+    cudaSurfaceObject_t tex_surf[CG_MAX_LEVELS] = {};
+    cudaTextureObject_t tex_obj[CG_MAX_LEVELS] = {};
+    long long gen = 0, tex_gen = -1;
+};
+
+cg_status ensure_textures(cg_volume* v, cudaStream_t s);
+
+VolDesc desc_of(const cg_volume* v);
+BoardsDev boards_of(const cg_volume* v);
+cg_status check_params(const cg_render_params* p);
+TraceParams trace_params_of(const cg_render_params* p, const float sun_dir[3]);
+cg_status camera_of(const cg_camera* c, CamDesc& cam);
+cg_status ensure_noise(cg_context* ctx, const cg_volume* v, TraceParams& tp, cudaStream_t s);
+cudaStream_t pick_stream(cg_context* ctx, void* stream);
+void context_retain(cg_context* ctx);
+void context_release(cg_context* ctx);
+// Stage timing: stage_begin records the start event of a call, stage_mark the
+// end of a named stage (no-ops unless timing is on).
+void stage_begin(cg_context* ctx, cudaStream_t s);
+void stage_mark(cg_context* ctx, cudaStream_t s, const char* name);
+
+// cg_mlp.cpp
+struct SampleBuf;
+struct MlpDev;
+cg_status ensure_samples(cg_context* ctx, int width, int height, int view_steps, SampleBuf& sb);
+cg_status mlp_device_for_render(const cg_mlp* m, const cg_volume* v, const cg_render_params* p,
+                                MlpDev& md);
+
+#define CG_LAUNCH(ctx, expr)                                                          \
+    do {                                                                              \
+        cudaError_t e_ = (expr);                                                      \
+        if (e_ != cudaSuccess)                                                        \
+            return fail(CG_ERR_CUDA, "%s: %s", #expr, cudaGetErrorString(e_));        \
+        (ctx)->launches++;                                                            \
+    } while (0)

@@ -1,6 +1,7 @@
 // cg_internal.h -- structures shared by the host library and the kernels.
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -35,6 +36,9 @@ struct VolDesc {
     const uint8_t* occ;             // occupancy grids, concatenated by level
     int occ_nb[CG_MAX_LEVELS];
     int occ_off[CG_MAX_LEVELS];
+    // hardware-filtered half2 (density, light) copies of the levels for the
+    // surrogate renderer (cudaTextureObject_t; 0 when not built)
+    unsigned long long tex[CG_MAX_LEVELS];
 };
 
 // Hash-noise lattice values tabulated per octave over the world box: octave
@@ -46,6 +50,12 @@ struct NoiseTab {
     int off[CG_MAX_LEVELS];
     int lo[CG_MAX_LEVELS][3];
     int dim[CG_MAX_LEVELS][3];
+    // the same tables as 3D float textures for the surrogate renderer (0 = none)
+    unsigned long long tex[CG_MAX_LEVELS];
+    // the whole fBm sampled on a fbm_res^3 grid of texel centres over the world
+    // box (surrogate renderer; 8 texels per finest lattice cell)
+    unsigned long long fbm_tex;
+    int fbm_res;
 };
 
 // Camera in FP32 for the trace kernels.
@@ -85,6 +95,110 @@ struct Bins {
     uint32_t* cursor;  // nbricks
     uint32_t* list;    // pairs
 };
+
+// ---- deferred renderer ----------------------------------------------------
+// View samples recorded by the march pass, one region of `capacity` slots per
+// warp (8x4 pixel tile).  pos_w = level-0 voxel position + weight T*alpha;
+// light_lane = light channel G + the pixel's lane (int bits).
+struct SampleBuf {
+    float4* pos_w;
+    float2* light_lane;
+    unsigned* count;  // samples per region
+    unsigned* offset; // exclusive scan of count (regions + 1)
+    unsigned* chunk_region;  // region of the first sample of each 32-sample chunk
+    uint2* steps;     // per region, per emitting step: (first slot, lane ballot)
+    unsigned* nsteps; // emitting steps per region
+    int capacity;     // 32 * view_steps
+};
+
+// ---- MLP surrogate ----------------------------------------------------------
+#define MLP_IN 16
+#define MLP_H 64
+// flat FP32 parameter vector: W stored [out][in]
+#define MLP_W1 0
+#define MLP_B1 1024
+#define MLP_W2 1088
+#define MLP_B2 5184
+#define MLP_W3 5248
+#define MLP_B3 9344
+#define MLP_W4 9408
+#define MLP_B4 9472
+#define MLP_NPARAM 9473
+// FP16 weight image: W1 [64][16], W2 [64][64], W3 [64][64], W4 [8][64] (rows 1-7 zero)
+#define MLP_H_W1 0
+#define MLP_H_W2 1024
+#define MLP_H_W3 5120
+#define MLP_H_W4 9216
+#define MLP_NHALF 9728
+
+// Feature geometry and normalisation of a trained model.
+//   f[3i+k] = R at level lb+i (clamped to the pyramid) sampled at
+//             v + (h0 + (k + 0.5) * 2^(lb+i)) * s,   i = 0..3, k = 0..2
+//   f[12..14] = v / D,  f[15] = s.y (cosine of the sun's zenith angle)
+// Inputs are normalised x = (f - mu) * inv_sd; the output y gives
+// tau = tau_scale * softplus(y).  Samples with a feature outside
+// [fmin, fmax] fall back to the exact cone.
+struct MlpDev {
+    const float* params;  // FP32 master (biases read from here)
+    const __half* w16;    // FP16 weight image
+    float mu[MLP_IN], inv_sd[MLP_IN], fmin[MLP_IN], fmax[MLP_IN];
+    float tau_scale;
+    float h0;
+    int lb;
+};
+
+struct TrainArgs {
+    const float* feat;  // [N][16] raw features
+    const float* tau;   // [N] exact optical depth
+    long long N;
+    unsigned long long perm_mul;  // multiplier coprime with N
+    float mu[16], inv_sd[16];
+    float tau_scale, sigma;
+    const float* params;
+    const __half* w16;
+    float* partial;   // [ctas][MLP_NPARAM + 1]
+    const int* step;  // device step counter (NULL: 0)
+    int batch;
+    int sequential;   // 1: rows offset + r (gradient evaluation), padding past N
+    long long offset;
+};
+
+struct AdamArgs {
+    const float* partial;
+    int nparts;
+    float inv_batch;
+    float* params;
+    __half* w16;
+    float* m;
+    float* v;
+    float lr, beta1, beta2, eps;
+    int* step;           // device step counter (NULL: single evaluation)
+    unsigned* ticket;    // last-CTA detection
+    float* grad_out;     // non-NULL: write the reduced gradient, no update
+    float* loss_out;     // mean loss; index step - loss_base (or 0)
+    int loss_slot_by_step;
+    int loss_base;
+};
+
+cudaError_t launch_march(VolDesc vd, CamDesc cam, TraceParams tp, SampleBuf sb, float4* out,
+                         bool hw, cudaStream_t st);
+cudaError_t launch_shade_exact(VolDesc vd, CamDesc cam, TraceParams tp, SampleBuf sb,
+                               float4* out, cudaStream_t st);
+cudaError_t launch_pack_level(VolDesc vd, int l, cudaSurfaceObject_t surf, cudaStream_t st);
+cudaError_t launch_fbm_volume(TraceParams tp, const float wmin[3], const float range[3], int R,
+                              cudaSurfaceObject_t surf, cudaStream_t st);
+cudaError_t launch_region_scan(CamDesc cam, SampleBuf sb, unsigned* offset, cudaStream_t st);
+cudaError_t launch_shade_mlp(VolDesc vd, CamDesc cam, TraceParams tp, const MlpDev& m,
+                             SampleBuf sb, const unsigned* offset,
+                             unsigned long long* fallbacks, cudaStream_t st);
+cudaError_t launch_accumulate(CamDesc cam, TraceParams tp, SampleBuf sb, float4* out,
+                              cudaStream_t st);
+cudaError_t launch_mlp_features(VolDesc vd, const MlpDev& m, const float* pos, int n,
+                                const float dir[3], float* out, cudaStream_t st);
+cudaError_t launch_mlp_infer(const MlpDev& m, const float* feat, int n, float* out,
+                             cudaStream_t st);
+cudaError_t launch_mlp_train(const TrainArgs& ta, int ctas, cudaStream_t st);
+cudaError_t launch_mlp_adam(const AdamArgs& aa, cudaStream_t st);
 
 // Message returned by cg_last_error() on this thread (cg_host.cpp).
 void set_last_error(const char* msg);

@@ -140,6 +140,37 @@ __device__ __forceinline__ float2 quad(const VolDesc& vd, float px, float py, fl
     return quad_split<FMT, WANT_G, BORDER, SKIP_EMPTY>(vd, px, py, pz, l0, lod - (float)l0);
 }
 
+// ---- hardware-filtered sampling (surrogate renderer) ----------------------
+// Same coordinates as tri(): the texture unit samples texel space at
+// (p * N_l / D) with unnormalised coordinates, so its trilinear weights match
+// the software path up to their 8-bit fixed-point precision; border
+// addressing reads 0 outside the level.
+template <bool SKIP_EMPTY>
+__device__ __forceinline__ float2 tri_hw(const VolDesc& vd, int l, float px, float py, float pz) {
+    const float sc = (float)vd.dims[l] / (float)vd.D;
+    const float x = px * sc, y = py * sc, z = pz * sc;
+    if (SKIP_EMPTY && !occupied(vd, l, (int)floorf(x - 0.5f), (int)floorf(y - 0.5f),
+                                (int)floorf(z - 0.5f)))
+        return make_float2(0.f, 0.f);
+    return tex3D<float2>((cudaTextureObject_t)vd.tex[l], x, y, z);
+}
+
+template <bool SKIP_EMPTY>
+__device__ __forceinline__ float2 quad_hw(const VolDesc& vd, float px, float py, float pz,
+                                          float lod) {
+    const float maxl = (float)(vd.L - 1);
+    lod = fminf(fmaxf(lod, 0.f), maxl);
+    const int l0 = (int)floorf(lod);
+    const float fr = lod - (float)l0;
+    float2 a = tri_hw<SKIP_EMPTY>(vd, l0, px, py, pz);
+    if (fr > 0.f && l0 + 1 < vd.L) {
+        float2 b = tri_hw<SKIP_EMPTY>(vd, l0 + 1, px, py, pz);
+        a.x = a.x + fr * (b.x - a.x);
+        a.y = a.y + fr * (b.y - a.y);
+    }
+    return a;
+}
+
 // Neumaier compensated accumulation.
 __device__ __forceinline__ void neumaier(float& sum, float& comp, float term) {
     float t = sum + term;
@@ -261,6 +292,47 @@ __device__ __forceinline__ float value_noise(const TraceParams& tp, int o, float
         c[7] = lattice(ix + 1, iy + 1, iz + 1, k);
     }
     return lerp3(c, wx, wy, wz);
+}
+
+// Value noise by one hardware trilinear fetch: with i = floor(x) and w the
+// smoothstep weights, the smoothstep-weighted blend of the 8 lattice values
+// is the texture's linear filter at texel coordinate (i - lo) + w + 0.5.
+__device__ __forceinline__ float value_noise_hw(const TraceParams& tp, int o, float x, float y,
+                                                float z) {
+    float fx = floorf(x), fy = floorf(y), fz = floorf(z);
+    int tx = (int)fx - tp.nt.lo[o][0], ty = (int)fy - tp.nt.lo[o][1], tz = (int)fz - tp.nt.lo[o][2];
+    if (tp.nt.tex[o] && tx >= 0 && ty >= 0 && tz >= 0 && tx + 1 < tp.nt.dim[o][0] &&
+        ty + 1 < tp.nt.dim[o][1] && tz + 1 < tp.nt.dim[o][2]) {
+        float ux = x - fx, uy = y - fy, uz = z - fz;
+        float wx = ux * ux * (3.f - 2.f * ux);
+        float wy = uy * uy * (3.f - 2.f * uy);
+        float wz = uz * uz * (3.f - 2.f * uz);
+        return tex3D<float>((cudaTextureObject_t)tp.nt.tex[o], (float)tx + wx + 0.5f,
+                            (float)ty + wy + 0.5f, (float)tz + wz + 0.5f);
+    }
+    return value_noise(tp, o, x, y, z);
+}
+
+__device__ __forceinline__ float fbm_hw(const TraceParams& tp, float px, float py, float pz) {
+    if (tp.noise_octaves <= 0) return 1.f;
+    float amp = 1.f, sum = 0.f, f = tp.noise_freq;
+    for (int o = 0; o < tp.noise_octaves; ++o) {
+        sum += amp * value_noise_hw(tp, o, px * f, py * f, pz * f);
+        amp *= tp.noise_gain;
+        f *= tp.noise_lac;
+    }
+    return sum * tp.noise_inv_norm;
+}
+
+// fBm from its precomputed volume (surrogate renderer): one hardware
+// trilinear fetch at level-0 voxel position v; the volume holds fBm at its
+// texel centres over the world box (NoiseTab.fbm_res texels per axis).
+__device__ __forceinline__ float fbm_volume(const TraceParams& tp, float px, float py, float pz,
+                                            float vx, float vy, float vz, float D) {
+    if (tp.noise_octaves <= 0) return 1.f;
+    if (!tp.nt.fbm_tex) return fbm_hw(tp, px, py, pz);
+    const float s = (float)tp.nt.fbm_res / D;
+    return tex3D<float>((cudaTextureObject_t)tp.nt.fbm_tex, vx * s, vy * s, vz * s);
 }
 
 // fBm = sum_o gain^o noise_o(p * freq * lac^o) / sum_o gain^o; 1 without octaves.

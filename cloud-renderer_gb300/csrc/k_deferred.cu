@@ -1,0 +1,426 @@
+// k_deferred.cu -- the deferred renderer: a march pass that records every
+// contributing view sample, then shading passes that evaluate the sun term for
+// those samples in full warps (exact cone, or the MLP surrogate) and
+// accumulate each pixel's colour.
+//
+// Phase A (k_march): one thread per pixel, one warp per 8x4 pixel tile.  The
+// warp marches its rays in lockstep over the view steps; at every step the
+// lanes whose sample has alpha > 0 append (voxel position, w = T*alpha,
+// light G, lane) to the warp's region of the sample buffer (capacity 32 *
+// view_steps), in (step, lane) order.  The pixel's alpha 1 - T is final after
+// this pass.
+// Exact shading (k_shade_exact): one warp per region, 32 samples at a time,
+// then each pixel sums its own samples in step order (shuffle broadcast),
+// exactly the order of the fused kernel.
+// MLP shading: the region counts are scanned (k_region_scan); a persistent
+// kernel walks all samples in flat chunks of 32 -- every chunk full except
+// the last -- computing features, running the network on the tensor cores and
+// writing each sample's contribution in place (k_shade_mlp); k_accumulate
+// then sums each pixel's contributions in step order.
+#include "cg_deferred.cuh"
+#include "cg_internal.h"
+#include "cg_mlp.cuh"
+#include "cg_sample.cuh"
+
+namespace {
+
+__device__ __forceinline__ void tile_pixel(int& px, int& py) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    px = blockIdx.x * 16 + (w & 1) * 8 + (lane & 7);
+    py = blockIdx.y * 16 + (w >> 1) * 4 + (lane >> 3);
+}
+
+// pixel of lane `lane` in region `region` (k_march's mapping)
+__device__ __forceinline__ void region_pixel(int region, int lane, int tiles_x, int& px,
+                                             int& py) {
+    const int blk = region >> 3, w = region & 7;
+    px = (blk % tiles_x) * 16 + (w & 1) * 8 + (lane & 7);
+    py = (blk / tiles_x) * 16 + (w >> 1) * 4 + (lane >> 3);
+}
+
+__device__ __forceinline__ bool pixel_ray(const CamDesc& cam, const VolDesc& vd, int px, int py,
+                                          float3& d, float& tin, float& tout) {
+    float ndx = (2.f * ((float)px + 0.5f) / (float)cam.W - 1.f) * cam.tanh * cam.aspect;
+    float ndy = (1.f - 2.f * ((float)py + 0.5f) / (float)cam.H) * cam.tanh;
+    float dx = cam.f[0] + ndx * cam.s[0] + ndy * cam.u[0];
+    float dy = cam.f[1] + ndx * cam.s[1] + ndy * cam.u[1];
+    float dz = cam.f[2] + ndx * cam.s[2] + ndy * cam.u[2];
+    float inv = rsqrtf(dx * dx + dy * dy + dz * dz);
+    d = make_float3(dx * inv, dy * inv, dz * inv);
+    float dd[3] = {d.x, d.y, d.z};
+    float tmin = -1e30f, tmax = 1e30f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float lo = vd.wmin[a], hi = vd.wmin[a] + vd.range[a];
+        if (dd[a] == 0.f) {
+            if (cam.eye[a] < lo || cam.eye[a] > hi) return false;
+            continue;
+        }
+        float iv = 1.f / dd[a];
+        float t0 = (lo - cam.eye[a]) * iv, t1 = (hi - cam.eye[a]) * iv;
+        tmin = fmaxf(tmin, fminf(t0, t1));
+        tmax = fminf(tmax, fmaxf(t0, t1));
+    }
+    tin = fmaxf(tmin, 0.f);
+    tout = tmax;
+    return tout > tin;
+}
+
+// HW: view samples and noise filtered by the texture unit (surrogate renderer).
+template <int FMT, bool HW>
+__global__ void __launch_bounds__(256) k_march(VolDesc vd, CamDesc cam, TraceParams tp,
+                                               SampleBuf sb, float4* out) {
+    int px, py;
+    tile_pixel(px, py);
+    const int lane = threadIdx.x & 31;
+    const int region = (blockIdx.y * gridDim.x + blockIdx.x) * 8 + (threadIdx.x >> 5);
+    const bool valid = px < cam.W && py < cam.H;
+    float3 d = make_float3(0.f, 0.f, 0.f);
+    float tin = 0.f, tout = 0.f;
+    bool live = valid && pixel_ray(cam, vd, px, py, d, tin, tout);
+    const int Nv = tp.view_steps;
+    const float dt = (tout - tin) / (float)Nv;
+    const float D = (float)vd.D;
+    const float vsx = D / vd.range[0], vsy = D / vd.range[1], vsz = D / vd.range[2];
+    const float pixk = cam.tanh / (float)cam.H * vsx;
+    // the pixel cone spans less than one voxel before t_lod1: lod is exactly 0
+    const float t_lod1 = 0.5f / pixk;
+    float T = 1.f;
+    unsigned cnt = 0, nsteps = 0;
+    float4* pw = sb.pos_w + (size_t)region * sb.capacity;
+    float2* gl = sb.light_lane + (size_t)region * sb.capacity;
+    for (int k = 0; k < Nv; ++k) {
+        if (!__any_sync(0xffffffffu, live)) break;
+        bool emit = false;
+        float v0 = 0.f, v1 = 0.f, v2 = 0.f, w = 0.f, G = 0.f;
+        if (live) {
+            float t = tin + ((float)k + 0.5f) * dt;
+            float p0 = cam.eye[0] + t * d.x, p1 = cam.eye[1] + t * d.y, p2 = cam.eye[2] + t * d.z;
+            v0 = (p0 - vd.wmin[0]) * vsx;
+            v1 = (p1 - vd.wmin[1]) * vsy;
+            v2 = (p2 - vd.wmin[2]) * vsz;
+            float lod = t < t_lod1 ? 0.f : log2f(fmaxf(1.f, 2.f * t * pixk));
+            float2 rg = HW ? cgs::quad_hw<true>(vd, v0, v1, v2, lod)
+                           : cgs::quad<FMT, true, true, true>(vd, v0, v1, v2, lod);
+            if (rg.x > 0.f) {
+                float rho = rg.x * (HW ? cgs::fbm_volume(tp, p0, p1, p2, v0, v1, v2, D)
+                                       : cgs::fbm(tp, p0, p1, p2));
+                if (rho > 0.f) {
+                    float alpha = 1.f - (HW ? __expf(-tp.sigma * rho * dt) : expf(-tp.sigma * rho * dt));
+                    w = T * alpha;
+                    G = rg.y;
+                    emit = true;
+                    T *= 1.f - alpha;
+                    if (T < tp.cutoff) live = false;
+                }
+            }
+        }
+        const unsigned ballot = __ballot_sync(0xffffffffu, emit);
+        if (emit) {
+            const unsigned slot = cnt + __popc(ballot & ((1u << lane) - 1u));
+            pw[slot] = make_float4(v0, v1, v2, w);
+            gl[slot] = make_float2(G, __int_as_float(lane));
+        }
+        // step table: where this step's samples start and which lanes emitted
+        if (ballot) {
+            if (lane == 0) sb.steps[(size_t)region * Nv + nsteps] = make_uint2(cnt, ballot);
+            nsteps++;
+        }
+        cnt += __popc(ballot);
+    }
+    if (lane == 0) {
+        sb.count[region] = cnt;
+        sb.nsteps[region] = nsteps;
+    }
+    if (valid) out[(size_t)py * cam.W + px] = make_float4(0.f, 0.f, 0.f, 1.f - T);
+}
+
+// Sum of each lane's contributions over one chunk of up to 32 samples:
+// sample j (held by lane j) belongs to pixel lane lj; pixels accumulate in j
+// order with Neumaier compensation.
+__device__ __forceinline__ void scatter_chunk(float c, int lj, int m, float& acc, float& comp) {
+    const int lane = threadIdx.x & 31;
+    for (int j = 0; j < m; ++j) {
+        float cj = __shfl_sync(0xffffffffu, c, j);
+        int pj = __shfl_sync(0xffffffffu, lj, j);
+        if (pj == lane) cgs::neumaier(acc, comp, cj);
+    }
+}
+
+__device__ __forceinline__ void write_rgb(float4* out, const CamDesc& cam, int px, int py,
+                                          float C, const TraceParams& tp) {
+    if (px < cam.W && py < cam.H) {
+        float4* o = out + (size_t)py * cam.W + px;
+        float4 v = *o;
+        v.x = C * tp.sun_color[0];
+        v.y = C * tp.sun_color[1];
+        v.z = C * tp.sun_color[2];
+        *o = v;
+    }
+}
+
+template <int FMT>
+__global__ void __launch_bounds__(128) k_shade_exact(VolDesc vd, CamDesc cam, TraceParams tp,
+                                                     ConeSchedule cs, SampleBuf sb, int regions,
+                                                     int tiles_x, float4* out) {
+    const int region = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (region >= regions) return;
+    const int lane = threadIdx.x & 31;
+    const unsigned n = sb.count[region];
+    const float4* pw = sb.pos_w + (size_t)region * sb.capacity;
+    const float2* gl = sb.light_lane + (size_t)region * sb.capacity;
+    float acc = 0.f, comp = 0.f;
+    for (unsigned base = 0; base < n; base += 32) {
+        const unsigned i = base + lane;
+        float c = 0.f;
+        int lj = -1;
+        if (i < n) {
+            float4 s = pw[i];
+            float2 g = gl[i];
+            float tau = cgs::sun_cone<FMT>(vd, cs, s.x, s.y, s.z, tp.sun[0], tp.sun[1], tp.sun[2]);
+            float L = expf(-tp.sigma * tau) * (tp.ambient + (1.f - tp.ambient) * g.x);
+            c = s.w * L;
+            lj = __float_as_int(g.y);
+        }
+        scatter_chunk(c, lj, (int)min(32u, n - base), acc, comp);
+    }
+    int px, py;
+    region_pixel(region, lane, tiles_x, px, py);
+    write_rgb(out, cam, px, py, acc + comp, tp);
+}
+
+// For every 32-sample chunk of the flat order, the region holding its first
+// sample (one thread per region writes the chunks that start inside it).
+__global__ void k_chunk_fill(const unsigned* offset, int regions, unsigned* chunk_region) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= regions) return;
+    const unsigned o0 = offset[r], o1 = offset[r + 1];
+    for (unsigned ch = (o0 + 31) / 32; ch * 32 < o1; ++ch) chunk_region[ch] = (unsigned)r;
+}
+
+// Exclusive scan of the region sample counts (one CTA, 4096 per tile).
+__global__ void __launch_bounds__(1024) k_region_scan(const unsigned* count, int n,
+                                                      unsigned* offset) {
+    __shared__ unsigned warp_sums[32];
+    __shared__ unsigned carry_s;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (tid == 0) carry_s = 0;
+    __syncthreads();
+    for (int base = 0; base < n; base += 4096) {
+        const int i0 = base + tid * 4;
+        unsigned c[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) c[k] = (i0 + k < n) ? count[i0 + k] : 0u;
+        const unsigned s = c[0] + c[1] + c[2] + c[3];
+        unsigned x = s;
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_sums[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            unsigned w = warp_sums[lane], z = w;
+            for (int o = 1; o < 32; o <<= 1) {
+                unsigned y = __shfl_up_sync(0xffffffffu, z, o);
+                if (lane >= o) z += y;
+            }
+            warp_sums[lane] = z - w;
+        }
+        __syncthreads();
+        const unsigned carry = carry_s;
+        unsigned run = carry + warp_sums[wid] + x - s;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (i0 + k < n) offset[i0 + k] = run;
+            run += c[k];
+        }
+        __syncthreads();
+        if (tid == 1023) carry_s = carry + warp_sums[wid] + x;
+        __syncthreads();
+    }
+    if (tid == 0) offset[n] = carry_s;
+}
+
+// MLP shading over flat chunks of 32 samples (persistent warps).  Each lane
+// finds its sample's region from the scanned offsets, computes the 16
+// features, the warp runs the network (two 16-row blocks), and samples with
+// a feature outside the trained range take the exact cone instead.  The
+// contribution w * T_sun * (ambient + (1 - ambient) G) replaces w in place.
+template <int FMT>
+__global__ void __launch_bounds__(128, 4) k_shade_mlp(VolDesc vd, TraceParams tp, ConeSchedule cs,
+                                                   MlpDev m, SampleBuf sb, const unsigned* offset,
+                                                   const unsigned* chunk_region, int regions,
+                                                   unsigned long long* fallbacks) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __half* sW = reinterpret_cast<__half*>(smem);
+    float* sB = reinterpret_cast<float*>(sW + MLP_SMEM_W_HALFS);
+    __half* sXall = reinterpret_cast<__half*>(sB + 3 * 64 + 4);
+    float* sYall = reinterpret_cast<float*>(sXall + 4 * 32 * MLP_S16);
+    mlp::load_weights(m.w16, sW);
+    for (int i = threadIdx.x; i < 3 * 64 + 1; i += blockDim.x)
+        sB[i] = i < 64 ? m.params[MLP_B1 + i]
+                       : (i < 128 ? m.params[MLP_B2 + i - 64]
+                                  : (i < 192 ? m.params[MLP_B3 + i - 128] : m.params[MLP_B4]));
+    __syncthreads();
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    __half* sX = sXall + w * 32 * MLP_S16;
+    float* sY = sYall + w * 32;
+    const unsigned total = offset[regions];
+    const unsigned nchunks = (total + 31) / 32;
+    unsigned n_fallback = 0;
+    for (unsigned c = blockIdx.x * 4 + w; c < nchunks; c += gridDim.x * 4) {
+        const unsigned i = c * 32 + lane;
+        // region of the chunk's first sample (filled by the scan), then walk
+        int r = (int)chunk_region[c];
+        const bool have = i < total;
+        float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+        float2 gv = make_float2(0.f, 0.f);
+        size_t idx = 0;
+        bool fb = false;
+        if (have) {
+            while (offset[r + 1] <= i) ++r;
+            idx = (size_t)r * sb.capacity + (i - offset[r]);
+            s = sb.pos_w[idx];
+            gv = sb.light_lane[idx];
+            float f[MLP_IN];
+            mlp::features<FMT, true>(vd, m, s.x, s.y, s.z, tp.sun[0], tp.sun[1], tp.sun[2], f);
+            fb = !mlp::in_range(m, f);
+#pragma unroll
+            for (int j = 0; j < MLP_IN; j += 2)
+                *reinterpret_cast<__half2*>(sX + lane * MLP_S16 + j) = __floats2half2_rn(
+                    (f[j] - m.mu[j]) * m.inv_sd[j], (f[j + 1] - m.mu[j + 1]) * m.inv_sd[j + 1]);
+        } else {
+#pragma unroll
+            for (int j = 0; j < MLP_IN; j += 2)
+                *reinterpret_cast<__half2*>(sX + lane * MLP_S16 + j) = __floats2half2_rn(0.f, 0.f);
+        }
+        __syncwarp();
+        {
+            float y[2][2];
+            mlp::forward32(sX, sW, sB, sB + 64, sB + 128, sB[192], y);
+            if (t == 0) {
+                sY[g] = y[0][0];
+                sY[g + 8] = y[0][1];
+                sY[16 + g] = y[1][0];
+                sY[24 + g] = y[1][1];
+            }
+        }
+        __syncwarp();
+        if (have) {
+            float tau;
+            if (fb) {
+                tau = cgs::sun_cone<FMT>(vd, cs, s.x, s.y, s.z, tp.sun[0], tp.sun[1], tp.sun[2]);
+                n_fallback++;
+            } else {
+                tau = m.tau_scale * mlp::softplus(sY[lane]);
+            }
+            const float L = __expf(-tp.sigma * tau) * (tp.ambient + (1.f - tp.ambient) * gv.x);
+            sb.pos_w[idx].w = s.w * L;
+        }
+        __syncwarp();
+    }
+    if (fallbacks) {
+        unsigned tot = n_fallback;
+        for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+        if (lane == 0 && tot) atomicAdd(fallbacks, (unsigned long long)tot);
+    }
+}
+
+// Per region: each pixel sums the contributions of its own samples in step
+// order, locating them through the march's step table (base slot, ballot).
+__global__ void __launch_bounds__(128) k_accumulate(CamDesc cam, TraceParams tp, SampleBuf sb,
+                                                    int regions, int tiles_x, int view_steps,
+                                                    float4* out) {
+    const int region = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (region >= regions) return;
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    const unsigned ns = sb.nsteps[region];
+    const uint2* steps = sb.steps + (size_t)region * view_steps;
+    const float4* pw = sb.pos_w + (size_t)region * sb.capacity;
+    float acc = 0.f, comp = 0.f;
+    for (unsigned e = 0; e < ns; ++e) {
+        const uint2 st = steps[e];
+        if ((st.y >> lane) & 1u) cgs::neumaier(acc, comp, pw[st.x + __popc(st.y & below)].w);
+    }
+    int px, py;
+    region_pixel(region, lane, tiles_x, px, py);
+    write_rgb(out, cam, px, py, acc + comp, tp);
+}
+
+}  // namespace
+
+static int regions_of(const CamDesc& cam) { return ((cam.W + 15) / 16) * ((cam.H + 15) / 16) * 8; }
+
+cudaError_t launch_march(VolDesc vd, CamDesc cam, TraceParams tp, SampleBuf sb, float4* out,
+                         bool hw, cudaStream_t st) {
+    dim3 grd((cam.W + 15) / 16, (cam.H + 15) / 16);
+    if (hw)
+        k_march<0, true><<<grd, 256, 0, st>>>(vd, cam, tp, sb, out);
+    else if (vd.fmt == 0)
+        k_march<0, false><<<grd, 256, 0, st>>>(vd, cam, tp, sb, out);
+    else
+        k_march<1, false><<<grd, 256, 0, st>>>(vd, cam, tp, sb, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shade_exact(VolDesc vd, CamDesc cam, TraceParams tp, SampleBuf sb,
+                               float4* out, cudaStream_t st) {
+    ConeSchedule cs = make_cone_schedule(vd, tp);
+    const int regions = regions_of(cam), tiles_x = (cam.W + 15) / 16;
+    const int blocks = (regions + 3) / 4;
+    if (vd.fmt == 0)
+        k_shade_exact<0><<<blocks, 128, 0, st>>>(vd, cam, tp, cs, sb, regions, tiles_x, out);
+    else
+        k_shade_exact<1><<<blocks, 128, 0, st>>>(vd, cam, tp, cs, sb, regions, tiles_x, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_region_scan(CamDesc cam, SampleBuf sb, unsigned* offset, cudaStream_t st) {
+    const int regions = regions_of(cam);
+    k_region_scan<<<1, 1024, 0, st>>>(sb.count, regions, offset);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_chunk_fill<<<(regions + 255) / 256, 256, 0, st>>>(offset, regions, sb.chunk_region);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shade_mlp(VolDesc vd, CamDesc cam, TraceParams tp, const MlpDev& m,
+                             SampleBuf sb, const unsigned* offset,
+                             unsigned long long* fallbacks, cudaStream_t st) {
+    ConeSchedule cs = make_cone_schedule(vd, tp);
+    const size_t sm = (size_t)MLP_SMEM_W_HALFS * 2 + (3 * 64 + 4) * 4 + 4 * 32 * MLP_S16 * 2 +
+                      4 * 32 * 4;
+    const int blocks = 152 * 8;  // persistent warps; weights staged once per CTA
+    static bool configured[2][64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    const int f = vd.fmt == 0 ? 0 : 1;
+    if (!configured[f][dev]) {
+        e = f == 0 ? cudaFuncSetAttribute(k_shade_mlp<0>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)
+                   : cudaFuncSetAttribute(k_shade_mlp<1>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        configured[f][dev] = true;
+    }
+    const int regions = regions_of(cam);
+    if (f == 0)
+        k_shade_mlp<0><<<blocks, 128, sm, st>>>(vd, tp, cs, m, sb, offset, sb.chunk_region,
+                                                regions, fallbacks);
+    else
+        k_shade_mlp<1><<<blocks, 128, sm, st>>>(vd, tp, cs, m, sb, offset, sb.chunk_region,
+                                                regions, fallbacks);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_accumulate(CamDesc cam, TraceParams tp, SampleBuf sb, float4* out,
+                              cudaStream_t st) {
+    const int regions = regions_of(cam), tiles_x = (cam.W + 15) / 16;
+    k_accumulate<<<(regions + 3) / 4, 128, 0, st>>>(cam, tp, sb, regions, tiles_x, tp.view_steps,
+                                                    out);
+    return cudaGetLastError();
+}

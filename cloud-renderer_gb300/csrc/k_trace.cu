@@ -1,5 +1,6 @@
 // k_trace.cu -- per-pixel view march with the exact sun cone (one thread per
 // pixel), and the traceCone evaluator.
+#include "cg_deferred.cuh"
 #include "cg_internal.h"
 #include "cg_sample.cuh"
 
@@ -114,7 +115,7 @@ __global__ void k_trace_cones(VolDesc vd, TraceParams tp, ConeSchedule cs, const
 }  // namespace
 
 // Cone schedule in FP64 on the host (see ConeSchedule).
-static ConeSchedule make_schedule(const VolDesc& vd, const TraceParams& tp) {
+ConeSchedule make_cone_schedule(const VolDesc& vd, const TraceParams& tp) {
     ConeSchedule cs;
     cs.steps = tp.sun_steps;
     cs.mode = tp.cone_mode;
@@ -150,7 +151,7 @@ static ConeSchedule make_schedule(const VolDesc& vd, const TraceParams& tp) {
 
 cudaError_t launch_trace_fused(VolDesc vd, CamDesc cam, TraceParams tp, float4* out,
                                unsigned long long* stats, cudaStream_t st) {
-    ConeSchedule cs = make_schedule(vd, tp);
+    ConeSchedule cs = make_cone_schedule(vd, tp);
     dim3 grd((cam.W + 15) / 16, (cam.H + 15) / 16);
     if (stats) {
         if (vd.fmt == 0)
@@ -190,7 +191,7 @@ cudaError_t launch_noise_table(TraceParams tp, float* tab, int total, cudaStream
 cudaError_t launch_trace_cones(VolDesc vd, TraceParams tp, const float* pos, int n, float* out,
                                cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    ConeSchedule cs = make_schedule(vd, tp);
+    ConeSchedule cs = make_cone_schedule(vd, tp);
     int blocks = (n + 127) / 128;
     if (vd.fmt == 0)
         k_trace_cones<0><<<blocks, 128, 0, st>>>(vd, tp, cs, pos, n, out);

@@ -111,7 +111,15 @@ typedef struct cg_render_params {
     cg_noise noise;
     int use_mlp;               /* 1: sun cone replaced by the MLP surrogate */
     const cg_mlp* mlp;         /* required when use_mlp != 0 */
+    int pipeline;              /* cg_pipeline (exact cone only; the MLP is always deferred) */
 } cg_render_params;
+
+/* Kernel organisation of an exact-cone render.  Both give the same image
+ * (same samples, same per-pixel summation order). */
+typedef enum cg_pipeline {
+    CG_PIPELINE_FUSED = 0,   /* one thread per pixel marches and traces its cones */
+    CG_PIPELINE_DEFERRED = 1 /* march records contributing samples; cones in full warps */
+} cg_pipeline;
 
 /* Snapshot of a volume's layout, for readback. */
 typedef struct cg_volume_info {
@@ -143,6 +151,13 @@ cg_status cg_context_synchronize(cg_context* ctx);
 uint64_t cg_context_launch_count(const cg_context* ctx);
 /* Fill p with the documented defaults. */
 void cg_render_params_default(cg_render_params* p);
+/* Per-stage CUDA-event timing (cf. the reference's FPS/dt counters,
+ * Window.cpp:127-137): when on, cg_voxelize and cg_render record an event
+ * after each stage; cg_context_stage_times returns the stage durations (ms)
+ * of the last such call and their names, ';'-separated. */
+cg_status cg_context_set_timing(cg_context* ctx, int enable);
+cg_status cg_context_stage_times(cg_context* ctx, float* ms, int max_stages, int* count,
+                                 char* names, size_t names_len);
 
 /* Memory helpers so that callers without a CUDA binding can pass pinned host
  * or device buffers (the reference's VBO/texture storage, CloudVolume.cpp:27-48).
@@ -189,6 +204,15 @@ cg_status cg_render(cg_context* ctx, const cg_volume* vol, const cg_camera* cam,
 cg_status cg_render_stats(cg_context* ctx, const cg_volume* vol, const cg_camera* cam,
                           const cg_render_params* params, uint64_t counts[4]);
 
+/* The march pass of the deferred renderer alone: every view sample that
+ * contributes to the image (alpha > 0), as level-0 voxel positions (3 floats)
+ * and compositing weights T*alpha, in pixel-tile order.  Writes at most
+ * `capacity` samples; *count receives the total.  Used to draw training
+ * samples for the surrogate from the renderer's own query distribution. */
+cg_status cg_march_samples(cg_context* ctx, const cg_volume* vol, const cg_camera* cam,
+                           const cg_render_params* params, float* positions, float* weights,
+                           int capacity, int* count);
+
 /* traceCone(sampler3D, position, direction, steps, angle, height)
  * (conetrace_frag.glsl:64-79) evaluated at n level-0 voxel-space positions
  * (n*3 floats) toward direction.  out[i] = optical depth (CG_CONE_TRANSMITTANCE)
@@ -217,6 +241,78 @@ cg_status cg_volume_read_highlight(const cg_volume* vol, uint8_t* mask);
 /* activeVoxels statistic (VoxelShader.cpp:110-119): voxels with count > 0 or
  * a highlight mark, counted on the device. */
 cg_status cg_volume_active_voxels(const cg_volume* vol, uint64_t* active);
+
+/* ---- MLP sun-transmittance surrogate ------------------------------------
+ * No counterpart in the reference (its traceCone is the exact method).  A
+ * 16 -> 64 -> 64 -> 64 -> 1 SiLU network predicts the sun cone's optical
+ * depth from 16 features of a view sample:
+ *   f[3i+k] = density at level base_level+i sampled at
+ *             v + (initial_height + (k + 0.5) * 2^(base_level+i)) * s  (i<4, k<3)
+ *   f[12..14] = v / dimension,  f[15] = s.y
+ * (v: level-0 voxel position, s: unit sun direction).  FP16 weights and
+ * activations on the tensor cores, FP32 accumulation and master weights.
+ * Training, inference and the render use the project's own kernels. */
+#define CG_MLP_FEATURES 16
+#define CG_MLP_PARAMS 9473
+
+typedef struct cg_mlp_config {
+    int base_level;        /* feature levels base_level .. base_level+3 */
+    float initial_height;  /* feature offsets start here (level-0 voxels) */
+    /* the volume resolution and exact cone the model replaces; cg_render
+     * rejects a model whose values differ from the render's */
+    int dimension;
+    int sun_steps;
+    float cone_half_angle, cone_initial_height, cone_min_radius, lod_offset;
+    /* input normalisation x = (f - mean) / stddev, output tau = tau_scale * softplus(y) */
+    float mean[CG_MLP_FEATURES], stddev[CG_MLP_FEATURES];
+    /* trusted feature range: samples outside use the exact cone */
+    float feature_min[CG_MLP_FEATURES], feature_max[CG_MLP_FEATURES];
+    float tau_scale;
+} cg_mlp_config;
+
+typedef struct cg_train_params {
+    int steps;        /* optimiser steps */
+    int batch;        /* rows per step, multiple of 128 */
+    float lr, beta1, beta2, eps; /* Adam */
+    float sigma;      /* extinction of the loss (exp(-sigma tau_pred) - exp(-sigma tau))^2 */
+    uint64_t seed;    /* batch permutation */
+} cg_train_params;
+
+void cg_mlp_config_default(cg_mlp_config* c);
+void cg_train_params_default(cg_train_params* p);
+int cg_mlp_param_count(void);
+/* He-uniform initialisation from a SplitMix64 stream seeded with `seed`. */
+cg_status cg_mlp_create(cg_context* ctx, uint64_t seed, cg_mlp** out);
+void cg_mlp_destroy(cg_mlp* mlp);
+cg_status cg_mlp_configure(cg_mlp* mlp, const cg_mlp_config* config);
+cg_status cg_mlp_get_config(const cg_mlp* mlp, cg_mlp_config* config);
+/* Raw features (n*16) at n level-0 voxel positions (n*3) of a voxelized volume. */
+cg_status cg_mlp_features(const cg_volume* vol, const cg_mlp* mlp, const float* positions, int n,
+                          const float direction[3], float* out, int on_device, void* stream);
+/* Optical depth predicted from raw features (n*16 -> n). */
+cg_status cg_mlp_infer(const cg_mlp* mlp, const float* features, int n, float* out,
+                       int on_device, void* stream);
+/* Mean loss and its gradient (CG_MLP_PARAMS floats, host) over n rows,
+ * without an update: the training step's forward and backward kernels. */
+cg_status cg_mlp_gradient(cg_mlp* mlp, const float* features, const float* tau, int n,
+                          float sigma, float* grad, float* loss, int on_device);
+/* Train on n device-resident rows (features n*16, exact optical depth n). */
+cg_status cg_mlp_train(cg_mlp* mlp, const float* d_features, const float* d_tau, long long n,
+                       const cg_train_params* params, float* loss_per_step);
+/* FP32 parameters (W stored [out][in]: W1 16x64, b1, W2, b2, W3, b3, W4, b4),
+ * Adam moments and step; m, v, step may be NULL. */
+cg_status cg_mlp_get_params(const cg_mlp* mlp, float* params, float* adam_m, float* adam_v,
+                            int* step);
+cg_status cg_mlp_set_params(cg_mlp* mlp, const float* params, const float* adam_m,
+                            const float* adam_v, int step);
+/* Versioned checkpoint (magic, version, shapes, config, params, Adam state,
+ * step, CRC32); training resumes bit-identically from it. */
+cg_status cg_mlp_save(const cg_mlp* mlp, const char* path);
+cg_status cg_mlp_load(cg_context* ctx, const char* path, cg_mlp** out);
+/* Samples of the last MLP render that fell back to the exact cone. */
+cg_status cg_context_mlp_fallbacks(cg_context* ctx, uint64_t* out);
+/* View samples the last MLP render shaded (one surrogate inference each). */
+cg_status cg_context_last_samples(cg_context* ctx, uint64_t* samples);
 
 /* ---- allocation-free variant ------------------------------------------- */
 

@@ -1016,3 +1016,135 @@ OR_API int or_render(const or_volume* v, const or_camera* cam, const or_params* 
 }
 
 OR_API int or_real_bytes(void) { return (int)sizeof(real); }
+
+/* ------------------------------------------------------------------ */
+/* MLP sun-transmittance surrogate in FP64 (build-defined; the reference    */
+/* has no learned part).  Parameter layout: W1[64][16] b1[64] W2[64][64]    */
+/* b2[64] W3[64][64] b3[64] W4[1][64] b4[1] (9473 values, W as [out][in]).   */
+/* ------------------------------------------------------------------ */
+#define M_W1 0
+#define M_B1 1024
+#define M_W2 1088
+#define M_B2 5184
+#define M_W3 5248
+#define M_B3 9344
+#define M_W4 9408
+#define M_B4 9472
+#define M_NPARAM 9473
+
+/* f[3i+k] = level (lb+i) trilinear density (border 0) at
+ * p + (h0 + (k + 0.5) * 2^(lb+i)) * s; f[12..14] = p / D; f[15] = s.y. */
+OR_API void or_mlp_features(const or_volume* v, const double p[3], const double s[3], int lb,
+                            double h0, double out[16]) {
+    for (int i = 0; i < 4; ++i) {
+        int lv = lb + i;
+        int l = lv < 0 ? 0 : (lv > v->L - 1 ? v->L - 1 : lv);
+        double span = (double)(1 << lv);
+        for (int k = 0; k < 3; ++k) {
+            double d = h0 + ((double)k + 0.5) * span;
+            real q[3] = {(real)(p[0] + d * s[0]), (real)(p[1] + d * s[1]), (real)(p[2] + d * s[2])};
+            out[3 * i + k] = (double)sample_level(v, l, q, 0, 1);
+        }
+    }
+    for (int a = 0; a < 3; ++a) out[12 + a] = p[a] / (double)v->D;
+    out[15] = s[1];
+}
+
+static double silu_d(double z) { return z / (1.0 + exp(-z)); }
+static double silu_grad_d(double z) {
+    double s = 1.0 / (1.0 + exp(-z));
+    return s * (1.0 + z * (1.0 - s));
+}
+
+static void mlp_layer(const double* W, const double* b, const double* x, int nin, double* z) {
+    for (int o = 0; o < 64; ++o) {
+        double acc = b[o];
+        for (int i = 0; i < nin; ++i) acc += W[o * nin + i] * x[i];
+        z[o] = acc;
+    }
+}
+
+/* Normalised output y of one row of raw features f. */
+OR_API double or_mlp_forward(const double* P, const double* mu, const double* sd,
+                             const double f[16]) {
+    double x[16], z[64], h1[64], h2[64], h3[64];
+    for (int j = 0; j < 16; ++j) x[j] = (f[j] - mu[j]) / sd[j];
+    mlp_layer(P + M_W1, P + M_B1, x, 16, z);
+    for (int o = 0; o < 64; ++o) h1[o] = silu_d(z[o]);
+    mlp_layer(P + M_W2, P + M_B2, h1, 64, z);
+    for (int o = 0; o < 64; ++o) h2[o] = silu_d(z[o]);
+    mlp_layer(P + M_W3, P + M_B3, h2, 64, z);
+    for (int o = 0; o < 64; ++o) h3[o] = silu_d(z[o]);
+    double y = P[M_B4];
+    for (int i = 0; i < 64; ++i) y += P[M_W4 + i] * h3[i];
+    return y;
+}
+
+/* Mean over n rows of (exp(-sigma*scale*softplus(y)) - exp(-sigma*tau))^2 and
+ * its gradient with respect to the 9473 parameters (grad, zeroed here).  The
+ * predicted optical depth is scale * softplus(y). */
+OR_API double or_mlp_loss_grad(const double* P, const double* mu, const double* sd,
+                               double tau_scale, double sigma, const double* feats,
+                               const double* tau, int n, double* grad) {
+    for (int i = 0; i < M_NPARAM; ++i) grad[i] = 0.0;
+    double loss = 0.0;
+    for (int r = 0; r < n; ++r) {
+        double x[16], z1[64], z2[64], z3[64], h1[64], h2[64], h3[64];
+        for (int j = 0; j < 16; ++j) x[j] = (feats[r * 16 + j] - mu[j]) / sd[j];
+        mlp_layer(P + M_W1, P + M_B1, x, 16, z1);
+        for (int o = 0; o < 64; ++o) h1[o] = silu_d(z1[o]);
+        mlp_layer(P + M_W2, P + M_B2, h1, 64, z2);
+        for (int o = 0; o < 64; ++o) h2[o] = silu_d(z2[o]);
+        mlp_layer(P + M_W3, P + M_B3, h2, 64, z3);
+        for (int o = 0; o < 64; ++o) h3[o] = silu_d(z3[o]);
+        double y = P[M_B4];
+        for (int i = 0; i < 64; ++i) y += P[M_W4 + i] * h3[i];
+        double k = sigma * tau_scale;
+        double sp = (y > 0 ? y : 0.0) + log1p(exp(-fabs(y)));
+        double sg = 1.0 / (1.0 + exp(-y));
+        double Th = exp(-k * sp), T = exp(-sigma * tau[r]);
+        double diff = Th - T;
+        loss += diff * diff;
+        double dy = 2.0 * diff * (-k * sg * Th) / (double)n;
+        double d3[64], d2[64], d1[64];
+        grad[M_B4] += dy;
+        for (int i = 0; i < 64; ++i) {
+            grad[M_W4 + i] += dy * h3[i];
+            d3[i] = dy * P[M_W4 + i] * silu_grad_d(z3[i]);
+        }
+        for (int o = 0; o < 64; ++o) {
+            grad[M_B3 + o] += d3[o];
+            for (int i = 0; i < 64; ++i) grad[M_W3 + o * 64 + i] += d3[o] * h2[i];
+        }
+        for (int i = 0; i < 64; ++i) {
+            double s = 0.0;
+            for (int o = 0; o < 64; ++o) s += P[M_W3 + o * 64 + i] * d3[o];
+            d2[i] = s * silu_grad_d(z2[i]);
+        }
+        for (int o = 0; o < 64; ++o) {
+            grad[M_B2 + o] += d2[o];
+            for (int i = 0; i < 64; ++i) grad[M_W2 + o * 64 + i] += d2[o] * h1[i];
+        }
+        for (int i = 0; i < 64; ++i) {
+            double s = 0.0;
+            for (int o = 0; o < 64; ++o) s += P[M_W2 + o * 64 + i] * d2[o];
+            d1[i] = s * silu_grad_d(z1[i]);
+        }
+        for (int o = 0; o < 64; ++o) {
+            grad[M_B1 + o] += d1[o];
+            for (int i = 0; i < 16; ++i) grad[M_W1 + o * 16 + i] += d1[o] * x[i];
+        }
+    }
+    return loss / (double)n;
+}
+
+/* One Adam step on FP64 state (t = the step number after this update). */
+OR_API void or_adam_step(double* w, double* m, double* v, const double* g, int n, double lr,
+                         double b1, double b2, double eps, int t) {
+    for (int i = 0; i < n; ++i) {
+        m[i] = b1 * m[i] + (1.0 - b1) * g[i];
+        v[i] = b2 * v[i] + (1.0 - b2) * g[i] * g[i];
+        double mh = m[i] / (1.0 - pow(b1, t)), vh = v[i] / (1.0 - pow(b2, t));
+        w[i] -= lr * mh / (sqrt(vh) + eps);
+    }
+}

@@ -80,6 +80,12 @@ def load(bits=64):
         "or_render": (I, [P, ctypes.POINTER(or_camera), ctypes.POINTER(or_params), FP, I, I, I,
                           I, DP, P, I]),
         "or_real_bytes": (I, []),
+        "or_mlp_features": (None, [P, DP, DP, I, ctypes.c_double, DP]),
+        "or_mlp_forward": (ctypes.c_double, [DP, DP, DP, DP]),
+        "or_mlp_loss_grad": (ctypes.c_double, [DP, DP, DP, ctypes.c_double, ctypes.c_double, DP,
+                                               DP, I, DP]),
+        "or_adam_step": (None, [DP, DP, DP, DP, I, ctypes.c_double, ctypes.c_double,
+                                ctypes.c_double, ctypes.c_double, I]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -249,6 +255,58 @@ class OracleVolume:
         self.lib.or_render(self.h, ctypes.byref(c), ctypes.byref(params), _f3(sun_dir), x0, y0, w,
                            h, out.ctypes.data_as(DP), st.ctypes.data_as(ctypes.c_void_p), threads)
         return (out, st) if stats else out
+
+
+def _dp(a):
+    return a.ctypes.data_as(DP)
+
+
+class OracleMLP:
+    """FP64 forward / loss gradient / Adam of the surrogate (or_mlp_*)."""
+
+    NPARAM = 9473
+
+    def __init__(self, params, mean, stddev, tau_scale):
+        self.lib = load(64)
+        self.P = np.ascontiguousarray(params, np.float64)
+        self.mu = np.ascontiguousarray(mean, np.float64)
+        self.sd = np.ascontiguousarray(stddev, np.float64)
+        self.tau_scale = float(tau_scale)
+
+    def forward(self, feats):
+        f = np.ascontiguousarray(feats, np.float64).reshape(-1, 16)
+        return np.array([self.lib.or_mlp_forward(_dp(self.P), _dp(self.mu), _dp(self.sd),
+                                                 _dp(np.ascontiguousarray(row))) for row in f])
+
+    def loss_grad(self, feats, tau, sigma, params=None):
+        P = self.P if params is None else np.ascontiguousarray(params, np.float64)
+        f = np.ascontiguousarray(feats, np.float64).reshape(-1, 16)
+        t = np.ascontiguousarray(tau, np.float64).reshape(-1)
+        g = np.zeros(self.NPARAM, np.float64)
+        loss = self.lib.or_mlp_loss_grad(_dp(P), _dp(self.mu), _dp(self.sd), self.tau_scale,
+                                         float(sigma), _dp(f), _dp(t), f.shape[0], _dp(g))
+        return loss, g
+
+
+def adam_step(w, m, v, g, lr, b1, b2, eps, t):
+    w = np.ascontiguousarray(w, np.float64).copy()
+    m = np.ascontiguousarray(m, np.float64).copy()
+    v = np.ascontiguousarray(v, np.float64).copy()
+    g = np.ascontiguousarray(g, np.float64)
+    load(64).or_adam_step(_dp(w), _dp(m), _dp(v), _dp(g), w.shape[0], lr, b1, b2, eps, int(t))
+    return w, m, v
+
+
+def mlp_features(vol, positions, direction, base_level, initial_height):
+    d = np.asarray(direction, np.float64)
+    d = d / np.sqrt((d * d).sum())
+    out = np.zeros((len(positions), 16))
+    for i, p in enumerate(positions):
+        o = np.zeros(16)
+        vol.lib.or_mlp_features(vol.h, _d3(p), _d3(d), int(base_level), float(initial_height),
+                                _dp(o))
+        out[i] = o
+    return out
 
 
 def fbm(p, params, bits=64):

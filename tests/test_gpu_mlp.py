@@ -1,0 +1,275 @@
+"""GPU tests of the learned sun-transmittance surrogate and the deferred renderer.
+
+Tolerances: the network runs with FP16 weights/activations on the tensor
+cores (FP32 accumulation), so forward and gradient are compared with the FP64
+oracle evaluated on the same FP16-rounded weights, within 2 % (forward,
+relative to the output scale) and 5 % relative L2 / cosine >= 0.998
+(gradient).  Renders with the surrogate must stay within RMSE 1e-2 of the FP64
+oracle's exact image.
+"""
+import ctypes
+import time
+
+import numpy as np
+import pytest
+
+import cloudgb
+from cloudgb import _lib, configs, surrogate, workload
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def fp16_round(p):
+    return p.astype(np.float16).astype(np.float64)
+
+
+def random_model(ctx, seed=3):
+    m = surrogate.SunMLP(ctx, seed=seed)
+    rng = np.random.default_rng(seed)
+    mu = rng.uniform(-0.5, 0.5, 16)
+    sd = rng.uniform(0.5, 2.0, 16)
+    m.configure(mean=mu, stddev=sd, tau_scale=0.8)
+    # non-zero biases so that every parameter group is exercised
+    p, _, _, _ = m.get_params()
+    p = p.copy()
+    p[1024:1088] = rng.uniform(-0.2, 0.2, 64)
+    p[5184:5248] = rng.uniform(-0.2, 0.2, 64)
+    p[9344:9408] = rng.uniform(-0.2, 0.2, 64)
+    p[9472] = 0.3
+    m.set_params(p)
+    return m, mu, sd, rng
+
+
+def oracle_of(m, mu, sd):
+    p, _, _, _ = m.get_params()
+    P = p.astype(np.float64)
+    # the GPU multiplies with FP16 weights; biases stay FP32
+    for a, b in [(0, 1024), (1088, 5184), (5248, 9344), (9408, 9472)]:
+        P[a:b] = fp16_round(P[a:b])
+    return O.OracleMLP(P, mu, sd, m.config.tau_scale)
+
+
+def test_forward_matches_oracle(ctx):
+    m, mu, sd, rng = random_model(ctx)
+    f = rng.uniform(-2, 2, (1000, 16)).astype(np.float32) * sd + mu
+    got = m.infer(f).astype(np.float64)
+    om = oracle_of(m, mu, sd)
+    y = om.forward(f.astype(np.float64))
+    ref = om.tau_scale * np.logaddexp(0.0, y)
+    assert np.abs(got - ref).max() <= 0.02 * om.tau_scale * max(1.0, np.abs(y).max())
+    assert np.corrcoef(got, ref)[0, 1] > 0.999
+
+
+def test_gradient_matches_oracle(ctx):
+    m, mu, sd, rng = random_model(ctx, seed=5)
+    n = 600  # not a multiple of 128: padding rows must contribute nothing
+    f = (rng.uniform(-2, 2, (n, 16)) * sd + mu).astype(np.float32)
+    tau = rng.uniform(0.0, 1.5, n).astype(np.float32)
+    sigma = 2.0
+    g, loss = m.gradient(f, tau, sigma)
+    om = oracle_of(m, mu, sd)
+    oloss, og = om.loss_grad(f.astype(np.float64), tau.astype(np.float64), sigma)
+    assert loss == pytest.approx(oloss, rel=2e-2)
+    rel = np.linalg.norm(g - og) / np.linalg.norm(og)
+    cos = float(g @ og / (np.linalg.norm(g) * np.linalg.norm(og)))
+    assert rel < 0.05 and cos > 0.998, (rel, cos)
+    for a, b in [(0, 1024), (1024, 1088), (1088, 5184), (5184, 5248), (5248, 9344),
+                 (9344, 9408), (9408, 9472), (9472, 9473)]:
+        seg_rel = np.linalg.norm(g[a:b] - og[a:b]) / max(np.linalg.norm(og[a:b]), 1e-12)
+        assert seg_rel < 0.08, (a, b, seg_rel)
+
+
+def test_adam_step_matches_torch(ctx):
+    torch = pytest.importorskip("torch")
+    m, mu, sd, rng = random_model(ctx, seed=7)
+    n = 256
+    f = (rng.uniform(-2, 2, (n, 16)) * sd + mu).astype(np.float32)
+    tau = rng.uniform(0.0, 1.5, n).astype(np.float32)
+    p0, _, _, _ = m.get_params()
+    g, _ = m.gradient(f, tau, 2.0)
+    losses = m.train(f, tau, steps=1, batch=n, lr=1e-3, sigma=2.0)
+    p1, m1, v1, step = m.get_params()
+    assert step == 1 and np.isfinite(losses).all()
+    w = torch.nn.Parameter(torch.tensor(p0.astype(np.float64)))
+    opt = torch.optim.Adam([w], lr=1e-3, betas=(0.9, 0.999), eps=1e-8)
+    w.grad = torch.tensor(g.astype(np.float64))
+    opt.step()
+    ref = w.detach().numpy()
+    big = np.abs(g) > 1e-5  # the first Adam step is lr*sign(g) there
+    np.testing.assert_allclose(p1[big], ref[big], rtol=0, atol=2e-6)
+    np.testing.assert_allclose(m1[big], 0.1 * g[big], rtol=2e-3, atol=1e-9)
+
+
+def synthetic_set(n, seed=11):
+    rng = np.random.default_rng(seed)
+    f = rng.uniform(0, 1, (n, 16)).astype(np.float32)
+    tau = (0.8 * f[:, 0] + 0.5 * f[:, 3] * f[:, 5] + 0.3 * np.sin(3 * f[:, 7])).astype(np.float32)
+    return f, tau
+
+
+def test_training_reduces_loss(ctx):
+    m = surrogate.SunMLP(ctx, seed=9)
+    f, tau = synthetic_set(65536)
+    m.fit_normalization(f, tau)
+    losses = m.train(f, tau, steps=600, batch=4096, lr=1e-3, sigma=2.0)
+    assert np.isfinite(losses).all()
+    assert losses[-20:].mean() < 0.2 * losses[:20].mean(), (losses[:5], losses[-5:])
+
+
+def test_checkpoint_resume_is_bit_identical(ctx, tmp_path):
+    m = surrogate.SunMLP(ctx, seed=13)
+    f, tau = synthetic_set(16384, seed=2)
+    m.fit_normalization(f, tau)
+    m.train(f, tau, steps=120, batch=2048, lr=1e-3, sigma=2.0)
+    path = str(tmp_path / "sun.ckpt")
+    m.save(path)
+    r = surrogate.SunMLP.load(ctx, path)
+    a, b = m.get_params(), r.get_params()
+    for x, y in zip(a[:3], b[:3]):
+        assert np.array_equal(x, y)
+    assert a[3] == b[3] == 120
+    m.train(f, tau, steps=70, batch=2048, lr=1e-3, sigma=2.0)
+    r.train(f, tau, steps=70, batch=2048, lr=1e-3, sigma=2.0)
+    assert np.array_equal(m.get_params()[0], r.get_params()[0])
+    # corrupted checkpoints are rejected
+    data = bytearray(open(path, "rb").read())
+    data[100] ^= 0xFF
+    bad = str(tmp_path / "bad.ckpt")
+    open(bad, "wb").write(bytes(data))
+    with pytest.raises(cloudgb.CloudError) as e:
+        surrogate.SunMLP.load(ctx, bad)
+    assert e.value.status == 8
+    open(bad, "wb").write(bytes(data[:50]))
+    with pytest.raises(cloudgb.CloudError):
+        surrogate.SunMLP.load(ctx, bad)
+
+
+def _pair(ctx, cfg, wl, fmt):
+    vol = cloudgb.CloudVolume(cfg["dim"], configs.VOLUME_BOUNDS, configs.VOLUME_POSITION,
+                              cfg["mips"], fmt=fmt, ctx=ctx)
+    vol.set_billboards(wl.positions, wl.scales, wl.densities)
+    vol.update()
+    sun = cloudgb.Sun(wl.sun_direction, *wl.sun_map)
+    cloudgb.VoxelizeShader().voxelize(vol, sun)
+    ov = O.OracleVolume(cfg["dim"], configs.VOLUME_BOUNDS, configs.VOLUME_POSITION, cfg["mips"])
+    ov.set_boards(wl.positions, wl.scales, wl.densities)
+    ov.voxelize(sun.direction, *wl.sun_map)
+    return vol, sun, ov
+
+
+def test_deferred_exact_matches_fused_and_oracle(ctx):
+    cfg = configs.SMALL_64
+    wl = workload.build(cfg)
+    vol, sun, ov = _pair(ctx, cfg, wl, cloudgb.FORMAT_RGBA32F)
+    cam = workload.make_camera(wl.cameras[0])
+    fused = cloudgb.ConeTraceShader(**wl.shader_kwargs()).coneTrace(vol, cam)
+    sh = cloudgb.ConeTraceShader(pipeline=_lib.PIPELINE_DEFERRED, **wl.shader_kwargs())
+    deferred = sh.coneTrace(vol, cam)
+    assert np.abs(deferred - fused).max() <= 1e-6
+    ref = ov.render(cam, O.params_from_shader(sh), sun.direction)
+    assert np.abs(deferred.astype(np.float64) - ref).max() <= 1e-4
+
+
+def test_features_match_oracle(ctx):
+    cfg = configs.SMALL_64
+    wl = workload.build(cfg)
+    vol, sun, ov = _pair(ctx, cfg, wl, cloudgb.FORMAT_RGBA32F)
+    sh = cloudgb.ConeTraceShader(**wl.shader_kwargs())
+    m = surrogate.SunMLP(ctx)
+    m.configure_for(vol, sh)
+    rng = np.random.default_rng(1)
+    pts = rng.uniform(4, 60, (300, 3)).astype(np.float32)
+    got = m.features(vol, pts, sun.direction).astype(np.float64)
+    c = m.config
+    ref = O.mlp_features(ov, pts.astype(np.float64), sun.direction, c.base_level,
+                         c.initial_height)
+    # density taps are filtered by the texture unit (8-bit fixed-point weights,
+    # FP16 texels): within 1 % of the feature range; the rest is exact
+    scale = ref[:, :12].max()
+    assert scale > 0
+    np.testing.assert_allclose(got[:, :12], ref[:, :12], rtol=0, atol=0.01 * scale)
+    np.testing.assert_allclose(got[:, 12:], ref[:, 12:], rtol=1e-6, atol=1e-6)
+
+
+@pytest.fixture(scope="module")
+def trained(ctx):
+    """A surrogate trained (reduced budget) for the 1080p workload's cone."""
+    cfg = configs.PLAIN_1080P
+    sh = cloudgb.ConeTraceShader(**workload.build(cfg, boards=8).shader_kwargs())
+    t0 = time.perf_counter()
+    mlp, losses = surrogate.train_surrogate(ctx, sh, samples=600_000, steps=3000, batch=16384,
+                                            scenes=6, seed=1000)
+    return mlp, losses, time.perf_counter() - t0
+
+
+def test_mlp_render_rmse_and_gain(ctx, trained):
+    mlp, losses, train_s = trained
+    assert losses[-50:].mean() < losses[:50].mean()
+    cfg = configs.PLAIN_1080P
+    wl = workload.build(cfg, width=480, height=270)
+    vol, sun, ov = _pair(ctx, cfg, wl, cloudgb.FORMAT_BF16_FP16)
+    cam = workload.make_camera(wl.cameras[3])
+    kw = wl.shader_kwargs()
+    exact = cloudgb.ConeTraceShader(**kw)
+    ref = ov.render(cam, O.params_from_shader(exact), sun.direction)
+    learned = cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, **kw)
+    img = learned.coneTrace(vol, cam).astype(np.float64)
+    rmse = float(np.sqrt(((img - ref) ** 2).mean()))
+    assert rmse <= 1e-2, rmse
+    # the method without it at a reduced budget: the exact cone with half the steps
+    cheap = cloudgb.ConeTraceShader(**dict(kw, vctSteps=kw["vctSteps"] // 2))
+    img_c = cheap.coneTrace(vol, cam).astype(np.float64)
+    rmse_c = float(np.sqrt(((img_c - ref) ** 2).mean()))
+    assert rmse <= rmse_c, (rmse, rmse_c)
+    # speed at 1080p on the same volume
+    big = cloudgb.Camera(cam.eye, cam.target, width=1920, height=1080)
+
+    def best(shader):
+        out = cloudgb.DeviceBuffer(1920 * 1080 * 16)
+        ts = []
+        for _ in range(5):
+            ctx.synchronize()
+            t0 = time.perf_counter()
+            shader.coneTrace(vol, big, out=out)
+            ctx.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return min(ts)
+
+    t_mlp = best(learned)
+    t_exact = best(exact)
+    assert t_mlp < t_exact, (t_mlp, t_exact)
+
+
+def test_fallback_outside_training_range(ctx, trained):
+    mlp, _, _ = trained
+    cfg = configs.PLAIN_1080P
+    wl = workload.build(cfg, width=160, height=90)
+    vol, sun, _ = _pair(ctx, cfg, wl, cloudgb.FORMAT_BF16_FP16)
+    cam = workload.make_camera(wl.cameras[0])
+    kw = wl.shader_kwargs()
+    saved = mlp.config
+    try:
+        mlp.configure(feature_max=[-1.0] * 16)  # nothing is in range
+        img = cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, **kw).coneTrace(vol, cam)
+        fb = ctypes.c_uint64()
+        _lib.check(_lib.load().cg_context_mlp_fallbacks(ctx.handle, ctypes.byref(fb)))
+        exact = cloudgb.ConeTraceShader(pipeline=_lib.PIPELINE_DEFERRED, **kw).coneTrace(vol, cam)
+        assert fb.value > 0
+        # every sun term is the exact cone; the march differs only by the
+        # texture unit's filtering of view samples and noise
+        assert float(np.sqrt(((img - exact) ** 2).mean())) <= 3e-3
+    finally:
+        _lib.check(_lib.load().cg_mlp_configure(mlp.handle, ctypes.byref(saved)))
+
+
+def test_mlp_rejects_mismatched_cone(ctx, trained):
+    mlp, _, _ = trained
+    cfg = configs.PLAIN_1080P
+    wl = workload.build(cfg, boards=16, width=32, height=32)
+    vol, _, _ = _pair(ctx, cfg, wl, cloudgb.FORMAT_BF16_FP16)
+    cam = workload.make_camera(wl.cameras[0])
+    kw = dict(wl.shader_kwargs(), vctSteps=10)
+    with pytest.raises(cloudgb.CloudError) as e:
+        cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, **kw).coneTrace(vol, cam)
+    assert e.value.status == 1
