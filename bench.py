@@ -39,7 +39,7 @@ MLP_FLOP_PER_SAMPLE = 2 * (16 * 64 + 64 * 64 + 64 * 64 + 64)
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -106,14 +106,12 @@ def cpu_frame_rate(wl, budget_s, threads):
                       noise_lacunarity=c["noise_lacunarity"], noise_gain=c["noise_gain"])
     W, H = cam.width, cam.height
     band = 8
-    order = list(range(H // 2, H, band)) + list(range(H // 2 - band, -band, -band))
-    order = [max(0, y) for y in order]
-    rows, t_render, done = 0, 0.0, set()
-    for y0 in order:
+    # bands of rows from the centre outward (the centre holds the cloud)
+    starts = list(range(0, H, band))
+    starts.sort(key=lambda y: abs(y + band // 2 - H // 2))
+    rows, t_render = 0, 0.0
+    for y0 in starts:
         h = min(band, H - y0)
-        if y0 in done or h <= 0:
-            continue
-        done.add(y0)
         t0 = time.perf_counter()
         ov.render(cam, P, wl.sun_direction, rect=(0, y0, W, h), threads=threads)
         t_render += time.perf_counter() - t0
@@ -178,10 +176,15 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            # the first sample takes a while: start timing once sampling runs
+            t0 = time.perf_counter()
+            while not self.lines and time.perf_counter() - t0 < 5.0:
+                time.sleep(0.01)
+            self.lines.clear()
         except OSError:
             self.proc = None
         return self
@@ -323,7 +326,12 @@ def run_ours(args):
             stages = {}
             for k in range(min(steps, 16)):
                 flush.zero_()
-                frame(k)
+                _lib.check(lib.cg_voxelize(vol.handle, ctypes.byref(csun), sp), "cg_voxelize")
+                for name, ms in ctx.stage_times().items():
+                    stages.setdefault("voxelize." + name, []).append(ms)
+                _lib.check(lib.cg_render(ctx.handle, vol.handle, ctypes.byref(ccams[k % len(ccams)]),
+                                         ctypes.byref(params), ctypes.c_void_p(img.data_ptr()), 1,
+                                         sp), "cg_render")
                 for name, ms in ctx.stage_times().items():
                     stages.setdefault(name, []).append(ms)
             ctx.set_timing(False)

@@ -62,6 +62,13 @@ class Context:
               "cg_context_mlp_fallbacks")
         return int(v.value)
 
+    def last_samples(self):
+        """View samples the last surrogate render shaded."""
+        v = ctypes.c_uint64()
+        check(self._lib.cg_context_last_samples(self.handle, ctypes.byref(v)),
+              "cg_context_last_samples")
+        return int(v.value)
+
     def close(self):
         if self.handle:
             self._lib.cg_context_destroy(self.handle)

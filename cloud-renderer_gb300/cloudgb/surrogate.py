@@ -198,8 +198,9 @@ def training_set(ctx, shader, samples=4_000_000, scenes=16, dim=256, mips=8, fmt
         # sun within ~30 degrees of the workload sun
         base = np.asarray(configs.SUN_DIRECTION, np.float64)
         base /= np.linalg.norm(base)
+        # the first scene keeps the workload sun so the feature range covers it
         jitter = rng.on_unit_sphere(1)[0] * 0.5 * u[2]
-        sd = base + jitter
+        sd = base + (jitter if k > 0 else 0.0)
         sd /= np.linalg.norm(sd)
         vol = cloudgb.CloudVolume(dim, configs.VOLUME_BOUNDS, configs.VOLUME_POSITION, mips,
                                   fmt=fmt, ctx=ctx)

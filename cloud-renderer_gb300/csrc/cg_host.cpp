@@ -89,7 +89,7 @@ extern "C" cg_status cg_context_last_samples(cg_context* ctx, uint64_t* samples)
     *samples = 0;
     if (!ctx->samples_cnt.p || ctx->last_regions <= 0) return CG_OK;
     CG_CUDA(cudaSetDevice(ctx->device));
-    CG_CUDA(cudaStreamSynchronize(ctx->stream));
+    CG_CUDA(cudaDeviceSynchronize());
     unsigned total = 0;
     CG_CUDA(cudaMemcpy(&total, ctx->samples_cnt.as<unsigned>() + 2 * ctx->last_regions, 4,
                        cudaMemcpyDeviceToHost));
@@ -536,6 +536,7 @@ VolDesc desc_of(const cg_volume* v) {
     d.pyr = v->pyr.p;
     d.occ = v->occ.as<const uint8_t>() + v->occ_total;
     for (int l = 0; l < CG_MAX_LEVELS; ++l) d.tex[l] = v->tex_obj[l];
+    for (int l = 0; l < CG_MAX_LEVELS; ++l) d.surf[l] = 0;
     for (int l = 0; l < CG_MAX_LEVELS; ++l) {
         d.occ_nb[l] = v->occ_nb[l];
         d.occ_off[l] = v->occ_off[l];
@@ -646,6 +647,11 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
     bins.cursor = v->bcursor.as<uint32_t>();
     bins.list = v->blist.as<uint32_t>();
     VolDesc vd = desc_of(v);
+    // once the surrogate renderer has built the texture copies, keep them
+    // current from the voxelize stores instead of a copy pass
+    const bool write_tex = v->tex_arr[0] != nullptr;
+    if (write_tex)
+        for (int l = 0; l < v->L; ++l) vd.surf[l] = v->tex_surf[l];
     stage_begin(ctx, s);
     // clearGPU (CloudVolume.cpp:96-100) + clearPositionMap (VoxelizeShader.cpp:185-187)
     CG_CUDA(cudaMemsetAsync(v->keys.p, 0xFF, texels * 8, s));
@@ -678,6 +684,7 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
     stage_mark(ctx, s, "mips");
     v->voxelized = true;
     v->gen++;
+    if (write_tex) v->tex_gen = v->gen;
     return CG_OK;
 }
 

@@ -39,6 +39,9 @@ struct VolDesc {
     // hardware-filtered half2 (density, light) copies of the levels for the
     // surrogate renderer (cudaTextureObject_t; 0 when not built)
     unsigned long long tex[CG_MAX_LEVELS];
+    // surfaces of the same arrays (cudaSurfaceObject_t): when set, voxelize
+    // writes each stored voxel there too, so the copies never need a pass
+    unsigned long long surf[CG_MAX_LEVELS];
 };
 
 // Hash-noise lattice values tabulated per octave over the world box: octave

@@ -242,7 +242,7 @@ extern "C" cg_status cg_context_mlp_fallbacks(cg_context* ctx, uint64_t* out) {
     *out = 0;
     if (!ctx->fallbacks.p) return CG_OK;
     CG_CUDA(cudaSetDevice(ctx->device));
-    CG_CUDA(cudaStreamSynchronize(ctx->stream));
+    CG_CUDA(cudaDeviceSynchronize());
     unsigned long long h = 0;
     CG_CUDA(cudaMemcpy(&h, ctx->fallbacks.p, 8, cudaMemcpyDeviceToHost));
     *out = h;

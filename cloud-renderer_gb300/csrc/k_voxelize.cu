@@ -290,10 +290,19 @@ __device__ __forceinline__ void store_voxel(const VolDesc& vd, void* pyr, int l,
                                             int z, float4 v) {
     const int N = vd.dims[l];
     size_t idx = (size_t)vd.offs[l] + ((size_t)z * N + y) * N + x;
-    if (vd.fmt == 0)
+    __half2 h;
+    if (vd.fmt == 0) {
         reinterpret_cast<float4*>(pyr)[idx] = v;
-    else
-        reinterpret_cast<uint32_t*>(pyr)[idx] = pack_bf16_fp16(v.x, v.y);
+        h = __floats2half2_rn(v.x, v.y);
+    } else {
+        const uint32_t w = pack_bf16_fp16(v.x, v.y);
+        reinterpret_cast<uint32_t*>(pyr)[idx] = w;
+        h = __halves2half2(__float2half_rn(__uint_as_float(w << 16)),
+                           __ushort_as_half((unsigned short)(w >> 16)));
+    }
+    // the half2 texture copy holds exactly what the level stores (the same
+    // conversion as the copy pass of k_textures.cu)
+    if (vd.surf[l]) surf3Dwrite(*reinterpret_cast<uint32_t*>(&h), vd.surf[l], x * 4, y, z);
 }
 
 __device__ __forceinline__ float4 load_voxel(const VolDesc& vd, const void* pyr, int l, int x,

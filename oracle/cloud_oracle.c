@@ -498,6 +498,24 @@ static void highlight_texel(or_volume* v, f3 p, float o) {
     }
 }
 
+/* Pass 2 alone over a given position map (W x H texels of xyzw, w > 0 =
+ * written): the marks go to mask_out (D^3 bytes, cleared here); the volume's
+ * own state is left unchanged. */
+OR_API float or_highlight_offset(const or_volume* v);
+OR_API void or_highlight_posmap(or_volume* v, const float* posmap, int W, int H,
+                                uint8_t* mask_out) {
+    uint8_t* keep = v->mask;
+    memset(mask_out, 0, (size_t)v->D * v->D * v->D);
+    v->mask = mask_out;
+    float o = or_highlight_offset(v);
+    for (size_t t = 0; t < (size_t)W * H; ++t) {
+        const float* pm = posmap + t * 4;
+        if (!(pm[3] > 0.0f)) continue;
+        highlight_texel(v, f3_make(pm[0], pm[1], pm[2]), o);
+    }
+    v->mask = keep;
+}
+
 OR_API float or_highlight_offset(const or_volume* v) {
     float vs0 = v->range[0] / (float)v->D, vs1 = v->range[1] / (float)v->D,
           vs2 = v->range[2] / (float)v->D;

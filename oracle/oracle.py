@@ -72,6 +72,7 @@ def load(bits=64):
         "or_volume_rebuild_mips": (None, [P, I]),
         "or_sun_frame_make": (I, [FP, F, F, FP, I, I, ctypes.POINTER(or_sun_frame)]),
         "or_highlight_offset": (F, [P]),
+        "or_highlight_posmap": (None, [P, FP, I, I, P]),
         "or_sample": (ctypes.c_double, [P, DP, ctypes.c_double, I, I]),
         "or_trace_cone": (ctypes.c_double, [P, DP, DP, ctypes.POINTER(or_params)]),
         "or_pcg3d": (None, [ctypes.POINTER(ctypes.c_uint32)]),
@@ -207,6 +208,14 @@ class OracleVolume:
         p = np.empty((H, W, 4), np.float32)
         self.lib.or_volume_get_sun_map(self.h, k.ctypes.data, p.ctypes.data)
         return k, p
+
+    def highlight_posmap(self, posmap):
+        """Pass 2 alone over a given (H, W, 4) position map -> (D, D, D) marks."""
+        pm = np.ascontiguousarray(posmap, np.float32)
+        H, W = pm.shape[:2]
+        m = np.empty((self.D,) * 3, np.uint8)
+        self.lib.or_highlight_posmap(self.h, pm.ctypes.data_as(FP), W, H, m.ctypes.data)
+        return m
 
     def frame(self):
         fr = or_sun_frame()

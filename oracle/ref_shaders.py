@@ -1,0 +1,89 @@
+"""ctypes binding of oracle/_ref/libref_shaders.so: the reference's own shader
+code (compiled through oracle/ref_shim/) run on the CPU.  TEST INFRASTRUCTURE
+ONLY -- used by tests/golden/make_golden.py and by the tests that check the
+oracle against it where the library exists."""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_ref", "libref_shaders.so")
+FP = ctypes.POINTER(ctypes.c_float)
+IP = ctypes.POINTER(ctypes.c_int)
+LP = ctypes.POINTER(ctypes.c_long)
+_lib = None
+
+
+def available():
+    return os.path.exists(LIB)
+
+
+def load():
+    global _lib
+    if _lib is None:
+        lib = ctypes.CDLL(LIB)
+        lib.ref_sun_pass.restype = ctypes.c_long
+        lib.ref_sun_pass.argtypes = [FP, FP, ctypes.c_int, FP, ctypes.c_float, ctypes.c_float, FP,
+                                     ctypes.c_int, ctypes.c_int, FP, IP, FP]
+        lib.ref_second_pass.restype = None
+        lib.ref_second_pass.argtypes = [FP, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_float, ctypes.c_float, FP, ctypes.c_void_p]
+        lib.ref_trace_cone.restype = ctypes.c_float
+        lib.ref_trace_cone.argtypes = [FP, IP, LP, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                       ctypes.c_float, FP, FP, FP, ctypes.c_int, ctypes.c_float,
+                                       ctypes.c_float, ctypes.c_float, ctypes.c_float, FP]
+        _lib = lib
+    return _lib
+
+
+def _f(a):
+    return np.ascontiguousarray(a, np.float32)
+
+
+def sun_pass(board_pos, board_scale, vol_pos, bounds, sun_dir, W, H):
+    """first_voxelize (+ billboard_vert_instanced) over the boards ->
+    (posmap (H, W, 4), winner (H, W), depth (H, W), fragments shaded)."""
+    lib = load()
+    bp, bs = _f(board_pos).reshape(-1, 3), _f(board_scale).reshape(-1)
+    pm = np.empty((H, W, 4), np.float32)
+    win = np.empty((H, W), np.int32)
+    dep = np.empty((H, W), np.float32)
+    vp, sd = _f(vol_pos), _f(sun_dir)
+    n = lib.ref_sun_pass(bp.ctypes.data_as(FP), bs.ctypes.data_as(FP), bp.shape[0],
+                         vp.ctypes.data_as(FP), float(bounds[0]), float(bounds[1]),
+                         sd.ctypes.data_as(FP), W, H, pm.ctypes.data_as(FP),
+                         win.ctypes.data_as(IP), dep.ctypes.data_as(FP))
+    return pm, win, dep, int(n)
+
+
+def second_pass(posmap, D, vol_pos, bounds):
+    """second_voxelize over a position map -> (D, D, D) uint8 marks (1 = stored)."""
+    lib = load()
+    pm = _f(posmap)
+    H, W = pm.shape[:2]
+    marks = np.empty((D, D, D), np.uint8)
+    vp = _f(vol_pos)
+    lib.ref_second_pass(pm.ctypes.data_as(FP), W, H, D, float(bounds[0]), float(bounds[1]),
+                        vp.ctypes.data_as(FP), marks.ctypes.data)
+    return (marks > 0).astype(np.uint8)
+
+
+def trace_cone(levels, D, vol_pos, bounds, world_pos, direction, steps, cone_angle, cone_h0,
+               lod_offset=0.0, down_scaling=1.0):
+    """traceCone over a one-channel mip chain (list of (n, n, n) arrays) ->
+    (value, voxel-space start position)."""
+    lib = load()
+    flat = _f(np.concatenate([np.asarray(l, np.float32).reshape(-1) for l in levels]))
+    dims = np.array([l.shape[0] for l in levels], np.int32)
+    offs = np.zeros(len(levels), np.int64)
+    offs[1:] = np.cumsum([l.size for l in levels])[:-1]
+    offs = offs.astype(np.int64)
+    vp, wp, dr = _f(vol_pos), _f(world_pos), _f(direction)
+    out = np.empty(3, np.float32)
+    v = lib.ref_trace_cone(flat.ctypes.data_as(FP), dims.ctypes.data_as(IP),
+                           offs.ctypes.data_as(LP), len(levels), D, float(bounds[0]),
+                           float(bounds[1]), vp.ctypes.data_as(FP), wp.ctypes.data_as(FP),
+                           dr.ctypes.data_as(FP), int(steps), float(cone_angle), float(cone_h0),
+                           float(lod_offset), float(down_scaling), out.ctypes.data_as(FP))
+    return float(v), out
