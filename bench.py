@@ -412,7 +412,7 @@ def run_ours(args):
     e2e_val = W * H / (float(np.median(e2e_ms)) / 1e3) / 1e6 * world
 
     if use_mlp:
-        roofline = {"bound": "tensor", "kernel": "k_shade_mlp", "achieved": round(mlp_tflops, 2),
+        roofline = {"bound": "tensor", "kernel": "k_shade_mlp_tc", "achieved": round(mlp_tflops, 2),
                     "peak": tensor_peak, "peak_kind": peak_kind, "unit": "TFLOP/s",
                     "frac": round(mlp_tflops / tensor_peak, 4),
                     "traffic": load_traffic("shade_mlp_bf16"),

@@ -28,6 +28,7 @@ SOURCES = [
     ("k_deferred.cu", []),
     ("k_mlp.cu", []),
     ("k_textures.cu", []),
+    ("k_shade_tc.cu", []),
     ("cg_mlp.cpp", ["-Xcompiler", "-ffp-contract=off"]),
 ]
 

@@ -87,13 +87,12 @@ void stage_mark(cg_context* ctx, cudaStream_t s, const char* name) {
 extern "C" cg_status cg_context_last_samples(cg_context* ctx, uint64_t* samples) {
     CG_CHECK(ctx && samples, CG_ERR_INVALID_ARGUMENT, "cg_context_last_samples: null pointer");
     *samples = 0;
-    if (!ctx->samples_cnt.p || ctx->last_regions <= 0) return CG_OK;
+    if (!ctx->fallbacks.p || !ctx->shaded_valid) return CG_OK;
     CG_CUDA(cudaSetDevice(ctx->device));
     CG_CUDA(cudaDeviceSynchronize());
-    unsigned total = 0;
-    CG_CUDA(cudaMemcpy(&total, ctx->samples_cnt.as<unsigned>() + 2 * ctx->last_regions, 4,
-                       cudaMemcpyDeviceToHost));
-    *samples = total;
+    unsigned long long h[3] = {0, 0, 0};
+    CG_CUDA(cudaMemcpy(h, ctx->fallbacks.p, sizeof(h), cudaMemcpyDeviceToHost));
+    *samples = h[2];
     return CG_OK;
 }
 
@@ -927,13 +926,10 @@ extern "C" cg_status cg_render(cg_context* ctx, const cg_volume* v, const cg_cam
         CG_LAUNCH(ctx, launch_march(vd, cd, tp, sb, out, params->use_mlp != 0, s));
         stage_mark(ctx, s, "march");
         if (params->use_mlp) {
-            CG_CUDA(cudaMemsetAsync(ctx->fallbacks.p, 0, 8, s));
-            CG_LAUNCH(ctx, launch_region_scan(cd, sb, sb.offset, s));
-            ctx->launches++;  // the scan and the chunk-table fill
-            ctx->last_regions = ((cam->width + 15) / 16) * ((cam->height + 15) / 16) * 8;
-            stage_mark(ctx, s, "scan");
-            CG_LAUNCH(ctx, launch_shade_mlp(vd, cd, tp, md, sb, sb.offset,
-                                            ctx->fallbacks.as<unsigned long long>(), s));
+            CG_CUDA(cudaMemsetAsync(ctx->fallbacks.p, 0, 32, s));
+            ctx->shaded_valid = true;
+            CG_LAUNCH(ctx, launch_shade_mlp_tc(vd, cd, tp, md, sb,
+                                               ctx->fallbacks.as<unsigned long long>(), s));
             stage_mark(ctx, s, "shade_mlp");
             CG_LAUNCH(ctx, launch_accumulate(cd, tp, sb, out, s));
             stage_mark(ctx, s, "accumulate");

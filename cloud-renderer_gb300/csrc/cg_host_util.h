@@ -81,7 +81,7 @@ struct cg_context {
     cudaStream_t stream = nullptr;
     uint64_t launches = 0;
     int refs = 1;  // the caller's handle + one per volume / model created on it
-    int last_regions = 0;  // regions of the last surrogate render (sample total lookup)
+    bool shaded_valid = false;  // the status words hold a surrogate render's counters
     // optional per-stage CUDA-event timing of voxelize/render calls
     bool timing = false;
     int n_marks = 0;
@@ -97,7 +97,7 @@ struct cg_context {
     NoiseTab noise_tab{};
     // deferred renderer: recorded view samples and the MLP fallback counter
     DevBuf samples_pw, samples_gl, samples_cnt;
-    DevBuf fallbacks;
+    DevBuf fallbacks;  // surrogate render status (see launch_shade_mlp_tc)
     // noise lattice tables as 3D float textures (surrogate renderer)
     cudaArray_t noise_arr[CG_MAX_LEVELS] = {};
     cudaTextureObject_t noise_tex[CG_MAX_LEVELS] = {};

@@ -107,8 +107,13 @@ struct SampleBuf {
     float4* pos_w;
     float2* light_lane;
     unsigned* count;  // samples per region
-    unsigned* offset; // exclusive scan of count (regions + 1)
-    unsigned* chunk_region;  // region of the first sample of each 32-sample chunk
+    // flat order (written by the march): each march CTA's 8 regions occupy a
+    // contiguous range padded to 32-sample chunks; offset[r] = region r's
+    // first flat index, chunk_region[c] = region holding chunk c's first
+    // sample, *flat_total = padded total (zeroed before the march)
+    unsigned* offset;
+    unsigned* chunk_region;
+    unsigned* flat_total;
     uint2* steps;     // per region, per emitting step: (first slot, lane ballot)
     unsigned* nsteps; // emitting steps per region
     int capacity;     // 32 * view_steps
@@ -190,10 +195,11 @@ cudaError_t launch_shade_exact(VolDesc vd, CamDesc cam, TraceParams tp, SampleBu
 cudaError_t launch_pack_level(VolDesc vd, int l, cudaSurfaceObject_t surf, cudaStream_t st);
 cudaError_t launch_fbm_volume(TraceParams tp, const float wmin[3], const float range[3], int R,
                               cudaSurfaceObject_t surf, cudaStream_t st);
-cudaError_t launch_region_scan(CamDesc cam, SampleBuf sb, unsigned* offset, cudaStream_t st);
-cudaError_t launch_shade_mlp(VolDesc vd, CamDesc cam, TraceParams tp, const MlpDev& m,
-                             SampleBuf sb, const unsigned* offset,
-                             unsigned long long* fallbacks, cudaStream_t st);
+// Surrogate shading on the tensor cores (k_shade_tc.cu).  status (4 words,
+// zeroed before the launch): [0] += exact-cone fallbacks, [1] |= 1 when a
+// bounded wait ran out, [2] += samples shaded, [3] region cursor.
+cudaError_t launch_shade_mlp_tc(VolDesc vd, CamDesc cam, TraceParams tp, const MlpDev& m,
+                                SampleBuf sb, unsigned long long* status, cudaStream_t st);
 cudaError_t launch_accumulate(CamDesc cam, TraceParams tp, SampleBuf sb, float4* out,
                               cudaStream_t st);
 cudaError_t launch_mlp_features(VolDesc vd, const MlpDev& m, const float* pos, int n,

@@ -213,8 +213,10 @@ cg_status ensure_samples(cg_context* ctx, int width, int height, int view_steps,
     const size_t n = regions * cap;
     CG_CHECK(n < (size_t)0xFFFFFFFFu, CG_ERR_OUT_OF_RANGE,
              "render: %zu sample slots (pixels x view_steps) exceed 2^32", n);
-    // counts, offsets, chunk regions, step counts, step tables (2 words each)
-    const size_t idx_words = 2 * regions + 1 + n / 32 + 1 + regions + 2 * regions * view_steps + 2;
+    // counts, offsets, step counts, flat total, chunk regions (one per chunk
+    // of the padded flat order), step tables (2 words each)
+    const size_t chunks = n / 32 + regions / 8 + 2;
+    const size_t idx_words = 3 * regions + 1 + chunks + 2 * regions * view_steps + 2;
     if (ctx->samples_pw.bytes < n * 16 || ctx->samples_gl.bytes < n * 8 ||
         ctx->samples_cnt.bytes < idx_words * 4) {
         CG_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -222,15 +224,16 @@ cg_status ensure_samples(cg_context* ctx, int width, int height, int view_steps,
         CG_CUDA(ctx->samples_gl.ensure(n * 8));
         CG_CUDA(ctx->samples_cnt.ensure(idx_words * 4));
     }
-    CG_CUDA(ctx->fallbacks.ensure(16));
+    CG_CUDA(ctx->fallbacks.ensure(32));
     sb.pos_w = ctx->samples_pw.as<float4>();
     sb.light_lane = ctx->samples_gl.as<float2>();
     sb.count = ctx->samples_cnt.as<unsigned>();
     sb.offset = sb.count + regions;
-    sb.chunk_region = sb.offset + regions + 1;
-    sb.nsteps = sb.chunk_region + n / 32 + 1;
+    sb.nsteps = sb.offset + regions;
+    sb.flat_total = sb.nsteps + regions;
+    sb.chunk_region = sb.flat_total + 1;
     // 8-byte aligned start for the (slot, ballot) pairs
-    size_t at = (size_t)(sb.nsteps + regions - ctx->samples_cnt.as<unsigned>());
+    size_t at = (size_t)(sb.chunk_region + chunks - ctx->samples_cnt.as<unsigned>());
     at = (at + 1) & ~(size_t)1;
     sb.steps = reinterpret_cast<uint2*>(ctx->samples_cnt.as<unsigned>() + at);
     sb.capacity = (int)cap;
@@ -243,9 +246,11 @@ extern "C" cg_status cg_context_mlp_fallbacks(cg_context* ctx, uint64_t* out) {
     if (!ctx->fallbacks.p) return CG_OK;
     CG_CUDA(cudaSetDevice(ctx->device));
     CG_CUDA(cudaDeviceSynchronize());
-    unsigned long long h = 0;
-    CG_CUDA(cudaMemcpy(&h, ctx->fallbacks.p, 8, cudaMemcpyDeviceToHost));
-    *out = h;
+    unsigned long long h[2] = {0, 0};
+    CG_CUDA(cudaMemcpy(h, ctx->fallbacks.p, 16, cudaMemcpyDeviceToHost));
+    *out = h[0];
+    CG_CHECK(h[1] == 0, CG_ERR_DEVICE_FAULT,
+             "surrogate render: a tensor-core wait ran out of its iteration limit");
     return CG_OK;
 }
 

@@ -133,6 +133,25 @@ __global__ void __launch_bounds__(256) k_march(VolDesc vd, CamDesc cam, TracePar
         sb.nsteps[region] = nsteps;
     }
     if (valid) out[(size_t)py * cam.W + px] = make_float4(0.f, 0.f, 0.f, 1.f - T);
+    // Flat order for the shading pass: the CTA's 8 regions take one contiguous
+    // range (reserved with one atomic, padded to whole 32-sample chunks so
+    // that no chunk spans two CTAs), and every chunk that starts inside a
+    // region records that region.
+    __shared__ unsigned s_cnt[8], s_base;
+    const int w = threadIdx.x >> 5;
+    if (lane == 0) s_cnt[w] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned tot = 0;
+        for (int k = 0; k < 8; ++k) tot += s_cnt[k];
+        s_base = tot ? atomicAdd(sb.flat_total, (tot + 31u) & ~31u) : 0u;
+    }
+    __syncthreads();
+    unsigned o0 = s_base;
+    for (int k = 0; k < w; ++k) o0 += s_cnt[k];
+    if (lane == 0) sb.offset[region] = o0;
+    for (unsigned ch = (o0 + 31u) / 32u + lane; ch * 32u < o0 + cnt; ch += 32u)
+        sb.chunk_region[ch] = (unsigned)region;
 }
 
 // Sum of each lane's contributions over one chunk of up to 32 samples:
@@ -189,144 +208,6 @@ __global__ void __launch_bounds__(128) k_shade_exact(VolDesc vd, CamDesc cam, Tr
     write_rgb(out, cam, px, py, acc + comp, tp);
 }
 
-// For every 32-sample chunk of the flat order, the region holding its first
-// sample (one thread per region writes the chunks that start inside it).
-__global__ void k_chunk_fill(const unsigned* offset, int regions, unsigned* chunk_region) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= regions) return;
-    const unsigned o0 = offset[r], o1 = offset[r + 1];
-    for (unsigned ch = (o0 + 31) / 32; ch * 32 < o1; ++ch) chunk_region[ch] = (unsigned)r;
-}
-
-// Exclusive scan of the region sample counts (one CTA, 4096 per tile).
-__global__ void __launch_bounds__(1024) k_region_scan(const unsigned* count, int n,
-                                                      unsigned* offset) {
-    __shared__ unsigned warp_sums[32];
-    __shared__ unsigned carry_s;
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    if (tid == 0) carry_s = 0;
-    __syncthreads();
-    for (int base = 0; base < n; base += 4096) {
-        const int i0 = base + tid * 4;
-        unsigned c[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) c[k] = (i0 + k < n) ? count[i0 + k] : 0u;
-        const unsigned s = c[0] + c[1] + c[2] + c[3];
-        unsigned x = s;
-        for (int o = 1; o < 32; o <<= 1) {
-            unsigned y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
-        }
-        if (lane == 31) warp_sums[wid] = x;
-        __syncthreads();
-        if (wid == 0) {
-            unsigned w = warp_sums[lane], z = w;
-            for (int o = 1; o < 32; o <<= 1) {
-                unsigned y = __shfl_up_sync(0xffffffffu, z, o);
-                if (lane >= o) z += y;
-            }
-            warp_sums[lane] = z - w;
-        }
-        __syncthreads();
-        const unsigned carry = carry_s;
-        unsigned run = carry + warp_sums[wid] + x - s;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            if (i0 + k < n) offset[i0 + k] = run;
-            run += c[k];
-        }
-        __syncthreads();
-        if (tid == 1023) carry_s = carry + warp_sums[wid] + x;
-        __syncthreads();
-    }
-    if (tid == 0) offset[n] = carry_s;
-}
-
-// MLP shading over flat chunks of 32 samples (persistent warps).  Each lane
-// finds its sample's region from the scanned offsets, computes the 16
-// features, the warp runs the network (two 16-row blocks), and samples with
-// a feature outside the trained range take the exact cone instead.  The
-// contribution w * T_sun * (ambient + (1 - ambient) G) replaces w in place.
-template <int FMT>
-__global__ void __launch_bounds__(128, 4) k_shade_mlp(VolDesc vd, TraceParams tp, ConeSchedule cs,
-                                                   MlpDev m, SampleBuf sb, const unsigned* offset,
-                                                   const unsigned* chunk_region, int regions,
-                                                   unsigned long long* fallbacks) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    __half* sW = reinterpret_cast<__half*>(smem);
-    float* sB = reinterpret_cast<float*>(sW + MLP_SMEM_W_HALFS);
-    __half* sXall = reinterpret_cast<__half*>(sB + 3 * 64 + 4);
-    float* sYall = reinterpret_cast<float*>(sXall + 4 * 32 * MLP_S16);
-    mlp::load_weights(m.w16, sW);
-    for (int i = threadIdx.x; i < 3 * 64 + 1; i += blockDim.x)
-        sB[i] = i < 64 ? m.params[MLP_B1 + i]
-                       : (i < 128 ? m.params[MLP_B2 + i - 64]
-                                  : (i < 192 ? m.params[MLP_B3 + i - 128] : m.params[MLP_B4]));
-    __syncthreads();
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    __half* sX = sXall + w * 32 * MLP_S16;
-    float* sY = sYall + w * 32;
-    const unsigned total = offset[regions];
-    const unsigned nchunks = (total + 31) / 32;
-    unsigned n_fallback = 0;
-    for (unsigned c = blockIdx.x * 4 + w; c < nchunks; c += gridDim.x * 4) {
-        const unsigned i = c * 32 + lane;
-        // region of the chunk's first sample (filled by the scan), then walk
-        int r = (int)chunk_region[c];
-        const bool have = i < total;
-        float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
-        float2 gv = make_float2(0.f, 0.f);
-        size_t idx = 0;
-        bool fb = false;
-        if (have) {
-            while (offset[r + 1] <= i) ++r;
-            idx = (size_t)r * sb.capacity + (i - offset[r]);
-            s = sb.pos_w[idx];
-            gv = sb.light_lane[idx];
-            float f[MLP_IN];
-            mlp::features<FMT, true>(vd, m, s.x, s.y, s.z, tp.sun[0], tp.sun[1], tp.sun[2], f);
-            fb = !mlp::in_range(m, f);
-#pragma unroll
-            for (int j = 0; j < MLP_IN; j += 2)
-                *reinterpret_cast<__half2*>(sX + lane * MLP_S16 + j) = __floats2half2_rn(
-                    (f[j] - m.mu[j]) * m.inv_sd[j], (f[j + 1] - m.mu[j + 1]) * m.inv_sd[j + 1]);
-        } else {
-#pragma unroll
-            for (int j = 0; j < MLP_IN; j += 2)
-                *reinterpret_cast<__half2*>(sX + lane * MLP_S16 + j) = __floats2half2_rn(0.f, 0.f);
-        }
-        __syncwarp();
-        {
-            float y[2][2];
-            mlp::forward32(sX, sW, sB, sB + 64, sB + 128, sB[192], y);
-            if (t == 0) {
-                sY[g] = y[0][0];
-                sY[g + 8] = y[0][1];
-                sY[16 + g] = y[1][0];
-                sY[24 + g] = y[1][1];
-            }
-        }
-        __syncwarp();
-        if (have) {
-            float tau;
-            if (fb) {
-                tau = cgs::sun_cone<FMT>(vd, cs, s.x, s.y, s.z, tp.sun[0], tp.sun[1], tp.sun[2]);
-                n_fallback++;
-            } else {
-                tau = m.tau_scale * mlp::softplus(sY[lane]);
-            }
-            const float L = __expf(-tp.sigma * tau) * (tp.ambient + (1.f - tp.ambient) * gv.x);
-            sb.pos_w[idx].w = s.w * L;
-        }
-        __syncwarp();
-    }
-    if (fallbacks) {
-        unsigned tot = n_fallback;
-        for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
-        if (lane == 0 && tot) atomicAdd(fallbacks, (unsigned long long)tot);
-    }
-}
-
 // Per region: each pixel sums the contributions of its own samples in step
 // order, locating them through the march's step table (base slot, ballot).
 __global__ void __launch_bounds__(128) k_accumulate(CamDesc cam, TraceParams tp, SampleBuf sb,
@@ -355,6 +236,9 @@ static int regions_of(const CamDesc& cam) { return ((cam.W + 15) / 16) * ((cam.H
 
 cudaError_t launch_march(VolDesc vd, CamDesc cam, TraceParams tp, SampleBuf sb, float4* out,
                          bool hw, cudaStream_t st) {
+    // the flat-order reservation counter starts from zero on every launch
+    cudaError_t e = cudaMemsetAsync(sb.flat_total, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
     dim3 grd((cam.W + 15) / 16, (cam.H + 15) / 16);
     if (hw)
         k_march<0, true><<<grd, 256, 0, st>>>(vd, cam, tp, sb, out);
@@ -374,46 +258,6 @@ cudaError_t launch_shade_exact(VolDesc vd, CamDesc cam, TraceParams tp, SampleBu
         k_shade_exact<0><<<blocks, 128, 0, st>>>(vd, cam, tp, cs, sb, regions, tiles_x, out);
     else
         k_shade_exact<1><<<blocks, 128, 0, st>>>(vd, cam, tp, cs, sb, regions, tiles_x, out);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_region_scan(CamDesc cam, SampleBuf sb, unsigned* offset, cudaStream_t st) {
-    const int regions = regions_of(cam);
-    k_region_scan<<<1, 1024, 0, st>>>(sb.count, regions, offset);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    k_chunk_fill<<<(regions + 255) / 256, 256, 0, st>>>(offset, regions, sb.chunk_region);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_shade_mlp(VolDesc vd, CamDesc cam, TraceParams tp, const MlpDev& m,
-                             SampleBuf sb, const unsigned* offset,
-                             unsigned long long* fallbacks, cudaStream_t st) {
-    ConeSchedule cs = make_cone_schedule(vd, tp);
-    const size_t sm = (size_t)MLP_SMEM_W_HALFS * 2 + (3 * 64 + 4) * 4 + 4 * 32 * MLP_S16 * 2 +
-                      4 * 32 * 4;
-    const int blocks = 152 * 8;  // persistent warps; weights staged once per CTA
-    static bool configured[2][64] = {};
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-    const int f = vd.fmt == 0 ? 0 : 1;
-    if (!configured[f][dev]) {
-        e = f == 0 ? cudaFuncSetAttribute(k_shade_mlp<0>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)
-                   : cudaFuncSetAttribute(k_shade_mlp<1>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        if (e != cudaSuccess) return e;
-        configured[f][dev] = true;
-    }
-    const int regions = regions_of(cam);
-    if (f == 0)
-        k_shade_mlp<0><<<blocks, 128, sm, st>>>(vd, tp, cs, m, sb, offset, sb.chunk_region,
-                                                regions, fallbacks);
-    else
-        k_shade_mlp<1><<<blocks, 128, sm, st>>>(vd, tp, cs, m, sb, offset, sb.chunk_region,
-                                                regions, fallbacks);
     return cudaGetLastError();
 }
 

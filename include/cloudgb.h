@@ -309,7 +309,9 @@ cg_status cg_mlp_set_params(cg_mlp* mlp, const float* params, const float* adam_
  * step, CRC32); training resumes bit-identically from it. */
 cg_status cg_mlp_save(const cg_mlp* mlp, const char* path);
 cg_status cg_mlp_load(cg_context* ctx, const char* path, cg_mlp** out);
-/* Samples of the last MLP render that fell back to the exact cone. */
+/* Samples of the last MLP render that fell back to the exact cone.  Returns
+ * CG_ERR_DEVICE_FAULT when that render's tensor-core pass stopped on a bounded
+ * wait (the image is then incomplete). */
 cg_status cg_context_mlp_fallbacks(cg_context* ctx, uint64_t* out);
 /* View samples the last MLP render shaded (one surrogate inference each). */
 cg_status cg_context_last_samples(cg_context* ctx, uint64_t* samples);
