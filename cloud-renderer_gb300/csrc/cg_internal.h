@@ -9,6 +9,7 @@
 #define CG_Q20 1048576LL
 #define CG_HALF_Q20 524288LL
 #define CG_KEY_EMPTY 0xFFFFFFFFFFFFFFFFULL
+#define CG_NO_SLOT 0xFFFFFFFFu
 #define CG_BRICK 8           // splat brick edge (voxels)
 #define CG_FUSED_MIPS 3      // levels produced inside the splat kernel
 #define CG_SPLAT_CHUNK 256   // boards staged in shared memory per pass
@@ -108,11 +109,10 @@ struct SampleBuf {
     float2* light_lane;
     unsigned* count;  // samples per region
     // flat order (written by the march): each march CTA's 8 regions occupy a
-    // contiguous range padded to 32-sample chunks; offset[r] = region r's
-    // first flat index, chunk_region[c] = region holding chunk c's first
-    // sample, *flat_total = padded total (zeroed before the march)
-    unsigned* offset;
-    unsigned* chunk_region;
+    // contiguous range, padded to 32-sample chunks; slot_of[i] = slot
+    // (region * capacity + j) of flat row i, or CG_NO_SLOT for padding;
+    // *flat_total = padded total (zeroed before the march)
+    unsigned* slot_of;
     unsigned* flat_total;
     uint2* steps;     // per region, per emitting step: (first slot, lane ballot)
     unsigned* nsteps; // emitting steps per region
@@ -146,6 +146,16 @@ struct SampleBuf {
 // Inputs are normalised x = (f - mu) * inv_sd; the output y gives
 // tau = tau_scale * softplus(y).  Samples with a feature outside
 // [fmin, fmax] fall back to the exact cone.
+// Biases and the output row by value (kernel parameters, so that unrolled
+// code reads them as constant operands): hb = (b1 | b2 | b3) / 2 for the
+// half-scaled hidden layers of the inference kernel, w4 = W4 row 0 as
+// FP16-rounded floats, b4 the output bias.
+struct MlpConsts {
+    float hb[3 * MLP_H];
+    float w4[MLP_H];
+    float b4;
+};
+
 struct MlpDev {
     const float* params;  // FP32 master (biases read from here)
     const __half* w16;    // FP16 weight image
@@ -153,7 +163,32 @@ struct MlpDev {
     float tau_scale;
     float h0;
     int lb;
+    MlpConsts k;          // copy of the current biases (for inference)
 };
+
+// Feature-tap geometry of a (model, volume) pair, precomputed on the host:
+// tap 3i+k reads level l_i (tex[i]) at texel coordinate v * sc[i] + dsc[3i+k] * s.
+struct FeatGeom {
+    float dsc[12];
+    float sc[4];
+    unsigned long long tex[4];
+    float invD;
+};
+
+inline FeatGeom feat_geom(const VolDesc& vd, const MlpDev& m) {
+    FeatGeom g;
+    for (int i = 0; i < 4; ++i) {
+        const int lv = m.lb + i;
+        const int l = lv < 0 ? 0 : (lv > vd.L - 1 ? vd.L - 1 : lv);
+        const float sc = (float)vd.dims[l] / (float)vd.D;
+        const float span = (float)(1 << lv);
+        for (int k = 0; k < 3; ++k) g.dsc[3 * i + k] = (m.h0 + ((float)k + 0.5f) * span) * sc;
+        g.sc[i] = sc;
+        g.tex[i] = vd.tex[l];
+    }
+    g.invD = 1.f / (float)vd.D;
+    return g;
+}
 
 struct TrainArgs {
     const float* feat;  // [N][16] raw features

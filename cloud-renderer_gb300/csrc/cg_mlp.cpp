@@ -13,6 +13,7 @@ struct cg_mlp {
     DevBuf params, w16, m, v, step, ticket, partial, loss, grad;
     cg_mlp_config cfg{};
     int host_step = 0;
+    MlpConsts consts{};  // host copy of the biases / output row (see MlpConsts)
 };
 
 namespace {
@@ -55,9 +56,21 @@ void half_image(const float* p, std::vector<__half>& h) {
     for (int i = 0; i < 64; ++i) h[MLP_H_W4 + i] = __float2half(p[MLP_W4 + i]);
 }
 
+void set_consts(cg_mlp* m, const float* b1, const float* b2, const float* b3, const float* w4,
+                float b4) {
+    for (int i = 0; i < MLP_H; ++i) {
+        m->consts.hb[i] = 0.5f * b1[i];
+        m->consts.hb[MLP_H + i] = 0.5f * b2[i];
+        m->consts.hb[2 * MLP_H + i] = 0.5f * b3[i];
+        m->consts.w4[i] = __half2float(__float2half(w4[i]));
+    }
+    m->consts.b4 = b4;
+}
+
 cg_status upload_params(cg_mlp* m, const float* p) {
     std::vector<__half> h;
     half_image(p, h);
+    set_consts(m, p + MLP_B1, p + MLP_B2, p + MLP_B3, p + MLP_W4, p[MLP_B4]);
     CG_CUDA(cudaMemcpy(m->params.p, p, MLP_NPARAM * 4, cudaMemcpyHostToDevice));
     CG_CUDA(cudaMemcpy(m->w16.p, h.data(), MLP_NHALF * 2, cudaMemcpyHostToDevice));
     return CG_OK;
@@ -76,6 +89,7 @@ MlpDev device_view(const cg_mlp* m) {
     d.tau_scale = m->cfg.tau_scale;
     d.h0 = m->cfg.initial_height;
     d.lb = m->cfg.base_level;
+    d.k = m->consts;
     return d;
 }
 
@@ -213,10 +227,10 @@ cg_status ensure_samples(cg_context* ctx, int width, int height, int view_steps,
     const size_t n = regions * cap;
     CG_CHECK(n < (size_t)0xFFFFFFFFu, CG_ERR_OUT_OF_RANGE,
              "render: %zu sample slots (pixels x view_steps) exceed 2^32", n);
-    // counts, offsets, step counts, flat total, chunk regions (one per chunk
-    // of the padded flat order), step tables (2 words each)
-    const size_t chunks = n / 32 + regions / 8 + 2;
-    const size_t idx_words = 3 * regions + 1 + chunks + 2 * regions * view_steps + 2;
+    // counts, step counts, flat total, step tables (2 words each), flat slots
+    // (the padded flat order has at most 31 padding rows per 8 regions)
+    const size_t flat = n + 32 * (regions / 8 + 1);
+    const size_t idx_words = 2 * regions + 2 + 2 * regions * view_steps + 2 + flat;
     if (ctx->samples_pw.bytes < n * 16 || ctx->samples_gl.bytes < n * 8 ||
         ctx->samples_cnt.bytes < idx_words * 4) {
         CG_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -228,14 +242,13 @@ cg_status ensure_samples(cg_context* ctx, int width, int height, int view_steps,
     sb.pos_w = ctx->samples_pw.as<float4>();
     sb.light_lane = ctx->samples_gl.as<float2>();
     sb.count = ctx->samples_cnt.as<unsigned>();
-    sb.offset = sb.count + regions;
-    sb.nsteps = sb.offset + regions;
+    sb.nsteps = sb.count + regions;
     sb.flat_total = sb.nsteps + regions;
-    sb.chunk_region = sb.flat_total + 1;
     // 8-byte aligned start for the (slot, ballot) pairs
-    size_t at = (size_t)(sb.chunk_region + chunks - ctx->samples_cnt.as<unsigned>());
+    size_t at = (size_t)(sb.flat_total + 1 - ctx->samples_cnt.as<unsigned>());
     at = (at + 1) & ~(size_t)1;
     sb.steps = reinterpret_cast<uint2*>(ctx->samples_cnt.as<unsigned>() + at);
+    sb.slot_of = ctx->samples_cnt.as<unsigned>() + at + 2 * regions * (size_t)view_steps;
     sb.capacity = (int)cap;
     return CG_OK;
 }
@@ -496,8 +509,15 @@ extern "C" cg_status cg_mlp_train(cg_mlp* m, const float* d_features, const floa
                                 cudaMemcpyDeviceToHost, s));
     int step = 0;
     CG_CUDA(cudaMemcpyAsync(&step, m->step.p, 4, cudaMemcpyDeviceToHost, s));
+    // the trained biases and output row for the renderer's constants
+    std::vector<float> tail(MLP_NPARAM - MLP_B1);
+    CG_CUDA(cudaMemcpyAsync(tail.data(), m->params.as<float>() + MLP_B1, tail.size() * 4,
+                            cudaMemcpyDeviceToHost, s));
     CG_CUDA(cudaStreamSynchronize(s));
     m->host_step = step;
+    const float* t = tail.data();  // flat layout from MLP_B1 on
+    set_consts(m, t, t + (MLP_B2 - MLP_B1), t + (MLP_B3 - MLP_B1), t + (MLP_W4 - MLP_B1),
+               t[MLP_B4 - MLP_B1]);
     return CG_OK;
 }
 

@@ -320,31 +320,26 @@ __device__ __forceinline__ void forward32(const __half* sX, const __half* sW, co
     }
 }
 
-// Features of one query (see MlpDev).  HW: density taps filtered by the
-// texture unit (the surrogate renderer's path; training uses the same).
-template <int FMT, bool HW>
-__device__ __forceinline__ void features(const VolDesc& vd, const MlpDev& m, float vx, float vy,
-                                         float vz, float sx, float sy, float sz,
-                                         float f[MLP_IN]) {
+// Features of one query (see MlpDev, FeatGeom): the 12 density taps are
+// filtered by the texture unit (training and inference share this function).
+__device__ __forceinline__ void features(const FeatGeom& g, float vx, float vy, float vz,
+                                         float sx, float sy, float sz, float f[MLP_IN]) {
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-        const int lv = m.lb + i;
-        const int l = min(max(lv, 0), vd.L - 1);
-        const float span = (float)(1 << lv);
+        const float X = vx * g.sc[i], Y = vy * g.sc[i], Z = vz * g.sc[i];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            const float d = m.h0 + ((float)k + 0.5f) * span;
-            const float x = vx + d * sx, y = vy + d * sy, z = vz + d * sz;
+            const float d = g.dsc[3 * i + k];
             // the texture returns exactly 0 on an empty footprint: no
             // occupancy branch, so the 12 fetches issue back to back
-            f[3 * i + k] = HW ? cgs::tri_hw<false>(vd, l, x, y, z).x
-                              : cgs::tri<FMT, false, true, true>(vd, l, x, y, z).x;
+            f[3 * i + k] = tex3D<float2>((cudaTextureObject_t)g.tex[i], fmaf(d, sx, X),
+                                         fmaf(d, sy, Y), fmaf(d, sz, Z))
+                               .x;
         }
     }
-    const float invD = 1.f / (float)vd.D;
-    f[12] = vx * invD;
-    f[13] = vy * invD;
-    f[14] = vz * invD;
+    f[12] = vx * g.invD;
+    f[13] = vy * g.invD;
+    f[14] = vz * g.invD;
     f[15] = sy;
 }
 

@@ -44,18 +44,21 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
 __device__ __forceinline__ void fence_mbar_init() {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
+// One test of the phase with parity `phase`; the thread may sleep (up to the
+// suspend-time hint, 10 ms) until the phase completes instead of spinning.
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned phase) {
     uint32_t ok;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
         " selp.u32 %0, 1, 0, p;\n}"
         : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(phase)
+        : "r"(smem_addr(bar)), "r"(phase), "r"(10000000u)
         : "memory");
     return ok != 0;
 }
 // Bounded wait for the phase with parity `phase` to complete; false when the
-// limit ran out (the caller reports an error instead of spinning forever).
+// limit (tests, each of which may sleep) ran out: the caller reports an error
+// instead of waiting forever.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned phase, unsigned limit) {
     for (unsigned i = 0; i < limit; ++i)
         if (mbar_try_wait(bar, phase)) return true;

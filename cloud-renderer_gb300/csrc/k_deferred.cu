@@ -134,24 +134,27 @@ __global__ void __launch_bounds__(256) k_march(VolDesc vd, CamDesc cam, TracePar
     }
     if (valid) out[(size_t)py * cam.W + px] = make_float4(0.f, 0.f, 0.f, 1.f - T);
     // Flat order for the shading pass: the CTA's 8 regions take one contiguous
-    // range (reserved with one atomic, padded to whole 32-sample chunks so
-    // that no chunk spans two CTAs), and every chunk that starts inside a
-    // region records that region.
-    __shared__ unsigned s_cnt[8], s_base;
+    // range (reserved with one atomic, padded to whole 32-sample chunks), and
+    // every flat row records its sample's slot.
+    __shared__ unsigned s_cnt[8], s_base, s_tot;
     const int w = threadIdx.x >> 5;
     if (lane == 0) s_cnt[w] = cnt;
     __syncthreads();
     if (threadIdx.x == 0) {
         unsigned tot = 0;
         for (int k = 0; k < 8; ++k) tot += s_cnt[k];
+        s_tot = tot;
         s_base = tot ? atomicAdd(sb.flat_total, (tot + 31u) & ~31u) : 0u;
     }
     __syncthreads();
     unsigned o0 = s_base;
     for (int k = 0; k < w; ++k) o0 += s_cnt[k];
-    if (lane == 0) sb.offset[region] = o0;
-    for (unsigned ch = (o0 + 31u) / 32u + lane; ch * 32u < o0 + cnt; ch += 32u)
-        sb.chunk_region[ch] = (unsigned)region;
+    const unsigned slot0 = (unsigned)region * (unsigned)sb.capacity;
+    for (unsigned j = lane; j < cnt; j += 32u) sb.slot_of[o0 + j] = slot0 + j;
+    if (w == 7) {
+        const unsigned end = s_base + s_tot, pad_end = s_base + ((s_tot + 31u) & ~31u);
+        if (end + lane < pad_end) sb.slot_of[end + lane] = CG_NO_SLOT;
+    }
 }
 
 // Sum of each lane's contributions over one chunk of up to 32 samples:

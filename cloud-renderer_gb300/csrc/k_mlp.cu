@@ -8,13 +8,12 @@ namespace {
 using namespace mlp;
 
 // ---- features ----------------------------------------------------------------
-template <int FMT>
-__global__ void k_mlp_features(VolDesc vd, MlpDev m, const float* pos, int n, float sx, float sy,
-                               float sz, float* out) {
+__global__ void k_mlp_features(FeatGeom g, const float* pos, int n, float sx, float sy, float sz,
+                               float* out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float f[MLP_IN];
-    features<FMT, true>(vd, m, pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], sx, sy, sz, f);
+    features(g, pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], sx, sy, sz, f);
 #pragma unroll
     for (int j = 0; j < MLP_IN; ++j) out[(size_t)i * MLP_IN + j] = f[j];
 }
@@ -410,10 +409,8 @@ __global__ void k_mlp_adam(AdamArgs aa) {
 cudaError_t launch_mlp_features(VolDesc vd, const MlpDev& m, const float* pos, int n,
                                 const float dir[3], float* out, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    if (vd.fmt == 0)
-        k_mlp_features<0><<<(n + 127) / 128, 128, 0, st>>>(vd, m, pos, n, dir[0], dir[1], dir[2], out);
-    else
-        k_mlp_features<1><<<(n + 127) / 128, 128, 0, st>>>(vd, m, pos, n, dir[0], dir[1], dir[2], out);
+    k_mlp_features<<<(n + 127) / 128, 128, 0, st>>>(feat_geom(vd, m), pos, n, dir[0], dir[1],
+                                                    dir[2], out);
     return cudaGetLastError();
 }
 

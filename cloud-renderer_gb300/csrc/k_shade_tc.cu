@@ -2,21 +2,26 @@
 // cores: sun transmittance of every recorded view sample through the MLP
 // (16 -> 64 -> 64 -> 64 SiLU -> 1, FP16 operands, FP32 accumulation).
 //
-// One CTA = 4 warps = one 128-row tile at a time (persistent over tiles).
+// One CTA = 4 warps (thread = row of a 128-row tile), persistent over tiles.
 // Per tile:
-//   1. each thread gathers its sample, computes the 16 features (12 texture
-//      taps), and writes the normalised FP16 row into the activation tile
-//      (shared memory, 128B-swizzled K-major);
+//   1. each thread's row holds the normalised FP16 features of its sample in
+//      the activation tile (shared memory, 128B-swizzled K-major);
 //   2. thread 0 issues layer 1 (one tcgen05.mma, M=128 N=64 K=16) into tensor
 //      memory and commits it to an mbarrier;
-//   3. each warp reads its 32 rows x 64 FP32 columns back (tcgen05.ld), adds
-//      the bias, applies SiLU in FP16 pairs and writes the next activation
-//      tile in place; layers 2 and 3 are 4 MMAs each (K = 64);
+//   3. each warp reads its 32 rows back (tcgen05.ld), adds the bias, applies
+//      SiLU in FP16 pairs and writes the next activation tile in place;
+//      layers 2 and 3 are 4 MMAs each (K = 64);
 //   4. the last epilogue folds the 64 -> 1 output layer into FP32 FMAs, then
-//      the softplus link, the transmittance and the sample's contribution.
-// The weights (three 64-row tiles) are staged once per CTA.  Every mbarrier
-// wait is bounded: on a timeout the CTA records an error, waits (bounded) for
-// its MMA to drain, frees its tensor memory and returns.
+//      the softplus link, the transmittance and the sample's contribution;
+//      the next tile's inputs go into the tile.
+// The next tile is fetched in stages while this one runs, so that no load is
+// consumed in the phase that issued it: its slot (layer 1), its sample
+// (layer 2), its 12 texture taps (layer 3), its inputs (output).
+// Layers 1-3 run on weights and biases pre-scaled by 1/2 (exact in FP16 and
+// FP32), so the accumulator holds z/2 and SiLU is z/2 * (1 + tanh(z/2)):
+// one MUFU and one FMA per FP16 pair.
+// Every mbarrier wait is bounded: on a timeout the CTA records an error,
+// waits (bounded) for its MMA to drain, frees its tensor memory and returns.
 #include <cuda_fp16.h>
 
 #include "cg_deferred.cuh"
@@ -30,87 +35,153 @@ namespace {
 constexpr uint32_t TC_TMEM_COLS = 64;
 constexpr unsigned TC_WAIT_LIMIT = 1u << 22;
 // shared memory map (bytes from the 1024-aligned base)
-constexpr int OFF_ACT = 0;               // 128 x 128 B activation tile
-constexpr int OFF_W1 = 16384;            // 64 x 128 B (K = 16 used)
-constexpr int OFF_W2 = OFF_W1 + 8192;    // 64 x 128 B
-constexpr int OFF_W3 = OFF_W2 + 8192;    // 64 x 128 B
-constexpr int OFF_BIAS = OFF_W3 + 8192;  // b1, b2, b3 (192 floats), w4 (64), b4
-constexpr int OFF_BAR = OFF_BIAS + (4 * 64 + 4) * 4;
-constexpr int SMEM_USED = OFF_BAR + 16;
+constexpr int OFF_ACT = 0;                 // 128 x 128 B activation tile
+constexpr int OFF_W1 = 16384;              // 64 x 128 B (K = 16 used)
+constexpr int OFF_W2 = OFF_W1 + 8192;      // 64 x 128 B
+constexpr int OFF_W3 = OFF_W2 + 8192;      // 64 x 128 B
+constexpr int OFF_BAR = OFF_W3 + 8192;     // mbarrier + tensor-memory address
+constexpr int SMEM_USED = OFF_BAR + 32;
 constexpr int SMEM_BYTES = SMEM_USED + 1024;  // + alignment slack
 
 constexpr uint32_t IDESC = tc::idesc_f16_f32(128, 64);
 
-// row r's 8 chunks of one FP16 weight row (64 halves) into a swizzled tile
-__device__ __forceinline__ void stage_row64(uint8_t* tile, int r, const __half* src, int chunks) {
+// One FP16 weight row (`chunks` x 8 halves, the rest zero) into row r of a
+// swizzled tile, optionally scaled by 1/2.
+__device__ __forceinline__ void stage_row(uint8_t* tile, int r, const __half* src, int chunks,
+                                          bool half_scale) {
+    const __half2 k = __floats2half2_rn(0.5f, 0.5f);
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
         uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (c < chunks) v = *reinterpret_cast<const uint4*>(src + 8 * c);
+        if (c < chunks) {
+            v = *reinterpret_cast<const uint4*>(src + 8 * c);
+            if (half_scale) {
+                __half2* h = reinterpret_cast<__half2*>(&v);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) h[q] = __hmul2(h[q], k);
+            }
+        }
         *reinterpret_cast<uint4*>(tile + tc::sw128_offset(r, c)) = v;
     }
 }
 
-// bias + SiLU of 32 accumulators -> 16 FP16 pairs
-__device__ __forceinline__ void bias_silu32(const uint32_t (&acc)[32], const float* bias,
-                                            uint32_t (&h)[16]) {
+// SiLU of 32 half-scaled accumulators (+ half-scaled bias) -> 16 FP16 pairs:
+// with h = z/2, silu(z) = h + h * tanh(h), evaluated in FP32 and rounded once.
+__device__ __forceinline__ void bias_silu32(const uint32_t (&acc)[32], const float* hb,
+                                            uint32_t (&out)[16]) {
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
-        const float a = __uint_as_float(acc[2 * j]) + bias[2 * j];
-        const float b = __uint_as_float(acc[2 * j + 1]) + bias[2 * j + 1];
-        h[j] = mlp::silu_h2(mlp::pack_h2(a, b));
+        const float a = __uint_as_float(acc[2 * j]) + hb[2 * j];
+        const float b = __uint_as_float(acc[2 * j + 1]) + hb[2 * j + 1];
+        float ta, tb;
+        asm("tanh.approx.f32 %0, %1;" : "=f"(ta) : "f"(a));
+        asm("tanh.approx.f32 %0, %1;" : "=f"(tb) : "f"(b));
+        out[j] = mlp::pack_h2(fmaf(a, ta, a), fmaf(b, tb, b));
     }
 }
 
-// Slot of flat row i: the chunk's first region, walked forward inside its
-// march CTA's group of 8 regions (padding rows past the group's samples are
-// not valid).
-__device__ __forceinline__ bool locate(const SampleBuf& sb, unsigned i, unsigned total,
-                                       size_t& idx) {
-    if (i >= total) return false;
-    unsigned r = sb.chunk_region[i >> 5];
-    const unsigned last = r | 7u;
-    unsigned o = sb.offset[r], e = o + sb.count[r];
-    while (i >= e && r < last) {
-        ++r;
-        o = sb.offset[r];
-        e = o + sb.count[r];
+// The exact cone for a sample whose features left the trained range (rare):
+// kept out of line so that the hot loop's registers are not sized for it.
+template <int FMT>
+__device__ __noinline__ float exact_tau(const VolDesc& vd, const ConeSchedule& cone, float x,
+                                        float y, float z, const float* sun) {
+    return cgs::sun_cone<FMT>(vd, cone, x, y, z, sun[0], sun[1], sun[2]);
+}
+
+// A tile row in flight: its sample slot, the output's inputs (weight, light)
+// and the exact-cone optical depth when a feature fell outside the trained
+// range (tau_fb >= 0), computed when the features were.
+struct Row {
+    unsigned slot;
+    float w, g, tau_fb;
+};
+
+// The 12 texture taps and the other inputs of a sample (issued early; the
+// results are consumed by pack_row).
+__device__ __forceinline__ void fetch_features(const FeatGeom& geo, const TraceParams& tp,
+                                               unsigned slot, const float4& s,
+                                               float (&f)[MLP_IN]) {
+    if (slot != CG_NO_SLOT) {
+        mlp::features(geo, s.x, s.y, s.z, tp.sun[0], tp.sun[1], tp.sun[2], f);
+    } else {
+#pragma unroll
+        for (int j = 0; j < MLP_IN; ++j) f[j] = 0.f;
     }
-    if (i >= e) return false;
-    idx = (size_t)r * sb.capacity + (i - o);
-    return true;
+}
+
+// Features -> the row state and the normalised FP16 inputs in chunks 0-1 of
+// the thread's tile row.
+template <int FMT>
+__device__ __forceinline__ void pack_row(const VolDesc& vd, const ConeSchedule& cone,
+                                         const MlpDev& m, const TraceParams& tp, unsigned slot,
+                                         const float4& s, float g, const float (&f)[MLP_IN],
+                                         Row& r, uint8_t* act) {
+    uint32_t x[8];
+    r.slot = slot;
+    r.w = s.w;
+    r.g = g;
+    r.tau_fb = -1.f;
+    if (slot != CG_NO_SLOT) {
+        if (!mlp::in_range(m, f)) r.tau_fb = exact_tau<FMT>(vd, cone, s.x, s.y, s.z, tp.sun);
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            x[q] = mlp::pack_h2((f[2 * q] - m.mu[2 * q]) * m.inv_sd[2 * q],
+                                (f[2 * q + 1] - m.mu[2 * q + 1]) * m.inv_sd[2 * q + 1]);
+    } else {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) x[q] = 0u;
+    }
+    const int tid = threadIdx.x;
+    *reinterpret_cast<uint4*>(act + tc::sw128_offset(tid, 0)) = make_uint4(x[0], x[1], x[2], x[3]);
+    *reinterpret_cast<uint4*>(act + tc::sw128_offset(tid, 1)) = make_uint4(x[4], x[5], x[6], x[7]);
+}
+
+__device__ __forceinline__ unsigned slot_at(const SampleBuf& sb, unsigned tile, unsigned ntiles,
+                                            unsigned total) {
+    const unsigned i = tile * 128u + threadIdx.x;
+    return (tile < ntiles && i < total) ? sb.slot_of[i] : CG_NO_SLOT;
+}
+
+// Issue one layer (thread 0) and commit it to the barrier.
+__device__ __forceinline__ void issue_layer(int layer, uint32_t d_tmem, uint32_t a_addr,
+                                            uint32_t w_addr, uint64_t* bar) {
+    const int ksteps = layer == 0 ? 1 : 4;
+    for (int k = 0; k < ksteps; ++k)
+        tc::mma_f16(d_tmem, tc::desc_sw128(a_addr + 32u * k), tc::desc_sw128(w_addr + 32u * k),
+                    IDESC, k > 0 ? 1u : 0u);
+    tc::mma_commit(bar);
+}
+
+// All writes of the CTA to the activation tiles -> visible to the tensor
+// core, then one thread issues.
+__device__ __forceinline__ void sync_for_mma() {
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
 }
 
 template <int FMT>
-__global__ void __launch_bounds__(128, 4) k_shade_mlp_tc(VolDesc vd, TraceParams tp,
-                                                         ConeSchedule cone, MlpDev m,
-                                                         SampleBuf sb,
-                                                         unsigned long long* status) {
+__global__ void __launch_bounds__(128, 4)
+    k_shade_mlp_tc(const __grid_constant__ VolDesc vd, const __grid_constant__ TraceParams tp,
+                   const __grid_constant__ ConeSchedule cone, const __grid_constant__ MlpDev m,
+                   const __grid_constant__ FeatGeom geo, SampleBuf sb,
+                   unsigned long long* status) {
     extern __shared__ uint8_t smem_raw[];
     const uint32_t raw = tc::smem_addr(smem_raw);
     uint8_t* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
     uint8_t* act = base + OFF_ACT;
-    float* sBias = reinterpret_cast<float*>(base + OFF_BIAS);  // [0,192) b1..b3, [192,256) w4
     uint64_t* bar = reinterpret_cast<uint64_t*>(base + OFF_BAR);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(base + OFF_BAR + 8);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-    // ---- stage weights (FP16 image: W1 [64][16], W2/W3 [64][64], W4 row 0)
+    // ---- stage weights: W1..W3 scaled by 1/2
     for (int r = tid; r < 64; r += blockDim.x) {
-        stage_row64(base + OFF_W1, r, m.w16 + MLP_H_W1 + r * 16, 2);
-        stage_row64(base + OFF_W2, r, m.w16 + MLP_H_W2 + r * 64, 8);
-        stage_row64(base + OFF_W3, r, m.w16 + MLP_H_W3 + r * 64, 8);
-    }
-    for (int i = tid; i < 256; i += blockDim.x) {
-        float v;
-        if (i < 64) v = m.params[MLP_B1 + i];
-        else if (i < 128) v = m.params[MLP_B2 + i - 64];
-        else if (i < 192) v = m.params[MLP_B3 + i - 128];
-        else v = __half2float(m.w16[MLP_H_W4 + (i - 192)]);
-        sBias[i] = v;
+        stage_row(base + OFF_W1, r, m.w16 + MLP_H_W1 + r * 16, 2, true);
+        stage_row(base + OFF_W2, r, m.w16 + MLP_H_W2 + r * 64, 8, true);
+        stage_row(base + OFF_W3, r, m.w16 + MLP_H_W3 + r * 64, 8, true);
     }
     if (tid == 0) {
-        sBias[256] = m.params[MLP_B4];
         tc::mbar_init(bar, 1);
         tc::fence_mbar_init();
     }
@@ -123,76 +194,50 @@ __global__ void __launch_bounds__(128, 4) k_shade_mlp_tc(VolDesc vd, TraceParams
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = *tslot;
-    const uint32_t tmem_warp = tmem + ((uint32_t)(warp * 32) << 16);
+    const uint32_t dw = tmem + ((uint32_t)(warp * 32) << 16);
     const uint32_t a_addr = tc::smem_addr(act);
-    const float b4 = sBias[256];
+    const uint32_t w_addr[3] = {tc::smem_addr(base + OFF_W1), tc::smem_addr(base + OFF_W2),
+                                tc::smem_addr(base + OFF_W3)};
     const float amb = tp.ambient;
     const unsigned total = *sb.flat_total;
     const unsigned ntiles = (total + 127u) / 128u;
     unsigned phase = 0, n_fallback = 0, n_valid = 0;
     bool failed = false;
 
-    // the current row: slot, position + weight, light; its features
+    // ---- the first tile's inputs
     unsigned tile = blockIdx.x;
-    size_t idx = 0;
-    bool valid = tile < ntiles && locate(sb, tile * 128u + tid, total, idx);
-    float4 s = valid ? sb.pos_w[idx] : make_float4(0.f, 0.f, 0.f, 0.f);
-    float g = valid ? sb.light_lane[idx].x : 0.f;
-    uint32_t xin[8];
-    bool fb = false;
-    auto featurize = [&](const float4& sp, bool v, uint32_t (&x)[8], bool& out_fb) {
-        if (v) {
-            float f[MLP_IN];
-            mlp::features<FMT, true>(vd, m, sp.x, sp.y, sp.z, tp.sun[0], tp.sun[1], tp.sun[2],
-                                     f);
-            out_fb = !mlp::in_range(m, f);
-#pragma unroll
-            for (int q = 0; q < 8; ++q)
-                x[q] = mlp::pack_h2((f[2 * q] - m.mu[2 * q]) * m.inv_sd[2 * q],
-                                    (f[2 * q + 1] - m.mu[2 * q + 1]) * m.inv_sd[2 * q + 1]);
-        } else {
-            out_fb = false;
-#pragma unroll
-            for (int q = 0; q < 8; ++q) x[q] = 0u;
+    Row row;
+    {
+        const unsigned slot = slot_at(sb, tile, ntiles, total);
+        float4 sp = make_float4(0.f, 0.f, 0.f, 0.f);
+        float g = 0.f;
+        if (slot != CG_NO_SLOT) {
+            sp = sb.pos_w[slot];
+            g = sb.light_lane[slot].x;
         }
-    };
-    featurize(s, valid, xin, fb);
+        float f[MLP_IN];
+        fetch_features(geo, tp, slot, sp, f);
+        pack_row<FMT>(vd, cone, m, tp, slot, sp, g, f, row, act);
+    }
 
     for (; tile < ntiles; tile += gridDim.x) {
-        // ---- A. the tile's inputs -> layer 1
-        *reinterpret_cast<uint4*>(act + tc::sw128_offset(tid, 0)) =
-            make_uint4(xin[0], xin[1], xin[2], xin[3]);
-        *reinterpret_cast<uint4*>(act + tc::sw128_offset(tid, 1)) =
-            make_uint4(xin[4], xin[5], xin[6], xin[7]);
-        // ---- B. the next tile's row: slot and sample loads (consumed in D)
         const unsigned ntile = tile + gridDim.x;
-        size_t nidx = 0;
-        const bool nvalid = ntile < ntiles && locate(sb, ntile * 128u + tid, total, nidx);
+        unsigned nslot = CG_NO_SLOT;
         float4 ns = make_float4(0.f, 0.f, 0.f, 0.f);
         float ng = 0.f;
-        if (nvalid) {
-            ns = sb.pos_w[nidx];
-            ng = sb.light_lane[nidx].x;
-        }
-        uint32_t nx[8];
-        bool nfb = false;
+        float nf[MLP_IN];
         float y = 0.f;
-#pragma unroll 1
+#pragma unroll
         for (int layer = 0; layer < 3; ++layer) {
-            tc::fence_proxy_async();
-            tc::fence_before_sync();
-            __syncthreads();
-            tc::fence_after_sync();
-            if (tid == 0) {
-                const uint32_t w_addr = tc::smem_addr(base + OFF_W1 + 8192 * layer);
-                const int ksteps = layer == 0 ? 1 : 4;
-                for (int k = 0; k < ksteps; ++k)
-                    tc::mma_f16(tmem, tc::desc_sw128(a_addr + 32u * k),
-                                tc::desc_sw128(w_addr + 32u * k), IDESC, k > 0 ? 1u : 0u);
-                tc::mma_commit(bar);
+            sync_for_mma();
+            if (tid == 0) issue_layer(layer, tmem, a_addr, w_addr[layer], bar);
+            // ---- the next tile, in stages
+            if (layer == 0) nslot = slot_at(sb, ntile, ntiles, total);
+            if (layer == 1 && nslot != CG_NO_SLOT) {
+                ns = sb.pos_w[nslot];
+                ng = sb.light_lane[nslot].x;
             }
-            // ---- D. while layer 2 runs: the next chunk's features
-            if (layer == 1) featurize(ns, nvalid, nx, nfb);
+            if (layer == 2) fetch_features(geo, tp, nslot, ns, nf);
             const bool ok = tc::mbar_wait(bar, phase, TC_WAIT_LIMIT);
             phase ^= 1u;
             if (__syncthreads_or(!ok)) {
@@ -200,26 +245,25 @@ __global__ void __launch_bounds__(128, 4) k_shade_mlp_tc(VolDesc vd, TraceParams
                 break;
             }
             tc::fence_after_sync();
-            // ---- C/E. epilogue: TMEM -> registers -> bias + SiLU, 32 columns
-            // at a time; the last layer folds the 64 -> 1 output in FP32
-            float yy = b4;
+            // ---- epilogue: TMEM -> bias + SiLU, 32 columns at a time; the
+            // last layer folds the 64 -> 1 output in FP32
+            float yy = m.k.b4;
 #pragma unroll
             for (int half = 0; half < 2; ++half) {
                 uint32_t acc[32];
-                tc::tmem_ld32(tmem_warp + 32u * half, acc);
+                tc::tmem_ld32(dw + 32u * half, acc);
                 uint32_t h[16];
-                bias_silu32(acc, sBias + 64 * layer + 32 * half, h);
+                bias_silu32(acc, m.k.hb + 64 * layer + 32 * half, h);
                 if (layer < 2) {
 #pragma unroll
                     for (int q = 0; q < 4; ++q)
                         *reinterpret_cast<uint4*>(act + tc::sw128_offset(tid, 4 * half + q)) =
                             make_uint4(h[4 * q], h[4 * q + 1], h[4 * q + 2], h[4 * q + 3]);
                 } else {
-                    const float* w4 = sBias + 192 + 32 * half;
+                    const float* w4 = m.k.w4 + 32 * half;
 #pragma unroll
                     for (int q = 0; q < 16; ++q) {
-                        const float2 v =
-                            __half22float2(*reinterpret_cast<const __half2*>(&h[q]));
+                        const float2 v = __half22float2(*reinterpret_cast<const __half2*>(&h[q]));
                         yy = fmaf(w4[2 * q], v.x, yy);
                         yy = fmaf(w4[2 * q + 1], v.y, yy);
                     }
@@ -229,26 +273,20 @@ __global__ void __launch_bounds__(128, 4) k_shade_mlp_tc(VolDesc vd, TraceParams
             tc::fence_before_sync();
         }
         if (failed) break;
-        if (valid) {
+        // ---- output
+        if (row.slot != CG_NO_SLOT) {
             n_valid++;
             float tau;
-            if (fb) {
-                tau = cgs::sun_cone<FMT>(vd, cone, s.x, s.y, s.z, tp.sun[0], tp.sun[1],
-                                         tp.sun[2]);
+            if (row.tau_fb >= 0.f) {
+                tau = row.tau_fb;
                 n_fallback++;
             } else {
                 tau = m.tau_scale * mlp::softplus(y);
             }
-            sb.pos_w[idx].w = s.w * __expf(-tp.sigma * tau) * (amb + (1.f - amb) * g);
+            sb.pos_w[row.slot].w = row.w * __expf(-tp.sigma * tau) * (amb + (1.f - amb) * row.g);
         }
-        // ---- G. advance
-        valid = nvalid;
-        idx = nidx;
-        s = ns;
-        g = ng;
-        fb = nfb;
-#pragma unroll
-        for (int q = 0; q < 8; ++q) xin[q] = nx[q];
+        // ---- the next tile's inputs
+        pack_row<FMT>(vd, cone, m, tp, nslot, ns, ng, nf, row, act);
     }
     if (failed) {
         // drain the outstanding commit (bounded), then report
@@ -273,27 +311,30 @@ __global__ void __launch_bounds__(128, 4) k_shade_mlp_tc(VolDesc vd, TraceParams
 
 cudaError_t launch_shade_mlp_tc(VolDesc vd, CamDesc cam, TraceParams tp, const MlpDev& m,
                                 SampleBuf sb, unsigned long long* status, cudaStream_t st) {
+    (void)cam;
     ConeSchedule cone = make_cone_schedule(vd, tp);
-    static bool configured[2][64] = {};
+    const FeatGeom geo = feat_geom(vd, m);
+    // one persistent wave: 4 CTAs per SM (the register and shared-memory
+    // budgets of __launch_bounds__(128, 4); 4 x 64 tensor-memory columns)
+    static int grid[2][64] = {};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
     const int f = vd.fmt == 0 ? 0 : 1;
-    if (!configured[f][dev]) {
-        e = f == 0 ? cudaFuncSetAttribute(k_shade_mlp_tc<0>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES)
-                   : cudaFuncSetAttribute(k_shade_mlp_tc<1>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (!grid[f][dev]) {
+        const void* fn = f == 0 ? (const void*)k_shade_mlp_tc<0> : (const void*)k_shade_mlp_tc<1>;
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
         if (e != cudaSuccess) return e;
-        configured[f][dev] = true;
+        int sms = 0;
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return e;
+        grid[f][dev] = sms * 4;
     }
-    (void)cam;
-    // 4 resident CTAs per SM (shared memory and 4 x 64 tensor-memory columns)
-    const int blocks = 152 * 4;
+    const int blocks = grid[f][dev];
     if (f == 0)
-        k_shade_mlp_tc<0><<<blocks, 128, SMEM_BYTES, st>>>(vd, tp, cone, m, sb, status);
+        k_shade_mlp_tc<0><<<blocks, 128, SMEM_BYTES, st>>>(vd, tp, cone, m, geo, sb, status);
     else
-        k_shade_mlp_tc<1><<<blocks, 128, SMEM_BYTES, st>>>(vd, tp, cone, m, sb, status);
+        k_shade_mlp_tc<1><<<blocks, 128, SMEM_BYTES, st>>>(vd, tp, cone, m, geo, sb, status);
     return cudaGetLastError();
 }
