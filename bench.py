@@ -371,9 +371,10 @@ def run_ours(args):
     # quality: surrogate image vs the plain FP32 image of the same view
     cloudgb.VoxelizeShader().voxelize(vol32, sun)
     cloudgb.VoxelizeShader().voxelize(vol16, sun)
-    ref = image_of(vol32, plain_shader, cams[0]).astype(np.float64)
-    got = image_of(vol16, mlp_shader, cams[0]).astype(np.float64)
-    rmse = float(np.sqrt(((got - ref) ** 2).mean()))
+    ref = image_of(vol32, plain_shader, cams[0])
+    got = image_of(vol16, mlp_shader, cams[0])
+    err = ctx.error_stats(got, ref)  # reduced on the GPU in FP64
+    rmse = float(err["rmse_all"])
     samples = int(ctypes.c_uint64(0).value)
     sc = ctypes.c_uint64()
     _lib.check(lib.cg_context_last_samples(ctx.handle, ctypes.byref(sc)))
@@ -445,7 +446,9 @@ def run_ours(args):
                                  "render_ms": round(learned["render_ms"], 4),
                                  "stages_ms": {k: round(v, 4) for k, v in learned["stages"].items()},
                                  "launches_per_step": learned["launches"] / args.steps,
-                                 "rmse_vs_plain_fp32": rmse, "samples_per_frame": samples,
+                                 "rmse_vs_plain_fp32": rmse,
+                                 "max_abs_vs_plain_fp32": float(err["max_abs_all"]),
+                                 "samples_per_frame": samples,
                                  "fallbacks": fallbacks, "train_s": round(train_s, 2),
                                  "train_steps": args.mlp_steps, "train_samples": args.mlp_samples,
                                  "final_loss": float(np.mean(losses[-100:]))},

@@ -29,6 +29,7 @@ SOURCES = [
     ("k_mlp.cu", []),
     ("k_textures.cu", []),
     ("k_shade_tc.cu", []),
+    ("k_stats.cu", []),
     ("cg_mlp.cpp", ["-Xcompiler", "-ffp-contract=off"]),
 ]
 

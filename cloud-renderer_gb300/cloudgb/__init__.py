@@ -69,6 +69,24 @@ class Context:
               "cg_context_last_samples")
         return int(v.value)
 
+    def error_stats(self, image, reference):
+        """GPU FP64 error statistics of an (H, W, 4) float32 image against a
+        reference of the same shape (float64 or float32): dict of max-abs and
+        RMSE per channel and overall."""
+        img = np.ascontiguousarray(image, np.float32)
+        ref = np.asarray(reference)
+        f64 = ref.dtype == np.float64
+        ref = np.ascontiguousarray(ref, np.float64 if f64 else np.float32)
+        if img.shape != ref.shape or img.shape[-1] != 4:
+            raise ValueError("error_stats: image and reference must be (..., 4) of equal shape")
+        out = (ctypes.c_double * 10)()
+        check(self._lib.cg_image_error_stats(self.handle, img.ctypes.data_as(ctypes.c_void_p),
+                                             ref.ctypes.data_as(ctypes.c_void_p), 1 if f64 else 0,
+                                             img.size // 4, 0, out, None),
+              "cg_image_error_stats")
+        return {"max_abs": list(out[0:4]), "rmse": list(out[4:8]), "max_abs_all": out[8],
+                "rmse_all": out[9]}
+
     def close(self):
         if self.handle:
             self._lib.cg_context_destroy(self.handle)

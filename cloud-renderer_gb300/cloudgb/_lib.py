@@ -149,6 +149,7 @@ SIGNATURES = [
     ("cg_mlp_load", I, [P, ctypes.c_char_p, PP]),
     ("cg_context_mlp_fallbacks", I, [P, U64P]),
     ("cg_context_last_samples", I, [P, U64P]),
+    ("cg_image_error_stats", I, [P, P, P, I, ctypes.c_uint64, I, ctypes.POINTER(ctypes.c_double), P]),
 ]
 NOALLOC_MAX_TEXELS = 1 << 20
 

@@ -219,6 +219,9 @@ void context_release(cg_context* ctx) {
     ctx->samples_gl.release();
     ctx->samples_cnt.release();
     ctx->fallbacks.release();
+    ctx->stats_scratch.release();
+    ctx->stats_a.release();
+    ctx->stats_ref.release();
     release_noise_textures(ctx);
     for (cudaEvent_t e : ctx->marks)
         if (e) cudaEventDestroy(e);
@@ -426,6 +429,7 @@ extern "C" cg_status cg_volume_set_billboards(cg_volume* v, const float* positio
     CG_CHECK(std::isfinite(fluffiness) && fluffiness >= 0.f, CG_ERR_INVALID_ARGUMENT,
              "cg_volume_set_billboards: fluffiness must be finite and >= 0");
     CG_CUDA(cudaSetDevice(v->ctx->device));
+    v->boards_dirty = true;  // the last voxelize's bins refer to the old list
     const size_t n = (size_t)count;
     const size_t bytes_cwr = n * 16, bytes_q = n * 16, bytes_thr = n * 8, bytes_dq = n * 4,
                  bytes_cul = n;
@@ -674,7 +678,7 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
     int fused = (v->D % CG_BRICK == 0) ? std::min(CG_FUSED_MIPS, v->L - 1) : 0;
     CG_LAUNCH(ctx, launch_splat(b, bins, v->mask.as<uint8_t>(), vd, v->pyr.p,
                                 v->count.as<uint32_t>(), v->dq.as<uint32_t>(), fused,
-                                v->occ.as<uint8_t>(), s));
+                                v->occ.as<uint8_t>(), false, s));
     stage_mark(ctx, s, "splat");
     CG_LAUNCH(ctx, launch_occ_dilate(vd, v->occ.as<uint8_t>(), v->occ.as<uint8_t>() + v->occ_total,
                                      v->occ_total, s));
@@ -682,6 +686,7 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
     for (int l = fused; l + 1 < v->L; ++l) CG_LAUNCH(ctx, launch_mip_level(vd, v->pyr.p, l, s));
     stage_mark(ctx, s, "mips");
     v->voxelized = true;
+    v->boards_dirty = false;
     v->gen++;
     if (write_tex) v->tex_gen = v->gen;
     return CG_OK;
@@ -1098,7 +1103,31 @@ extern "C" cg_status cg_volume_get_info(const cg_volume* v, cg_volume_info* info
 
 static cg_status sync_volume(const cg_volume* v) {
     CG_CUDA(cudaSetDevice(v->ctx->device));
-    CG_CUDA(cudaStreamSynchronize(v->ctx->stream));
+    CG_CUDA(cudaDeviceSynchronize());  // voxelize may have run on a caller's stream
+    return CG_OK;
+}
+
+// The integer coverage (count, Q16.16 density) of the last voxelize, computed
+// on demand by the coverage-only splat (voxelize itself stores only the
+// pyramid).
+static cg_status ensure_coverage(const cg_volume* cv) {
+    cg_volume* v = const_cast<cg_volume*>(cv);
+    if (v->cov_gen == v->gen) return CG_OK;
+    CG_CHECK(!v->boards_dirty, CG_ERR_NOT_READY,
+             "coverage: the billboards changed since the last voxelize; voxelize again");
+    cg_status st = sync_volume(v);
+    if (st != CG_OK) return st;
+    cudaStream_t s = v->ctx->stream;
+    Bins bins = v->bins;
+    bins.count = v->bcount.as<uint32_t>();
+    bins.offset = v->boff.as<uint32_t>();
+    bins.cursor = v->bcursor.as<uint32_t>();
+    bins.list = v->blist.as<uint32_t>();
+    CG_LAUNCH(v->ctx, launch_splat(boards_of(v), bins, v->mask.as<uint8_t>(), desc_of(v), v->pyr.p,
+                                   v->count.as<uint32_t>(), v->dq.as<uint32_t>(), 0,
+                                   v->occ.as<uint8_t>(), true, s));
+    CG_CUDA(cudaStreamSynchronize(s));
+    v->cov_gen = v->gen;
     return CG_OK;
 }
 
@@ -1123,7 +1152,7 @@ extern "C" cg_status cg_volume_read_coverage(const cg_volume* v, uint32_t* count
     CG_CHECK(v && count && density_q16, CG_ERR_INVALID_ARGUMENT,
              "cg_volume_read_coverage: null pointer");
     CG_CHECK(v->voxelized, CG_ERR_NOT_READY, "cg_volume_read_coverage: not voxelized");
-    cg_status st = sync_volume(v);
+    cg_status st = ensure_coverage(v);
     if (st != CG_OK) return st;
     const size_t n0 = (size_t)v->D * v->D * v->D;
     CG_CUDA(cudaMemcpy(count, v->count.p, n0 * 4, cudaMemcpyDeviceToHost));
@@ -1155,7 +1184,8 @@ extern "C" cg_status cg_volume_read_highlight(const cg_volume* v, uint8_t* mask)
 extern "C" cg_status cg_volume_active_voxels(const cg_volume* v, uint64_t* active) {
     CG_CHECK(v && active, CG_ERR_INVALID_ARGUMENT, "cg_volume_active_voxels: null pointer");
     CG_CHECK(v->voxelized, CG_ERR_NOT_READY, "cg_volume_active_voxels: not voxelized");
-    CG_CUDA(cudaSetDevice(v->ctx->device));
+    cg_status st = ensure_coverage(v);
+    if (st != CG_OK) return st;
     cudaStream_t s = v->ctx->stream;
     unsigned long long* d = const_cast<cg_volume*>(v)->scratch.as<unsigned long long>();
     CG_CUDA(cudaMemsetAsync(d, 0, 8, s));
@@ -1167,3 +1197,47 @@ extern "C" cg_status cg_volume_active_voxels(const cg_volume* v, uint64_t* activ
     *active = h;
     return CG_OK;
 }
+
+extern "C" cg_status cg_image_error_stats(cg_context* ctx, const float* image,
+                                          const void* reference, int reference_is_f64,
+                                          uint64_t pixels, int on_device, double out[10],
+                                          void* stream) {
+    CG_CHECK(ctx && image && reference && out, CG_ERR_INVALID_ARGUMENT,
+             "cg_image_error_stats: null pointer");
+    CG_CHECK(pixels > 0, CG_ERR_INVALID_ARGUMENT, "cg_image_error_stats: no pixels");
+    CG_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = pick_stream(ctx, stream);
+    const size_t ref_bytes = (size_t)pixels * 4 * (reference_is_f64 ? 8 : 4);
+    const float* a = image;
+    const void* ref = reference;
+    if (!on_device) {
+        CG_CUDA(ctx->stats_a.ensure((size_t)pixels * 16));
+        CG_CUDA(ctx->stats_ref.ensure(ref_bytes));
+        CG_CUDA(cudaMemcpyAsync(ctx->stats_a.p, image, (size_t)pixels * 16,
+                                cudaMemcpyHostToDevice, s));
+        CG_CUDA(cudaMemcpyAsync(ctx->stats_ref.p, reference, ref_bytes, cudaMemcpyHostToDevice,
+                                s));
+        a = ctx->stats_a.as<const float>();
+        ref = ctx->stats_ref.p;
+    }
+    CG_CUDA(ctx->stats_scratch.ensure(err_stats_scratch_bytes() + 8 * sizeof(double)));
+    double* part = ctx->stats_scratch.as<double>();
+    double* dres = part + (err_stats_scratch_bytes() / sizeof(double));
+    CG_LAUNCH(ctx, launch_err_stats(reinterpret_cast<const float4*>(a), ref, reference_is_f64,
+                                    (size_t)pixels, part, dres, s));
+    ctx->launches++;  // the final reduction
+    double h[8];
+    CG_CUDA(cudaMemcpyAsync(h, dres, sizeof(h), cudaMemcpyDeviceToHost, s));
+    CG_CUDA(cudaStreamSynchronize(s));
+    double mx = 0, ss = 0;
+    for (int c = 0; c < 4; ++c) {
+        out[c] = h[c];
+        out[4 + c] = std::sqrt(h[4 + c] / (double)pixels);
+        mx = h[c] > mx ? h[c] : mx;
+        ss += h[4 + c];
+    }
+    out[8] = mx;
+    out[9] = std::sqrt(ss / (4.0 * (double)pixels));
+    return CG_OK;
+}
+

@@ -98,6 +98,7 @@ struct cg_context {
     // deferred renderer: recorded view samples and the MLP fallback counter
     DevBuf samples_pw, samples_gl, samples_cnt;
     DevBuf fallbacks;  // surrogate render status (see launch_shade_mlp_tc)
+    DevBuf stats_scratch, stats_a, stats_ref;  // cg_image_error_stats staging
     // noise lattice tables as 3D float textures (surrogate renderer)
     cudaArray_t noise_arr[CG_MAX_LEVELS] = {};
     cudaTextureObject_t noise_tex[CG_MAX_LEVELS] = {};
@@ -145,6 +146,8 @@ struct cg_volume {
     cudaSurfaceObject_t tex_surf[CG_MAX_LEVELS] = {};
     cudaTextureObject_t tex_obj[CG_MAX_LEVELS] = {};
     long long gen = 0, tex_gen = -1;
+    long long cov_gen = -1;  // voxelization whose integer coverage is in count / dq
+    bool boards_dirty = false;  // billboards replaced since the last voxelize
 };
 
 cg_status ensure_textures(cg_volume* v, cudaStream_t s);

@@ -262,9 +262,10 @@ cudaError_t launch_highlight(const BoardsDev& b, const SunFrame& fr, const uint6
                              float4* posmap, int D, const float wmin[3],
                              const float range[3], float offset, uint8_t* mask,
                              cudaStream_t st);
+// coverage_only: write the integer coverage (count, dq) and nothing else
 cudaError_t launch_splat(const BoardsDev& b, Bins bins, const uint8_t* mask, VolDesc vd,
                          void* pyr, uint32_t* count, uint32_t* dq, int fused_levels,
-                         uint8_t* occ, cudaStream_t st);
+                         uint8_t* occ, bool coverage_only, cudaStream_t st);
 cudaError_t launch_mip_level(VolDesc vd, void* pyr, int l, cudaStream_t st);
 cudaError_t launch_occ_dilate(VolDesc vd, const uint8_t* raw, uint8_t* occ, int total,
                               cudaStream_t st);
@@ -276,3 +277,9 @@ cudaError_t launch_trace_fused(VolDesc vd, CamDesc cam, TraceParams tp, float4* 
 cudaError_t launch_noise_table(TraceParams tp, float* tab, int total, cudaStream_t st);
 cudaError_t launch_trace_cones(VolDesc vd, TraceParams tp, const float* pos, int n,
                                float* out, cudaStream_t st);
+
+// FP64 image error statistics (k_stats.cu): out[0..3] max |a - ref| per RGBA
+// channel, out[4..7] sums of squared differences.
+size_t err_stats_scratch_bytes();
+cudaError_t launch_err_stats(const float4* a, const void* ref, int ref_f64, size_t n,
+                             double* scratch, double* out, cudaStream_t st);

@@ -324,12 +324,17 @@ __device__ __forceinline__ float4 box8(float4 c000, float4 c100, float4 c010, fl
     return make_float4(s.x * 0.125f, s.y * 0.125f, s.z * 0.125f, s.w * 0.125f);
 }
 
-// One CTA per 8^3 brick, one thread per voxel.  Boards of the brick's bin are
-// staged through shared memory; each voxel tests its centre against each
-// board's ball on the Q20 grid (int64 squared distance) and sums count and
-// Q16.16 density.  Level 0 is assembled in registers and the next
-// `fused_levels` mip levels are reduced in shared memory.
-__global__ void __launch_bounds__(512) k_splat(BoardsDev b, Bins bins, const uint8_t* mask,
+// One CTA per 8^3 brick, 256 threads, two voxels per thread (z and z + 4,
+// so that each staged board is tested against both with one set of shared
+// memory reads).  Boards of the brick's bin are staged through shared memory;
+// each voxel tests its centre against each board's ball on the Q20 grid
+// (int64 squared distance) and sums count and Q16.16 density.
+// COV = false (voxelize): level 0 is assembled in registers, the next
+// `fused_levels` mip levels are reduced in shared memory, raw occupancy is
+// flagged.  COV = true: only the integer coverage (count, dq) is written
+// (the coverage readback and the active-voxel statistic compute it on demand).
+template <bool COV>
+__global__ void __launch_bounds__(256) k_splat(BoardsDev b, Bins bins, const uint8_t* mask,
                                                VolDesc vd, void* pyr, uint32_t* count,
                                                uint32_t* dqout, int fused_levels,
                                                uint8_t* occ_raw) {
@@ -345,17 +350,19 @@ __global__ void __launch_bounds__(512) k_splat(BoardsDev b, Bins bins, const uin
     const int by = (brick / bins.nbx) % bins.nby;
     const int bz = brick / (bins.nbx * bins.nby);
     const int tid = threadIdx.x;
-    const int lx = tid & 7, ly = (tid >> 3) & 7, lz = tid >> 6;
+    const int lx = tid & 7, ly = (tid >> 3) & 7, lz = tid >> 6;  // lz in 0..3, second voxel lz + 4
     const int D = vd.D;
-    const int x = bx * CG_BRICK + lx, y = by * CG_BRICK + ly, z = bz * CG_BRICK + lz;
-    const bool inside = (x < D && y < D && z < D);
+    const int x = bx * CG_BRICK + lx, y = by * CG_BRICK + ly;
+    const int z0 = bz * CG_BRICK + lz, z1 = z0 + 4;
+    const bool in0 = (x < D && y < D && z0 < D), in1 = (x < D && y < D && z1 < D);
     const int vx = (2 * x + 1) * (int)CG_HALF_Q20;
     const int vy = (2 * y + 1) * (int)CG_HALF_Q20;
-    const int vz = (2 * z + 1) * (int)CG_HALF_Q20;
+    const int vz0 = (2 * z0 + 1) * (int)CG_HALF_Q20;
+    const int vz1 = vz0 + 8 * (int)CG_HALF_Q20;
 
     const uint32_t beg = bins.offset[brick];
     const uint32_t n = bins.offset[brick + 1] - beg;
-    uint32_t cnt = 0, dsum = 0;
+    uint32_t cnt0 = 0, dsum0 = 0, cnt1 = 0, dsum1 = 0;
     for (uint32_t base = 0; base < n; base += CG_SPLAT_CHUNK) {
         const uint32_t m = min((uint32_t)CG_SPLAT_CHUNK, n - base);
         __syncthreads();
@@ -367,40 +374,67 @@ __global__ void __launch_bounds__(512) k_splat(BoardsDev b, Bins bins, const uin
         }
         __syncthreads();
         for (uint32_t k = 0; k < m; ++k) {
-            int4 q = sq[k];
-            int dx = vx - q.x, dy = vy - q.y, dz = vz - q.z;
-            unsigned long long d2 = (unsigned long long)((long long)dx * dx) +
-                                    (unsigned long long)((long long)dy * dy) +
-                                    (unsigned long long)((long long)dz * dz);
-            if (d2 <= sthr[k]) {
-                cnt += 1u;
-                dsum += sdq[k];
+            const int4 q = sq[k];
+            const unsigned long long thr = sthr[k];
+            const uint32_t dq = sdq[k];
+            const int dx = vx - q.x, dy = vy - q.y;
+            const unsigned long long dxy = (unsigned long long)((long long)dx * dx) +
+                                           (unsigned long long)((long long)dy * dy);
+            const int dz0 = vz0 - q.z, dz1 = vz1 - q.z;
+            const unsigned long long d0 = dxy + (unsigned long long)((long long)dz0 * dz0);
+            const unsigned long long d1 = dxy + (unsigned long long)((long long)dz1 * dz1);
+            if (d0 <= thr) {
+                cnt0 += 1u;
+                dsum0 += dq;
+            }
+            if (d1 <= thr) {
+                cnt1 += 1u;
+                dsum1 += dq;
             }
         }
     }
-    float4 v0 = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (inside) {
-        size_t i = ((size_t)z * D + y) * D + x;
-        uint8_t mk = mask[i];
-        count[i] = cnt;
-        dqout[i] = dsum;
-        v0.x = __uint2float_rn(dsum) * (1.0f / 65536.0f);
+    const size_t i0 = ((size_t)z0 * D + y) * D + x;
+    const size_t i1 = i0 + (size_t)4 * D * D;
+    if (COV) {
+        if (in0) {
+            count[i0] = cnt0;
+            dqout[i0] = dsum0;
+        }
+        if (in1) {
+            count[i1] = cnt1;
+            dqout[i1] = dsum1;
+        }
+        return;
+    }
+    float4 v0 = make_float4(0.f, 0.f, 0.f, 0.f), v1 = v0;
+    if (in0) {
+        const uint8_t mk = mask[i0];
+        v0.x = __uint2float_rn(dsum0) * (1.0f / 65536.0f);
         v0.y = mk ? 1.0f : 0.0f;
-        v0.z = __uint2float_rn(cnt);
-        v0.w = (cnt > 0u || mk) ? 1.0f : 0.0f;
-        store_voxel(vd, pyr, 0, x, y, z, v0);
+        v0.z = __uint2float_rn(cnt0);
+        v0.w = (cnt0 > 0u || mk) ? 1.0f : 0.0f;
+        store_voxel(vd, pyr, 0, x, y, z0, v0);
+    }
+    if (in1) {
+        const uint8_t mk = mask[i1];
+        v1.x = __uint2float_rn(dsum1) * (1.0f / 65536.0f);
+        v1.y = mk ? 1.0f : 0.0f;
+        v1.z = __uint2float_rn(cnt1);
+        v1.w = (cnt1 > 0u || mk) ? 1.0f : 0.0f;
+        store_voxel(vd, pyr, 0, x, y, z1, v1);
     }
     // Raw occupancy: a brick with any R > 0 flags the brick holding it at
     // every level, one level per thread (idempotent byte stores into grids
     // cleared before the launch; k_occ_dilate spreads them to neighbours).
-    if (__syncthreads_or(inside && v0.x > 0.f) && tid < vd.L) {
+    if (__syncthreads_or((in0 && v0.x > 0.f) || (in1 && v1.x > 0.f)) && tid < vd.L) {
         const int l = tid, nb = vd.occ_nb[l];
         const int cx = min(bx >> l, nb - 1), cy = min(by >> l, nb - 1), cz = min(bz >> l, nb - 1);
         uint8_t* p = occ_raw + vd.occ_off[l] + (cz * nb + cy) * nb + cx;
         if (!*(volatile uint8_t*)p) *p = 1;
     }
     if (fused_levels <= 0) return;
-    tile[tid] = v0;
+    tile[tid] = v0;        // voxel (lx, ly, lz)
+    tile[tid + 256] = v1;  // voxel (lx, ly, lz + 4)
     __syncthreads();
     // level 1: 4^3 parents
     if (tid < 64) {
@@ -529,8 +563,13 @@ cudaError_t launch_highlight(const BoardsDev& b, const SunFrame& fr, const uint6
 
 cudaError_t launch_splat(const BoardsDev& b, Bins bins, const uint8_t* mask, VolDesc vd,
                          void* pyr, uint32_t* count, uint32_t* dq, int fused_levels,
-                         uint8_t* occ, cudaStream_t st) {
-    k_splat<<<bins.nbricks, 512, 0, st>>>(b, bins, mask, vd, pyr, count, dq, fused_levels, occ);
+                         uint8_t* occ, bool coverage_only, cudaStream_t st) {
+    if (coverage_only)
+        k_splat<true><<<bins.nbricks, 256, 0, st>>>(b, bins, mask, vd, pyr, count, dq,
+                                                    fused_levels, occ);
+    else
+        k_splat<false><<<bins.nbricks, 256, 0, st>>>(b, bins, mask, vd, pyr, count, dq,
+                                                     fused_levels, occ);
     return cudaGetLastError();
 }
 

@@ -229,7 +229,9 @@ cg_status cg_volume_get_info(const cg_volume* vol, cg_volume_info* info);
 /* Raw level contents in the volume's format (level_dim^3 voxels). */
 cg_status cg_volume_read_level(const cg_volume* vol, int level, void* dst,
                                size_t dst_bytes);
-/* Level-0 integer coverage: per voxel board count and Q16.16 density sum. */
+/* Level-0 integer coverage of the last voxelize: per voxel board count and
+ * Q16.16 density sum (computed on demand; CG_ERR_NOT_READY when the
+ * billboards were replaced after that voxelize). */
 cg_status cg_volume_read_coverage(const cg_volume* vol, uint32_t* count,
                                   uint32_t* density_q16);
 /* Sun-view map of the last voxelize: keys (depth bits << 32 | board, or
@@ -309,6 +311,15 @@ cg_status cg_mlp_set_params(cg_mlp* mlp, const float* params, const float* adam_
  * step, CRC32); training resumes bit-identically from it. */
 cg_status cg_mlp_save(const cg_mlp* mlp, const char* path);
 cg_status cg_mlp_load(cg_context* ctx, const char* path, cg_mlp** out);
+/* No counterpart in the reference.  Error statistics of an RGBA32F image
+ * against a reference image (RGBA, FP64 when reference_is_f64, else FP32),
+ * reduced on the GPU in FP64 with a fixed reduction order: out[0..3] max-abs
+ * per channel, out[4..7] RMSE per channel, out[8] max-abs over all channels,
+ * out[9] RMSE over all channels.  Host pointers unless on_device.  Blocks
+ * until the result is on the host. */
+cg_status cg_image_error_stats(cg_context* ctx, const float* image, const void* reference,
+                               int reference_is_f64, uint64_t pixels, int on_device,
+                               double out[10], void* stream);
 /* Samples of the last MLP render that fell back to the exact cone.  Returns
  * CG_ERR_DEVICE_FAULT when that render's tensor-core pass stopped on a bounded
  * wait (the image is then incomplete). */

@@ -307,3 +307,71 @@ def test_gpu_matches_reference_shader_fixtures(ctx, name):
         ref = gold[f"cone_{name}_{kk}_value"]
         np.testing.assert_allclose(vals, ref, rtol=1e-4, atol=1e-5)
     vol.close()
+
+
+def test_error_stats_fp64_on_gpu(ctx):
+    """cg_image_error_stats: FP64 GPU reduction against numpy, FP64 and FP32
+    references, repeated calls bit-identical (fixed reduction order)."""
+    rng = np.random.default_rng(7)
+    img = rng.uniform(0, 1, (123, 77, 4)).astype(np.float32)
+    ref64 = img.astype(np.float64) + rng.normal(0, 1e-3, img.shape)
+    ref32 = ref64.astype(np.float32)
+    for ref in (ref64, ref32):
+        st = ctx.error_stats(img, ref)
+        d = img.astype(np.float64) - ref.astype(np.float64)
+        np.testing.assert_array_equal(st["max_abs"], np.abs(d).reshape(-1, 4).max(axis=0))
+        np.testing.assert_allclose(st["rmse"], np.sqrt((d ** 2).reshape(-1, 4).mean(axis=0)),
+                                   rtol=1e-12)
+        assert st["max_abs_all"] == np.abs(d).max()
+        np.testing.assert_allclose(st["rmse_all"], np.sqrt((d ** 2).mean()), rtol=1e-12)
+        assert ctx.error_stats(img, ref) == st
+
+
+def test_precision_form_512_4k(ctx):
+    """The precision workload (512^3, 16384 boards, 5-octave fBm, 3840x2160,
+    128 view steps, 32-step cone): the FP32 volume and the BF16/FP16 volume are
+    rendered on the GPU and 48x48 tiles are checked against the FP64 oracle,
+    with the error statistics reduced on the GPU in FP64.  FP32: max-abs <= 1e-4
+    (the plain-path bar); BF16/FP16: RMSE <= 1e-2, and its error is reported
+    against the FP32 run's."""
+    cfg = configs.PRECISION_4K
+    wl = workload.build(cfg)
+    shader = cloudgb.ConeTraceShader(**wl.shader_kwargs())
+    cam = workload.make_camera(wl.cameras[0])
+    W, H = cam.width, cam.height
+    sun = cloudgb.Sun(wl.sun_direction, *wl.sun_map)
+    ov = O.OracleVolume(cfg["dim"], configs.VOLUME_BOUNDS, configs.VOLUME_POSITION, cfg["mips"])
+    assert ov.set_boards(wl.positions, wl.scales, wl.densities) == 0
+    assert ov.voxelize(sun.direction, *wl.sun_map) == 0
+    images = {}
+    for fmt in (cloudgb.FORMAT_RGBA32F, cloudgb.FORMAT_BF16_FP16):
+        vol = cloudgb.CloudVolume(cfg["dim"], configs.VOLUME_BOUNDS, configs.VOLUME_POSITION,
+                                  cfg["mips"], fmt=fmt, ctx=ctx)
+        vol.set_billboards(wl.positions, wl.scales, wl.densities)
+        vol.update()
+        cloudgb.VoxelizeShader().voxelize(vol, sun)
+        images[fmt] = shader.coneTrace(vol, cam)
+        vol.close()
+    alpha = images[cloudgb.FORMAT_RGBA32F][..., 3]
+    ys, xs = np.nonzero(alpha > 0.2)
+    assert len(xs) > 0
+    rng = np.random.default_rng(3)
+    T = 48
+    picks = [(W // 2 - T // 2, H // 2 - T // 2)]
+    for k in rng.choice(len(xs), size=3, replace=False):
+        picks.append((int(min(max(xs[k] - T // 2, 0), W - T)),
+                      int(min(max(ys[k] - T // 2, 0), H - T))))
+    refs = [_oracle_image(ov, shader, cam, sun.direction, rect=(x0, y0, T, T))
+            for (x0, y0) in picks]
+    ref = np.concatenate(refs, axis=0)
+
+    def tiles(img):
+        return np.concatenate([img[y0:y0 + T, x0:x0 + T] for (x0, y0) in picks], axis=0)
+
+    st32 = ctx.error_stats(tiles(images[cloudgb.FORMAT_RGBA32F]), ref)
+    st16 = ctx.error_stats(tiles(images[cloudgb.FORMAT_BF16_FP16]), ref)
+    assert st32["max_abs_all"] <= IMAGE_TOL, st32
+    assert st16["rmse_all"] <= 1e-2, st16
+    assert st16["rmse_all"] >= st32["rmse_all"]
+    print(f"precision form: FP32 max-abs {st32['max_abs_all']:.3g} rmse {st32['rmse_all']:.3g}; "
+          f"BF16/FP16 max-abs {st16['max_abs_all']:.3g} rmse {st16['rmse_all']:.3g}")
