@@ -30,6 +30,8 @@ SOURCES = [
     ("k_textures.cu", []),
     ("k_shade_tc.cu", []),
     ("k_stats.cu", []),
+    ("k_batch.cu", []),
+    ("cg_batch.cpp", ["-Xcompiler", "-ffp-contract=off"]),
     ("cg_mlp.cpp", ["-Xcompiler", "-ffp-contract=off"]),
 ]
 

@@ -87,6 +87,61 @@ class Context:
         return {"max_abs": list(out[0:4]), "rmse": list(out[4:8]), "max_abs_all": out[8],
                 "rmse_all": out[9]}
 
+    # ---- many volumes and views per frame
+    @staticmethod
+    def _views(views):
+        def addr(p):
+            return p.value if isinstance(p, ctypes.c_void_p) else int(p)
+        arr = (_lib.cg_batch_view * len(views))()
+        for i, (vol, cam, out) in enumerate(views):
+            arr[i].volume = addr(vol.handle)
+            arr[i].camera = cam._c()
+            arr[i].rgba_out = addr(out.ptr)
+        return arr
+
+    def render_batch(self, views, shader, config=None, stream=None):
+        """Render [(CloudVolume, Camera, DeviceBuffer)] in one persistent
+        launch (plain FP32 method).  config: (lanes_per_ray, step_unroll,
+        brick) or None for the context's."""
+        arr = self._views(views)
+        p = shader.params()
+        cfg = None
+        if config is not None:
+            cfg = _lib.cg_trace_config(*config)
+        check(self._lib.cg_render_batch(self.handle, arr, len(views), ctypes.byref(p),
+                                        ctypes.byref(cfg) if cfg is not None else None,
+                                        stream),
+              "cg_render_batch")
+
+    @property
+    def trace_config(self):
+        c = _lib.cg_trace_config()
+        check(self._lib.cg_context_get_trace_config(self.handle, ctypes.byref(c)),
+              "cg_context_get_trace_config")
+        return (c.lanes_per_ray, c.step_unroll, c.brick)
+
+    @trace_config.setter
+    def trace_config(self, config):
+        c = _lib.cg_trace_config(*config)
+        check(self._lib.cg_context_set_trace_config(self.handle, ctypes.byref(c)),
+              "cg_context_set_trace_config")
+
+    def autotune(self, views, shader, repeats=3):
+        """Time the 36 launch shapes on a batch; returns (best, {config: ms})."""
+        arr = self._views(views)
+        p = shader.params()
+        best = _lib.cg_trace_config()
+        ms = (ctypes.c_float * 36)()
+        check(self._lib.cg_autotune(self.handle, arr, len(views), ctypes.byref(p), int(repeats),
+                                    ctypes.byref(best), ms), "cg_autotune")
+        table, k = {}, 0
+        for lanes in (1, 4, 8, 32):
+            for unroll in (1, 2, 4):
+                for brick in (4, 8, 16):
+                    table[(lanes, unroll, brick)] = float(ms[k])
+                    k += 1
+        return (best.lanes_per_ray, best.step_unroll, best.brick), table
+
     def close(self):
         if self.handle:
             self._lib.cg_context_destroy(self.handle)
@@ -314,6 +369,12 @@ class CloudVolume:
                      for a in range(3))
 
     # -- readback (VoxelShader::updateVoxelData, VoxelShader.cpp:102-133) --
+    def set_occupancy_brick(self, brick):
+        """Edge (4, 8 or 16 texels) of the empty-space bricks; images do not
+        depend on it."""
+        check(self._lib.cg_volume_set_occupancy_brick(self.handle, int(brick)),
+              "cg_volume_set_occupancy_brick")
+
     def info(self):
         inf = _lib.cg_volume_info()
         check(self._lib.cg_volume_get_info(self.handle, ctypes.byref(inf)), "cg_volume_get_info")
@@ -495,3 +556,38 @@ class ConeTraceShader:
 
 def deg(x):
     return math.degrees(x)
+
+
+class FrameGraph:
+    """A frame (voxelize every volume, then one batch render of the views) as
+    one CUDA graph, replayed by launch()."""
+
+    def __init__(self, ctx, volumes, sun, views, shader):
+        self.ctx = ctx
+        self._lib = load()
+        vols = (ctypes.c_void_p * len(volumes))(
+            *[v.handle.value if isinstance(v.handle, ctypes.c_void_p) else v.handle
+              for v in volumes])
+        arr = Context._views(views)
+        p = shader.params()
+        s = sun._c()
+        h = ctypes.c_void_p()
+        check(self._lib.cg_frame_graph_create(ctx.handle, vols, len(volumes), ctypes.byref(s), arr,
+                                              len(views), ctypes.byref(p), ctypes.byref(h)),
+              "cg_frame_graph_create")
+        self.handle = h
+
+    def launch(self, stream=None):
+        check(self._lib.cg_frame_graph_launch(self.handle, stream), "cg_frame_graph_launch")
+
+    def close(self):
+        if self.handle:
+            self._lib.cg_frame_graph_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+

@@ -80,6 +80,15 @@ class cg_train_params(ctypes.Structure):
                 ("sigma", ctypes.c_float), ("seed", ctypes.c_uint64)]
 
 
+class cg_trace_config(ctypes.Structure):
+    _fields_ = [("lanes_per_ray", ctypes.c_int), ("step_unroll", ctypes.c_int),
+                ("brick", ctypes.c_int)]
+
+
+class cg_batch_view(ctypes.Structure):
+    _fields_ = [("volume", ctypes.c_void_p), ("camera", cg_camera), ("rgba_out", ctypes.c_void_p)]
+
+
 class cg_volume_info(ctypes.Structure):
     _fields_ = [("dimension", ctypes.c_int), ("mips", ctypes.c_int), ("format", ctypes.c_int),
                 ("board_count", ctypes.c_int), ("world_min", ctypes.c_float * 3),
@@ -150,6 +159,17 @@ SIGNATURES = [
     ("cg_context_mlp_fallbacks", I, [P, U64P]),
     ("cg_context_last_samples", I, [P, U64P]),
     ("cg_image_error_stats", I, [P, P, P, I, ctypes.c_uint64, I, ctypes.POINTER(ctypes.c_double), P]),
+    ("cg_volume_set_occupancy_brick", I, [P, I]),
+    ("cg_render_batch", I, [P, ctypes.POINTER(cg_batch_view), I, ctypes.POINTER(cg_render_params),
+                            ctypes.POINTER(cg_trace_config), P]),
+    ("cg_context_set_trace_config", I, [P, ctypes.POINTER(cg_trace_config)]),
+    ("cg_context_get_trace_config", I, [P, ctypes.POINTER(cg_trace_config)]),
+    ("cg_autotune", I, [P, ctypes.POINTER(cg_batch_view), I, ctypes.POINTER(cg_render_params), I,
+                        ctypes.POINTER(cg_trace_config), FP]),
+    ("cg_frame_graph_create", I, [P, PP, I, ctypes.POINTER(cg_sun), ctypes.POINTER(cg_batch_view),
+                                  I, ctypes.POINTER(cg_render_params), PP]),
+    ("cg_frame_graph_launch", I, [P, P]),
+    ("cg_frame_graph_destroy", None, [P]),
 ]
 NOALLOC_MAX_TEXELS = 1 << 20
 

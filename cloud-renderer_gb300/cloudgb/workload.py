@@ -66,3 +66,52 @@ def make_camera(c):
     from . import Camera
     return Camera(c["eye"], c["target"], fov_y_degrees=c["fov"], width=c["width"],
                   height=c["height"])
+
+
+@dataclass
+class BatchWorkload:
+    """The batching form: independent clouds (sizes, board counts) and views
+    (cloud, camera dict with resolution)."""
+    cfg: dict
+    clouds: list  # dicts: dim, mips, positions, scales, densities
+    views: list   # dicts: cloud, eye, target, fov, width, height
+    sun_direction: tuple
+
+
+def build_batch(cfg, clouds=None, views=None, max_pixels=None):
+    """Seeded batch scene: cloud sizes uniform from cfg['dims'], board counts
+    uniform in cfg['boards_range'], the same board distributions as
+    the single-cloud workloads; view resolutions uniform from
+    cfg['resolutions'] (optionally capped at max_pixels), cameras on the
+    orbit sphere; view v renders cloud v mod clouds.  `clouds` / `views`
+    shrink the counts for tests."""
+    nc = clouds if clouds is not None else cfg["clouds"]
+    nv = views if views is not None else cfg["views"]
+    rng = scene.SplitMix64(cfg["seed"])
+    cl = []
+    for k in range(nc):
+        u = rng.uniform(2)
+        dim = cfg["dims"][min(int(u[0] * len(cfg["dims"])), len(cfg["dims"]) - 1)]
+        lo, hi = cfg["boards_range"]
+        n = int(lo + u[1] * (hi - lo))
+        pos, rad, dens = scene.billboards(cfg["seed"] * 1000 + k, n,
+                                          radius_range=cfg["radius_range"],
+                                          radius_scale=cfg["radius_scale"],
+                                          volume_position=configs.VOLUME_POSITION)
+        mips = int(np.floor(np.log2(dim))) + 1
+        cl.append(dict(dim=dim, mips=mips, positions=pos, scales=rad, densities=dens))
+    eyes = scene.orbit_cameras(cfg["seed"] + 1, nv, radius=1.5)
+    vs = []
+    for v in range(nv):
+        u = rng.uniform(1)
+        res = cfg["resolutions"][min(int(u[0] * len(cfg["resolutions"])),
+                                     len(cfg["resolutions"]) - 1)]
+        w, h = res
+        if max_pixels and w * h > max_pixels:
+            s = np.sqrt(max_pixels / (w * h))
+            w, h = max(16, int(w * s)), max(16, int(h * s))
+        vs.append(dict(cloud=v % nc, eye=eyes[v], target=(0.5, 0.5, 0.5), fov=60.0, width=w,
+                       height=h))
+    d = np.asarray(configs.SUN_DIRECTION, np.float64)
+    d = tuple(float(x) for x in d / np.sqrt((d * d).sum()))
+    return BatchWorkload(cfg=cfg, clouds=cl, views=vs, sun_direction=d)

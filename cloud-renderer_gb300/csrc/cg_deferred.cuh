@@ -4,5 +4,3 @@
 #include "cg_internal.h"
 #include "cg_sample.cuh"
 
-// Sun-cone schedule of a launch (k_trace.cu).
-ConeSchedule make_cone_schedule(const VolDesc& vd, const TraceParams& tp);

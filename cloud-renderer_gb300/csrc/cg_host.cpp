@@ -222,6 +222,8 @@ void context_release(cg_context* ctx) {
     ctx->stats_scratch.release();
     ctx->stats_a.release();
     ctx->stats_ref.release();
+    ctx->batch_pinned.release();
+    ctx->batch_dev.release();
     release_noise_textures(ctx);
     for (cudaEvent_t e : ctx->marks)
         if (e) cudaEventDestroy(e);
@@ -352,16 +354,18 @@ extern "C" cg_status cg_volume_create(cg_context* ctx, int dimension, float boun
     if (e == cudaSuccess) e = v->dq.ensure(n0 * 4);
     if (e == cudaSuccess) e = v->mask.ensure(n0);
     if (e == cudaSuccess) e = v->scratch.ensure(64);
-    int occ_total = 0;
+    // raw 4^3-cell grids (written by the splat) followed by the dilated brick
+    // grids (at most as many bytes as the raw ones: bricks are >= 4 texels)
+    int raw_total = 0;
     for (int l = 0; l < CG_MAX_LEVELS; ++l) {
-        int nbl = l < mips ? (v->dims[l] + 7) / 8 : 0;
-        v->occ_nb[l] = nbl;
-        v->occ_off[l] = occ_total;
-        occ_total += nbl * nbl * nbl;
+        int nbl = l < mips ? (v->dims[l] + 3) / 4 : 0;
+        v->raw_nb[l] = nbl;
+        v->raw_off[l] = raw_total;
+        raw_total += nbl * nbl * nbl;
     }
-    v->occ_total = occ_total;
-    // raw grids (written by the splat) followed by the dilated grids
-    if (e == cudaSuccess) e = v->occ.ensure(2 * (size_t)occ_total);
+    v->raw_total = raw_total;
+    set_occ_layout(v, 8);
+    if (e == cudaSuccess) e = v->occ.ensure(2 * (size_t)raw_total);
     const int nb = (dimension + CG_BRICK - 1) / CG_BRICK;
     v->bins.nbx = v->bins.nby = v->bins.nbz = nb;
     v->bins.nbricks = nb * nb * nb;
@@ -523,6 +527,29 @@ BoardsDev boards_of(const cg_volume* v) {
     return b;
 }
 
+// Brick grids of edge `brick` (4, 8 or 16) per level.
+void set_occ_layout(cg_volume* v, int brick) {
+    v->occ_brick = brick;
+    int total = 0;
+    for (int l = 0; l < CG_MAX_LEVELS; ++l) {
+        int nbl = l < v->L ? (v->dims[l] + brick - 1) / brick : 0;
+        v->occ_nb[l] = nbl;
+        v->occ_off[l] = total;
+        total += nbl * nbl * nbl;
+    }
+    v->occ_total = total;
+}
+
+OccRaw raw_of(const cg_volume* v) {
+    OccRaw r;
+    r.raw = v->occ.as<uint8_t>();
+    for (int l = 0; l < CG_MAX_LEVELS; ++l) {
+        r.nb[l] = v->raw_nb[l];
+        r.off[l] = v->raw_off[l];
+    }
+    return r;
+}
+
 VolDesc desc_of(const cg_volume* v) {
     VolDesc d;
     d.D = v->D;
@@ -537,7 +564,8 @@ VolDesc desc_of(const cg_volume* v) {
         d.range[a] = v->range[a];
     }
     d.pyr = v->pyr.p;
-    d.occ = v->occ.as<const uint8_t>() + v->occ_total;
+    d.occ = v->occ.as<const uint8_t>() + v->raw_total;
+    d.occ_shift = v->occ_brick == 4 ? 2 : (v->occ_brick == 16 ? 4 : 3);
     for (int l = 0; l < CG_MAX_LEVELS; ++l) d.tex[l] = v->tex_obj[l];
     for (int l = 0; l < CG_MAX_LEVELS; ++l) d.surf[l] = 0;
     for (int l = 0; l < CG_MAX_LEVELS; ++l) {
@@ -660,7 +688,7 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
     CG_CUDA(cudaMemsetAsync(v->keys.p, 0xFF, texels * 8, s));
     CG_CUDA(cudaMemsetAsync(v->mask.p, 0, n0, s));
     CG_CUDA(cudaMemsetAsync(bins.count, 0, (size_t)bins.nbricks * 4, s));
-    CG_CUDA(cudaMemsetAsync(v->occ.p, 0, (size_t)v->occ_total, s));
+    CG_CUDA(cudaMemsetAsync(v->occ.p, 0, (size_t)v->raw_total, s));
     // brick bins
     if (b.n) CG_LAUNCH(ctx, launch_bin_count(b, v->D, bins, s));
     CG_LAUNCH(ctx, launch_bin_scan(bins, s));
@@ -678,9 +706,9 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
     int fused = (v->D % CG_BRICK == 0) ? std::min(CG_FUSED_MIPS, v->L - 1) : 0;
     CG_LAUNCH(ctx, launch_splat(b, bins, v->mask.as<uint8_t>(), vd, v->pyr.p,
                                 v->count.as<uint32_t>(), v->dq.as<uint32_t>(), fused,
-                                v->occ.as<uint8_t>(), false, s));
+                                raw_of(v), false, s));
     stage_mark(ctx, s, "splat");
-    CG_LAUNCH(ctx, launch_occ_dilate(vd, v->occ.as<uint8_t>(), v->occ.as<uint8_t>() + v->occ_total,
+    CG_LAUNCH(ctx, launch_occ_dilate(vd, raw_of(v), v->occ.as<uint8_t>() + v->raw_total,
                                      v->occ_total, s));
     // remaining mips (glGenerateMipmap, VoxelizeShader.cpp:105)
     for (int l = fused; l + 1 < v->L; ++l) CG_LAUNCH(ctx, launch_mip_level(vd, v->pyr.p, l, s));
@@ -1125,7 +1153,7 @@ static cg_status ensure_coverage(const cg_volume* cv) {
     bins.list = v->blist.as<uint32_t>();
     CG_LAUNCH(v->ctx, launch_splat(boards_of(v), bins, v->mask.as<uint8_t>(), desc_of(v), v->pyr.p,
                                    v->count.as<uint32_t>(), v->dq.as<uint32_t>(), 0,
-                                   v->occ.as<uint8_t>(), true, s));
+                                   raw_of(v), true, s));
     CG_CUDA(cudaStreamSynchronize(s));
     v->cov_gen = v->gen;
     return CG_OK;
@@ -1238,6 +1266,24 @@ extern "C" cg_status cg_image_error_stats(cg_context* ctx, const float* image,
     }
     out[8] = mx;
     out[9] = std::sqrt(ss / (4.0 * (double)pixels));
+    return CG_OK;
+}
+
+extern "C" cg_status cg_volume_set_occupancy_brick(cg_volume* v, int brick) {
+    CG_CHECK(v, CG_ERR_INVALID_ARGUMENT, "cg_volume_set_occupancy_brick: volume is NULL");
+    CG_CHECK(brick == 4 || brick == 8 || brick == 16, CG_ERR_OUT_OF_RANGE,
+             "cg_volume_set_occupancy_brick: brick %d not in {4, 8, 16}", brick);
+    if (brick == v->occ_brick) return CG_OK;
+    CG_CUDA(cudaSetDevice(v->ctx->device));
+    CG_CUDA(cudaDeviceSynchronize());
+    set_occ_layout(v, brick);
+    if (v->voxelized) {
+        // rebuild the brick grids from the raw cells of the last voxelize
+        const VolDesc vd = desc_of(v);
+        CG_LAUNCH(v->ctx, launch_occ_dilate(vd, raw_of(v), v->occ.as<uint8_t>() + v->raw_total,
+                                            v->occ_total, v->ctx->stream));
+        CG_CUDA(cudaStreamSynchronize(v->ctx->stream));
+    }
     return CG_OK;
 }
 

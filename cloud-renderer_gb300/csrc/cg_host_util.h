@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "cg_internal.h"
 #include "cloudgb.h"
@@ -99,6 +100,12 @@ struct cg_context {
     DevBuf samples_pw, samples_gl, samples_cnt;
     DevBuf fallbacks;  // surrogate render status (see launch_shade_mlp_tc)
     DevBuf stats_scratch, stats_a, stats_ref;  // cg_image_error_stats staging
+    // batch render: launch shape, descriptors (host, pinned staging, device
+    // descriptors + tile counter)
+    cg_trace_config trace_cfg{1, 1, 0};
+    std::vector<BatchView> batch_host;
+    HostBuf batch_pinned;
+    DevBuf batch_dev;
     // noise lattice tables as 3D float textures (surrogate renderer)
     cudaArray_t noise_arr[CG_MAX_LEVELS] = {};
     cudaTextureObject_t noise_tex[CG_MAX_LEVELS] = {};
@@ -136,7 +143,11 @@ struct cg_volume {
     SunFrame frame{};
     float sun_dir[3] = {0, 1, 0};
     DevBuf scratch;  // small scalars (active voxel count)
-    DevBuf occ;      // occupancy grids (see VolDesc)
+    DevBuf occ;      // raw occupancy cells (OccRaw), then the brick grids (VolDesc)
+    int raw_nb[CG_MAX_LEVELS];
+    int raw_off[CG_MAX_LEVELS];
+    int raw_total = 0;
+    int occ_brick = 8;
     int occ_nb[CG_MAX_LEVELS];
     int occ_off[CG_MAX_LEVELS];
     int occ_total = 0;
@@ -153,6 +164,8 @@ struct cg_volume {
 cg_status ensure_textures(cg_volume* v, cudaStream_t s);
 
 VolDesc desc_of(const cg_volume* v);
+OccRaw raw_of(const cg_volume* v);
+void set_occ_layout(cg_volume* v, int brick);
 BoardsDev boards_of(const cg_volume* v);
 cg_status check_params(const cg_render_params* p);
 TraceParams trace_params_of(const cg_render_params* p, const float sun_dir[3]);

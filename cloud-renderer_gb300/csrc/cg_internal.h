@@ -10,6 +10,7 @@
 #define CG_HALF_Q20 524288LL
 #define CG_KEY_EMPTY 0xFFFFFFFFFFFFFFFFULL
 #define CG_NO_SLOT 0xFFFFFFFFu
+#define CG_MAX_SUN_STEPS 64
 #define CG_BRICK 8           // splat brick edge (voxels)
 #define CG_FUSED_MIPS 3      // levels produced inside the splat kernel
 #define CG_SPLAT_CHUNK 256   // boards staged in shared memory per pass
@@ -24,10 +25,11 @@ struct SunFrame {
 // Pyramid description passed by value to kernels.
 //
 // Occupancy: for every level l a grid of occ_nb[l]^3 bytes, one per brick of
-// 8^3 level-l texels (level-0 bricks map to level-l bricks by b >> l).  A byte
-// is 1 when the brick or one of its 26 neighbours holds a voxel with density
-// R > 0.  Because the mips are means of non-negative values, a trilinear
-// footprint whose brick reads 0 has R = 0 exactly, so samplers may skip it.
+// B^3 level-l texels, B = 1 << occ_shift (4, 8 or 16; a texel (x,y,z) is in
+// brick (x,y,z) >> occ_shift).  A byte is 1 when the brick or one of its 26
+// neighbours holds a voxel with density R > 0.  Because the mips are means of
+// non-negative values, a trilinear footprint whose brick reads 0 has R = 0
+// exactly, so samplers may skip it.
 struct VolDesc {
     int D, L, fmt;
     int dims[CG_MAX_LEVELS];
@@ -35,6 +37,7 @@ struct VolDesc {
     float wmin[3], range[3];
     const void* pyr;                // float4* (RGBA32F) or uint32_t* (BF16_FP16)
     const uint8_t* occ;             // occupancy grids, concatenated by level
+    int occ_shift;
     int occ_nb[CG_MAX_LEVELS];
     int occ_off[CG_MAX_LEVELS];
     // hardware-filtered half2 (density, light) copies of the levels for the
@@ -82,6 +85,21 @@ struct TraceParams {
     NoiseTab nt;
 };
 
+// Sun-cone schedule.  The cone's heights and radii do not depend on the
+// volume, so they are computed once per launch on the host (FP64) and read
+// from the kernel parameters: step i samples at v + h[i] * s with lod l0[i] +
+// frac[i] and weight w[i] (r_i * voxel_world for the transmittance cone,
+// i / (steps * downScaling) for the reference cone).
+struct ConeSchedule {
+    int steps;
+    int mode;         // 0 transmittance (border 0), 1 reference (clamp to edge)
+    float edge;       // break when a sample lies further than this outside the box
+    float h[CG_MAX_SUN_STEPS];
+    float w[CG_MAX_SUN_STEPS];
+    float frac[CG_MAX_SUN_STEPS];
+    unsigned char l0[CG_MAX_SUN_STEPS];
+};
+
 // Per-board device arrays (SoA).
 struct BoardsDev {
     int n;
@@ -90,6 +108,14 @@ struct BoardsDev {
     const uint64_t* thr;    // squared-radius threshold, Q40
     const uint32_t* dq;     // Q16.16 density
     const uint8_t* culled;  // 1 = no coverage contribution
+};
+
+// Raw occupancy written by the splat: per level, one byte per 4^3 texels
+// (nb[l] = ceil(dims[l] / 4)), 1 when a voxel of the cell has R > 0.
+struct OccRaw {
+    uint8_t* raw;
+    int nb[CG_MAX_LEVELS];
+    int off[CG_MAX_LEVELS];
 };
 
 struct Bins {
@@ -265,10 +291,10 @@ cudaError_t launch_highlight(const BoardsDev& b, const SunFrame& fr, const uint6
 // coverage_only: write the integer coverage (count, dq) and nothing else
 cudaError_t launch_splat(const BoardsDev& b, Bins bins, const uint8_t* mask, VolDesc vd,
                          void* pyr, uint32_t* count, uint32_t* dq, int fused_levels,
-                         uint8_t* occ, bool coverage_only, cudaStream_t st);
+                         OccRaw raw, bool coverage_only, cudaStream_t st);
 cudaError_t launch_mip_level(VolDesc vd, void* pyr, int l, cudaStream_t st);
-cudaError_t launch_occ_dilate(VolDesc vd, const uint8_t* raw, uint8_t* occ, int total,
-                              cudaStream_t st);
+// Dilated occupancy grids of brick B = 1 << vd.occ_shift from the raw cells.
+cudaError_t launch_occ_dilate(VolDesc vd, OccRaw raw, uint8_t* occ, int total, cudaStream_t st);
 cudaError_t launch_count_active(const uint32_t* count, const uint8_t* mask, size_t n,
                                 unsigned long long* out, cudaStream_t st);
 
@@ -283,3 +309,25 @@ cudaError_t launch_trace_cones(VolDesc vd, TraceParams tp, const float* pos, int
 size_t err_stats_scratch_bytes();
 cudaError_t launch_err_stats(const float4* a, const void* ref, int ref_f64, size_t n,
                              double* scratch, double* out, cudaStream_t st);
+
+// Sun-cone schedule of a launch (k_trace.cu, host, FP64).
+ConeSchedule make_cone_schedule(const VolDesc& vd, const TraceParams& tp);
+
+// ---- batched rendering (k_batch.cu) -----------------------------------------
+// One view of a batch: its volume, camera, parameters (sun and noise of its
+// volume), cone schedule, output, and its tiles' numbers [tile0, tile0 +
+// tiles_x * tiles_y).
+struct BatchView {
+    VolDesc vd;
+    CamDesc cam;
+    TraceParams tp;
+    ConeSchedule cs;
+    float4* out;
+    int tiles_x, tiles_y;
+    unsigned tile0;
+    unsigned pad;
+};
+void batch_tiles(int lanes_per_ray, int width, int height, int& tiles_x, int& tiles_y);
+cudaError_t launch_trace_batch(int fmt, int lanes_per_ray, int unroll, const BatchView* views,
+                               int n, unsigned total_tiles, unsigned* counter, cudaStream_t st);
+

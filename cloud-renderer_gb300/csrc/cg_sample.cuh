@@ -6,22 +6,7 @@
 
 #include "cg_internal.h"
 
-#define CG_MAX_SUN_STEPS 64
 
-// Sun-cone schedule.  The cone's heights and radii do not depend on the
-// volume, so they are computed once per launch on the host (FP64) and read
-// from the kernel parameters: step i samples at v + h[i] * s with lod l0[i] +
-// frac[i] and weight w[i] (r_i * voxel_world for the transmittance cone,
-// i / (steps * downScaling) for the reference cone).
-struct ConeSchedule {
-    int steps;
-    int mode;         // 0 transmittance (border 0), 1 reference (clamp to edge)
-    float edge;       // break when a sample lies further than this outside the box
-    float h[CG_MAX_SUN_STEPS];
-    float w[CG_MAX_SUN_STEPS];
-    float frac[CG_MAX_SUN_STEPS];
-    unsigned char l0[CG_MAX_SUN_STEPS];
-};
 
 namespace cgs {
 
@@ -54,10 +39,10 @@ __device__ __forceinline__ float lerp3(const float c[8], float wx, float wy, flo
 
 // Occupancy of the level-l brick holding texel (ix, iy, iz) (see VolDesc).
 __device__ __forceinline__ bool occupied(const VolDesc& vd, int l, int ix, int iy, int iz) {
-    const int nb = vd.occ_nb[l];
-    int bx = min(max(ix >> 3, 0), nb - 1);
-    int by = min(max(iy >> 3, 0), nb - 1);
-    int bz = min(max(iz >> 3, 0), nb - 1);
+    const int nb = vd.occ_nb[l], sh = vd.occ_shift;
+    int bx = min(max(ix >> sh, 0), nb - 1);
+    int by = min(max(iy >> sh, 0), nb - 1);
+    int bz = min(max(iz >> sh, 0), nb - 1);
     return __ldg(vd.occ + vd.occ_off[l] + (bz * nb + by) * nb + bx) != 0;
 }
 

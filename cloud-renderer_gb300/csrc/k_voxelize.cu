@@ -337,8 +337,9 @@ template <bool COV>
 __global__ void __launch_bounds__(256) k_splat(BoardsDev b, Bins bins, const uint8_t* mask,
                                                VolDesc vd, void* pyr, uint32_t* count,
                                                uint32_t* dqout, int fused_levels,
-                                               uint8_t* occ_raw) {
+                                               OccRaw occ_raw) {
     __shared__ int4 sq[CG_SPLAT_CHUNK];
+    __shared__ unsigned s_cells;  // raw occupancy of the brick's eight 4^3 cells
     __shared__ unsigned long long sthr[CG_SPLAT_CHUNK];
     __shared__ uint32_t sdq[CG_SPLAT_CHUNK];
     __shared__ float4 tile[CG_BRICK * CG_BRICK * CG_BRICK];
@@ -423,14 +424,41 @@ __global__ void __launch_bounds__(256) k_splat(BoardsDev b, Bins bins, const uin
         v1.w = (cnt1 > 0u || mk) ? 1.0f : 0.0f;
         store_voxel(vd, pyr, 0, x, y, z1, v1);
     }
-    // Raw occupancy: a brick with any R > 0 flags the brick holding it at
-    // every level, one level per thread (idempotent byte stores into grids
-    // cleared before the launch; k_occ_dilate spreads them to neighbours).
-    if (__syncthreads_or((in0 && v0.x > 0.f) || (in1 && v1.x > 0.f)) && tid < vd.L) {
-        const int l = tid, nb = vd.occ_nb[l];
-        const int cx = min(bx >> l, nb - 1), cy = min(by >> l, nb - 1), cz = min(bz >> l, nb - 1);
-        uint8_t* p = occ_raw + vd.occ_off[l] + (cz * nb + cy) * nb + cx;
-        if (!*(volatile uint8_t*)p) *p = 1;
+    // Raw occupancy (4^3 cells, every level): the brick's eight level-0 cells
+    // from its voxels, and at level l >= 1 the one cell holding the brick
+    // (level-l cell = brick >> (l - 1)).  Idempotent byte stores into grids
+    // cleared before the launch; k_occ_dilate builds the brick grids.
+    if (tid == 0) s_cells = 0u;
+    __syncthreads();
+    const int sxy = (lx >> 2) + 2 * (ly >> 2);
+    if (in0 && v0.x > 0.f) atomicOr(&s_cells, 1u << sxy);
+    if (in1 && v1.x > 0.f) atomicOr(&s_cells, 1u << (sxy + 4));
+    __syncthreads();
+    const unsigned cells = s_cells;
+    if (cells && tid < 8 + vd.L - 1) {
+        int l, cx, cy, cz;
+        bool set;
+        if (tid < 8) {
+            l = 0;
+            set = (cells >> tid) & 1u;
+            cx = 2 * bx + (tid & 1);
+            cy = 2 * by + ((tid >> 1) & 1);
+            cz = 2 * bz + (tid >> 2);
+        } else {
+            l = tid - 7;
+            set = true;
+            cx = bx >> (l - 1);
+            cy = by >> (l - 1);
+            cz = bz >> (l - 1);
+        }
+        const int nb = occ_raw.nb[l];
+        if (set) {
+            cx = min(cx, nb - 1);
+            cy = min(cy, nb - 1);
+            cz = min(cz, nb - 1);
+            uint8_t* p = occ_raw.raw + occ_raw.off[l] + ((size_t)cz * nb + cy) * nb + cx;
+            if (!*(volatile uint8_t*)p) *p = 1;
+        }
     }
     if (fused_levels <= 0) return;
     tile[tid] = v0;        // voxel (lx, ly, lz)
@@ -471,21 +499,26 @@ __global__ void __launch_bounds__(256) k_splat(BoardsDev b, Bins bins, const uin
     }
 }
 
-// Dilated occupancy: occ[l][c] = OR of raw[l] over c's 3x3x3 neighbourhood,
-// one thread per brick of every level.
-__global__ void k_occ_dilate(VolDesc vd, const uint8_t* raw, uint8_t* occ, int total) {
+// Dilated occupancy: occ[l][c] = 1 when a raw 4^3 cell of level l inside
+// brick c (B = 1 << occ_shift texels) or one of its 26 neighbours is set; one
+// thread per brick of every level.
+__global__ void k_occ_dilate(VolDesc vd, OccRaw raw, uint8_t* occ, int total) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= total) return;
     int l = 0;
     while (l + 1 < vd.L && i >= vd.occ_off[l + 1]) ++l;
     const int nb = vd.occ_nb[l], r = i - vd.occ_off[l];
     const int cx = r % nb, cy = (r / nb) % nb, cz = r / (nb * nb);
-    const uint8_t* g = raw + vd.occ_off[l];
+    const int k = vd.occ_shift - 2;  // raw cells per brick edge: 1 << k
+    const int rn = raw.nb[l];
+    const uint8_t* g = raw.raw + raw.off[l];
+    const int x0 = max((cx - 1) << k, 0), x1 = min((cx + 2) << k, rn);
+    const int y0 = max((cy - 1) << k, 0), y1 = min((cy + 2) << k, rn);
+    const int z0 = max((cz - 1) << k, 0), z1 = min((cz + 2) << k, rn);
     uint8_t any = 0;
-    for (int z = max(cz - 1, 0); z <= min(cz + 1, nb - 1); ++z)
-        for (int y = max(cy - 1, 0); y <= min(cy + 1, nb - 1); ++y)
-            for (int x = max(cx - 1, 0); x <= min(cx + 1, nb - 1); ++x)
-                any |= g[(z * nb + y) * nb + x];
+    for (int z = z0; z < z1 && !any; ++z)
+        for (int y = y0; y < y1 && !any; ++y)
+            for (int x = x0; x < x1; ++x) any |= g[((size_t)z * rn + y) * rn + x];
     occ[i] = any ? 1 : 0;
 }
 
@@ -563,7 +596,7 @@ cudaError_t launch_highlight(const BoardsDev& b, const SunFrame& fr, const uint6
 
 cudaError_t launch_splat(const BoardsDev& b, Bins bins, const uint8_t* mask, VolDesc vd,
                          void* pyr, uint32_t* count, uint32_t* dq, int fused_levels,
-                         uint8_t* occ, bool coverage_only, cudaStream_t st) {
+                         OccRaw occ, bool coverage_only, cudaStream_t st) {
     if (coverage_only)
         k_splat<true><<<bins.nbricks, 256, 0, st>>>(b, bins, mask, vd, pyr, count, dq,
                                                     fused_levels, occ);
@@ -573,8 +606,7 @@ cudaError_t launch_splat(const BoardsDev& b, Bins bins, const uint8_t* mask, Vol
     return cudaGetLastError();
 }
 
-cudaError_t launch_occ_dilate(VolDesc vd, const uint8_t* raw, uint8_t* occ, int total,
-                              cudaStream_t st) {
+cudaError_t launch_occ_dilate(VolDesc vd, OccRaw raw, uint8_t* occ, int total, cudaStream_t st) {
     k_occ_dilate<<<(total + 255) / 256, 256, 0, st>>>(vd, raw, occ, total);
     return cudaGetLastError();
 }

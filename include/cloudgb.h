@@ -352,6 +352,66 @@ cg_status cg_sun_map_noalloc(int dimension, float bound_min, float bound_max,
                              const cg_sun* sun, float* d_positions, uint8_t* d_mask,
                              void* stream);
 
+/* ---- many volumes and views per frame --------------------------------------
+ * No counterpart in the reference (it renders one volume for one camera per
+ * frame).  These serve the batching workload: many independent clouds and
+ * views of uneven sizes rendered in one persistent launch, a whole frame
+ * (every voxelize plus the batch render) replayed as one CUDA graph, and an
+ * autotuner for the launch shape. */
+
+/* Occupancy brick edge (4, 8 or 16 texels) of a volume's empty-space grids;
+ * rendered images do not depend on it (empty bricks read exactly 0). */
+cg_status cg_volume_set_occupancy_brick(cg_volume* vol, int brick);
+
+/* Launch shape of the fused renderer: lanes per ray 1 (one ray per thread,
+ * 32 rays per warp), 4, 8 or 32 (one ray per warp); step-loop unroll 1, 2 or 4;
+ * occupancy brick 4, 8 or 16 (0 = leave the volumes' own). */
+typedef struct cg_trace_config {
+    int lanes_per_ray;
+    int step_unroll;
+    int brick;
+} cg_trace_config;
+
+/* One view of a batch: a voxelized volume of the context, a camera, and a
+ * device buffer of width * height RGBA32F pixels (row 0 = top). */
+typedef struct cg_batch_view {
+    const cg_volume* volume;
+    cg_camera camera;
+    float* rgba_out;
+} cg_batch_view;
+
+/* Render n views with the plain FP32 exact method (params->use_mlp = 0,
+ * fused pipeline) in one persistent launch; config NULL = the context's
+ * (cg_context_set_trace_config / cg_autotune).  Images equal cg_render's for
+ * every configuration.  The launch is asynchronous on `stream`; the call
+ * first waits for the context's previous batch upload. */
+cg_status cg_render_batch(cg_context* ctx, const cg_batch_view* views, int n,
+                          const cg_render_params* params, const cg_trace_config* config,
+                          void* stream);
+cg_status cg_context_set_trace_config(cg_context* ctx, const cg_trace_config* config);
+cg_status cg_context_get_trace_config(const cg_context* ctx, cg_trace_config* config);
+
+/* Time every configuration (lanes per ray x unroll x brick, 36 of them) on a
+ * batch, keep the fastest as the context's and apply its brick to the
+ * volumes.  ms (optional, 36 entries) receives each configuration's time in
+ * the order lanes (1, 4, 8, 32) x unroll (1, 2, 4) x brick (4, 8, 16), brick
+ * fastest.  Blocks. */
+cg_status cg_autotune(cg_context* ctx, const cg_batch_view* views, int n,
+                      const cg_render_params* params, int repeats, cg_trace_config* best,
+                      float* ms);
+
+/* A frame as one CUDA graph: voxelize each volume with `sun`, then the batch
+ * render, captured once (after one eager run that allocates) and replayed by
+ * cg_frame_graph_launch.  The volumes, views and parameters are fixed at
+ * creation; billboards may be re-uploaded between launches with the same
+ * count (cg_volume_set_billboards). */
+typedef struct cg_frame_graph cg_frame_graph;
+cg_status cg_frame_graph_create(cg_context* ctx, cg_volume* const* volumes, int nvol,
+                                const cg_sun* sun, const cg_batch_view* views, int nviews,
+                                const cg_render_params* params, cg_frame_graph** out);
+cg_status cg_frame_graph_launch(cg_frame_graph* graph, void* stream);
+void cg_frame_graph_destroy(cg_frame_graph* graph);
+
 #ifdef __cplusplus
 }
 #endif
