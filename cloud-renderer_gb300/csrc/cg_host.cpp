@@ -364,7 +364,7 @@ extern "C" cg_status cg_volume_create(cg_context* ctx, int dimension, float boun
         raw_total += nbl * nbl * nbl;
     }
     v->raw_total = raw_total;
-    set_occ_layout(v, 8);
+    set_occ_layout(v, 4);  // the autotuner's pick on the batching and 1080p workloads
     if (e == cudaSuccess) e = v->occ.ensure(2 * (size_t)raw_total);
     const int nb = (dimension + CG_BRICK - 1) / CG_BRICK;
     v->bins.nbx = v->bins.nby = v->bins.nbz = nb;

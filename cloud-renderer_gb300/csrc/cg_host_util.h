@@ -147,7 +147,7 @@ struct cg_volume {
     int raw_nb[CG_MAX_LEVELS];
     int raw_off[CG_MAX_LEVELS];
     int raw_total = 0;
-    int occ_brick = 8;
+    int occ_brick = 4;
     int occ_nb[CG_MAX_LEVELS];
     int occ_off[CG_MAX_LEVELS];
     int occ_total = 0;
