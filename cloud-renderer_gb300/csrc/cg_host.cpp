@@ -558,6 +558,7 @@ VolDesc desc_of(const cg_volume* v) {
     for (int l = 0; l < CG_MAX_LEVELS; ++l) {
         d.dims[l] = v->dims[l];
         d.offs[l] = (long long)v->offs[l];
+        d.lsc[l] = l < v->L ? (float)v->dims[l] / (float)v->D : 0.f;
     }
     for (int a = 0; a < 3; ++a) {
         d.wmin[a] = v->wmin[a];

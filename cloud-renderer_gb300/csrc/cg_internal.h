@@ -34,6 +34,7 @@ struct VolDesc {
     int D, L, fmt;
     int dims[CG_MAX_LEVELS];
     long long offs[CG_MAX_LEVELS];  // voxels
+    float lsc[CG_MAX_LEVELS];       // (float)dims[l] / (float)D, level-0 voxel -> level-l texel
     float wmin[3], range[3];
     const void* pyr;                // float4* (RGBA32F) or uint32_t* (BF16_FP16)
     const uint8_t* occ;             // occupancy grids, concatenated by level

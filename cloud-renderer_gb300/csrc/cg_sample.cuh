@@ -55,7 +55,7 @@ __device__ __forceinline__ bool occupied(const VolDesc& vd, int l, int ix, int i
 template <int FMT, bool WANT_G, bool BORDER, bool SKIP_EMPTY>
 __device__ __forceinline__ float2 tri(const VolDesc& vd, int l, float px, float py, float pz) {
     const int N = vd.dims[l];
-    const float sc = (float)N / (float)vd.D;
+    const float sc = vd.lsc[l];  // N_l / D
     float x = px * sc - 0.5f, y = py * sc - 0.5f, z = pz * sc - 0.5f;
     float fx = floorf(x), fy = floorf(y), fz = floorf(z);
     float wx = x - fx, wy = y - fy, wz = z - fz;
@@ -132,7 +132,7 @@ __device__ __forceinline__ float2 quad(const VolDesc& vd, float px, float py, fl
 // addressing reads 0 outside the level.
 template <bool SKIP_EMPTY>
 __device__ __forceinline__ float2 tri_hw(const VolDesc& vd, int l, float px, float py, float pz) {
-    const float sc = (float)vd.dims[l] / (float)vd.D;
+    const float sc = vd.lsc[l];  // N_l / D
     const float x = px * sc, y = py * sc, z = pz * sc;
     if (SKIP_EMPTY && !occupied(vd, l, (int)floorf(x - 0.5f), (int)floorf(y - 0.5f),
                                 (int)floorf(z - 0.5f)))

@@ -87,18 +87,33 @@ __global__ void k_bin_fill(BoardsDev b, int D, Bins bins) { bin_walk<true>(b, D,
 // Exclusive scan of the brick counts in one CTA: tiles of 4096 counts, four
 // per thread, block scan per tile with a running carry.  Seeds the cursors.
 __global__ void __launch_bounds__(1024) k_bin_scan(Bins bins) {
+    // 4 consecutive counts per thread (4096 per pass)
+    constexpr int PER = 4;
     __shared__ uint32_t warp_sums[32];
     __shared__ uint32_t carry_s;
     const int n = bins.nbricks;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     if (tid == 0) carry_s = 0;
     __syncthreads();
-    for (int base = 0; base < n; base += 4096) {
-        const int i0 = base + tid * 4;
-        uint32_t c[4];
+    for (int base = 0; base < n; base += 1024 * PER) {
+        const int i0 = base + tid * PER;
+        uint32_t c[PER];
+        if (i0 + PER <= n) {  // one 16-byte load
 #pragma unroll
-        for (int k = 0; k < 4; ++k) c[k] = (i0 + k < n) ? bins.count[i0 + k] : 0u;
-        const uint32_t s = c[0] + c[1] + c[2] + c[3];
+            for (int k = 0; k < PER; k += 4) {
+                const uint4 q = *reinterpret_cast<const uint4*>(bins.count + i0 + k);
+                c[k] = q.x;
+                c[k + 1] = q.y;
+                c[k + 2] = q.z;
+                c[k + 3] = q.w;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < PER; ++k) c[k] = (i0 + k < n) ? bins.count[i0 + k] : 0u;
+        }
+        uint32_t s = 0;
+#pragma unroll
+        for (int k = 0; k < PER; ++k) s += c[k];
         uint32_t x = s;
         for (int o = 1; o < 32; o <<= 1) {
             uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
@@ -118,7 +133,7 @@ __global__ void __launch_bounds__(1024) k_bin_scan(Bins bins) {
         const uint32_t carry = carry_s;
         uint32_t run = carry + warp_sums[wid] + x - s;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < PER; ++k) {
             if (i0 + k < n) {
                 bins.offset[i0 + k] = run;
                 bins.cursor[i0 + k] = run;
@@ -203,6 +218,12 @@ __global__ void __launch_bounds__(256) k_sunmap(BoardsDev b, SunFrame fr,
         int ti = ia + t % nx, tj = ja + t / nx;
         float xv = texel_coord(fr.lo, fr.hi, ti, fr.W);
         float yv = texel_coord(fr.lo, fr.hi, tj, fr.H);
+        // texels well outside the disc (d^2 > 1.0001 r^2, where the exact
+        // profile test cannot pass) skip the square roots and the division
+        {
+            const float ex = xv - cv.x, ey = yv - cv.y;
+            if (ex * ex + ey * ey > 1.0001f * (r * r)) continue;
+        }
         float zs, depth;
         if (!sun_fragment(xv, yv, cv, r, fr.near_z, zs, depth)) continue;
         unsigned long long key =
@@ -364,6 +385,7 @@ __global__ void __launch_bounds__(256) k_splat(BoardsDev b, Bins bins, const uin
     const uint32_t beg = bins.offset[brick];
     const uint32_t n = bins.offset[brick + 1] - beg;
     uint32_t cnt0 = 0, dsum0 = 0, cnt1 = 0, dsum1 = 0;
+    const int w = tid >> 5;
     for (uint32_t base = 0; base < n; base += CG_SPLAT_CHUNK) {
         const uint32_t m = min((uint32_t)CG_SPLAT_CHUNK, n - base);
         __syncthreads();
@@ -430,9 +452,19 @@ __global__ void __launch_bounds__(256) k_splat(BoardsDev b, Bins bins, const uin
     // cleared before the launch; k_occ_dilate builds the brick grids.
     if (tid == 0) s_cells = 0u;
     __syncthreads();
-    const int sxy = (lx >> 2) + 2 * (ly >> 2);
-    if (in0 && v0.x > 0.f) atomicOr(&s_cells, 1u << sxy);
-    if (in1 && v1.x > 0.f) atomicOr(&s_cells, 1u << (sxy + 4));
+    {
+        // the warp's voxels lie in cell y = w & 1, z = 0 (first voxel) or 1
+        // (second), x = lane bit 2 (lanes 0-3 of each row in x cell 0)
+        const unsigned b0 = __ballot_sync(0xffffffffu, in0 && v0.x > 0.f);
+        const unsigned b1 = __ballot_sync(0xffffffffu, in1 && v1.x > 0.f);
+        const int cy = 2 * (w & 1);
+        unsigned bits = 0u;
+        if (b0 & 0x0F0F0F0Fu) bits |= 1u << cy;
+        if (b0 & 0xF0F0F0F0u) bits |= 1u << (cy + 1);
+        if (b1 & 0x0F0F0F0Fu) bits |= 1u << (cy + 4);
+        if (b1 & 0xF0F0F0F0u) bits |= 1u << (cy + 5);
+        if ((tid & 31) == 0 && bits) atomicOr(&s_cells, bits);
+    }
     __syncthreads();
     const unsigned cells = s_cells;
     if (cells && tid < 8 + vd.L - 1) {
