@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--cpu-budget-s", type=float, default=15.0)
     ap.add_argument("--mlp-steps", type=int, default=20000)
     ap.add_argument("--mlp-samples", type=int, default=4_000_000)
+    ap.add_argument("--width", type=int, default=None,
+                    help="override the image width (small cases for profiling)")
+    ap.add_argument("--height", type=int, default=None)
     return ap.parse_args()
 
 
@@ -57,8 +60,10 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
-def workload():
+def workload(args=None):
     from cloudgb import configs, workload as W
+    if args is not None and (args.width or args.height):
+        return W.build(configs.PLAIN_1080P, width=args.width, height=args.height)
     return W.build(configs.PLAIN_1080P)
 
 
@@ -68,7 +73,7 @@ def config_block(wl, extra=None):
                      "64 view steps, 24-step sun cone, 16 orbit views",
          "volume": f"{c['dim']}^3, {c['mips']} mips (plain: RGBA32F; surrogate: BF16 density + "
                    f"FP16 light)", "boards": c["boards"],
-         "image": f"{c['camera']['width']}x{c['camera']['height']}",
+         "image": f"{wl.cameras[0]['width']}x{wl.cameras[0]['height']}",
          "view_steps": c["view_steps"], "sun_steps": c["sun_steps"],
          "cone_half_angle": c["cone_half_angle"], "noise_octaves": c["noise_octaves"],
          "sun_map": f"{c['sun_map'][0]}x{c['sun_map'][1]}", "views": c["orbits"],
@@ -265,7 +270,7 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    wl = workload()
+    wl = workload(args)
     c = wl.cfg
     ctx = cloudgb.Context(local)
     lib = _lib.load()
