@@ -23,6 +23,19 @@ __device__ __forceinline__ uint32_t sw128_offset(int row, int chunk) {
     return (uint32_t)((row >> 3) * 1024 + (row & 7) * 128 + ((chunk ^ (row & 7)) << 4));
 }
 
+// byte offset of (row, 16-byte chunk) in a 32B-swizzled K-major tile (rows of
+// 32 B, 8-row atoms of 256 B; chunk c of row r at c ^ ((r >> 2) & 1))
+__device__ __forceinline__ uint32_t sw32_offset(int row, int chunk) {
+    return (uint32_t)((row >> 3) * 256 + (row & 7) * 32 + ((chunk ^ ((row >> 2) & 1)) << 4));
+}
+
+// Descriptor of a 32B-swizzled K-major tile (K = 16 FP16 per row): stride
+// byte offset 256 (one 8-row atom), layout SWIZZLE_32B (6).
+__device__ __forceinline__ uint64_t desc_sw32(uint32_t saddr) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) |
+           ((uint64_t)(256 >> 4) << 32) | ((uint64_t)1 << 46) | ((uint64_t)6 << 61);
+}
+
 // Shared memory matrix descriptor: start address, leading byte offset (unused
 // by swizzled K-major layouts), stride byte offset = 1024 (one 8-row atom),
 // descriptor version 1, layout SWIZZLE_128B (2).

@@ -8,9 +8,10 @@
 //      the activation tile (shared memory, 128B-swizzled K-major);
 //   2. thread 0 issues layer 1 (one tcgen05.mma, M=128 N=64 K=16) into tensor
 //      memory and commits it to an mbarrier;
-//   3. each warp reads its 32 rows back (tcgen05.ld), adds the bias, applies
-//      SiLU in FP16 pairs and writes the next activation tile in place;
-//      layers 2 and 3 are 4 MMAs each (K = 64);
+//   3. each warp reads its 32 rows back (tcgen05.ld), applies SiLU and writes
+//      the next activation tile in place as FP16; layers 2 and 3 are 4 MMAs
+//      each (K = 64); every layer ends with one more K = 16 MMA that adds the
+//      bias (a column of ones against the bias split into two FP16 halves);
 //   4. the last epilogue folds the 64 -> 1 output layer into FP32 FMAs, then
 //      the softplus link, the transmittance and the sample's contribution;
 //      the next tile's inputs go into the tile.
@@ -18,8 +19,7 @@
 // consumed in the phase that issued it: its slot (layer 1), its sample
 // (layer 2), its 12 texture taps (layer 3), its inputs (output).
 // Layers 1-3 run on weights and biases pre-scaled by 1/2 (exact in FP16 and
-// FP32), so the accumulator holds z/2 and SiLU is z/2 * (1 + tanh(z/2)):
-// one MUFU and one FMA per FP16 pair.
+// FP32), so the accumulator holds z/2 and SiLU is z/2 * (1 + tanh(z/2)).
 // Every mbarrier wait is bounded: on a timeout the CTA records an error,
 // waits (bounded) for its MMA to drain, frees its tensor memory and returns.
 #include <cuda_fp16.h>
@@ -39,7 +39,9 @@ constexpr int OFF_ACT = 0;                 // 128 x 128 B activation tile
 constexpr int OFF_W1 = 16384;              // 64 x 128 B (K = 16 used)
 constexpr int OFF_W2 = OFF_W1 + 8192;      // 64 x 128 B
 constexpr int OFF_W3 = OFF_W2 + 8192;      // 64 x 128 B
-constexpr int OFF_BAR = OFF_W3 + 8192;     // mbarrier + tensor-memory address
+constexpr int OFF_ONES = OFF_W3 + 8192;    // 128 x 32 B: each row (1, 1, 0, ...) (SW32)
+constexpr int OFF_BIAS = OFF_ONES + 4096;  // 3 x (64 x 32 B): row n (b_hi[n], b_lo[n], 0, ...)
+constexpr int OFF_BAR = OFF_BIAS + 3 * 2048;  // mbarrier + tensor-memory address
 constexpr int SMEM_USED = OFF_BAR + 32;
 constexpr int SMEM_BYTES = SMEM_USED + 1024;  // + alignment slack
 
@@ -65,14 +67,14 @@ __device__ __forceinline__ void stage_row(uint8_t* tile, int r, const __half* sr
     }
 }
 
-// SiLU of 32 half-scaled accumulators (+ half-scaled bias) -> 16 FP16 pairs:
-// with h = z/2, silu(z) = h + h * tanh(h), evaluated in FP32 and rounded once.
-__device__ __forceinline__ void bias_silu32(const uint32_t (&acc)[32], const float* hb,
-                                            uint32_t (&out)[16]) {
+// SiLU of 32 half-scaled accumulators (the bias is already in them) -> 16
+// FP16 pairs: with h = z/2, silu(z) = h + h * tanh(h), evaluated in FP32 and
+// rounded once.
+__device__ __forceinline__ void silu32(const uint32_t (&acc)[32], uint32_t (&out)[16]) {
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
-        const float a = __uint_as_float(acc[2 * j]) + hb[2 * j];
-        const float b = __uint_as_float(acc[2 * j + 1]) + hb[2 * j + 1];
+        const float a = __uint_as_float(acc[2 * j]);
+        const float b = __uint_as_float(acc[2 * j + 1]);
         float ta, tb;
         asm("tanh.approx.f32 %0, %1;" : "=f"(ta) : "f"(a));
         asm("tanh.approx.f32 %0, %1;" : "=f"(tb) : "f"(b));
@@ -142,13 +144,17 @@ __device__ __forceinline__ unsigned slot_at(const SampleBuf& sb, unsigned tile, 
     return (tile < ntiles && i < total) ? sb.slot_of[i] : CG_NO_SLOT;
 }
 
-// Issue one layer (thread 0) and commit it to the barrier.
+// Issue one layer (thread 0) and commit it to the barrier: the K slices of
+// the activations, then one more K = 16 slice that adds the bias (a column of
+// ones against the split bias b_hi + b_lo, exact to ~2^-22 relative).
 __device__ __forceinline__ void issue_layer(int layer, uint32_t d_tmem, uint32_t a_addr,
-                                            uint32_t w_addr, uint64_t* bar) {
+                                            uint32_t w_addr, uint32_t ones_addr,
+                                            uint32_t bias_addr, uint64_t* bar) {
     const int ksteps = layer == 0 ? 1 : 4;
     for (int k = 0; k < ksteps; ++k)
         tc::mma_f16(d_tmem, tc::desc_sw128(a_addr + 32u * k), tc::desc_sw128(w_addr + 32u * k),
                     IDESC, k > 0 ? 1u : 0u);
+    tc::mma_f16(d_tmem, tc::desc_sw32(ones_addr), tc::desc_sw32(bias_addr), IDESC, 1u);
     tc::mma_commit(bar);
 }
 
@@ -181,6 +187,25 @@ __global__ void __launch_bounds__(128, 4)
         stage_row(base + OFF_W2, r, m.w16 + MLP_H_W2 + r * 64, 8, true);
         stage_row(base + OFF_W3, r, m.w16 + MLP_H_W3 + r * 64, 8, true);
     }
+    // the ones column and the split half-scaled biases (32B-swizzled, K = 16)
+    {
+        const __half one = __float2half_rn(1.f);
+        const uint32_t ones = (uint32_t)__half_as_ushort(one) | ((uint32_t)__half_as_ushort(one) << 16);
+        *reinterpret_cast<uint4*>(base + OFF_ONES + tc::sw32_offset(tid, 0)) =
+            make_uint4(ones, 0u, 0u, 0u);
+        *reinterpret_cast<uint4*>(base + OFF_ONES + tc::sw32_offset(tid, 1)) =
+            make_uint4(0u, 0u, 0u, 0u);
+        for (int i = tid; i < 3 * 64; i += blockDim.x) {
+            const int l = i >> 6, n = i & 63;
+            const float hb = m.k.hb[i];
+            const __half hi = __float2half_rn(hb);
+            const __half lo = __float2half_rn(hb - __half2float(hi));
+            uint8_t* tile = base + OFF_BIAS + 2048 * l;
+            *reinterpret_cast<uint4*>(tile + tc::sw32_offset(n, 0)) = make_uint4(
+                (uint32_t)__half_as_ushort(hi) | ((uint32_t)__half_as_ushort(lo) << 16), 0u, 0u, 0u);
+            *reinterpret_cast<uint4*>(tile + tc::sw32_offset(n, 1)) = make_uint4(0u, 0u, 0u, 0u);
+        }
+    }
     if (tid == 0) {
         tc::mbar_init(bar, 1);
         tc::fence_mbar_init();
@@ -198,6 +223,8 @@ __global__ void __launch_bounds__(128, 4)
     const uint32_t a_addr = tc::smem_addr(act);
     const uint32_t w_addr[3] = {tc::smem_addr(base + OFF_W1), tc::smem_addr(base + OFF_W2),
                                 tc::smem_addr(base + OFF_W3)};
+    const uint32_t ones_addr = tc::smem_addr(base + OFF_ONES);
+    const uint32_t bias_addr = tc::smem_addr(base + OFF_BIAS);
     const float amb = tp.ambient;
     const unsigned total = *sb.flat_total;
     const unsigned ntiles = (total + 127u) / 128u;
@@ -230,7 +257,9 @@ __global__ void __launch_bounds__(128, 4)
 #pragma unroll
         for (int layer = 0; layer < 3; ++layer) {
             sync_for_mma();
-            if (tid == 0) issue_layer(layer, tmem, a_addr, w_addr[layer], bar);
+            if (tid == 0)
+                issue_layer(layer, tmem, a_addr, w_addr[layer], ones_addr,
+                            bias_addr + 2048u * layer, bar);
             // ---- the next tile, in stages
             if (layer == 0) nslot = slot_at(sb, ntile, ntiles, total);
             if (layer == 1 && nslot != CG_NO_SLOT) {
@@ -253,7 +282,7 @@ __global__ void __launch_bounds__(128, 4)
                 uint32_t acc[32];
                 tc::tmem_ld32(dw + 32u * half, acc);
                 uint32_t h[16];
-                bias_silu32(acc, m.k.hb + 64 * layer + 32 * half, h);
+                silu32(acc, h);
                 if (layer < 2) {
 #pragma unroll
                     for (int q = 0; q < 4; ++q)
