@@ -449,7 +449,10 @@ class ConeTraceShader:
 
     Field names follow ConeTraceShader.hpp:15-32.  vctConeAngle is the full
     cone aperture as in the reference (its half is the cone half-angle);
-    freqStep / persStep are the fBm lacunarity / gain."""
+    freqStep / persStep are the fBm lacunarity / gain.  The noise domain moves
+    with the wind: offset = windVel * runTime in base-frequency lattice units
+    (the reference's octaveOffsets, ConeTraceShader.cpp:55-61, with runTime its
+    Window::runTime, here set by the caller)."""
 
     def __init__(self, **kw):
         p = _lib.cg_render_params()
@@ -471,6 +474,8 @@ class ConeTraceShader:
         self.noiseFrequency = p.noise.frequency
         self.freqStep = p.noise.lacunarity
         self.persStep = p.noise.gain
+        self.windVel = (0.01, 0.0, 0.0)
+        self.runTime = 0.0
         self.useMlp = False
         self.mlp = None
         self.pipeline = p.pipeline
@@ -498,6 +503,7 @@ class ConeTraceShader:
         p.noise.frequency = float(self.noiseFrequency)
         p.noise.lacunarity = float(self.freqStep)
         p.noise.gain = float(self.persStep)
+        p.noise.offset[:] = [float(w) * float(self.runTime) for w in self.windVel]
         p.use_mlp = 1 if self.useMlp else 0
         p.mlp = self.mlp.handle if (self.useMlp and self.mlp is not None) else None
         p.pipeline = int(self.pipeline)

@@ -44,7 +44,7 @@ class cg_camera(ctypes.Structure):
 class cg_noise(ctypes.Structure):
     _fields_ = [("seed", ctypes.c_uint32), ("octaves", ctypes.c_int),
                 ("frequency", ctypes.c_float), ("lacunarity", ctypes.c_float),
-                ("gain", ctypes.c_float)]
+                ("gain", ctypes.c_float), ("offset", ctypes.c_float * 3)]
 
 
 class cg_render_params(ctypes.Structure):

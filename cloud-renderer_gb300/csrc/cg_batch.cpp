@@ -359,7 +359,17 @@ extern "C" cg_status cg_frame_graph_launch(cg_frame_graph* g, void* stream) {
         cg_status st = capture(g);
         if (st != CG_OK) return st;
     }
-    CG_CUDA(cudaGraphLaunch(g->exec, pick_stream(g->ctx, stream)));
+    cudaStream_t s = pick_stream(g->ctx, stream);
+    // the replay reads each volume's boards: order it after their uploads, and
+    // later uploads after it
+    for (cg_volume* v : g->volumes)
+        if (v->ready_pending && s != g->ctx->stream)
+            CG_CUDA(cudaStreamWaitEvent(s, v->boards_ready, 0));
+    CG_CUDA(cudaGraphLaunch(g->exec, s));
+    for (cg_volume* v : g->volumes) {
+        CG_CUDA(cudaEventRecord(v->boards_read, s));
+        v->read_pending = true;
+    }
     g->ctx->launches += 1;
     // the replay voxelized every volume with its current billboards
     for (size_t i = 0; i < g->volumes.size(); ++i) {

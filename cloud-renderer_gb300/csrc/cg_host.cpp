@@ -142,16 +142,25 @@ void release_noise_textures(cg_context* ctx) {
 }
 
 // The fBm of the current noise tables sampled at R^3 texel centres over the
-// volume's box (R = 8 texels per finest lattice cell, at most 512), as a
-// half-precision 3D texture: one fetch per view sample in the surrogate path.
+// tables' noise domain (R = 8 texels per finest lattice cell, at most 512 for
+// a static domain, 640 for one widened for a moving shift), as a half-precision
+// 3D texture: one fetch per view sample in the surrogate path.
 cg_status ensure_fbm_volume(cg_context* ctx, const cg_volume* v, TraceParams& tp, cudaStream_t s) {
+    (void)v;
     if (tp.noise_octaves <= 0 || !ctx->noise_valid) return CG_OK;
     if (!ctx->fbm_valid) {
         double fmax = (double)tp.noise_freq;
         for (int o = 1; o < tp.noise_octaves; ++o) fmax *= (double)tp.noise_lac;
-        double rmax = std::max((double)v->range[0], std::max((double)v->range[1], (double)v->range[2]));
+        float org[3], ext[3];
+        double rmax = 0.0;
+        for (int a = 0; a < 3; ++a) {
+            org[a] = ctx->noise_dom[a];
+            ext[a] = ctx->noise_dom[3 + a] - ctx->noise_dom[a];
+            rmax = std::max(rmax, (double)ext[a]);
+        }
         double cells = std::ceil(std::fabs(fmax) * rmax);
-        int R = (int)std::min(512.0, std::max(8.0, 8.0 * cells));
+        const double cap = ctx->noise_moving ? 640.0 : 512.0;
+        int R = (int)std::min(cap, std::max(8.0, 8.0 * cells));
         cudaChannelFormatDesc fd = cudaCreateChannelDescHalf();
         CG_CUDA(cudaMalloc3DArray(&ctx->fbm_arr, &fd, make_cudaExtent(R, R, R),
                                   cudaArraySurfaceLoadStore));
@@ -165,14 +174,22 @@ cg_status ensure_fbm_volume(cg_context* ctx, const cg_volume* v, TraceParams& tp
         td.readMode = cudaReadModeElementType;
         td.normalizedCoords = 0;
         CG_CUDA(cudaCreateTextureObject(&ctx->fbm_tex, &rd, &td, nullptr));
-        CG_LAUNCH(ctx, launch_fbm_volume(tp, v->wmin, v->range, R, ctx->fbm_surf, s));
+        CG_LAUNCH(ctx, launch_fbm_volume(tp, org, ext, R, ctx->fbm_surf, s));
         ctx->fbm_res = R;
         ctx->fbm_valid = true;
         ctx->noise_tab.fbm_tex = ctx->fbm_tex;
         ctx->noise_tab.fbm_res = R;
+        for (int a = 0; a < 3; ++a) {
+            ctx->noise_tab.fbm_org[a] = org[a];
+            ctx->noise_tab.fbm_sc[a] = (float)((double)R / (double)ext[a]);
+        }
     }
     tp.nt.fbm_tex = ctx->fbm_tex;
     tp.nt.fbm_res = ctx->fbm_res;
+    for (int a = 0; a < 3; ++a) {
+        tp.nt.fbm_org[a] = ctx->noise_tab.fbm_org[a];
+        tp.nt.fbm_sc[a] = ctx->noise_tab.fbm_sc[a];
+    }
     return CG_OK;
 }
 
@@ -271,6 +288,7 @@ extern "C" void cg_render_params_default(cg_render_params* p) {
     p->noise.frequency = 4.0f;
     p->noise.lacunarity = 2.0f;
     p->noise.gain = 0.5f;
+    p->noise.offset[0] = p->noise.offset[1] = p->noise.offset[2] = 0.0f;
     p->use_mlp = 0;
     p->mlp = nullptr;
 }
@@ -372,6 +390,8 @@ extern "C" cg_status cg_volume_create(cg_context* ctx, int dimension, float boun
     if (e == cudaSuccess) e = v->bcount.ensure((size_t)v->bins.nbricks * 4);
     if (e == cudaSuccess) e = v->boff.ensure(((size_t)v->bins.nbricks + 1) * 4);
     if (e == cudaSuccess) e = v->bcursor.ensure((size_t)v->bins.nbricks * 4);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&v->boards_ready, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&v->boards_read, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         cg_volume_destroy(v);
         return fail(e == cudaErrorMemoryAllocation ? CG_ERR_OUT_OF_MEMORY : CG_ERR_CUDA,
@@ -390,6 +410,8 @@ extern "C" void cg_volume_destroy(cg_volume* v) {
                       &v->keys, &v->posmap, &v->scratch, &v->occ};
     for (DevBuf* b : bufs) b->release();
     v->h_stage.release();
+    if (v->boards_ready) cudaEventDestroy(v->boards_ready);
+    if (v->boards_read) cudaEventDestroy(v->boards_read);
     for (int l = 0; l < CG_MAX_LEVELS; ++l) {
         if (v->tex_obj[l]) cudaDestroyTextureObject(v->tex_obj[l]);
         if (v->tex_surf[l]) cudaDestroySurfaceObject(v->tex_surf[l]);
@@ -433,6 +455,12 @@ extern "C" cg_status cg_volume_set_billboards(cg_volume* v, const float* positio
     CG_CHECK(std::isfinite(fluffiness) && fluffiness >= 0.f, CG_ERR_INVALID_ARGUMENT,
              "cg_volume_set_billboards: fluffiness must be finite and >= 0");
     CG_CUDA(cudaSetDevice(v->ctx->device));
+    // a voxelize still running on another stream reads the board buffers that
+    // this upload overwrites (or reallocates): wait for it
+    if (v->read_pending) {
+        CG_CUDA(cudaEventSynchronize(v->boards_read));
+        v->read_pending = false;
+    }
     v->boards_dirty = true;  // the last voxelize's bins refer to the old list
     const size_t n = (size_t)count;
     const size_t bytes_cwr = n * 16, bytes_q = n * 16, bytes_thr = n * 8, bytes_dq = n * 4,
@@ -477,8 +505,10 @@ extern "C" cg_status cg_volume_set_billboards(cg_volume* v, const float* positio
         CG_CHECK(rv <= (double)D, CG_ERR_OUT_OF_RANGE,
                  "billboard %zu: radius %g exceeds the volume extent", b, (double)r);
         long long rq = llrint(rv * (double)CG_Q20);
-        unsigned __int128 r2 = (unsigned __int128)(uint64_t)rq * (uint64_t)rq;
-        thr[b] = (uint64_t)((r2 * 9999u) / 10000u);
+        // rq <= 512 * 2^20 < 2^30, so rq^2 < 2^60 fits; floor(r2 * 9999 / 10000)
+        // = r2 - ceil(r2 / 10000) without a 128-bit division
+        const uint64_t r2 = (uint64_t)rq * (uint64_t)rq;
+        thr[b] = r2 - (r2 + 9999u) / 10000u;
         dqv[b] = (uint32_t)llrint((double)d * 65536.0);
         for (int a = 0; a < 3; ++a) qv[4 * b + a] = (int)q[a];
         qv[4 * b + 3] = (int)rq;
@@ -510,6 +540,8 @@ extern "C" cg_status cg_volume_set_billboards(cg_volume* v, const float* positio
         CG_CUDA(cudaMemcpyAsync(v->dqb.p, dqv, bytes_dq, cudaMemcpyHostToDevice, s));
         CG_CUDA(cudaMemcpyAsync(v->culled.p, cul, bytes_cul, cudaMemcpyHostToDevice, s));
     }
+    CG_CUDA(cudaEventRecord(v->boards_ready, s));
+    v->ready_pending = true;
     v->n = count;
     v->pairs = pairs;
     v->voxelized = false;
@@ -684,6 +716,13 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
     const bool write_tex = v->tex_arr[0] != nullptr;
     if (write_tex)
         for (int l = 0; l < v->L; ++l) vd.surf[l] = v->tex_surf[l];
+    // order after the last board upload (made on the context stream); a
+    // stream being captured into a graph is ordered at graph launch instead
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    CG_CUDA(cudaStreamIsCapturing(s, &cap));
+    const bool capturing = cap != cudaStreamCaptureStatusNone;
+    if (v->ready_pending && s != ctx->stream && !capturing)
+        CG_CUDA(cudaStreamWaitEvent(s, v->boards_ready, 0));
     stage_begin(ctx, s);
     // clearGPU (CloudVolume.cpp:96-100) + clearPositionMap (VoxelizeShader.cpp:185-187)
     CG_CUDA(cudaMemsetAsync(v->keys.p, 0xFF, texels * 8, s));
@@ -714,6 +753,10 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
     // remaining mips (glGenerateMipmap, VoxelizeShader.cpp:105)
     for (int l = fused; l + 1 < v->L; ++l) CG_LAUNCH(ctx, launch_mip_level(vd, v->pyr.p, l, s));
     stage_mark(ctx, s, "mips");
+    if (!capturing) {
+        CG_CUDA(cudaEventRecord(v->boards_read, s));
+        v->read_pending = true;
+    }
     v->voxelized = true;
     v->boards_dirty = false;
     v->gen++;
@@ -755,6 +798,9 @@ cg_status check_params(const cg_render_params* p) {
                  std::isfinite(p->noise.gain) && p->noise.gain > 0.f,
              CG_ERR_INVALID_ARGUMENT, "render params: noise values must be finite, gain > 0");
     for (int a = 0; a < 3; ++a)
+        CG_CHECK(std::isfinite(p->noise.offset[a]) && std::fabs(p->noise.offset[a]) < 1e6f,
+                 CG_ERR_OUT_OF_RANGE, "render params: noise offset must be finite, |offset| < 1e6");
+    for (int a = 0; a < 3; ++a)
         CG_CHECK(std::isfinite(p->sun_color[a]), CG_ERR_INVALID_ARGUMENT,
                  "render params: non-finite sun colour");
     return CG_OK;
@@ -790,6 +836,11 @@ TraceParams trace_params_of(const cg_render_params* p, const float sun_dir[3]) {
         amp *= (double)p->noise.gain;
     }
     tp.noise_inv_norm = norm > 0.0 ? (float)(1.0 / norm) : 1.0f;
+    // the lattice offset as a world shift: (p * f + o) * lac^k = (p + o / f) * f * lac^k
+    for (int a = 0; a < 3; ++a)
+        tp.noise_shift[a] = p->noise.frequency != 0.f
+                                ? (float)((double)p->noise.offset[a] / (double)p->noise.frequency)
+                                : 0.f;
     memset(&tp.nt, 0, sizeof(tp.nt));
     return tp;
 }
@@ -833,18 +884,37 @@ cg_status camera_of(const cg_camera* c, CamDesc& cam) {
     return CG_OK;
 }
 
-// Lattice tables for the render's noise parameters over the volume's box,
-// rebuilt only when those change.  Each octave covers floor(wmin*f) - 1 ..
-// floor(wmax*f) + 2 per axis, f = frequency * lacunarity^o in FP32 as the
-// kernel computes it; samples outside fall back to hashing.
+// Lattice tables for the render's noise parameters over the noise domain,
+// rebuilt only when those change.  The domain is the volume's box; with a
+// nonzero shift (wind) it is the box moved by the shift the tables were built
+// for and widened by range/8 per side, so the tables (and the fBm volume) are
+// rebuilt only when the shift has moved further than that.  Each octave covers
+// floor(lo*f) - 1 .. floor(hi*f) + 2 per axis, f = frequency * lacunarity^o in
+// FP32 as the kernel computes it; samples outside fall back to hashing (the
+// same values).
 cg_status ensure_noise(cg_context* ctx, const cg_volume* v, TraceParams& tp,
                               cudaStream_t s) {
     if (tp.noise_octaves <= 0) return CG_OK;
     float box[6] = {v->wmin[0], v->wmin[1], v->wmin[2], v->wmax[0], v->wmax[1], v->wmax[2]};
+    const bool moving = tp.noise_shift[0] != 0.f || tp.noise_shift[1] != 0.f ||
+                        tp.noise_shift[2] != 0.f;
     bool same = ctx->noise_valid && ctx->noise_seed == tp.noise_seed &&
                 ctx->noise_octaves == tp.noise_octaves && ctx->noise_freq == tp.noise_freq &&
-                ctx->noise_lac == tp.noise_lac && memcmp(ctx->noise_box, box, sizeof(box)) == 0;
+                ctx->noise_lac == tp.noise_lac && memcmp(ctx->noise_box, box, sizeof(box)) == 0 &&
+                ctx->noise_moving == moving;
+    if (same && moving)
+        for (int a = 0; a < 3; ++a)
+            if (!(std::fabs((double)tp.noise_shift[a] - (double)ctx->noise_ref[a]) <=
+                  (double)ctx->noise_margin[a]))
+                same = false;
     if (!same) {
+        double dom[6];
+        for (int a = 0; a < 3; ++a) {
+            const double m = moving ? 0.125 * ((double)box[3 + a] - (double)box[a]) : 0.0;
+            const double ref = moving ? (double)tp.noise_shift[a] : 0.0;
+            dom[a] = (double)box[a] + ref - m;
+            dom[3 + a] = (double)box[3 + a] + ref + m;
+        }
         NoiseTab nt{};
         long long total = 0;
         float f = tp.noise_freq;
@@ -852,8 +922,8 @@ cg_status ensure_noise(cg_context* ctx, const cg_volume* v, TraceParams& tp,
             nt.off[o] = (int)total;
             long long n = 1;
             for (int a = 0; a < 3; ++a) {
-                double lo = std::floor((double)box[a] * (double)f) - 1.0;
-                double hi = std::floor((double)box[3 + a] * (double)f) + 2.0;
+                double lo = std::floor(dom[a] * (double)f) - 1.0;
+                double hi = std::floor(dom[3 + a] * (double)f) + 2.0;
                 if (!(hi - lo < 4096.0) || !(lo > -1e9) || !(hi < 1e9)) {
                     n = -1;
                     break;
@@ -908,6 +978,13 @@ cg_status ensure_noise(cg_context* ctx, const cg_volume* v, TraceParams& tp,
             ctx->noise_freq = tp.noise_freq;
             ctx->noise_lac = tp.noise_lac;
             memcpy(ctx->noise_box, box, sizeof(box));
+            ctx->noise_moving = moving;
+            for (int a = 0; a < 3; ++a) {
+                ctx->noise_dom[a] = (float)dom[a];
+                ctx->noise_dom[3 + a] = (float)dom[3 + a];
+                ctx->noise_ref[a] = moving ? tp.noise_shift[a] : 0.f;
+                ctx->noise_margin[a] = moving ? (float)(0.125 * ((double)box[3 + a] - (double)box[a])) : 0.f;
+            }
         } else {
             memset(&ctx->noise_tab, 0, sizeof(ctx->noise_tab));
         }

@@ -95,6 +95,11 @@ struct cg_context {
     uint32_t noise_seed = 0;
     int noise_octaves = 0;
     float noise_freq = 0, noise_lac = 0, noise_box[6] = {0, 0, 0, 0, 0, 0};
+    // noise domain the tables cover; for a moving (wind) shift: the shift they
+    // were built around and how far it may move before a rebuild
+    bool noise_moving = false;
+    float noise_dom[6] = {0, 0, 0, 0, 0, 0};
+    float noise_ref[3] = {0, 0, 0}, noise_margin[3] = {0, 0, 0};
     NoiseTab noise_tab{};
     // deferred renderer: recorded view samples and the MLP fallback counter
     DevBuf samples_pw, samples_gl, samples_cnt;
@@ -159,6 +164,11 @@ struct cg_volume {
     long long gen = 0, tex_gen = -1;
     long long cov_gen = -1;  // voxelization whose integer coverage is in count / dq
     bool boards_dirty = false;  // billboards replaced since the last voxelize
+    // cross-stream order of board uploads (context stream) and voxelizes (any
+    // stream): boards_ready follows the last upload's copies, boards_read the
+    // last voxelize that read the board buffers (direct or graph replay)
+    cudaEvent_t boards_ready = nullptr, boards_read = nullptr;
+    bool ready_pending = false, read_pending = false;
 };
 
 cg_status ensure_textures(cg_volume* v, cudaStream_t s);

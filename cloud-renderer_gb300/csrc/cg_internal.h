@@ -60,10 +60,12 @@ struct NoiseTab {
     int dim[CG_MAX_LEVELS][3];
     // the same tables as 3D float textures for the surrogate renderer (0 = none)
     unsigned long long tex[CG_MAX_LEVELS];
-    // the whole fBm sampled on a fbm_res^3 grid of texel centres over the world
-    // box (surrogate renderer; 8 texels per finest lattice cell)
+    // the whole fBm sampled on a fbm_res^3 grid of texel centres over the noise
+    // domain (surrogate renderer; 8 texels per finest lattice cell): noise
+    // coordinate q sits at texel coordinate (q - fbm_org) * fbm_sc
     unsigned long long fbm_tex;
     int fbm_res;
+    float fbm_org[3], fbm_sc[3];
 };
 
 // Camera in FP32 for the trace kernels.
@@ -83,6 +85,7 @@ struct TraceParams {
     uint32_t noise_seed;
     int noise_octaves;
     float noise_freq, noise_lac, noise_gain, noise_inv_norm;
+    float noise_shift[3];  // world shift of the noise domain (offset / frequency)
     NoiseTab nt;
 };
 
@@ -255,7 +258,7 @@ cudaError_t launch_march(VolDesc vd, CamDesc cam, TraceParams tp, SampleBuf sb, 
 cudaError_t launch_shade_exact(VolDesc vd, CamDesc cam, TraceParams tp, SampleBuf sb,
                                float4* out, cudaStream_t st);
 cudaError_t launch_pack_level(VolDesc vd, int l, cudaSurfaceObject_t surf, cudaStream_t st);
-cudaError_t launch_fbm_volume(TraceParams tp, const float wmin[3], const float range[3], int R,
+cudaError_t launch_fbm_volume(TraceParams tp, const float org[3], const float ext[3], int R,
                               cudaSurfaceObject_t surf, cudaStream_t st);
 // Surrogate shading on the tensor cores (k_shade_tc.cu).  status (4 words,
 // zeroed before the launch): [0] += exact-cone fallbacks, [1] |= 1 when a

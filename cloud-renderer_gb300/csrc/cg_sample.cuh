@@ -298,8 +298,13 @@ __device__ __forceinline__ float value_noise_hw(const TraceParams& tp, int o, fl
     return value_noise(tp, o, x, y, z);
 }
 
+// fBm at world position p: the noise domain is shifted by tp.noise_shift
+// (q = p + shift; a zero shift leaves p unchanged).
 __device__ __forceinline__ float fbm_hw(const TraceParams& tp, float px, float py, float pz) {
     if (tp.noise_octaves <= 0) return 1.f;
+    px += tp.noise_shift[0];
+    py += tp.noise_shift[1];
+    pz += tp.noise_shift[2];
     float amp = 1.f, sum = 0.f, f = tp.noise_freq;
     for (int o = 0; o < tp.noise_octaves; ++o) {
         sum += amp * value_noise_hw(tp, o, px * f, py * f, pz * f);
@@ -310,26 +315,35 @@ __device__ __forceinline__ float fbm_hw(const TraceParams& tp, float px, float p
 }
 
 // fBm from its precomputed volume (surrogate renderer): one hardware
-// trilinear fetch at level-0 voxel position v; the volume holds fBm at its
-// texel centres over the world box (NoiseTab.fbm_res texels per axis).
-__device__ __forceinline__ float fbm_volume(const TraceParams& tp, float px, float py, float pz,
-                                            float vx, float vy, float vz, float D) {
+// trilinear fetch at the noise coordinate q = p + shift; the volume holds fBm
+// at its texel centres over the noise domain (NoiseTab.fbm_org / fbm_sc).
+__device__ __forceinline__ float fbm_volume(const TraceParams& tp, float px, float py,
+                                            float pz) {
     if (tp.noise_octaves <= 0) return 1.f;
     if (!tp.nt.fbm_tex) return fbm_hw(tp, px, py, pz);
-    const float s = (float)tp.nt.fbm_res / D;
-    return tex3D<float>((cudaTextureObject_t)tp.nt.fbm_tex, vx * s, vy * s, vz * s);
+    const float tx = (px + tp.noise_shift[0] - tp.nt.fbm_org[0]) * tp.nt.fbm_sc[0];
+    const float ty = (py + tp.noise_shift[1] - tp.nt.fbm_org[1]) * tp.nt.fbm_sc[1];
+    const float tz = (pz + tp.noise_shift[2] - tp.nt.fbm_org[2]) * tp.nt.fbm_sc[2];
+    return tex3D<float>((cudaTextureObject_t)tp.nt.fbm_tex, tx, ty, tz);
 }
 
-// fBm = sum_o gain^o noise_o(p * freq * lac^o) / sum_o gain^o; 1 without octaves.
-__device__ __forceinline__ float fbm(const TraceParams& tp, float px, float py, float pz) {
+// fBm = sum_o gain^o noise_o(q * freq * lac^o) / sum_o gain^o at the noise
+// coordinate q (already shifted); 1 without octaves.
+__device__ __forceinline__ float fbm_q(const TraceParams& tp, float qx, float qy, float qz) {
     if (tp.noise_octaves <= 0) return 1.f;
     float amp = 1.f, sum = 0.f, f = tp.noise_freq;
     for (int o = 0; o < tp.noise_octaves; ++o) {
-        sum += amp * value_noise(tp, o, px * f, py * f, pz * f);
+        sum += amp * value_noise(tp, o, qx * f, qy * f, qz * f);
         amp *= tp.noise_gain;
         f *= tp.noise_lac;
     }
     return sum * tp.noise_inv_norm;
+}
+
+// fBm at world position p (noise domain shifted by tp.noise_shift).
+__device__ __forceinline__ float fbm(const TraceParams& tp, float px, float py, float pz) {
+    if (tp.noise_octaves <= 0) return 1.f;
+    return fbm_q(tp, px + tp.noise_shift[0], py + tp.noise_shift[1], pz + tp.noise_shift[2]);
 }
 
 }  // namespace cgs

@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(256) k_march(VolDesc vd, CamDesc cam, TracePar
             float2 rg = HW ? cgs::quad_hw<true>(vd, v0, v1, v2, lod)
                            : cgs::quad<FMT, true, true, true>(vd, v0, v1, v2, lod);
             if (rg.x > 0.f) {
-                float rho = rg.x * (HW ? cgs::fbm_volume(tp, p0, p1, p2, v0, v1, v2, D)
+                float rho = rg.x * (HW ? cgs::fbm_volume(tp, p0, p1, p2)
                                        : cgs::fbm(tp, p0, p1, p2));
                 if (rho > 0.f) {
                     float alpha = 1.f - (HW ? __expf(-tp.sigma * rho * dt) : expf(-tp.sigma * rho * dt));

@@ -39,30 +39,31 @@ __global__ void k_pack_level(VolDesc vd, int l, cudaSurfaceObject_t surf) {
     }
 }
 
-// fBm at the texel centres of an R^3 grid over the world box.
-__global__ void k_fbm_volume(TraceParams tp, float wx, float wy, float wz, float rx, float ry,
-                             float rz, int R, cudaSurfaceObject_t surf) {
+// fBm at the texel centres of an R^3 grid over the noise domain (origin org,
+// extent ext per axis), in noise coordinates (no further shift).
+__global__ void k_fbm_volume(TraceParams tp, float ox, float oy, float oz, float ex, float ey,
+                             float ez, int R, cudaSurfaceObject_t surf) {
     const long long total = (long long)R * R * R;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
          i += (long long)gridDim.x * blockDim.x) {
         const int x = (int)(i % R), y = (int)((i / R) % R), z = (int)(i / ((long long)R * R));
-        const float px = wx + ((float)x + 0.5f) / (float)R * rx;
-        const float py = wy + ((float)y + 0.5f) / (float)R * ry;
-        const float pz = wz + ((float)z + 0.5f) / (float)R * rz;
-        __half h = __float2half_rn(cgs::fbm(tp, px, py, pz));
+        const float qx = ox + ((float)x + 0.5f) / (float)R * ex;
+        const float qy = oy + ((float)y + 0.5f) / (float)R * ey;
+        const float qz = oz + ((float)z + 0.5f) / (float)R * ez;
+        __half h = __float2half_rn(cgs::fbm_q(tp, qx, qy, qz));
         surf3Dwrite(__half_as_ushort(h), surf, x * 2, y, z);
     }
 }
 
 }  // namespace
 
-cudaError_t launch_fbm_volume(TraceParams tp, const float wmin[3], const float range[3], int R,
+cudaError_t launch_fbm_volume(TraceParams tp, const float org[3], const float ext[3], int R,
                               cudaSurfaceObject_t surf, cudaStream_t st) {
     const long long total = (long long)R * R * R;
     int blocks = (int)((total + 255) / 256);
     if (blocks > 152 * 16) blocks = 152 * 16;
-    k_fbm_volume<<<blocks, 256, 0, st>>>(tp, wmin[0], wmin[1], wmin[2], range[0], range[1],
-                                         range[2], R, surf);
+    k_fbm_volume<<<blocks, 256, 0, st>>>(tp, org[0], org[1], org[2], ext[0], ext[1], ext[2], R,
+                                         surf);
     return cudaGetLastError();
 }
 

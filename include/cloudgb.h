@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define CLOUDGB_ABI_VERSION 1
+#define CLOUDGB_ABI_VERSION 2
 
 typedef enum cg_status {
     CG_OK = 0,
@@ -91,6 +91,12 @@ typedef struct cg_noise {
     float frequency;  /* base lattice frequency over world units */
     float lacunarity; /* reference freqStep */
     float gain;       /* reference persStep */
+    /* Shift of the noise domain in base-frequency lattice units: octave k
+     * samples noise_k((p * frequency + offset) * lacunarity^k).  The
+     * reference's per-octave octaveOffsets = windVel * runTime
+     * (ConeTraceShader.cpp:55-61), added to the noise coordinate before the
+     * octave's frequency step (conetrace_frag.glsl:110); 0 = static noise. */
+    float offset[3];
 } cg_noise;
 
 /* Render parameters (reference: ConeTraceShader public fields,

@@ -741,6 +741,7 @@ typedef struct {
     uint32_t noise_seed;
     int noise_octaves;
     float noise_frequency, noise_lacunarity, noise_gain;
+    float noise_offset[3]; /* base-frequency lattice units (octaveOffsets) */
 } or_params;
 
 /* ---- sun cone -------------------------------------------------------
@@ -867,12 +868,19 @@ static real value_noise(const real x[3], uint32_t seed, int octave) {
     return y0 + w[2] * (y1 - y0);
 }
 
-/* fBm = sum_k gain^k noise_k(p * freq * lac^k) / sum_k gain^k; 1 when octaves = 0. */
+/* fBm = sum_k gain^k noise_k((p * freq + offset) * lac^k) / sum_k gain^k; 1 when
+ * octaves = 0.  The offset is the reference's per-octave octaveOffsets = windVel *
+ * runTime (ConeTraceShader.cpp:55-61), added to the base-frequency noise
+ * coordinate before the octave's frequency step (conetrace_frag.glsl:110); it is
+ * applied here as the world shift offset / freq. */
 static real fbm(const real p[3], const or_params* P) {
     if (P->noise_octaves <= 0) return (real)1;
     real amp = 1, norm = 0, sum = 0, f = (real)P->noise_frequency;
+    real q[3];
+    for (int a = 0; a < 3; ++a)
+        q[a] = p[a] + (real)((double)P->noise_offset[a] / (double)P->noise_frequency);
     for (int k = 0; k < P->noise_octaves; ++k) {
-        real x[3] = {p[0] * f, p[1] * f, p[2] * f};
+        real x[3] = {q[0] * f, q[1] * f, q[2] * f};
         sum += amp * value_noise(x, P->noise_seed, k);
         norm += amp;
         amp *= (real)P->noise_gain;

@@ -22,7 +22,7 @@ class or_params(ctypes.Structure):
                 ("transmittance_cutoff", ctypes.c_float), ("cone_mode", ctypes.c_int),
                 ("noise_seed", ctypes.c_uint32), ("noise_octaves", ctypes.c_int),
                 ("noise_frequency", ctypes.c_float), ("noise_lacunarity", ctypes.c_float),
-                ("noise_gain", ctypes.c_float)]
+                ("noise_gain", ctypes.c_float), ("noise_offset", ctypes.c_float * 3)]
 
 
 class or_sun_frame(ctypes.Structure):
@@ -124,6 +124,8 @@ def params_from_shader(shader):
     p.noise_frequency = float(shader.noiseFrequency)
     p.noise_lacunarity = float(shader.freqStep)
     p.noise_gain = float(shader.persStep)
+    wind = getattr(shader, "windVel", (0.0, 0.0, 0.0))
+    p.noise_offset[:] = [float(w) * float(getattr(shader, "runTime", 0.0)) for w in wind]
     return p
 
 
@@ -136,8 +138,8 @@ def make_params(**kw):
                     noise_lacunarity=2.0, noise_gain=0.5)
     defaults.update(kw)
     for k, v in defaults.items():
-        if k == "sun_color":
-            p.sun_color[:] = [float(x) for x in v]
+        if k in ("sun_color", "noise_offset"):
+            getattr(p, k)[:] = [float(x) for x in v]
         else:
             setattr(p, k, v)
     return p

@@ -39,7 +39,7 @@ def test_every_declared_symbol_is_bound():
 
 def test_status_strings_and_version():
     lib = _lib.load()
-    assert lib.cg_abi_version() == 1
+    assert lib.cg_abi_version() == 2
     assert lib.cg_status_string(0) == b"ok"
     assert lib.cg_status_string(5) == b"not ready"
 
@@ -50,6 +50,7 @@ def test_defaults():
     assert p.view_steps == 64 and p.sun_steps == 24
     assert abs(p.cone_half_angle - 0.03) < 1e-9
     assert p.use_mlp == 0
+    assert tuple(p.noise.offset) == (0.0, 0.0, 0.0)
 
 
 def test_null_arguments_are_rejected():

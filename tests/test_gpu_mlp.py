@@ -244,6 +244,32 @@ def test_mlp_render_rmse_and_gain(ctx, trained):
     assert t_mlp < t_exact, (t_mlp, t_exact)
 
 
+def test_mlp_render_with_wind(ctx, trained):
+    """The surrogate path's fBm volume follows the wind: renders at run times
+    inside and past the noise domain's margin stay within RMSE 1e-2 of the
+    oracle with the same octave offsets."""
+    mlp, _, _ = trained
+    cfg = configs.PLAIN_1080P
+    wl = workload.build(cfg, width=240, height=135)
+    vol, sun, ov = _pair(ctx, cfg, wl, cloudgb.FORMAT_BF16_FP16)
+    cam = workload.make_camera(wl.cameras[2])
+    kw = wl.shader_kwargs()
+    exact = cloudgb.ConeTraceShader(**kw)
+    learned = cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, **kw)
+    prev = None
+    for t in (0.4, 0.6, 2.5):
+        for sh in (exact, learned):
+            sh.windVel = (0.8, 0.1, -0.3)
+            sh.runTime = t
+        ref = ov.render(cam, O.params_from_shader(exact), sun.direction)
+        img = learned.coneTrace(vol, cam).astype(np.float64)
+        rmse = float(np.sqrt(((img - ref) ** 2).mean()))
+        assert rmse <= 1e-2, (t, rmse)
+        if prev is not None:
+            assert not np.array_equal(img, prev)
+        prev = img
+
+
 def test_fallback_outside_training_range(ctx, trained):
     mlp, _, _ = trained
     cfg = configs.PLAIN_1080P

@@ -255,6 +255,69 @@ def test_noise_scene_small_image_full_parity(ctx):
         assert ref[..., 3].max() > 0.5
 
 
+def test_wind_offset_noise_parity_and_table_reuse(ctx):
+    """Wind (octaveOffsets = windVel * runTime) moves the noise domain: each
+    image matches the oracle with the same offset; a shift within the tables'
+    margin reuses them (one launch fewer), a larger one rebuilds them, and
+    either way the image is bit-identical (the tables hold the hashed values)."""
+    cfg = configs.PLAIN_1080P
+    wl = workload.build(cfg, width=160, height=90)
+    vol, sun, ov = make_pair(ctx, cfg["dim"], cfg["mips"], wl.positions, wl.scales, wl.densities,
+                             wl.sun_direction, wl.sun_map)
+    shader = cloudgb.ConeTraceShader(**wl.shader_kwargs())
+    shader.windVel = (0.8, 0.1, -0.3)
+    cam = workload.make_camera(wl.cameras[1])
+    imgs, launches = {}, {}
+    for t in (0.0, 0.5, 0.7, 3.0):
+        shader.runTime = t
+        n0 = ctx.launch_count
+        imgs[t] = shader.coneTrace(vol, cam)
+        launches[t] = ctx.launch_count - n0
+        ref = _oracle_image(ov, shader, cam, sun.direction)
+        err = np.abs(imgs[t].astype(np.float64) - ref).max(axis=(0, 1))
+        assert np.all(err <= IMAGE_TOL), f"runTime {t}: max-abs per channel {err}"
+    assert not np.array_equal(imgs[0.5], imgs[0.0])
+    assert not np.array_equal(imgs[3.0], imgs[0.5])
+    assert launches[0.7] == launches[0.5] - 1   # reused the tables built for 0.5
+    assert launches[3.0] == launches[0.5]       # moved past the margin: rebuilt
+    shader.runTime = 0.7                        # rebuilt around 0.7 this time
+    assert np.array_equal(shader.coneTrace(vol, cam), imgs[0.7])
+
+
+def test_board_uploads_order_with_voxelize_on_a_user_stream(ctx):
+    """Uploads (made on the context's stream) and voxelizes on a caller's
+    stream, back to back with no host synchronisation: each voxelize sees its
+    own upload, and an upload waits for the voxelize still reading the last
+    boards.  The final pyramid equals a default-stream voxelize of the last
+    boards."""
+    torch = pytest.importorskip("torch")
+    cfg = configs.PLAIN_1080P
+    wl = workload.build(cfg, width=64, height=36)
+    sun = cloudgb.Sun(wl.sun_direction, *wl.sun_map)
+    s = torch.cuda.Stream()
+    vol = cloudgb.CloudVolume(cfg["dim"], configs.VOLUME_BOUNDS, configs.VOLUME_POSITION,
+                              cfg["mips"], ctx=ctx)
+    ref = cloudgb.CloudVolume(cfg["dim"], configs.VOLUME_BOUNDS, configs.VOLUME_POSITION,
+                              cfg["mips"], ctx=ctx)
+    rng = np.random.default_rng(5)
+    sets = []
+    for i in range(6):
+        n = len(wl.scales) - 300 * (i % 3)  # board counts (and buffer sizes) change too
+        pos = wl.positions[:n] + rng.uniform(-0.02, 0.02, (n, 3)).astype(np.float32)
+        sets.append((pos, wl.scales[:n] * (1.0 + 0.2 * (i % 2)), wl.densities[:n]))
+    for pos, sc, de in sets:
+        vol.set_billboards(pos, sc, de)
+        vol.update()
+        cloudgb.VoxelizeShader().voxelize(vol, sun, stream=s.cuda_stream)
+    ref.set_billboards(*sets[-1])
+    ref.update()
+    cloudgb.VoxelizeShader().voxelize(ref, sun)
+    for l in (0, 2):
+        assert np.array_equal(vol.read_level(l), ref.read_level(l)), f"level {l}"
+    vol.close()
+    ref.close()
+
+
 def test_render_is_deterministic(ctx):
     cfg = configs.SMALL_64
     wl = workload.build(cfg, width=96, height=64)

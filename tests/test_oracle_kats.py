@@ -252,6 +252,27 @@ def test_fbm_range_and_continuity():
     assert O.fbm((0.3, 0.3, 0.3), O.make_params(noise_octaves=0)) == 1.0
 
 
+def test_fbm_wind_offset_is_a_domain_shift():
+    """octaveOffsets (base-frequency lattice units) move the whole fBm: with
+    offset o and frequency f, fbm_o(p) = fbm_0(p + o / f), every octave alike."""
+    f = np.float32(4.0)
+    off = np.float32([0.37, -1.25, 2.5])
+    P0 = O.make_params(noise_octaves=4, noise_seed=7, noise_frequency=float(f))
+    P1 = O.make_params(noise_octaves=4, noise_seed=7, noise_frequency=float(f),
+                       noise_offset=off)
+    rng = np.random.default_rng(3)
+    for p in rng.uniform(-1, 1, (50, 3)):
+        q = p + off.astype(np.float64) / np.float64(f)
+        assert O.fbm(p, P1) == O.fbm(q, P0)
+    # a whole lattice cell of offset at the base frequency is a shift by one
+    # base cell (1 / f world units), not the identity
+    P2 = O.make_params(noise_octaves=4, noise_seed=7, noise_frequency=float(f),
+                       noise_offset=(1.0, 0.0, 0.0))
+    p = np.array([0.1, 0.2, 0.3])
+    assert O.fbm(p, P2) == O.fbm(p + np.array([0.25, 0.0, 0.0]), P0)
+    assert O.fbm(p, P2) != O.fbm(p, P0)
+
+
 def test_sun_frame_orthonormal():
     rc, fr = O.sun_frame(POS, BOUNDS, (0.3, 1.0, 0.2), 1280, 720)
     assert rc == 0
