@@ -42,10 +42,12 @@ def parse():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["frame", "batch", "animated"], default="frame",
+    ap.add_argument("--workload", choices=["frame", "batch", "animated", "compat"],
+                    default="frame",
                     help="frame: the headline 1080p frame; batch: 48 clouds x 128 views per "
                          "frame (one persistent launch, CUDA-graph replay, autotuned); "
-                         "animated: moving boards re-voxelized every frame, wind-moved noise")
+                         "animated: moving boards re-voxelized every frame, wind-moved noise; "
+                         "compat: the reference's billboard image formation")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget-s", type=float, default=15.0)
     ap.add_argument("--mlp-steps", type=int, default=20000)
@@ -730,6 +732,122 @@ def run_animated(args):
     vol.close()
 
 
+def run_compat(args):
+    """The compat pass (the reference's own image formation: camera-facing
+    billboards shaded by its fragment program, blended in distance order) on
+    its own scene scale: 200 boards, 32^3 volume, 1080p, the 8 orbit views.
+    One step = voxelize + compat render of one view.  Metric: Mpix/s."""
+    import numpy as np
+    import torch
+
+    import cloudgb
+    from cloudgb import _lib, configs, workload as Wm
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    ctx = cloudgb.Context(local)
+    lib = _lib.load()
+    cfg = configs.COMPAT_REF
+    wl = Wm.build_compat(cfg, width=args.width, height=args.height)
+    vol = cloudgb.CloudVolume(cfg["dim"], cfg["bounds"], cfg["position"], cfg["mips"], ctx=ctx)
+    vol.set_billboards(wl.positions, wl.scales)
+    vol.update()
+    sun = cloudgb.Sun(wl.sun_direction, *cfg["sun_map"])
+    csun = sun._c()
+    cams = [Wm.make_camera(cd) for cd in wl.cameras]
+    ccams = [c._c() for c in cams]
+    W, H = cams[0].width, cams[0].height
+    shader = cloudgb.CompatShader()
+    params = shader.params()
+    stream = torch.cuda.Stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    img = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def frame(k):
+        _lib.check(lib.cg_voxelize(vol.handle, ctypes.byref(csun), sp), "cg_voxelize")
+        _lib.check(lib.cg_render_compat(ctx.handle, vol.handle, ctypes.byref(ccams[k % len(cams)]),
+                                        ctypes.byref(params), ctypes.c_void_p(img.data_ptr()), 1,
+                                        sp), "cg_render_compat")
+
+    with torch.cuda.stream(stream):
+        for k in range(args.warmup):
+            frame(k)
+        torch.cuda.synchronize()
+        l0 = ctx.launch_count
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+        sampler = ClockSampler(gpu_index(local))
+        sampler.__enter__()
+        for k in range(args.steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            frame(k)
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        sampler.__exit__()
+        launches = ctx.launch_count - l0
+        ctx.set_timing(True)
+        stages = {}
+        for k in range(min(args.steps, 8)):
+            frame(k)
+            for name, ms_ in ctx.stage_times().items():
+                stages.setdefault(name, []).append(ms_)
+        ctx.set_timing(False)
+    ms = np.array([a.elapsed_time(b) for a, b in ev])
+    total_ms = float(ms.sum())
+    value = W * H * args.steps / (total_ms / 1e3) / 1e6
+    # e2e through the public API: host boards in, host image out
+    out = cloudgb.HostBuffer((H, W, 4))
+    e2e = []
+    for k in range(9):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        vol.update()
+        cloudgb.VoxelizeShader().voxelize(vol, sun)
+        shader.coneTrace(vol, cams[k % len(cams)], out=out)
+        if k:
+            e2e.append(time.perf_counter() - t0)
+    line = {"metric": "Mpix/s, compat pass (the reference's billboard image formation), 1080p, "
+                      "200 boards, 32³ volume",
+            "value": round(value, 3), "unit": "Mpix/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded SplitMix64 scene at the reference's scale)",
+            "config": {"workload": "compat pass: voxelize + billboard render, reference scene "
+                                   "(200 boards r in [1, 2.5], 32^3, bounds +-5), 8 orbit views",
+                       "image": f"{W}x{H}",
+                       "stages_ms": {k: round(float(np.mean(v)), 4) for k, v in stages.items()},
+                       "frame_ms_median": round(float(np.median(ms)), 4),
+                       "l2": "256 MiB buffer written between timed steps"},
+            "gpu_launches": int(launches),
+            "clocks": sampler.summary(),
+            "e2e": {"value": round(W * H / float(np.median(e2e)) / 1e6, 3), "unit": "Mpix/s",
+                    "h2d_bytes_per_step": vol.count * 45, "d2h_bytes_per_step": W * H * 16}}
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        threads = os.cpu_count() or 1
+        ov = O.OracleVolume(cfg["dim"], cfg["bounds"], cfg["position"], cfg["mips"], bits=32)
+        ov.set_boards(wl.positions, wl.scales, np.ones(len(wl.scales), np.float32))
+        t0 = time.perf_counter()
+        ov.voxelize(wl.sun_direction, *cfg["sun_map"], threads=threads)
+        t_vox = time.perf_counter() - t0
+        small = cloudgb.Camera(cams[0].eye, cams[0].target, width=W // 4, height=H // 4)
+        t0 = time.perf_counter()
+        ov.compat_render(small, params, wl.sun_direction, O.compat_noise_map(params.noise_seed),
+                         threads=threads)
+        t_r = time.perf_counter() - t0
+        frame_s = t_vox + t_r * 16.0
+        line["cpu_baseline"] = {"value": round(W * H / frame_s / 1e6, 4), "unit": "Mpix/s",
+                                "cores": threads, "kind": "port",
+                                "sample": f"FP32 oracle: voxelize ({t_vox:.3f} s) + view 0 at "
+                                          f"{W // 4}x{H // 4} ({t_r:.2f} s), frame time "
+                                          f"extrapolated per pixel"}
+    print(json.dumps(line), flush=True)
+    vol.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -738,6 +856,8 @@ def main():
         run_batch(args)
     elif args.workload == "animated":
         run_animated(args)
+    elif args.workload == "compat":
+        run_compat(args)
     else:
         run_ours(args)
 

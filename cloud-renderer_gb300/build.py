@@ -33,6 +33,8 @@ SOURCES = [
     ("k_batch.cu", []),
     ("cg_batch.cpp", ["-Xcompiler", "-ffp-contract=off"]),
     ("cg_mlp.cpp", ["-Xcompiler", "-ffp-contract=off"]),
+    ("k_compat.cu", []),
+    ("cg_compat.cpp", ["-Xcompiler", "-ffp-contract=off"]),
 ]
 
 

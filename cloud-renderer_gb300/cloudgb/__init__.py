@@ -18,7 +18,7 @@ from ._lib import (CONE_REFERENCE, CONE_TRANSMITTANCE, FORMAT_BF16_FP16, FORMAT_
                    CloudError, check, load)
 
 __all__ = ["Context", "CloudVolume", "Sun", "Camera", "VoxelizeShader", "ConeTraceShader",
-           "CloudError", "FORMAT_RGBA32F", "FORMAT_BF16_FP16", "CONE_TRANSMITTANCE",
+           "CompatShader", "FrameGraph", "CloudError", "FORMAT_RGBA32F", "FORMAT_BF16_FP16", "CONE_TRANSMITTANCE",
            "CONE_REFERENCE", "default_context", "HostBuffer", "DeviceBuffer"]
 
 
@@ -558,6 +558,83 @@ class ConeTraceShader:
     @staticmethod
     def half_angle_to_cone_angle(half):
         return 2.0 * half
+
+
+class CompatShader:
+    """The reference's own image formation (ConeTraceShader::coneTrace,
+    ConeTraceShader.cpp:15-82): one camera-facing billboard per board shaded
+    by its fragment program (soft-particle noise, traceCone from the sphere
+    surface) and blended in distance order over the clear colour.  Field
+    names and defaults follow ConeTraceShader.hpp:15-32; octaveOffsets =
+    windVel * runTime (ConeTraceShader.cpp:55-61)."""
+
+    _FIELDS = dict(showQuad="show_quad", doNoiseSample="do_noise", doConeTrace="do_cone_trace",
+                   stepSize="step_size", noiseOpacity="noise_opacity", numOctaves="num_octaves",
+                   freqStep="freq_step", persStep="pers_step", adjustSize="adjust_size",
+                   minNoiseSteps="min_noise_steps", maxNoiseSteps="max_noise_steps",
+                   minNoiseColor="min_noise_color", noiseColorScale="noise_color_scale",
+                   noiseSeed="noise_seed", vctSteps="vct_steps", vctConeAngle="vct_cone_angle",
+                   vctConeInitialHeight="vct_cone_initial_height",
+                   vctLodOffset="vct_lod_offset", vctDownScaling="vct_down_scaling",
+                   nearPlane="near_plane", transmittanceCutoff="transmittance_cutoff")
+
+    def __init__(self, **kw):
+        p = _lib.cg_compat_params()
+        load().cg_compat_params_default(ctypes.byref(p))
+        for name, field in self._FIELDS.items():
+            v = getattr(p, field)
+            setattr(self, name, bool(v) if field in ("show_quad", "do_noise", "do_cone_trace")
+                    else v)
+        self.clearColor = tuple(p.clear_color)
+        self.windVel = (0.01, 0.0, 0.0)
+        self.runTime = 0.0
+        for k, v in kw.items():
+            if not hasattr(self, k):
+                raise AttributeError(f"CompatShader has no parameter {k!r}")
+            setattr(self, k, v)
+
+    def params(self):
+        p = _lib.cg_compat_params()
+        for name, field in self._FIELDS.items():
+            v = getattr(self, name)
+            ftype = dict(p._fields_)[field]
+            setattr(p, field, int(v) & 0xFFFFFFFF if field == "noise_seed" else
+                    (int(v) if ftype is ctypes.c_int else float(v)))
+        p.clear_color[:] = [float(x) for x in self.clearColor]
+        p.octave_offsets[:] = [float(w) * float(self.runTime) for w in self.windVel]
+        return p
+
+    def coneTrace(self, volume, camera, out=None, stream=None):
+        """The compat image of camera over volume's boards: H x W x 4 float32
+        (row 0 = top); `out` as in ConeTraceShader.coneTrace."""
+        p = self.params()
+        c = camera._c()
+        lib = load()
+        if isinstance(out, DeviceBuffer):
+            check(lib.cg_render_compat(volume.ctx.handle, volume.handle, ctypes.byref(c),
+                                       ctypes.byref(p), out.ptr, 1, stream), "cg_render_compat")
+            return out
+        if isinstance(out, HostBuffer):
+            arr = out.array
+        elif out is None:
+            arr = np.empty((camera.height, camera.width, 4), np.float32)
+        else:
+            arr = out
+        assert arr.dtype == np.float32 and arr.flags["C_CONTIGUOUS"]
+        assert arr.size >= camera.width * camera.height * 4
+        check(lib.cg_render_compat(volume.ctx.handle, volume.handle, ctypes.byref(c),
+                                   ctypes.byref(p), arr.ctypes.data_as(ctypes.c_void_p), 0,
+                                   stream), "cg_render_compat")
+        return arr
+
+    @staticmethod
+    def noise_map(seed):
+        """The decoded 32^3 RGBA noise map of a seed: (32, 32, 32, 4) float32."""
+        out = np.empty((32, 32, 32, 4), np.float32)
+        check(load().cg_compat_noise_map(int(seed) & 0xFFFFFFFF,
+                                         out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))),
+              "cg_compat_noise_map")
+        return out
 
 
 def deg(x):

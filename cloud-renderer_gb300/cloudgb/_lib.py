@@ -89,6 +89,21 @@ class cg_batch_view(ctypes.Structure):
     _fields_ = [("volume", ctypes.c_void_p), ("camera", cg_camera), ("rgba_out", ctypes.c_void_p)]
 
 
+class cg_compat_params(ctypes.Structure):
+    _fields_ = [("show_quad", ctypes.c_int), ("do_noise", ctypes.c_int),
+                ("do_cone_trace", ctypes.c_int), ("step_size", ctypes.c_float),
+                ("noise_opacity", ctypes.c_float), ("num_octaves", ctypes.c_int),
+                ("freq_step", ctypes.c_float), ("pers_step", ctypes.c_float),
+                ("adjust_size", ctypes.c_float), ("min_noise_steps", ctypes.c_int),
+                ("max_noise_steps", ctypes.c_int), ("min_noise_color", ctypes.c_float),
+                ("noise_color_scale", ctypes.c_float), ("octave_offsets", ctypes.c_float * 3),
+                ("noise_seed", ctypes.c_uint32), ("vct_steps", ctypes.c_int),
+                ("vct_cone_angle", ctypes.c_float), ("vct_cone_initial_height", ctypes.c_float),
+                ("vct_lod_offset", ctypes.c_float), ("vct_down_scaling", ctypes.c_float),
+                ("clear_color", ctypes.c_float * 4), ("near_plane", ctypes.c_float),
+                ("transmittance_cutoff", ctypes.c_float)]
+
+
 class cg_volume_info(ctypes.Structure):
     _fields_ = [("dimension", ctypes.c_int), ("mips", ctypes.c_int), ("format", ctypes.c_int),
                 ("board_count", ctypes.c_int), ("world_min", ctypes.c_float * 3),
@@ -170,6 +185,10 @@ SIGNATURES = [
                                   I, ctypes.POINTER(cg_render_params), PP]),
     ("cg_frame_graph_launch", I, [P, P]),
     ("cg_frame_graph_destroy", None, [P]),
+    ("cg_compat_params_default", None, [ctypes.POINTER(cg_compat_params)]),
+    ("cg_compat_noise_map", I, [ctypes.c_uint32, FP]),
+    ("cg_render_compat", I, [P, P, ctypes.POINTER(cg_camera), ctypes.POINTER(cg_compat_params), P,
+                             I, P]),
 ]
 NOALLOC_MAX_TEXELS = 1 << 20
 

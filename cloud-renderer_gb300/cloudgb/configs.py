@@ -61,5 +61,18 @@ LEARNED = dict(
     lr=1e-3, eval_base="PLAIN_1080P", eval_fmt="bf16_fp16",
 )
 
+# The compat render's scene at the reference's own scale (main.cpp:29-37, :82):
+# a 32^3 volume of bounds +-5 at (25, 0, 0), 4 mips, 200 boards offset
+# uniformly in +-2.5 with radii in [1, 2.5], the sun at (5, 20, -5); the
+# views orbit the cloud at 14 world units.
+COMPAT_REF = dict(
+    name="compat_reference_scene_1080p",
+    dim=32, mips=4, bounds=(-5.0, 5.0), position=(25.0, 0.0, 0.0),
+    boards=200, board_seed=21, offset_range=(-2.5, 2.5), scale_range=(1.0, 2.5),
+    sun_position=(5.0, 20.0, -5.0), sun_map=(256, 256),
+    orbit_seed=23, orbits=8, orbit_radius=14.0, orbit_height=(1.0, 6.0),
+    camera=dict(fov=60.0, width=1920, height=1080),
+)
+
 ALL = dict(SMALL_64=SMALL_64, PLAIN_1080P=PLAIN_1080P, PRECISION_4K=PRECISION_4K,
-           BATCH_48x128=BATCH_48x128, LEARNED=LEARNED)
+           BATCH_48x128=BATCH_48x128, LEARNED=LEARNED, COMPAT_REF=COMPAT_REF)

@@ -115,3 +115,39 @@ def build_batch(cfg, clouds=None, views=None, max_pixels=None):
     d = np.asarray(configs.SUN_DIRECTION, np.float64)
     d = tuple(float(x) for x in d / np.sqrt((d * d).sum()))
     return BatchWorkload(cfg=cfg, clouds=cl, views=vs, sun_direction=d)
+
+
+@dataclass
+class CompatWorkload:
+    """The compat render's scene: boards as offsets from the volume position
+    (CloudVolume::regenerateBillboards, CloudVolume.cpp:120-133), the sun as
+    the direction from the volume toward the reference's sun position."""
+    cfg: dict
+    positions: np.ndarray
+    scales: np.ndarray
+    sun_direction: tuple
+    sun_map: tuple
+    cameras: list
+
+
+def build_compat(cfg, boards=None, width=None, height=None):
+    n = boards if boards is not None else cfg["boards"]
+    rng = scene.SplitMix64(cfg["board_seed"])
+    lo, hi = cfg["offset_range"]
+    pos = (lo + (hi - lo) * rng.uniform(3 * n).reshape(n, 3)).astype(np.float32)
+    sc = rng.uniform_range(n, *cfg["scale_range"]).astype(np.float32)
+    c = np.asarray(cfg["position"], np.float64)
+    d = np.asarray(cfg["sun_position"], np.float64) - c
+    sun = tuple(float(x) for x in d / np.linalg.norm(d))
+    cam = cfg["camera"]
+    crng = scene.SplitMix64(cfg["orbit_seed"])
+    m = cfg["orbits"]
+    ang = 2.0 * np.pi * (np.arange(m) + crng.uniform(m)) / m
+    hgt = crng.uniform_range(m, *cfg["orbit_height"])
+    R = cfg["orbit_radius"]
+    cams = [dict(eye=(float(c[0] + R * np.sin(a)), float(c[1] + h), float(c[2] - R * np.cos(a))),
+                 target=tuple(float(x) for x in c), fov=cam["fov"],
+                 width=width or cam["width"], height=height or cam["height"])
+            for a, h in zip(ang, hgt)]
+    return CompatWorkload(cfg=cfg, positions=pos, scales=sc, sun_direction=sun,
+                          sun_map=cfg["sun_map"], cameras=cams)

@@ -241,6 +241,12 @@ void context_release(cg_context* ctx) {
     ctx->stats_ref.release();
     ctx->batch_pinned.release();
     ctx->batch_dev.release();
+    ctx->compat_noise.release();
+    ctx->compat_rect.release();
+    ctx->compat_key.release();
+    ctx->compat_tiles.release();
+    ctx->compat_list.release();
+    ctx->compat_total.release();
     release_noise_textures(ctx);
     for (cudaEvent_t e : ctx->marks)
         if (e) cudaEventDestroy(e);

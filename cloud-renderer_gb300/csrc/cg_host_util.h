@@ -111,6 +111,13 @@ struct cg_context {
     std::vector<BatchView> batch_host;
     HostBuf batch_pinned;
     DevBuf batch_dev;
+    // compat render: noise map (green, alpha) of compat_seed, per-board tile
+    // rectangles and keys, per-tile counts / offsets / cursors, the lists
+    DevBuf compat_noise;
+    bool compat_noise_valid = false;
+    uint32_t compat_seed = 0;
+    DevBuf compat_rect, compat_key, compat_tiles, compat_list;
+    HostBuf compat_total;
     // noise lattice tables as 3D float textures (surrogate renderer)
     cudaArray_t noise_arr[CG_MAX_LEVELS] = {};
     cudaTextureObject_t noise_tex[CG_MAX_LEVELS] = {};

@@ -335,3 +335,36 @@ void batch_tiles(int lanes_per_ray, int width, int height, int& tiles_x, int& ti
 cudaError_t launch_trace_batch(int fmt, int lanes_per_ray, int unroll, const BatchView* views,
                                int n, unsigned total_tiles, unsigned* counter, cudaStream_t st);
 
+
+// ---- compat render (k_compat.cu) ------------------------------------------
+// The reference's billboard image formation; see cg_render_compat.
+constexpr int CG_COMPAT_TILE = 16;  // pixel tile edge
+struct CompatDev {
+    CamDesc cam;
+    int n;                 // boards
+    const float4* cwr;     // world centre, radius
+    int tiles_x, tiles_y;
+    float near_z;
+    int show_quad, do_noise, do_cone;
+    float step_size, noise_opacity;
+    int octaves;
+    float freq_step, pers_step, inv_adjust;
+    int min_steps, max_steps;
+    float min_color, color_scale;
+    float off[3];
+    float clear[4];
+    float cutoff;
+    float sun[3];
+    const float2* noise;   // green and alpha of the decoded 32^3 noise map
+};
+// Per board: tile rectangle (x0, y0, x1, y1; empty when x0 > x1) and the
+// squared eye distance; per tile: the number of boards whose quad may cover it.
+cudaError_t launch_compat_count(const CompatDev& P, int4* rect, float* key, uint32_t* tile_count,
+                                cudaStream_t st);
+// Per tile: (distance bits << 32 | board) at the tile's cursor.
+cudaError_t launch_compat_fill(const CompatDev& P, const int4* rect, const float* key,
+                               uint32_t* cursor, unsigned long long* list, cudaStream_t st);
+// Per tile: order its list by distance and blend its pixels front to back.
+cudaError_t launch_compat_tiles(const VolDesc& vd, const ConeSchedule& cs, const CompatDev& P,
+                                const uint32_t* offset, unsigned long long* list, float4* out,
+                                cudaStream_t st);

@@ -418,6 +418,60 @@ cg_status cg_frame_graph_create(cg_context* ctx, cg_volume* const* volumes, int 
 cg_status cg_frame_graph_launch(cg_frame_graph* graph, void* stream);
 void cg_frame_graph_destroy(cg_frame_graph* graph);
 
+/* ---- compat render: the reference's own image formation ------------------
+ * ConeTraceShader::coneTrace (ConeTraceShader.cpp:15-82) as the reference
+ * draws it: one camera-facing billboard of radius scale * fluffiness per
+ * board (billboard_vert_instanced.glsl), shaded by the fragment program of
+ * conetrace_frag.glsl:122-201 (soft-particle noise march through the board's
+ * sphere, traceCone from the sphere surface toward the sun over the light
+ * channel), blended SRC_ALPHA / ONE_MINUS_SRC_ALPHA over the clear colour in
+ * distance order (main.cpp:94-95, sortBoards CloudVolume.cpp:65-82), without
+ * a global sort: boards are binned to 16x16-pixel tiles and each tile orders
+ * its own list.  Field names follow ConeTraceShader.hpp:15-32. */
+typedef struct cg_compat_params {
+    int show_quad;              /* showQuad: debug quad (sphere profile, white border) */
+    int do_noise;               /* doNoiseSample */
+    int do_cone_trace;          /* doConeTrace */
+    float step_size;            /* stepSize, noise-map units */
+    float noise_opacity;        /* noiseOpacity */
+    int num_octaves;            /* numOctaves */
+    float freq_step;            /* freqStep */
+    float pers_step;            /* persStep */
+    float adjust_size;          /* adjustSize: world units per noise-map period */
+    int min_noise_steps;        /* minNoiseSteps (>= 2) */
+    int max_noise_steps;        /* maxNoiseSteps (>= minNoiseSteps) */
+    float min_noise_color;      /* minNoiseColor */
+    float noise_color_scale;    /* noiseColorScale */
+    float octave_offsets[3];    /* windVel * runTime (ConeTraceShader.cpp:55-61); octave k
+                                   adds component k (k < 3) to all three coordinates */
+    uint32_t noise_seed;        /* seed of the 32^3 noise map (initNoiseMap) */
+    int vct_steps;              /* vctSteps (<= 64) */
+    float vct_cone_angle;       /* vctConeAngle (full aperture, radians) */
+    float vct_cone_initial_height; /* vctConeInitialHeight, level-0 voxels */
+    float vct_lod_offset;       /* vctLodOffset */
+    float vct_down_scaling;     /* vctDownScaling */
+    float clear_color[4];       /* glClearColor (main.cpp:112) */
+    float near_plane;           /* camera near plane (Camera.cpp:59); far = 2500 */
+    float transmittance_cutoff; /* stop a pixel once the boards in front leave less than
+                                   this of the background visible (0 = blend every board) */
+} cg_compat_params;
+
+/* The reference's defaults (ConeTraceShader.hpp:15-32, main.cpp:112). */
+void cg_compat_params_default(cg_compat_params* p);
+
+/* The decoded 32^3 RGBA noise map of a seed (initNoiseMap,
+ * ConeTraceShader.cpp:127-159, from a seeded stream; exact integer
+ * arithmetic): 32*32*32*4 floats, x fastest.  Host only, no device needed. */
+cg_status cg_compat_noise_map(uint32_t seed, float* out);
+
+/* Render the compat image of the volume's billboards.  The volume must have
+ * been voxelized when do_cone_trace is set (the cone reads its light
+ * channel; the sun is the one of that voxelize).  rgba_out as in cg_render
+ * (row 0 = top); one host synchronisation sizes the tile lists. */
+cg_status cg_render_compat(cg_context* ctx, const cg_volume* vol, const cg_camera* cam,
+                           const cg_compat_params* params, float* rgba_out, int out_on_device,
+                           void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -6,7 +6,8 @@ of jaafersheriff/Cloud-Renderer, read where they lie under /root/reference --
 as C++ through oracle/ref_shim/glsl_shim.hpp, together with the driver
 oracle/ref_shim/ref_driver.inc that runs them the way the reference's host
 code does.  The translation unit is assembled in memory and piped to g++:
-each shader's text goes into its own namespace, its `#version` line blanked;
+each shader's text goes into its own namespace, its `#version` line blanked
+and its `inout` parameters written as C++ references;
 no copy of a reference source is written anywhere.  The output (and only it)
 goes to oracle/_ref/, which git ignores.
 
@@ -15,6 +16,7 @@ skip otherwise, and the fixtures under tests/golden/ (made from it by
 tests/golden/make_golden.py) carry its results everywhere else.
 """
 import os
+import re
 import subprocess
 import sys
 
@@ -44,6 +46,8 @@ def translation_unit():
         with open(path) as f:
             lines = f.read().split("\n")
         lines = ["" if ln.lstrip().startswith("#version") else ln for ln in lines]
+        # `inout T name` parameters become C++ references (GLSL copies them back)
+        lines = [re.sub(r"\binout\s+(\w+)\s+(\w+)", r"\1& \2", ln) for ln in lines]
         parts.append(f"namespace {ns} {{\nusing namespace glsl;\n"
                      "vec4 gl_Position; vec4 gl_FragCoord; float gl_FragDepth;\n"
                      f'#line 1 "{rel}"\n')

@@ -1044,6 +1044,337 @@ OR_API int or_render(const or_volume* v, const or_camera* cam, const or_params* 
 OR_API int or_real_bytes(void) { return (int)sizeof(real); }
 
 /* ------------------------------------------------------------------ */
+/* Compat render: the reference's own image formation, one camera-facing   */
+/* billboard per board shaded by conetrace_frag.glsl:122-201 and blended    */
+/* back to front (ConeTraceShader::coneTrace, ConeTraceShader.cpp:15-82;     */
+/* sortBoards, CloudVolume.cpp:65-82; blend state main.cpp:94-95), restated  */
+/* per pixel:                                                               */
+/*  - quad: c + r (x s + y u), x, y in [-1, 1] (billboard_vert_instanced.glsl */
+/*    with Library::createQuad), camera-facing, so every pixel's fragment is  */
+/*    the plane point e + z d (z = (c - e).f, d the pixel ray with d.f = 1);  */
+/*    the quad is drawn only when near < z < 2500 (Camera.cpp:59);           */
+/*  - fragment: the shader's noise march and traceCone, with lightPos far     */
+/*    along the sun direction (dir = sun) and the noise map supplied as a    */
+/*    decoded 32^3 RGBA table (REPEAT, LINEAR; octave k adds the scalar      */
+/*    octaveOffsets[k], k < 3, else 0 -- the shader indexes a vec3);         */
+/*  - blend: source clamped to [0, 1] (fixed-point target), then            */
+/*    C = a src + (1 - a) C for RGB and A = a a + (1 - a) A over the clear    */
+/*    colour, boards in descending (distance to the eye, index) order.       */
+/* ------------------------------------------------------------------ */
+typedef struct {
+    int show_quad, do_noise, do_cone_trace;
+    float step_size, noise_opacity;
+    int num_octaves;
+    float freq_step, pers_step, adjust_size;
+    int min_noise_steps, max_noise_steps;
+    float min_noise_color, noise_color_scale;
+    float octave_offsets[3];
+    uint32_t noise_seed;
+    int vct_steps;
+    float vct_cone_angle, vct_cone_initial_height, vct_lod_offset, vct_down_scaling;
+    float clear_color[4];
+    float near_plane;
+    float transmittance_cutoff;
+} or_compat_params;
+
+#define CN 32 /* noise map edge (ConeTraceShader.cpp:12, initNoiseMap(32)) */
+
+static uint64_t splitmix_next(uint64_t* st) {
+    uint64_t z = (*st += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+/* Largest c >= 0 with c^2 * S <= 16384 * g^2 (= floor(128 |g| / sqrt(S))). */
+static int snorm_component(int g, int64_t S) {
+    if (S == 0) return 0;
+    int64_t G2 = (int64_t)16384 * g * g;
+    int c = (int)floor(sqrt((double)G2 / (double)S));
+    while (c > 0 && (int64_t)c * c * S > G2) --c;
+    while ((int64_t)(c + 1) * (c + 1) * S <= G2) ++c;
+    if (c > 127) c = 127;
+    return g < 0 ? -c : c;
+}
+
+/* The 32^3 noise map of initNoiseMap (ConeTraceShader.cpp:127-159) from a
+ * seeded stream: alpha a = uniform integer in [-128, 127]; RGB = the unit
+ * "gradient" with the reference's operator precedence,
+ * g_x = d(x+1) - d(x-1) / 0.5 with d = a / 128 (neighbours wrap), i.e. the
+ * integer G = a(x+1) - 2 a(x-1), stored as trunc(128 n) with n = G / |G|
+ * (0 where G = 0, at most 127 in magnitude), evaluated exactly; decoded as
+ * GL_RGBA8_SNORM: max(c / 127, -1).  out: 32^3 x 4 floats, x fastest. */
+OR_API void or_compat_noise_map(uint32_t seed, float* out) {
+    static int8_t a[CN * CN * CN];
+    uint64_t st = (uint64_t)seed * 0x2545F4914F6CDD1DULL + 0x632BE59BD9B4E019ULL;
+    for (int i = 0; i < CN * CN * CN; ++i) a[i] = (int8_t)((int)(splitmix_next(&st) >> 56) - 128);
+#define WRAP(i) (((i) % CN + CN) % CN)
+#define AT(x, y, z) a[WRAP(x) + WRAP(y) * CN + WRAP(z) * CN * CN]
+    for (int z = 0; z < CN; ++z)
+        for (int y = 0; y < CN; ++y)
+            for (int x = 0; x < CN; ++x) {
+                int g[3] = {AT(x + 1, y, z) - 2 * AT(x - 1, y, z),
+                            AT(x, y + 1, z) - 2 * AT(x, y - 1, z),
+                            AT(x, y, z + 1) - 2 * AT(x, y, z - 1)};
+                int64_t S = (int64_t)g[0] * g[0] + (int64_t)g[1] * g[1] + (int64_t)g[2] * g[2];
+                float* o = out + 4 * (size_t)(x + y * CN + z * CN * CN);
+                for (int k = 0; k < 3; ++k) o[k] = (float)snorm_component(g[k], S) / 127.0f;
+                float av = (float)AT(x, y, z) / 127.0f;
+                o[3] = av < -1.0f ? -1.0f : av;
+            }
+#undef AT
+#undef WRAP
+}
+
+/* texture(noiseMap, q): LINEAR with REPEAT at normalised coordinates. */
+static void noise_tap(const float* tab, const real q[3], real out[4]) {
+    int i0[3], i1[3];
+    real f[3];
+    for (int a = 0; a < 3; ++a) {
+        real x = q[a] * (real)CN - (real)0.5;
+        real fl = RFLOOR(x);
+        f[a] = x - fl;
+        long long ii = (long long)fl;
+        int m = (int)(((ii % CN) + CN) % CN);
+        i0[a] = m;
+        i1[a] = (m + 1) % CN;
+    }
+    for (int ch = 0; ch < 4; ++ch) {
+        real c[2][2][2];
+        for (int dz = 0; dz < 2; ++dz)
+            for (int dy = 0; dy < 2; ++dy)
+                for (int dx = 0; dx < 2; ++dx) {
+                    int x = dx ? i1[0] : i0[0], y = dy ? i1[1] : i0[1], z = dz ? i1[2] : i0[2];
+                    c[dz][dy][dx] = (real)tab[4 * (size_t)(x + y * CN + z * CN * CN) + ch];
+                }
+        real x00 = c[0][0][0] + f[0] * (c[0][0][1] - c[0][0][0]);
+        real x10 = c[0][1][0] + f[0] * (c[0][1][1] - c[0][1][0]);
+        real x01 = c[1][0][0] + f[0] * (c[1][0][1] - c[1][0][0]);
+        real x11 = c[1][1][0] + f[0] * (c[1][1][1] - c[1][1][0]);
+        real y0 = x00 + f[1] * (x10 - x00);
+        real y1 = x01 + f[1] * (x11 - x01);
+        out[ch] = y0 + f[2] * (y1 - y0);
+    }
+}
+
+typedef struct {
+    const or_volume* v;
+    const or_camera* cam;
+    const or_compat_params* P;
+    const float* noise;
+    real f[3], s[3], u[3], e[3];
+    real tanh, aspect, sun[3];
+    const int* order; /* boards back to front */
+    int n_order;
+    const real* cw; /* per board: centre xyz, radius, z */
+    int W, H;
+    double* out;
+} compat_ctx;
+
+static real dot3(const real a[3], const real b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+static real sat(real x) { return x < 0 ? 0 : (x > 1 ? 1 : x); }
+
+/* traceCone (conetrace_frag.glsl:64-79) from level-0 voxel position vp along
+ * the unit direction dir, over the light channel with CLAMP_TO_EDGE. */
+static real compat_trace_cone(const compat_ctx* cc, const real vp[3]) {
+    const or_compat_params* P = cc->P;
+    real h = (real)P->vct_cone_initial_height, acc = 0;
+    real th = RTAN((real)P->vct_cone_angle / (real)2);
+    for (int i = 1; i <= P->vct_steps; ++i) {
+        real cr = h * th;
+        real lod = RLOG2(2 * cr > 1 ? 2 * cr : (real)1);
+        real q[3] = {vp[0] + h * cc->sun[0], vp[1] + h * cc->sun[1], vp[2] + h * cc->sun[2]};
+        real smp = sample_lod(cc->v, q, lod + (real)P->vct_lod_offset, 1, 0);
+        acc += smp * (real)i / ((real)P->vct_steps * (real)P->vct_down_scaling);
+        h += cr;
+    }
+    return acc;
+}
+
+/* The fragment shader at plane point fp (quad texture coordinate ft) of the
+ * board with centre c and radius r; returns 0 when it discards. */
+static int compat_fragment(const compat_ctx* cc, const real fp[3], const real ft[2],
+                           const real c[3], real r, real o[4]) {
+    const or_compat_params* P = cc->P;
+    real dc[3] = {fp[0] - c[0], fp[1] - c[1], fp[2] - c[2]};
+    if (P->show_quad) {
+        real sc = RSQRT(dot3(dc, dc)) / r;
+        real t = 1 - sc * sc;
+        sc = RSQRT(t > 0 ? t : (real)0);
+        o[0] = o[1] = o[2] = o[3] = sc;
+        if (ft[0] < (real)0.01f || ft[1] < (real)0.01f || ft[0] > (real)0.99f || ft[1] > (real)0.99f)
+            o[0] = o[1] = o[2] = o[3] = 1;
+        return 1;
+    }
+    const real back[3] = {-cc->f[0], -cc->f[1], -cc->f[2]};
+    if (P->do_noise) {
+        real A = dot3(back, back), B = 2 * dot3(dc, back), C = dot3(dc, dc) - r * r;
+        real disc = B * B - 4 * A * C;
+        if (disc < (real)0.01f) return 0;
+        real sq = RSQRT(disc);
+        real tn = (-B - sq) / (2 * A), tf = (-B + sq) / (2 * A);
+        real wn[3], wf[3], ut[3], ct[3], dl[3];
+        real k = (real)1 / (real)P->adjust_size;
+        for (int a = 0; a < 3; ++a) {
+            wn[a] = fp[a] + back[a] * tn;
+            wf[a] = fp[a] + back[a] * tf;
+            ut[a] = (wn[a] - c[a]) / r;
+            ct[a] = wn[a] * k;
+        }
+        real len2 = 0;
+        for (int a = 0; a < 3; ++a) {
+            real dd = wf[a] * k - ct[a];
+            len2 += dd * dd;
+        }
+        real is = RSQRT(len2) / (real)P->step_size;
+        real span = (real)(P->max_noise_steps - P->min_noise_steps);
+        is = (is < span ? is : span) + (real)P->min_noise_steps;
+        for (int a = 0; a < 3; ++a) dl[a] = (wf[a] * k - ct[a]) / (is - 1);
+        real oa = (real)P->noise_opacity / (is - 1), la = (real)1 / (is - 1);
+        real ro = 0, rl = 0;
+        for (int i = 0; (real)i < is; ++i) {
+            real nv[4] = {0, 0, 0, 0}, fr = 1, pe = 1;
+            for (int oc = 0; oc < P->num_octaves; ++oc) {
+                real off = oc < 3 ? (real)P->octave_offsets[oc] : 0;
+                real q[3] = {(ct[0] + off) * fr, (ct[1] + off) * fr, (ct[2] + off) * fr};
+                real tv[4];
+                noise_tap(cc->noise, q, tv);
+                for (int ch = 0; ch < 4; ++ch) nv[ch] += pe * tv[ch];
+                fr *= (real)P->freq_step;
+                pe *= (real)P->pers_step;
+            }
+            nv[3] = nv[3] < 0 ? -nv[3] : nv[3];
+            real un = RSQRT(dot3(ut, ut));
+            for (int a = 0; a < 3; ++a) nv[a] += ut[a] / un;
+            ro += nv[3] * (1 - dot3(ut, ut));
+            rl += sat(nv[1] * (real)0.5 + (real)0.5);
+            for (int a = 0; a < 3; ++a) {
+                ct[a] += dl[a];
+                ut[a] += dl[a];
+            }
+        }
+        real col = (real)P->min_noise_color + (real)P->noise_color_scale * rl * la;
+        real tx = ft[0] - (real)0.5, ty = ft[1] - (real)0.5;
+        real alpha = 1 - RSQRT(tx * tx + ty * ty) * 2;
+        ro = sat(ro * oa);
+        o[0] = o[1] = o[2] = col;
+        o[3] = ro * alpha;
+    }
+    if (P->do_cone_trace) {
+        real sc = RSQRT(dot3(dc, dc)) / r;
+        real t = 1 - sc * sc;
+        sc = RSQRT(t > 0 ? t : (real)0);
+        if (sc < (real)0.01f) return 0;
+        const or_volume* v = cc->v;
+        real vp[3];
+        for (int a = 0; a < 3; ++a) {
+            real pos = fp[a] + back[a] * r * sc;
+            vp[a] = (real)v->D * ((pos - (real)v->wmin[a]) / (real)v->range[a]);
+        }
+        real ind = compat_trace_cone(cc, vp);
+        if (P->do_noise) {
+            o[0] *= ind;
+            o[1] *= ind;
+            o[2] *= ind;
+        } else {
+            o[0] = o[1] = o[2] = o[3] = ind;
+        }
+    }
+    return 1;
+}
+
+static void compat_row(void* p, long row) {
+    const compat_ctx* cc = (const compat_ctx*)p;
+    const or_compat_params* P = cc->P;
+    for (int px = 0; px < cc->W; ++px) {
+        real ndx = ((real)2 * ((real)px + (real)0.5) / (real)cc->W - (real)1) * cc->tanh * cc->aspect;
+        real ndy = ((real)1 - (real)2 * ((real)row + (real)0.5) / (real)cc->H) * cc->tanh;
+        real d[3];
+        for (int a = 0; a < 3; ++a) d[a] = cc->f[a] + ndx * cc->s[a] + ndy * cc->u[a];
+        real C[4] = {(real)P->clear_color[0], (real)P->clear_color[1], (real)P->clear_color[2],
+                     (real)P->clear_color[3]};
+        if (P->show_quad || P->do_noise || P->do_cone_trace)
+            for (int k = 0; k < cc->n_order; ++k) {
+                const real* b = cc->cw + 5 * cc->order[k];
+                real z = b[4], r = b[3];
+                real fp[3], dc[3];
+                for (int a = 0; a < 3; ++a) {
+                    fp[a] = cc->e[a] + z * d[a];
+                    dc[a] = fp[a] - b[a];
+                }
+                real x = dot3(dc, cc->s) / r, y = dot3(dc, cc->u) / r;
+                if (!(x >= -1 && x <= 1 && y >= -1 && y <= 1)) continue;
+                real ft[2] = {(x + 1) / 2, (y + 1) / 2};
+                real o[4];
+                if (!compat_fragment(cc, fp, ft, b, r, o)) continue;
+                for (int ch = 0; ch < 4; ++ch) o[ch] = sat(o[ch]);
+                real al = o[3];
+                for (int ch = 0; ch < 3; ++ch) C[ch] = al * o[ch] + (1 - al) * C[ch];
+                C[3] = al * al + (1 - al) * C[3];
+            }
+        double* out = cc->out + ((size_t)row * cc->W + px) * 4;
+        for (int ch = 0; ch < 4; ++ch) out[ch] = (double)C[ch];
+    }
+}
+
+static const real* g_sort_keys;
+static int compat_cmp(const void* a, const void* b) {
+    int i = *(const int*)a, j = *(const int*)b;
+    real di = g_sort_keys[i], dj = g_sort_keys[j];
+    if (di != dj) return di > dj ? -1 : 1; /* farthest first */
+    return i > j ? -1 : (i < j ? 1 : 0);
+}
+
+/* The compat image of the volume's boards (world centres and radii as
+ * uploaded) seen by cam, sun direction sun_dir (light channel of the
+ * pyramid for the cone), noise map tab (or_compat_noise_map).  out: W*H*4
+ * doubles, row 0 = top. */
+OR_API int or_compat_render(const or_volume* v, const or_camera* cam, const or_compat_params* P,
+                            const float sun_dir[3], const float* tab, double* out, int nthreads) {
+    compat_ctx cc;
+    memset(&cc, 0, sizeof(cc));
+    cc.v = v;
+    cc.cam = cam;
+    cc.P = P;
+    cc.noise = tab;
+    camera_basis(cam, cc.f, cc.s, cc.u);
+    for (int a = 0; a < 3; ++a) cc.e[a] = (real)cam->eye[a];
+    cc.tanh = RTAN((real)(cam->fov_y_degrees * 3.14159265358979323846 / 180.0) / (real)2);
+    cc.aspect = (real)cam->width / (real)cam->height;
+    real sd[3] = {(real)sun_dir[0], (real)sun_dir[1], (real)sun_dir[2]};
+    normalize_r(sd);
+    for (int a = 0; a < 3; ++a) cc.sun[a] = sd[a];
+    cc.W = cam->width;
+    cc.H = cam->height;
+    cc.out = out;
+    int n = v->n;
+    real* cw = (real*)malloc((size_t)(n > 0 ? n : 1) * 5 * sizeof(real));
+    real* key = (real*)malloc((size_t)(n > 0 ? n : 1) * sizeof(real));
+    int* order = (int*)malloc((size_t)(n > 0 ? n : 1) * sizeof(int));
+    int m = 0;
+    for (int b = 0; b < n; ++b) {
+        real c[3] = {(real)v->cw[3 * b], (real)v->cw[3 * b + 1], (real)v->cw[3 * b + 2]};
+        real dc[3] = {c[0] - cc.e[0], c[1] - cc.e[1], c[2] - cc.e[2]};
+        real z = dot3(dc, cc.f);
+        for (int a = 0; a < 3; ++a) cw[5 * b + a] = c[a];
+        cw[5 * b + 3] = (real)v->rad[b];
+        cw[5 * b + 4] = z;
+        key[b] = RSQRT(dot3(dc, dc));
+        if (z > (real)P->near_plane && z < (real)2500 && v->rad[b] > 0) order[m++] = b;
+    }
+    g_sort_keys = key;
+    qsort(order, (size_t)m, sizeof(int), compat_cmp);
+    cc.order = order;
+    cc.n_order = m;
+    cc.cw = cw;
+    or_parallel_for(cc.H, nthreads, compat_row, &cc);
+    free(cw);
+    free(key);
+    free(order);
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
 /* MLP sun-transmittance surrogate in FP64 (build-defined; the reference    */
 /* has no learned part).  Parameter layout: W1[64][16] b1[64] W2[64][64]    */
 /* b2[64] W3[64][64] b3[64] W4[1][64] b4[1] (9473 values, W as [out][in]).   */

@@ -33,6 +33,23 @@ class or_sun_frame(ctypes.Structure):
                 ("H", ctypes.c_int)]
 
 
+class or_compat_params(ctypes.Structure):
+    """Mirror of or_compat_params (the same layout as the product's
+    cg_compat_params)."""
+    _fields_ = [("show_quad", ctypes.c_int), ("do_noise", ctypes.c_int),
+                ("do_cone_trace", ctypes.c_int), ("step_size", ctypes.c_float),
+                ("noise_opacity", ctypes.c_float), ("num_octaves", ctypes.c_int),
+                ("freq_step", ctypes.c_float), ("pers_step", ctypes.c_float),
+                ("adjust_size", ctypes.c_float), ("min_noise_steps", ctypes.c_int),
+                ("max_noise_steps", ctypes.c_int), ("min_noise_color", ctypes.c_float),
+                ("noise_color_scale", ctypes.c_float), ("octave_offsets", ctypes.c_float * 3),
+                ("noise_seed", ctypes.c_uint32), ("vct_steps", ctypes.c_int),
+                ("vct_cone_angle", ctypes.c_float), ("vct_cone_initial_height", ctypes.c_float),
+                ("vct_lod_offset", ctypes.c_float), ("vct_down_scaling", ctypes.c_float),
+                ("clear_color", ctypes.c_float * 4), ("near_plane", ctypes.c_float),
+                ("transmittance_cutoff", ctypes.c_float)]
+
+
 class or_camera(ctypes.Structure):
     _fields_ = [("eye", ctypes.c_double * 3), ("target", ctypes.c_double * 3),
                 ("up", ctypes.c_double * 3), ("fov_y_degrees", ctypes.c_double),
@@ -81,6 +98,9 @@ def load(bits=64):
         "or_render": (I, [P, ctypes.POINTER(or_camera), ctypes.POINTER(or_params), FP, I, I, I,
                           I, DP, P, I]),
         "or_real_bytes": (I, []),
+        "or_compat_noise_map": (None, [ctypes.c_uint32, FP]),
+        "or_compat_render": (I, [P, ctypes.POINTER(or_camera), ctypes.POINTER(or_compat_params),
+                                 FP, FP, DP, I]),
         "or_mlp_features": (None, [P, DP, DP, I, ctypes.c_double, DP]),
         "or_mlp_forward": (ctypes.c_double, [DP, DP, DP, DP]),
         "or_mlp_loss_grad": (ctypes.c_double, [DP, DP, DP, ctypes.c_double, ctypes.c_double, DP,
@@ -266,6 +286,32 @@ class OracleVolume:
         self.lib.or_render(self.h, ctypes.byref(c), ctypes.byref(params), _f3(sun_dir), x0, y0, w,
                            h, out.ctypes.data_as(DP), st.ctypes.data_as(ctypes.c_void_p), threads)
         return (out, st) if stats else out
+
+
+    def compat_render(self, camera, params, sun_dir, noise_map, threads=None):
+        """The compat (billboard) image of camera over the volume's boards;
+        params an or_compat_params (or a product cg_compat_params: same
+        layout), noise_map from compat_noise_map."""
+        threads = threads or os.cpu_count() or 1
+        c = or_camera()
+        c.eye[:] = [float(x) for x in camera.eye]
+        c.target[:] = [float(x) for x in camera.target]
+        c.up[:] = [float(x) for x in camera.up]
+        c.fov_y_degrees = float(camera.fov_y_degrees)
+        c.width, c.height = int(camera.width), int(camera.height)
+        p = or_compat_params.from_buffer_copy(bytes(params))
+        tab = np.ascontiguousarray(noise_map, np.float32)
+        out = np.zeros((camera.height, camera.width, 4), np.float64)
+        self.lib.or_compat_render(self.h, ctypes.byref(c), ctypes.byref(p), _f3(sun_dir),
+                                  tab.ctypes.data_as(FP), out.ctypes.data_as(DP), threads)
+        return out
+
+
+def compat_noise_map(seed, bits=64):
+    """The decoded 32^3 RGBA noise map (32, 32, 32, 4) float32, z-major."""
+    out = np.zeros((32, 32, 32, 4), np.float32)
+    load(bits).or_compat_noise_map(int(seed) & 0xFFFFFFFF, out.ctypes.data_as(FP))
+    return out
 
 
 def _dp(a):

@@ -29,6 +29,11 @@ def load():
         lib.ref_second_pass.restype = None
         lib.ref_second_pass.argtypes = [FP, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_float, ctypes.c_float, FP, ctypes.c_void_p]
+        lib.ref_compat_render.restype = ctypes.c_long
+        lib.ref_compat_render.argtypes = [FP, FP, ctypes.c_int, FP, ctypes.c_float,
+                                          ctypes.c_float, ctypes.c_int, FP, IP, LP, ctypes.c_int,
+                                          FP, FP, FP, FP, ctypes.c_float, ctypes.c_int,
+                                          ctypes.c_int, FP, ctypes.c_void_p, FP]
         lib.ref_trace_cone.restype = ctypes.c_float
         lib.ref_trace_cone.argtypes = [FP, IP, LP, ctypes.c_int, ctypes.c_int, ctypes.c_float,
                                        ctypes.c_float, FP, FP, FP, ctypes.c_int, ctypes.c_float,
@@ -87,3 +92,29 @@ def trace_cone(levels, D, vol_pos, bounds, world_pos, direction, steps, cone_ang
                            dr.ctypes.data_as(FP), int(steps), float(cone_angle), float(cone_h0),
                            float(lod_offset), float(down_scaling), out.ctypes.data_as(FP))
     return float(v), out
+
+
+def compat_render(board_pos, board_scale, vol_pos, bounds, D, light_levels, noise_map, eye,
+                  target, up, fov_deg, W, H, sun_dir, params):
+    """The reference's cone-trace pass (billboards shaded by its fragment
+    shader, sorted and blended as its host code does) -> ((H, W, 4) float32
+    image, row 0 = top; fragments shaded).  light_levels: the light channel's
+    mip chain; params: an or_compat_params (or the same layout)."""
+    lib = load()
+    bp, bs = _f(board_pos).reshape(-1), _f(board_scale).reshape(-1)
+    flat = _f(np.concatenate([np.asarray(l, np.float32).reshape(-1) for l in light_levels]))
+    dims = np.array([l.shape[0] for l in light_levels], np.int32)
+    offs = np.zeros(len(light_levels), np.int64)
+    offs[1:] = np.cumsum([l.size for l in light_levels])[:-1]
+    nm = _f(noise_map).reshape(-1)
+    out = np.empty((H, W, 4), np.float32)
+    f3 = [_f(x) for x in (vol_pos, eye, target, up, sun_dir)]
+    pbuf = ctypes.create_string_buffer(bytes(params), len(bytes(params)))
+    shaded = lib.ref_compat_render(
+        bp.ctypes.data_as(FP), bs.ctypes.data_as(FP), int(bs.shape[0]), f3[0].ctypes.data_as(FP),
+        float(bounds[0]), float(bounds[1]), int(D), flat.ctypes.data_as(FP),
+        dims.ctypes.data_as(IP), offs.ctypes.data_as(LP), len(light_levels),
+        nm.ctypes.data_as(FP), f3[1].ctypes.data_as(FP), f3[2].ctypes.data_as(FP),
+        f3[3].ctypes.data_as(FP), float(fov_deg), int(W), int(H), f3[4].ctypes.data_as(FP),
+        ctypes.cast(pbuf, ctypes.c_void_p), out.ctypes.data_as(FP))
+    return out, int(shaded)

@@ -286,22 +286,30 @@ inline vec4 imageLoad(image2D img, ivec2 p) {
 }
 
 // ---- 3D textures -------------------------------------------------------------------
-// Single-channel mip chain (level l is dims[l]^3, x fastest) read as .r.
+// Mip chain of 1 channel (level l is dims[l]^3, x fastest, read as .r with
+// g = b = 0, a = 1) or of 4 interleaved channels (RGBA), CLAMP_TO_EDGE or
+// REPEAT wrapping (8.14.2).
 struct sampler3D {
     const float* data = nullptr;
     const int* dims = nullptr;
     const long* offs = nullptr;
     int levels = 0;
+    int channels = 1;
+    bool repeat = false;
 };
-inline float texel(const sampler3D& s, int l, int i, int j, int k) {
+inline int wrap_index(const sampler3D& s, int i, int n) {
+    if (s.repeat) return ((i % n) + n) % n;
+    return i < 0 ? 0 : (i >= n ? n - 1 : i);
+}
+inline float texel(const sampler3D& s, int l, int i, int j, int k, int ch) {
     const int n = s.dims[l];
-    i = i < 0 ? 0 : (i >= n ? n - 1 : i);  // CLAMP_TO_EDGE
-    j = j < 0 ? 0 : (j >= n ? n - 1 : j);
-    k = k < 0 ? 0 : (k >= n ? n - 1 : k);
-    return s.data[s.offs[l] + ((long)k * n + j) * n + i];
+    i = wrap_index(s, i, n);
+    j = wrap_index(s, j, n);
+    k = wrap_index(s, k, n);
+    return s.data[(s.offs[l] + ((long)k * n + j) * n + i) * s.channels + ch];
 }
 // LINEAR filter of one level at normalised coordinates (8.14.2, eq. 8.9-8.11)
-inline float linear_level(const sampler3D& s, int l, const vec3& P) {
+inline float linear_level(const sampler3D& s, int l, const vec3& P, int ch) {
     const float n = (float)s.dims[l];
     const float u = P.x * n, v = P.y * n, w = P.z * n;
     const float uf = u - 0.5f, vf = v - 0.5f, wf = w - 0.5f;
@@ -310,7 +318,8 @@ inline float linear_level(const sampler3D& s, int l, const vec3& P) {
     float t[2][2][2];
     for (int dk = 0; dk < 2; ++dk)
         for (int dj = 0; dj < 2; ++dj)
-            for (int di = 0; di < 2; ++di) t[dk][dj][di] = texel(s, l, i0 + di, j0 + dj, k0 + dk);
+            for (int di = 0; di < 2; ++di)
+                t[dk][dj][di] = texel(s, l, i0 + di, j0 + dj, k0 + dk, ch);
     float r = 0.f;
     for (int dk = 0; dk < 2; ++dk)
         for (int dj = 0; dj < 2; ++dj)
@@ -324,25 +333,28 @@ inline float linear_level(const sampler3D& s, int l, const vec3& P) {
 // (8.14.1-8.14.3): lambda <= 0 magnifies from the base level; otherwise
 // levels d1 = floor(lambda) and d1 + 1 (clamped to the last level q) blend by
 // frac(lambda), and lambda >= q reads level q alone.
-inline vec4 textureLod(const sampler3D& s, const vec3& P, float lod) {
+inline float lod_channel(const sampler3D& s, const vec3& P, float lod, int ch) {
     const int q = s.levels - 1;
-    float r;
-    if (!(lod > 0.f)) {
-        r = linear_level(s, 0, P);
-    } else if (lod >= (float)q) {
-        r = linear_level(s, q, P);
-    } else {
-        const int d1 = (int)std::floor(lod);
-        const float f = lod - std::floor(lod);
-        const float t1 = linear_level(s, d1, P), t2 = linear_level(s, d1 + 1, P);
-        r = (1.f - f) * t1 + f * t2;
-    }
-    return vec4(r, 0.f, 0.f, 1.f);
+    if (!(lod > 0.f)) return linear_level(s, 0, P, ch);
+    if (lod >= (float)q) return linear_level(s, q, P, ch);
+    const int d1 = (int)std::floor(lod);
+    const float f = lod - std::floor(lod);
+    const float t1 = linear_level(s, d1, P, ch), t2 = linear_level(s, d1 + 1, P, ch);
+    return (1.f - f) * t1 + f * t2;
+}
+inline vec4 textureLod(const sampler3D& s, const vec3& P, float lod) {
+    if (s.channels == 1) return vec4(lod_channel(s, P, lod, 0), 0.f, 0.f, 1.f);
+    return vec4(lod_channel(s, P, lod, 0), lod_channel(s, P, lod, 1), lod_channel(s, P, lod, 2),
+                lod_channel(s, P, lod, 3));
 }
 inline vec4 texture(const sampler3D& s, const vec3& P) {
     if (!s.data) return vec4(0.f);
     return textureLod(s, P, 0.f);
 }
+
+// Set by `discard` (see the macro below); the driver clears it before each
+// fragment.
+inline bool g_discarded = false;
 
 }  // namespace glsl
 
@@ -353,6 +365,6 @@ inline vec4 texture(const sampler3D& s, const vec3& P) {
 #define flat
 #define uniform
 #define layout(...)
-#define discard return
+#define discard { ::glsl::g_discarded = true; return; }
 // GLSL's matrix-narrowing constructor mat3(m4)
 #define mat3(m) glsl::make_mat3(m)

@@ -1,0 +1,151 @@
+"""GPU compat render (cg_render_compat) against the oracle and the
+reference-shader fixtures.
+
+Tolerance: the GPU blends front to back in FP32, the oracle back to front in
+FP64; pixel values agree within 1e-3 except for rare fragments whose discard
+test, quad-edge test or noise step count sits on a threshold and resolves
+differently in the two precisions: at most 0.2 % of the values may differ by
+more.
+"""
+import numpy as np
+import pytest
+
+import cloudgb
+from cloudgb import configs, workload
+from oracle import oracle as O
+
+import os
+import sys
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+import make_compat_golden as G  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_compat.npz")
+
+
+def gpu_volume(ctx, wl, n=None, fmt=cloudgb.FORMAT_RGBA32F):
+    cfg = configs.COMPAT_REF
+    vol = cloudgb.CloudVolume(cfg["dim"], cfg["bounds"], cfg["position"], cfg["mips"], fmt=fmt,
+                              ctx=ctx)
+    k = len(wl.scales) if n is None else n
+    vol.set_billboards(wl.positions[:k], wl.scales[:k], np.ones(k, np.float32))
+    vol.update()
+    cloudgb.VoxelizeShader().voxelize(vol, cloudgb.Sun(wl.sun_direction, *cfg["sun_map"]))
+    return vol
+
+
+def shader_of(P):
+    """A CompatShader carrying an or_compat_params block."""
+    sh = cloudgb.CompatShader()
+    for name, field in cloudgb.CompatShader._FIELDS.items():
+        setattr(sh, name, getattr(P, field))
+    sh.clearColor = tuple(P.clear_color)
+    sh.windVel = tuple(P.octave_offsets)
+    sh.runTime = 1.0
+    return sh
+
+
+def assert_close(img, ref, tol=1e-3, frac=2e-3, what=""):
+    err = np.abs(np.asarray(img, np.float64) - np.asarray(ref, np.float64))
+    bad = float((err > tol).mean())
+    assert bad <= frac, f"{what}: {bad:.4%} of values beyond {tol} (max {err.max():.3g})"
+
+
+@pytest.mark.parametrize("name", list(G.CASES))
+def test_gpu_matches_oracle_and_reference_fixture(ctx, name):
+    gold = np.load(GOLD)
+    cam_spec, n, _ = G.CASES[name]
+    wl, c, ov = G.case_inputs(cam_spec, n)
+    vol = gpu_volume(ctx, wl)
+    P = O.or_compat_params.from_buffer_copy(gold[f"{name}_params"].tobytes())
+    cam = cloudgb.Camera(c["eye"], c["target"], fov_y_degrees=c["fov"], width=G.W, height=G.H)
+    img = shader_of(P).coneTrace(vol, cam)
+    ref = ov.compat_render(cam, P, wl.sun_direction, O.compat_noise_map(P.noise_seed))
+    assert_close(img, ref, what=f"{name} vs oracle")
+    assert_close(img, gold[f"{name}_image"], what=f"{name} vs reference shaders")
+    vol.close()
+
+
+def test_full_size_view_and_cutoff(ctx):
+    """A 1080p view of the reference-scale scene: the default early-out
+    (1e-4) changes pixels by at most about the cutoff; sampled rows match the
+    oracle; the render is deterministic."""
+    cfg = configs.COMPAT_REF
+    wl = workload.build_compat(cfg)
+    vol = gpu_volume(ctx, wl)
+    cam = workload.make_camera(wl.cameras[4])
+    sh = cloudgb.CompatShader()
+    a = sh.coneTrace(vol, cam)
+    assert np.array_equal(a, sh.coneTrace(vol, cam))
+    sh0 = cloudgb.CompatShader(transmittanceCutoff=0.0)
+    b = sh0.coneTrace(vol, cam)
+    assert np.abs(a - b).max() <= 2e-4
+    # oracle on a band of rows through the cloud
+    ov = O.OracleVolume(cfg["dim"], cfg["bounds"], cfg["position"], cfg["mips"])
+    ov.set_boards(wl.positions, wl.scales, np.ones(len(wl.scales), np.float32))
+    ov.voxelize(wl.sun_direction, *cfg["sun_map"])
+    small = cloudgb.Camera(cam.eye, cam.target, fov_y_degrees=60.0, width=480, height=270)
+    ref = ov.compat_render(small, sh0.params(), wl.sun_direction, O.compat_noise_map(1))
+    img = sh0.coneTrace(vol, small)
+    assert_close(img, ref, what="480x270 vs oracle")
+    assert np.abs(ref - np.array([0.2, 0.3, 0.5, 1.0])).max() > 0.1  # the cloud is in view
+    vol.close()
+
+
+def test_long_tile_lists_sort_in_global_memory(ctx):
+    """More than 4096 boards over one tile: the tile's list is sorted in
+    global memory; the image still matches the oracle."""
+    cfg = dict(configs.COMPAT_REF, boards=5000)
+    wl = workload.build_compat(cfg, width=32, height=24)
+    vol = gpu_volume(ctx, wl)
+    ov = O.OracleVolume(cfg["dim"], cfg["bounds"], cfg["position"], cfg["mips"])
+    ov.set_boards(wl.positions, wl.scales, np.ones(len(wl.scales), np.float32))
+    ov.voxelize(wl.sun_direction, *cfg["sun_map"])
+    far = dict(wl.cameras[0])
+    far["eye"] = tuple(np.array(far["target"]) + 3.0 * (np.array(far["eye"]) - far["target"]))
+    cam = workload.make_camera(far)
+    for kw in (dict(showQuad=True), dict(doNoiseSample=False)):
+        sh = cloudgb.CompatShader(transmittanceCutoff=0.0, **kw)
+        img = sh.coneTrace(vol, cam)
+        ref = ov.compat_render(cam, sh.params(), wl.sun_direction, O.compat_noise_map(1))
+        assert_close(img, ref, what=str(kw))
+    vol.close()
+
+
+def test_formats_and_edge_cases(ctx):
+    cfg = configs.COMPAT_REF
+    wl = workload.build_compat(cfg, width=128, height=72)
+    cam = workload.make_camera(wl.cameras[0])
+    v32 = gpu_volume(ctx, wl)
+    v16 = gpu_volume(ctx, wl, fmt=cloudgb.FORMAT_BF16_FP16)
+    sh = cloudgb.CompatShader()
+    a, b = sh.coneTrace(v32, cam), sh.coneTrace(v16, cam)
+    assert np.abs(a - b).max() < 2e-2  # FP16 light channel in the cone
+    clear = np.array(sh.clearColor, np.float32)
+    # every stage off: the clear colour
+    off = cloudgb.CompatShader(doNoiseSample=False, doConeTrace=False)
+    assert np.array_equal(off.coneTrace(v32, cam), np.broadcast_to(clear, (72, 128, 4)))
+    # no boards
+    empty = cloudgb.CloudVolume(cfg["dim"], cfg["bounds"], cfg["position"], cfg["mips"], ctx=ctx)
+    empty.set_billboards(np.zeros((0, 3), np.float32), np.zeros(0, np.float32))
+    empty.update()
+    cloudgb.VoxelizeShader().voxelize(empty, cloudgb.Sun(wl.sun_direction, 64, 64))
+    assert np.array_equal(sh.coneTrace(empty, cam), np.broadcast_to(clear, (72, 128, 4)))
+    # looking away: every board clipped
+    away = cloudgb.Camera(cam.eye, tuple(2 * np.array(cam.eye) - np.array(cam.target)),
+                          width=128, height=72)
+    assert np.array_equal(sh.coneTrace(v32, away), np.broadcast_to(clear, (72, 128, 4)))
+    # the cone needs a voxelized volume; bad parameters are rejected
+    fresh = cloudgb.CloudVolume(cfg["dim"], cfg["bounds"], cfg["position"], cfg["mips"], ctx=ctx)
+    fresh.set_billboards(wl.positions, wl.scales)
+    fresh.update()
+    with pytest.raises(cloudgb.CloudError):
+        sh.coneTrace(fresh, cam)
+    cloudgb.CompatShader(doConeTrace=False).coneTrace(fresh, cam)  # noise alone needs no voxelize
+    for bad in (dict(minNoiseSteps=1), dict(maxNoiseSteps=1), dict(vctSteps=65),
+                dict(stepSize=0.0), dict(transmittanceCutoff=1.0)):
+        with pytest.raises(cloudgb.CloudError):
+            cloudgb.CompatShader(**bad).coneTrace(v32, cam)
+    for v in (v32, v16, empty, fresh):
+        v.close()
