@@ -338,7 +338,7 @@ cudaError_t launch_trace_batch(int fmt, int lanes_per_ray, int unroll, const Bat
 
 // ---- compat render (k_compat.cu) ------------------------------------------
 // The reference's billboard image formation; see cg_render_compat.
-constexpr int CG_COMPAT_TILE = 16;  // pixel tile edge
+constexpr int CG_COMPAT_TILE = 8;  // pixel tile edge
 struct CompatDev {
     CamDesc cam;
     int n;                 // boards

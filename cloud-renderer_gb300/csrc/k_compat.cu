@@ -6,16 +6,18 @@
 // fragment with conetrace_frag.glsl:122-201 and blends back to front
 // (SRC_ALPHA, ONE_MINUS_SRC_ALPHA, main.cpp:94-95) after sorting the boards by
 // distance on the CPU (CloudVolume.cpp:65-82).  Here:
-//   count  one thread per board: the quad's conservative pixel rectangle, its
-//          16x16 tiles (atomic per-tile counts) and the squared eye distance;
+//   count  one warp per board: the quad's conservative pixel rectangle, its
+//          8x8 tiles (atomic per-tile counts) and the squared eye distance;
 //   scan   the per-tile counts (k_bin_scan);
-//   fill   one thread per board: (distance bits << 32 | board) into each
+//   fill   one warp per board: (distance bits << 32 | board) into each
 //          tile's list;
-//   tiles  one 256-thread CTA per tile: sorts its list (bitonic, in shared
-//          memory up to 4096 entries, in place in global memory beyond) and
-//          blends its pixels front to back, C += T a src, T *= 1 - a, which
-//          equals the back-to-front blend; a pixel stops once T falls below
-//          the cutoff, the CTA once all its pixels have.
+//   tiles  one 256-thread CTA per 8x8 tile: sorts its list (bitonic, in
+//          shared memory up to 4096 entries, in place in global memory
+//          beyond); four threads per pixel blend a quarter of the list each
+//          front to back, C += T a src, T *= 1 - a, and the quarters combine
+//          in order (the over operator is associative), which equals the
+//          back-to-front blend; a thread stops once its T falls below the
+//          cutoff, the CTA once all its threads have.
 // The quad is perpendicular to the view axis f, so the fragment of pixel ray
 // d (d.f = 1) is the plane point e + z d with z = (c - e).f; the quad covers
 // the pixel when both plane coordinates (x, y) = ((p - c).s, (p - c).u) / r
@@ -30,55 +32,68 @@ namespace {
 constexpr int CAP = 4096;      // sort keys held in shared memory per tile
 constexpr int NOISE_N = 32;    // noise map edge (ConeTraceShader.cpp:12)
 
+// One warp per board: lane 0 derives the board's tile rectangle, the lanes
+// split its tiles for the per-tile count.
 __global__ void k_compat_count(CompatDev P, int4* rect, float* key, uint32_t* tile_count) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
     if (b >= P.n) return;
-    const CamDesc& cam = P.cam;
-    const float4 c = P.cwr[b];
-    const float dx = c.x - cam.eye[0], dy = c.y - cam.eye[1], dz = c.z - cam.eye[2];
-    const float z = dx * cam.f[0] + dy * cam.f[1] + dz * cam.f[2];
-    key[b] = dx * dx + dy * dy + dz * dz;
     int4 R = make_int4(1, 1, 0, 0);
-    if (z > P.near_z && z < 2500.f && c.w > 0.f) {
-        // plane coordinates of the centre and the half extent at unit depth
-        const float xs = (dx * cam.s[0] + dy * cam.s[1] + dz * cam.s[2]) / z;
-        const float ys = (dx * cam.u[0] + dy * cam.u[1] + dz * cam.u[2]) / z;
-        const float h = c.w / z;
-        const float ta = cam.tanh * cam.aspect;
-        // pixel i lies at ndc (2 (i + 0.5) / W - 1) * ta; row j at (1 - 2 (j + 0.5) / H) tanh;
-        // one pixel of margin either side, the exact test is per pixel
-        float lo_x = ((xs - h) / ta + 1.f) * 0.5f * (float)cam.W - 0.5f;
-        float hi_x = ((xs + h) / ta + 1.f) * 0.5f * (float)cam.W - 0.5f;
-        float lo_y = (1.f - (ys + h) / cam.tanh) * 0.5f * (float)cam.H - 0.5f;
-        float hi_y = (1.f - (ys - h) / cam.tanh) * 0.5f * (float)cam.H - 0.5f;
-        lo_x = fmaxf(lo_x, -2.f);
-        lo_y = fmaxf(lo_y, -2.f);
-        hi_x = fminf(hi_x, (float)cam.W + 1.f);
-        hi_y = fminf(hi_y, (float)cam.H + 1.f);
-        const int i0 = max(0, (int)floorf(lo_x) - 1), i1 = min(cam.W - 1, (int)ceilf(hi_x) + 1);
-        const int j0 = max(0, (int)floorf(lo_y) - 1), j1 = min(cam.H - 1, (int)ceilf(hi_y) + 1);
-        if (i0 <= i1 && j0 <= j1) {
-            R = make_int4(i0 / CG_COMPAT_TILE, j0 / CG_COMPAT_TILE, i1 / CG_COMPAT_TILE,
-                          j1 / CG_COMPAT_TILE);
-            for (int ty = R.y; ty <= R.w; ++ty)
-                for (int tx = R.x; tx <= R.z; ++tx) atomicAdd(tile_count + ty * P.tiles_x + tx, 1u);
+    if (lane == 0) {
+        const CamDesc& cam = P.cam;
+        const float4 c = P.cwr[b];
+        const float dx = c.x - cam.eye[0], dy = c.y - cam.eye[1], dz = c.z - cam.eye[2];
+        const float z = dx * cam.f[0] + dy * cam.f[1] + dz * cam.f[2];
+        key[b] = dx * dx + dy * dy + dz * dz;
+        if (z > P.near_z && z < 2500.f && c.w > 0.f) {
+            // plane coordinates of the centre and the half extent at unit depth
+            const float xs = (dx * cam.s[0] + dy * cam.s[1] + dz * cam.s[2]) / z;
+            const float ys = (dx * cam.u[0] + dy * cam.u[1] + dz * cam.u[2]) / z;
+            const float h = c.w / z;
+            const float ta = cam.tanh * cam.aspect;
+            // pixel i lies at ndc (2 (i + 0.5) / W - 1) ta; row j at (1 - 2 (j + 0.5) / H) tanh;
+            // one pixel of margin either side, the exact test is per pixel
+            float lo_x = ((xs - h) / ta + 1.f) * 0.5f * (float)cam.W - 0.5f;
+            float hi_x = ((xs + h) / ta + 1.f) * 0.5f * (float)cam.W - 0.5f;
+            float lo_y = (1.f - (ys + h) / cam.tanh) * 0.5f * (float)cam.H - 0.5f;
+            float hi_y = (1.f - (ys - h) / cam.tanh) * 0.5f * (float)cam.H - 0.5f;
+            lo_x = fmaxf(lo_x, -2.f);
+            lo_y = fmaxf(lo_y, -2.f);
+            hi_x = fminf(hi_x, (float)cam.W + 1.f);
+            hi_y = fminf(hi_y, (float)cam.H + 1.f);
+            const int i0 = max(0, (int)floorf(lo_x) - 1), i1 = min(cam.W - 1, (int)ceilf(hi_x) + 1);
+            const int j0 = max(0, (int)floorf(lo_y) - 1), j1 = min(cam.H - 1, (int)ceilf(hi_y) + 1);
+            if (i0 <= i1 && j0 <= j1)
+                R = make_int4(i0 / CG_COMPAT_TILE, j0 / CG_COMPAT_TILE, i1 / CG_COMPAT_TILE,
+                              j1 / CG_COMPAT_TILE);
         }
+        rect[b] = R;
     }
-    rect[b] = R;
+    R.x = __shfl_sync(0xffffffffu, R.x, 0);
+    R.y = __shfl_sync(0xffffffffu, R.y, 0);
+    R.z = __shfl_sync(0xffffffffu, R.z, 0);
+    R.w = __shfl_sync(0xffffffffu, R.w, 0);
+    const int nx = R.z - R.x + 1, ny = R.w - R.y + 1;
+    if (nx <= 0 || ny <= 0) return;
+    for (int t = lane; t < nx * ny; t += 32)
+        atomicAdd(tile_count + (R.y + t / nx) * P.tiles_x + R.x + t % nx, 1u);
 }
 
+// One warp per board: the lanes split its tiles.
 __global__ void k_compat_fill(CompatDev P, const int4* rect, const float* key, uint32_t* cursor,
                               unsigned long long* list) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
     if (b >= P.n) return;
     const int4 R = rect[b];
+    const int nx = R.z - R.x + 1, ny = R.w - R.y + 1;
+    if (nx <= 0 || ny <= 0) return;
     const unsigned long long k =
         ((unsigned long long)__float_as_uint(key[b]) << 32) | (unsigned long long)(unsigned)b;
-    for (int ty = R.y; ty <= R.w; ++ty)
-        for (int tx = R.x; tx <= R.z; ++tx) {
-            const uint32_t slot = atomicAdd(cursor + ty * P.tiles_x + tx, 1u);
-            list[slot] = k;
-        }
+    for (int t = lane; t < nx * ny; t += 32) {
+        const uint32_t slot = atomicAdd(cursor + (R.y + t / nx) * P.tiles_x + R.x + t % nx, 1u);
+        list[slot] = k;
+    }
 }
 
 // Ascending sort of a[0, m) by a sorting network over the next power of two
@@ -239,11 +254,22 @@ __device__ bool compat_fragment(const VolDesc& vd, const ConeSchedule& cs, const
     return true;
 }
 
+// One 256-thread CTA per 8x8-pixel tile: the tile's list is sorted once,
+// then split into SEG contiguous segments; thread (segment g, pixel p) blends
+// its segment front to back into (C_g, T_g) and the segments are combined in
+// order with the associative over operator, C = C_0 + T_0 (C_1 + T_1 (...)),
+// T = T_0 T_1 ...  A segment stops early on its own transmittance (the
+// combined image moves by at most the cutoff).
+constexpr int SEG = 4;
+constexpr int TILE_PX = CG_COMPAT_TILE * CG_COMPAT_TILE;  // 64
+
 template <int FMT>
 __global__ void __launch_bounds__(256) k_compat_tiles(VolDesc vd, ConeSchedule cs, CompatDev P,
                                                       const uint32_t* offset,
                                                       unsigned long long* list, float4* out) {
     __shared__ unsigned long long s_keys[CAP];
+    __shared__ float4 s_c[SEG][TILE_PX];
+    __shared__ float s_t[SEG][TILE_PX];
     const int tile = blockIdx.x;
     const int tx = tile % P.tiles_x, ty = tile / P.tiles_x;
     const uint32_t beg = offset[tile];
@@ -258,8 +284,9 @@ __global__ void __launch_bounds__(256) k_compat_tiles(VolDesc vd, ConeSchedule c
     }
     const unsigned long long* keys = in_smem ? s_keys : list + beg;
     const CamDesc& cam = P.cam;
-    const int pxi = tx * CG_COMPAT_TILE + (threadIdx.x & (CG_COMPAT_TILE - 1));
-    const int pyi = ty * CG_COMPAT_TILE + (threadIdx.x / CG_COMPAT_TILE);
+    const int pix = threadIdx.x & (TILE_PX - 1), seg = threadIdx.x / TILE_PX;
+    const int pxi = tx * CG_COMPAT_TILE + (pix & (CG_COMPAT_TILE - 1));
+    const int pyi = ty * CG_COMPAT_TILE + (pix / CG_COMPAT_TILE);
     const bool active = pxi < cam.W && pyi < cam.H;
     const float ndx = (2.f * ((float)pxi + 0.5f) / (float)cam.W - 1.f) * cam.tanh * cam.aspect;
     const float ndy = (1.f - 2.f * ((float)pyi + 0.5f) / (float)cam.H) * cam.tanh;
@@ -269,9 +296,12 @@ __global__ void __launch_bounds__(256) k_compat_tiles(VolDesc vd, ConeSchedule c
     float4 C = make_float4(0.f, 0.f, 0.f, 0.f);
     float T = 1.f;
     const bool drawing = P.show_quad || P.do_noise || P.do_cone;
-    for (int k = 0; k < m && drawing; ++k) {
-        if ((k & 15) == 0 && !__syncthreads_or(active && T >= P.cutoff)) break;
-        if (!active || T < P.cutoff) continue;
+    const int k0 = (int)((long long)m * seg / SEG), k1 = (int)((long long)m * (seg + 1) / SEG);
+    const int span = (m + SEG - 1) / SEG;  // the longest segment: uniform trip count
+    for (int i = 0; i < span && drawing; ++i) {
+        if ((i & 15) == 0 && !__syncthreads_or(active && T >= P.cutoff && k0 + i < k1)) break;
+        const int k = k0 + i;
+        if (!active || T < P.cutoff || k >= k1) continue;
         const int b = (int)(unsigned)(keys[k] & 0xFFFFFFFFull);
         const float4 c = __ldg(P.cwr + b);
         const float ox = c.x - cam.eye[0], oy = c.y - cam.eye[1], oz = c.z - cam.eye[2];
@@ -292,10 +322,23 @@ __global__ void __launch_bounds__(256) k_compat_tiles(VolDesc vd, ConeSchedule c
         C.w += ta * a;
         T *= 1.f - a;
     }
-    if (active)
+    s_c[seg][pix] = C;
+    s_t[seg][pix] = T;
+    __syncthreads();
+    if (seg == 0 && active) {
+        float4 A = s_c[SEG - 1][pix];
+        float TA = s_t[SEG - 1][pix];
+#pragma unroll
+        for (int g = SEG - 2; g >= 0; --g) {  // segment g in front of the combined rest
+            const float4 F = s_c[g][pix];
+            const float TF = s_t[g][pix];
+            A = make_float4(F.x + TF * A.x, F.y + TF * A.y, F.z + TF * A.z, F.w + TF * A.w);
+            TA *= TF;
+        }
         out[(size_t)pyi * cam.W + pxi] =
-            make_float4(C.x + T * P.clear[0], C.y + T * P.clear[1], C.z + T * P.clear[2],
-                        C.w + T * P.clear[3]);
+            make_float4(A.x + TA * P.clear[0], A.y + TA * P.clear[1], A.z + TA * P.clear[2],
+                        A.w + TA * P.clear[3]);
+    }
 }
 
 }  // namespace
@@ -303,14 +346,14 @@ __global__ void __launch_bounds__(256) k_compat_tiles(VolDesc vd, ConeSchedule c
 cudaError_t launch_compat_count(const CompatDev& P, int4* rect, float* key, uint32_t* tile_count,
                                 cudaStream_t st) {
     if (P.n == 0) return cudaSuccess;
-    k_compat_count<<<(P.n + 127) / 128, 128, 0, st>>>(P, rect, key, tile_count);
+    k_compat_count<<<(P.n + 3) / 4, 128, 0, st>>>(P, rect, key, tile_count);
     return cudaGetLastError();
 }
 
 cudaError_t launch_compat_fill(const CompatDev& P, const int4* rect, const float* key,
                                uint32_t* cursor, unsigned long long* list, cudaStream_t st) {
     if (P.n == 0) return cudaSuccess;
-    k_compat_fill<<<(P.n + 127) / 128, 128, 0, st>>>(P, rect, key, cursor, list);
+    k_compat_fill<<<(P.n + 3) / 4, 128, 0, st>>>(P, rect, key, cursor, list);
     return cudaGetLastError();
 }
 

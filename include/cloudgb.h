@@ -426,7 +426,7 @@ void cg_frame_graph_destroy(cg_frame_graph* graph);
  * sphere, traceCone from the sphere surface toward the sun over the light
  * channel), blended SRC_ALPHA / ONE_MINUS_SRC_ALPHA over the clear colour in
  * distance order (main.cpp:94-95, sortBoards CloudVolume.cpp:65-82), without
- * a global sort: boards are binned to 16x16-pixel tiles and each tile orders
+ * a global sort: boards are binned to 8x8-pixel tiles and each tile orders
  * its own list.  Field names follow ConeTraceShader.hpp:15-32. */
 typedef struct cg_compat_params {
     int show_quad;              /* showQuad: debug quad (sphere profile, white border) */
