@@ -17,7 +17,7 @@
 //          front to back, C += T a src, T *= 1 - a, and the quarters combine
 //          in order (the over operator is associative), which equals the
 //          back-to-front blend; a thread stops once its T falls below the
-//          cutoff, the CTA once all its threads have.
+//          cutoff, a warp once all its threads have.
 // The quad is perpendicular to the view axis f, so the fragment of pixel ray
 // d (d.f = 1) is the plane point e + z d with z = (c - e).f; the quad covers
 // the pixel when both plane coordinates (x, y) = ((p - c).s, (p - c).u) / r
@@ -299,7 +299,8 @@ __global__ void __launch_bounds__(256) k_compat_tiles(VolDesc vd, ConeSchedule c
     const int k0 = (int)((long long)m * seg / SEG), k1 = (int)((long long)m * (seg + 1) / SEG);
     const int span = (m + SEG - 1) / SEG;  // the longest segment: uniform trip count
     for (int i = 0; i < span && drawing; ++i) {
-        if ((i & 15) == 0 && !__syncthreads_or(active && T >= P.cutoff && k0 + i < k1)) break;
+        if ((i & 7) == 0 && !__any_sync(0xffffffffu, active && T >= P.cutoff && k0 + i < k1))
+            break;  // the whole warp is done (warp-uniform trip count)
         const int k = k0 + i;
         if (!active || T < P.cutoff || k >= k1) continue;
         const int b = (int)(unsigned)(keys[k] & 0xFFFFFFFFull);
