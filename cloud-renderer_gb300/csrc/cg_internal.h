@@ -262,7 +262,7 @@ cudaError_t launch_fbm_volume(TraceParams tp, const float org[3], const float ex
                               cudaSurfaceObject_t surf, cudaStream_t st);
 // Surrogate shading on the tensor cores (k_shade_tc.cu).  status (4 words,
 // zeroed before the launch): [0] += exact-cone fallbacks, [1] |= 1 when a
-// bounded wait ran out, [2] += samples shaded, [3] region cursor.
+// bounded wait ran out, [2] += samples shaded, [3] tile claim counter.
 cudaError_t launch_shade_mlp_tc(VolDesc vd, CamDesc cam, TraceParams tp, const MlpDev& m,
                                 SampleBuf sb, unsigned long long* status, cudaStream_t st);
 cudaError_t launch_accumulate(CamDesc cam, TraceParams tp, SampleBuf sb, float4* out,

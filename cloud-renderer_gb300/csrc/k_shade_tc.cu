@@ -17,7 +17,10 @@
 //      the next tile's inputs go into the tile.
 // The next tile is fetched in stages while this one runs, so that no load is
 // consumed in the phase that issued it: its slot (layer 1), its sample
-// (layer 2), its 12 texture taps (layer 3), its inputs (output).
+// (layer 2), its 12 texture taps (layer 3), its inputs (output).  Tiles are
+// claimed dynamically (an atomic counter, two tiles ahead of the one being
+// shaded): CTAs on slower SMs (the far die's L2, texture misses) take fewer
+// tiles instead of setting the kernel's tail.
 // Layers 1-3 run on weights and biases pre-scaled by 1/2 (exact in FP16 and
 // FP32), so the accumulator holds z/2 and SiLU is z/2 * (1 + tanh(z/2)).
 // Every mbarrier wait is bounded: on a timeout the CTA records an error,
@@ -179,6 +182,7 @@ __global__ void __launch_bounds__(128, 4)
     uint8_t* act = base + OFF_ACT;
     uint64_t* bar = reinterpret_cast<uint64_t*>(base + OFF_BAR);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(base + OFF_BAR + 8);
+    unsigned* s_claim = reinterpret_cast<unsigned*>(base + OFF_BAR + 12);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     // ---- stage weights: W1..W3 scaled by 1/2
@@ -247,8 +251,9 @@ __global__ void __launch_bounds__(128, 4)
         pack_row<FMT>(vd, cone, m, tp, slot, sp, g, f, row, act);
     }
 
-    for (; tile < ntiles; tile += gridDim.x) {
-        const unsigned ntile = tile + gridDim.x;
+    // the first two tiles are static, later ones are claimed from status[3]
+    unsigned ntile = tile + gridDim.x;
+    for (; tile < ntiles;) {
         unsigned nslot = CG_NO_SLOT;
         float4 ns = make_float4(0.f, 0.f, 0.f, 0.f);
         float ng = 0.f;
@@ -257,9 +262,14 @@ __global__ void __launch_bounds__(128, 4)
 #pragma unroll
         for (int layer = 0; layer < 3; ++layer) {
             sync_for_mma();
-            if (tid == 0)
+            if (tid == 0) {
                 issue_layer(layer, tmem, a_addr, w_addr[layer], ones_addr,
                             bias_addr + 2048u * layer, bar);
+                // claim the tile after next (read by all after the next sync)
+                if (layer == 0)
+                    *s_claim = 2u * gridDim.x +
+                               (unsigned)atomicAdd(status + 3, 1ull);
+            }
             // ---- the next tile, in stages
             if (layer == 0) nslot = slot_at(sb, ntile, ntiles, total);
             if (layer == 1 && nslot != CG_NO_SLOT) {
@@ -316,6 +326,8 @@ __global__ void __launch_bounds__(128, 4)
         }
         // ---- the next tile's inputs
         pack_row<FMT>(vd, cone, m, tp, nslot, ns, ng, nf, row, act);
+        tile = ntile;
+        ntile = *s_claim;  // written at layer 0, two barriers ago
     }
     if (failed) {
         // drain the outstanding commit (bounded), then report
