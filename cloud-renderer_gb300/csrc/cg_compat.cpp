@@ -215,21 +215,28 @@ extern "C" cg_status cg_render_compat(cg_context* ctx, const cg_volume* v, const
     const size_t nb = (size_t)(v->n > 0 ? v->n : 1);
     CG_CUDA(ctx->compat_rect.ensure(nb * 16));
     CG_CUDA(ctx->compat_key.ensure(nb * 4));
-    CG_CUDA(ctx->compat_tiles.ensure((cnt_words + off_words + cnt_words) * 4));
+    // counts | offsets | cursors (u32, 16-byte aligned regions) | 64-bit pair total
+    CG_CUDA(ctx->compat_tiles.ensure((cnt_words + off_words + cnt_words) * 4 + 16));
     CG_CUDA(ctx->compat_total.ensure(16));
     Bins bins{};
     bins.nbricks = ntiles;
     bins.count = ctx->compat_tiles.as<uint32_t>();
     bins.offset = bins.count + cnt_words;
     bins.cursor = bins.offset + off_words;
+    unsigned long long* pairs64 = reinterpret_cast<unsigned long long*>(bins.cursor + cnt_words);
     stage_begin(ctx, s);
     CG_CUDA(cudaMemsetAsync(bins.count, 0, cnt_words * 4, s));
+    CG_CUDA(cudaMemsetAsync(pairs64, 0, 8, s));
     CG_LAUNCH(ctx, launch_compat_count(P, ctx->compat_rect.as<int4>(), ctx->compat_key.as<float>(),
-                                       bins.count, s));
+                                       bins.count, pairs64, s));
     CG_LAUNCH(ctx, launch_bin_scan(bins, s));
-    uint32_t* total = reinterpret_cast<uint32_t*>(ctx->compat_total.p);
-    CG_CUDA(cudaMemcpyAsync(total, bins.offset + ntiles, 4, cudaMemcpyDeviceToHost, s));
+    uint64_t* total = reinterpret_cast<uint64_t*>(ctx->compat_total.p);
+    CG_CUDA(cudaMemcpyAsync(total, pairs64, 8, cudaMemcpyDeviceToHost, s));
     CG_CUDA(cudaStreamSynchronize(s));
+    // the per-tile offsets are 32-bit
+    CG_CHECK(*total < 0xFFFFFFFFull, CG_ERR_OUT_OF_RANGE,
+             "cg_render_compat: %llu board-tile pairs exceed 2^32 (fewer boards or pixels)",
+             (unsigned long long)*total);
     CG_CUDA(ctx->compat_list.ensure((size_t)(*total > 0 ? *total : 1) * 8));
     CG_LAUNCH(ctx, launch_compat_fill(P, ctx->compat_rect.as<const int4>(),
                                       ctx->compat_key.as<const float>(), bins.cursor,

@@ -358,9 +358,10 @@ struct CompatDev {
     const float2* noise;   // green and alpha of the decoded 32^3 noise map
 };
 // Per board: tile rectangle (x0, y0, x1, y1; empty when x0 > x1) and the
-// squared eye distance; per tile: the number of boards whose quad may cover it.
+// squared eye distance; per tile: the number of boards whose quad may cover it;
+// *pairs (64-bit) += every board's tile count.
 cudaError_t launch_compat_count(const CompatDev& P, int4* rect, float* key, uint32_t* tile_count,
-                                cudaStream_t st);
+                                unsigned long long* pairs, cudaStream_t st);
 // Per tile: (distance bits << 32 | board) at the tile's cursor.
 cudaError_t launch_compat_fill(const CompatDev& P, const int4* rect, const float* key,
                                uint32_t* cursor, unsigned long long* list, cudaStream_t st);

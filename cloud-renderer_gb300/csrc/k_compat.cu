@@ -34,7 +34,8 @@ constexpr int NOISE_N = 32;    // noise map edge (ConeTraceShader.cpp:12)
 
 // One warp per board: lane 0 derives the board's tile rectangle, the lanes
 // split its tiles for the per-tile count.
-__global__ void k_compat_count(CompatDev P, int4* rect, float* key, uint32_t* tile_count) {
+__global__ void k_compat_count(CompatDev P, int4* rect, float* key, uint32_t* tile_count,
+                               unsigned long long* pairs) {
     const int b = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (b >= P.n) return;
@@ -75,6 +76,7 @@ __global__ void k_compat_count(CompatDev P, int4* rect, float* key, uint32_t* ti
     R.w = __shfl_sync(0xffffffffu, R.w, 0);
     const int nx = R.z - R.x + 1, ny = R.w - R.y + 1;
     if (nx <= 0 || ny <= 0) return;
+    if (lane == 0) atomicAdd(pairs, (unsigned long long)nx * (unsigned long long)ny);
     for (int t = lane; t < nx * ny; t += 32)
         atomicAdd(tile_count + (R.y + t / nx) * P.tiles_x + R.x + t % nx, 1u);
 }
@@ -345,9 +347,9 @@ __global__ void __launch_bounds__(256) k_compat_tiles(VolDesc vd, ConeSchedule c
 }  // namespace
 
 cudaError_t launch_compat_count(const CompatDev& P, int4* rect, float* key, uint32_t* tile_count,
-                                cudaStream_t st) {
+                                unsigned long long* pairs, cudaStream_t st) {
     if (P.n == 0) return cudaSuccess;
-    k_compat_count<<<(P.n + 3) / 4, 128, 0, st>>>(P, rect, key, tile_count);
+    k_compat_count<<<(P.n + 3) / 4, 128, 0, st>>>(P, rect, key, tile_count, pairs);
     return cudaGetLastError();
 }
 

@@ -84,11 +84,14 @@ __device__ __forceinline__ void bin_walk(const BoardsDev& b, int D, Bins& bins) 
 __global__ void k_bin_count(BoardsDev b, int D, Bins bins) { bin_walk<false>(b, D, bins); }
 __global__ void k_bin_fill(BoardsDev b, int D, Bins bins) { bin_walk<true>(b, D, bins); }
 
-// Exclusive scan of the brick counts in one CTA: tiles of 4096 counts, four
-// per thread, block scan per tile with a running carry.  Seeds the cursors.
+// Exclusive scan of the brick counts in one CTA; seeds the cursors.  Each
+// pass covers 1024 x 32 counts: every thread loads its 32 consecutive counts
+// with eight 16-byte loads issued together (one memory latency per pass
+// instead of one per 4096 counts), sums them, and a block scan of the thread
+// sums gives the offsets; a running carry links the passes.  count, offset
+// and cursor are 16-byte aligned.
 __global__ void __launch_bounds__(1024) k_bin_scan(Bins bins) {
-    // 4 consecutive counts per thread (4096 per pass)
-    constexpr int PER = 4;
+    constexpr int PER = 32;
     __shared__ uint32_t warp_sums[32];
     __shared__ uint32_t carry_s;
     const int n = bins.nbricks;
@@ -98,7 +101,7 @@ __global__ void __launch_bounds__(1024) k_bin_scan(Bins bins) {
     for (int base = 0; base < n; base += 1024 * PER) {
         const int i0 = base + tid * PER;
         uint32_t c[PER];
-        if (i0 + PER <= n) {  // one 16-byte load
+        if (i0 + PER <= n) {
 #pragma unroll
             for (int k = 0; k < PER; k += 4) {
                 const uint4 q = *reinterpret_cast<const uint4*>(bins.count + i0 + k);
@@ -132,13 +135,30 @@ __global__ void __launch_bounds__(1024) k_bin_scan(Bins bins) {
         __syncthreads();
         const uint32_t carry = carry_s;
         uint32_t run = carry + warp_sums[wid] + x - s;
+        if (i0 + PER <= n) {
 #pragma unroll
-        for (int k = 0; k < PER; ++k) {
-            if (i0 + k < n) {
-                bins.offset[i0 + k] = run;
-                bins.cursor[i0 + k] = run;
+            for (int k = 0; k < PER; k += 4) {
+                uint4 q;
+                q.x = run;
+                run += c[k];
+                q.y = run;
+                run += c[k + 1];
+                q.z = run;
+                run += c[k + 2];
+                q.w = run;
+                run += c[k + 3];
+                *reinterpret_cast<uint4*>(bins.offset + i0 + k) = q;
+                *reinterpret_cast<uint4*>(bins.cursor + i0 + k) = q;
             }
-            run += c[k];
+        } else {
+#pragma unroll
+            for (int k = 0; k < PER; ++k) {
+                if (i0 + k < n) {
+                    bins.offset[i0 + k] = run;
+                    bins.cursor[i0 + k] = run;
+                }
+                run += c[k];
+            }
         }
         __syncthreads();
         if (tid == 1023) carry_s = carry + warp_sums[wid] + x;
