@@ -57,25 +57,32 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
 __device__ __forceinline__ void fence_mbar_init() {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
-// One test of the phase with parity `phase`; the thread may sleep (up to the
-// suspend-time hint, 10 ms) until the phase completes instead of spinning.
+// One test of the phase with parity `phase` (true once that phase has
+// completed); the thread may be suspended for up to 1 ms while it waits.
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned phase) {
     uint32_t ok;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
         " selp.u32 %0, 1, 0, p;\n}"
         : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(phase), "r"(10000000u)
+        : "r"(smem_addr(bar)), "r"(phase), "r"(1000000u)
         : "memory");
     return ok != 0;
 }
-// Bounded wait for the phase with parity `phase` to complete; false when the
-// limit (tests, each of which may sleep) ran out: the caller reports an error
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Wait for the phase with parity `phase` for at most limit_ns nanoseconds of
+// the global timer; false when the time ran out: the caller reports an error
 // instead of waiting forever.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned phase, unsigned limit) {
-    for (unsigned i = 0; i < limit; ++i)
-        if (mbar_try_wait(bar, phase)) return true;
-    return false;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned phase, uint64_t limit_ns) {
+    if (mbar_try_wait(bar, phase)) return true;
+    const uint64_t t0 = global_ns();
+    while (!mbar_try_wait(bar, phase))
+        if (global_ns() - t0 > limit_ns) return false;
+    return true;
 }
 
 // Tensor memory: one warp allocates / frees; the address lands in shared memory.

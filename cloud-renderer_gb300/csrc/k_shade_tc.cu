@@ -23,8 +23,9 @@
 // tiles instead of setting the kernel's tail.
 // Layers 1-3 run on weights and biases pre-scaled by 1/2 (exact in FP16 and
 // FP32), so the accumulator holds z/2 and SiLU is z/2 * (1 + tanh(z/2)).
-// Every mbarrier wait is bounded: on a timeout the CTA records an error,
-// waits (bounded) for its MMA to drain, frees its tensor memory and returns.
+// Every mbarrier wait is bounded (1 s of the global timer): on a timeout the
+// CTA records an error, waits (bounded) for its MMA to drain, frees its tensor
+// memory and returns.
 #include <cuda_fp16.h>
 
 #include "cg_deferred.cuh"
@@ -36,7 +37,7 @@
 namespace {
 
 constexpr uint32_t TC_TMEM_COLS = 64;
-constexpr unsigned TC_WAIT_LIMIT = 1u << 22;
+constexpr uint64_t TC_WAIT_NS = 1000000000ull;  // 1 s: a wait longer than this is a fault
 // shared memory map (bytes from the 1024-aligned base)
 constexpr int OFF_ACT = 0;                 // 128 x 128 B activation tile
 constexpr int OFF_W1 = 16384;              // 64 x 128 B (K = 16 used)
@@ -277,12 +278,12 @@ __global__ void __launch_bounds__(128, 4)
                 ng = sb.light_lane[nslot].x;
             }
             if (layer == 2) fetch_features(geo, tp, nslot, ns, nf);
-            const bool ok = tc::mbar_wait(bar, phase, TC_WAIT_LIMIT);
-            phase ^= 1u;
-            if (__syncthreads_or(!ok)) {
+            const bool ok = tc::mbar_wait(bar, phase, TC_WAIT_NS);
+            if (__syncthreads_or(!ok)) {  // the commit of parity `phase` is still pending
                 failed = true;
                 break;
             }
+            phase ^= 1u;
             tc::fence_after_sync();
             // ---- epilogue: TMEM -> bias + SiLU, 32 columns at a time; the
             // last layer folds the 64 -> 1 output in FP32
@@ -331,7 +332,7 @@ __global__ void __launch_bounds__(128, 4)
     }
     if (failed) {
         // drain the outstanding commit (bounded), then report
-        tc::mbar_wait(bar, phase, TC_WAIT_LIMIT);
+        tc::mbar_wait(bar, phase, TC_WAIT_NS);
         if (tid == 0) atomicOr(status + 1, 1ull);
     }
     unsigned tot = n_fallback, nv = n_valid;
