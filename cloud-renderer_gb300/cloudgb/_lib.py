@@ -186,6 +186,7 @@ SIGNATURES = [
     ("cg_frame_graph_launch", I, [P, P]),
     ("cg_frame_graph_destroy", None, [P]),
     ("cg_compat_params_default", None, [ctypes.POINTER(cg_compat_params)]),
+    ("cg_context_check_wait_timeout", I, [P, ctypes.c_uint32, U64P]),
     ("cg_compat_noise_map", I, [ctypes.c_uint32, FP]),
     ("cg_render_compat", I, [P, P, ctypes.POINTER(cg_camera), ctypes.POINTER(cg_compat_params), P,
                              I, P]),

@@ -265,6 +265,9 @@ cudaError_t launch_fbm_volume(TraceParams tp, const float org[3], const float ex
 // bounded wait ran out, [2] += samples shaded, [3] tile claim counter.
 cudaError_t launch_shade_mlp_tc(VolDesc vd, CamDesc cam, TraceParams tp, const MlpDev& m,
                                 SampleBuf sb, unsigned long long* status, cudaStream_t st);
+// One CTA waits on an mbarrier nothing arrives on, bounded by limit_ns
+// (status: [1] |= 1 on the timeout, [3] = nanoseconds waited).
+cudaError_t launch_wait_probe(uint64_t limit_ns, unsigned long long* status, cudaStream_t st);
 cudaError_t launch_accumulate(CamDesc cam, TraceParams tp, SampleBuf sb, float4* out,
                               cudaStream_t st);
 cudaError_t launch_mlp_features(VolDesc vd, const MlpDev& m, const float* pos, int n,

@@ -263,7 +263,30 @@ extern "C" cg_status cg_context_mlp_fallbacks(cg_context* ctx, uint64_t* out) {
     CG_CUDA(cudaMemcpy(h, ctx->fallbacks.p, 16, cudaMemcpyDeviceToHost));
     *out = h[0];
     CG_CHECK(h[1] == 0, CG_ERR_DEVICE_FAULT,
-             "surrogate render: a tensor-core wait ran out of its iteration limit");
+             "surrogate render: a tensor-core wait ran out of its time limit (1 s)");
+    return CG_OK;
+}
+
+extern "C" cg_status cg_context_check_wait_timeout(cg_context* ctx, uint32_t limit_us,
+                                                   uint64_t* waited_us) {
+    CG_CHECK(ctx && waited_us, CG_ERR_INVALID_ARGUMENT,
+             "cg_context_check_wait_timeout: null pointer");
+    CG_CHECK(limit_us >= 1 && limit_us <= 1000000, CG_ERR_OUT_OF_RANGE,
+             "cg_context_check_wait_timeout: limit %u us not in [1, 1e6]", limit_us);
+    CG_CUDA(cudaSetDevice(ctx->device));
+    CG_CUDA(ctx->fallbacks.ensure(32));
+    cudaStream_t s = ctx->stream;
+    CG_CUDA(cudaMemsetAsync(ctx->fallbacks.p, 0, 32, s));
+    CG_LAUNCH(ctx, launch_wait_probe((uint64_t)limit_us * 1000ull,
+                                     ctx->fallbacks.as<unsigned long long>(), s));
+    CG_CUDA(cudaStreamSynchronize(s));
+    unsigned long long h[4] = {0, 0, 0, 0};
+    CG_CUDA(cudaMemcpy(h, ctx->fallbacks.p, 32, cudaMemcpyDeviceToHost));
+    *waited_us = h[3] / 1000ull;
+    ctx->shaded_valid = false;
+    CG_CHECK(h[1] == 0, CG_ERR_DEVICE_FAULT,
+             "wait probe: the bounded mbarrier wait ran out after %llu us, as it must",
+             (unsigned long long)(h[3] / 1000ull));
     return CG_OK;
 }
 

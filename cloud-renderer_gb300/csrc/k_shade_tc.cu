@@ -349,7 +349,32 @@ __global__ void __launch_bounds__(128, 4)
     if (warp == 0) tc::tmem_dealloc(tmem, TC_TMEM_COLS);
 }
 
+// The bounded wait on an mbarrier that nothing arrives on: one CTA inits the
+// barrier, waits for its first phase with the time limit, and records the
+// outcome in the status block ([1] |= 1 on a timeout, [3] = nanoseconds
+// waited); the kernel then returns normally.
+__global__ void k_wait_probe(uint64_t limit_ns, unsigned long long* status) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&bar, 1);
+        tc::fence_mbar_init();
+    }
+    __syncthreads();
+    const uint64_t t0 = tc::global_ns();
+    const bool ok = tc::mbar_wait(&bar, 0u, limit_ns);
+    const uint64_t dt = tc::global_ns() - t0;
+    if (__syncthreads_or(!ok) && threadIdx.x == 0) {
+        atomicOr(status + 1, 1ull);
+        status[3] = dt;
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_wait_probe(uint64_t limit_ns, unsigned long long* status, cudaStream_t st) {
+    k_wait_probe<<<1, 32, 0, st>>>(limit_ns, status);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_shade_mlp_tc(VolDesc vd, CamDesc cam, TraceParams tp, const MlpDev& m,
                                 SampleBuf sb, unsigned long long* status, cudaStream_t st) {

@@ -332,6 +332,12 @@ cg_status cg_image_error_stats(cg_context* ctx, const float* image, const void* 
 cg_status cg_context_mlp_fallbacks(cg_context* ctx, uint64_t* out);
 /* View samples the last MLP render shaded (one surrogate inference each). */
 cg_status cg_context_last_samples(cg_context* ctx, uint64_t* samples);
+/* Failure-detection check (no reference counterpart): one CTA waits on a
+ * tensor-core mbarrier that nothing completes, with the same bounded wait the
+ * surrogate kernel uses, limited to limit_us (1 .. 1e6).  The wait must run
+ * out: returns CG_ERR_DEVICE_FAULT with *waited_us = the time waited, and the
+ * context stays usable.  CG_OK would mean the bound did not fire. */
+cg_status cg_context_check_wait_timeout(cg_context* ctx, uint32_t limit_us, uint64_t* waited_us);
 
 /* ---- allocation-free variant ------------------------------------------- */
 
