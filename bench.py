@@ -42,12 +42,13 @@ def parse():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["frame", "batch", "animated", "compat"],
+    ap.add_argument("--workload", choices=["frame", "batch", "animated", "compat", "precision"],
                     default="frame",
                     help="frame: the headline 1080p frame; batch: 48 clouds x 128 views per "
                          "frame (one persistent launch, CUDA-graph replay, autotuned); "
                          "animated: moving boards re-voxelized every frame, wind-moved noise; "
-                         "compat: the reference's billboard image formation")
+                         "compat: the reference's billboard image formation; precision: "
+                         "4K over a 512^3 BF16/FP16 volume")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget-s", type=float, default=15.0)
     ap.add_argument("--mlp-steps", type=int, default=20000)
@@ -848,6 +849,108 @@ def run_compat(args):
     vol.close()
 
 
+def run_precision(args):
+    """The precision form: 512^3 volume (16384 boards, 5-octave fBm) rendered at
+    3840x2160 (128 view steps, 32-step sun cone), one step = voxelize + render
+    of one of the 16 orbit views, with the BF16/FP16 volume (exact cone) and
+    the RGBA32F volume; value = BF16/FP16 Mpix/s; the BF16/FP16 image's error
+    against the FP32 image is reduced on the GPU in FP64."""
+    import numpy as np
+    import torch
+
+    import cloudgb
+    from cloudgb import _lib, configs, workload as Wm
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    ctx = cloudgb.Context(local)
+    lib = _lib.load()
+    cfg = configs.PRECISION_4K
+    wl = Wm.build(cfg, width=args.width, height=args.height)
+    sun = cloudgb.Sun(wl.sun_direction, *wl.sun_map)
+    csun = sun._c()
+    cams = [Wm.make_camera(cd) for cd in wl.cameras]
+    ccams = [c._c() for c in cams]
+    W, H = cams[0].width, cams[0].height
+    shader = cloudgb.ConeTraceShader(**wl.shader_kwargs())
+    params = shader.params()
+    stream = torch.cuda.Stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    img = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    res = {}
+    images = {}
+    for name, fmt in (("fp32", cloudgb.FORMAT_RGBA32F), ("bf16_fp16", cloudgb.FORMAT_BF16_FP16)):
+        vol = cloudgb.CloudVolume(cfg["dim"], configs.VOLUME_BOUNDS, configs.VOLUME_POSITION,
+                                  cfg["mips"], fmt=fmt, ctx=ctx)
+        vol.set_billboards(wl.positions, wl.scales, wl.densities)
+        vol.update()
+
+        def frame(k):
+            _lib.check(lib.cg_voxelize(vol.handle, ctypes.byref(csun), sp), "cg_voxelize")
+            _lib.check(lib.cg_render(ctx.handle, vol.handle, ctypes.byref(ccams[k % len(cams)]),
+                                     ctypes.byref(params), ctypes.c_void_p(img.data_ptr()), 1,
+                                     sp), "cg_render")
+
+        with torch.cuda.stream(stream):
+            for k in range(args.warmup):
+                frame(k)
+            torch.cuda.synchronize()
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                  for _ in range(args.steps)]
+            sampler = ClockSampler(gpu_index(local))
+            sampler.__enter__()
+            l0 = ctx.launch_count
+            for k in range(args.steps):
+                flush.zero_()
+                ev[k][0].record(stream)
+                frame(k)
+                ev[k][1].record(stream)
+            torch.cuda.synchronize()
+            sampler.__exit__()
+            launches = ctx.launch_count - l0
+            ctx.set_timing(True)
+            stages = {}
+            for k in range(min(args.steps, 4)):
+                _lib.check(lib.cg_voxelize(vol.handle, ctypes.byref(csun), sp), "cg_voxelize")
+                for nm, v in ctx.stage_times().items():
+                    stages.setdefault("voxelize." + nm, []).append(v)
+                _lib.check(lib.cg_render(ctx.handle, vol.handle, ctypes.byref(ccams[k % len(cams)]),
+                                         ctypes.byref(params), ctypes.c_void_p(img.data_ptr()), 1,
+                                         sp), "cg_render")
+                for nm, v in ctx.stage_times().items():
+                    stages.setdefault(nm, []).append(v)
+            ctx.set_timing(False)
+            frame(0)
+            torch.cuda.synchronize()
+            images[name] = img.cpu().numpy()
+        ms = np.array([a.elapsed_time(b) for a, b in ev])
+        res[name] = {"total_ms": float(ms.sum()), "frame_ms": float(np.median(ms)),
+                     "launches": launches, "clocks": sampler.summary(),
+                     "stages_ms": {k: round(float(np.mean(v)), 4) for k, v in stages.items()}}
+        vol.close()
+    err = ctx.error_stats(images["bf16_fp16"], images["fp32"])
+    head = res["bf16_fp16"]
+    value = W * H * args.steps / (head["total_ms"] / 1e3) / 1e6
+    line = {"metric": "Mpix/s, precision form: 4K over a 512³ BF16/FP16 volume (exact cone)",
+            "value": round(value, 3), "unit": "Mpix/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(head["total_ms"] / args.steps, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16/fp16 storage, f32 arithmetic",
+            "data": "synthetic (seeded SplitMix64 scene)",
+            "config": {"workload": "512^3, 16384 boards, 5-octave fBm, 3840x2160, 128 view "
+                                   "steps, 32-step sun cone, 16 orbit views; voxelize + render",
+                       "paths": {k: {"frame_mpix_s": round(W * H / (v["frame_ms"] / 1e3) / 1e6, 2),
+                                     "frame_ms": round(v["frame_ms"], 4),
+                                     "stages_ms": v["stages_ms"]} for k, v in res.items()},
+                       "bf16_rmse_vs_fp32": float(err["rmse_all"]),
+                       "bf16_max_abs_vs_fp32": float(err["max_abs_all"]),
+                       "l2": "256 MiB buffer written between timed steps"},
+            "gpu_launches": int(head["launches"]),
+            "clocks": head["clocks"]}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -858,6 +961,8 @@ def main():
         run_animated(args)
     elif args.workload == "compat":
         run_compat(args)
+    elif args.workload == "precision":
+        run_precision(args)
     else:
         run_ours(args)
 
