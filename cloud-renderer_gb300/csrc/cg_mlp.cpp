@@ -30,17 +30,20 @@ struct SplitMix64 {
     double uniform() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }
 };
 
-uint32_t crc32_update(uint32_t crc, const void* data, size_t n) {
-    static uint32_t table[256];
-    static bool init = false;
-    if (!init) {
+struct Crc32Table {
+    uint32_t t[256];
+    Crc32Table() {
         for (uint32_t i = 0; i < 256; ++i) {
             uint32_t c = i;
             for (int k = 0; k < 8; ++k) c = (c & 1) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
-            table[i] = c;
+            t[i] = c;
         }
-        init = true;
     }
+};
+
+uint32_t crc32_update(uint32_t crc, const void* data, size_t n) {
+    static const Crc32Table tab;  // initialised once, thread-safe
+    const uint32_t* table = tab.t;
     const uint8_t* p = reinterpret_cast<const uint8_t*>(data);
     crc = ~crc;
     for (size_t i = 0; i < n; ++i) crc = table[(crc ^ p[i]) & 0xFFu] ^ (crc >> 8);

@@ -1,6 +1,7 @@
 // k_mlp.cu -- the sun-transmittance surrogate's kernels: feature extraction,
 // inference, the fused training step (forward + backward, tensor cores) and
 // the gradient reduction with Adam.
+#include <atomic>
 #include "cg_mlp.cuh"
 
 namespace {
@@ -434,16 +435,16 @@ cudaError_t launch_mlp_infer(const MlpDev& m, const float* feat, int n, float* o
 
 cudaError_t launch_mlp_train(const TrainArgs& ta, int ctas, cudaStream_t st) {
     // the attribute is set once per device, outside any stream capture
-    static bool configured[64] = {};
+    static std::atomic<bool> configured[64];
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-    if (!configured[dev]) {
+    if (!configured[dev].load(std::memory_order_acquire)) {
         e = cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)TrainSmem::BYTES);
         if (e != cudaSuccess) return e;
-        configured[dev] = true;
+        configured[dev].store(true, std::memory_order_release);
     }
     k_mlp_train<<<ctas, 128, TrainSmem::BYTES, st>>>(ta);
     return cudaGetLastError();

@@ -28,6 +28,8 @@
 // memory and returns.
 #include <cuda_fp16.h>
 
+#include <atomic>
+
 #include "cg_deferred.cuh"
 #include "cg_internal.h"
 #include "cg_mlp.cuh"
@@ -383,22 +385,24 @@ cudaError_t launch_shade_mlp_tc(VolDesc vd, CamDesc cam, TraceParams tp, const M
     const FeatGeom geo = feat_geom(vd, m);
     // one persistent wave: 4 CTAs per SM (the register and shared-memory
     // budgets of __launch_bounds__(128, 4); 4 x 64 tensor-memory columns)
-    static int grid[2][64] = {};
+    // (the per-device launch shape and the shared-memory attribute are
+    // configured once; atomics keep concurrent host threads well-defined)
+    static std::atomic<int> grid[2][64];
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
     const int f = vd.fmt == 0 ? 0 : 1;
-    if (!grid[f][dev]) {
+    if (!grid[f][dev].load(std::memory_order_acquire)) {
         const void* fn = f == 0 ? (const void*)k_shade_mlp_tc<0> : (const void*)k_shade_mlp_tc<1>;
         e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
         if (e != cudaSuccess) return e;
         int sms = 0;
         e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (e != cudaSuccess) return e;
-        grid[f][dev] = sms * 4;
+        grid[f][dev].store(sms * 4, std::memory_order_release);
     }
-    const int blocks = grid[f][dev];
+    const int blocks = grid[f][dev].load(std::memory_order_acquire);
     if (f == 0)
         k_shade_mlp_tc<0><<<blocks, 128, SMEM_BYTES, st>>>(vd, tp, cone, m, geo, sb, status);
     else
