@@ -64,6 +64,41 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+# Replicas: every rank renders the same workload on its own GPU; the only
+# cross-rank steps are the barrier before timing and the max of the ranks'
+# times (no data-path collective: the path has no exchange step).
+def init_replicas(world, local, backend="nccl"):
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        if backend == "nccl":
+            dist.init_process_group(backend, device_id=torch.device("cuda", local))
+        else:
+            dist.init_process_group(backend)
+
+
+def replica_barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world, device="cuda"):
+    """The largest of the ranks' values (all ranks receive it)."""
+    if world == 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(pixels_per_step, steps, world, max_ms):
+    """Whole-job Mpix/s: the pixels of all ranks over the slowest rank's time."""
+    return pixels_per_step * steps * world / (max_ms / 1e3) / 1e6
+
+
 def workload(args=None):
     from cloudgb import configs, workload as W
     if args is not None and (args.width or args.height):
@@ -271,9 +306,7 @@ def run_ours(args):
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    init_replicas(world, local)
     wl = workload(args)
     c = wl.cfg
     ctx = cloudgb.Context(local)
@@ -312,8 +345,7 @@ def run_ours(args):
             for k in range(warmup):
                 frame(k)
             stream.synchronize()
-            if world > 1:
-                torch.distributed.barrier()
+            replica_barrier(world)
             torch.cuda.synchronize()
             l0 = ctx.launch_count
             ev = []
@@ -399,12 +431,8 @@ def run_ours(args):
     head = learned if use_mlp else plain
     head_shader = mlp_shader if use_mlp else plain_shader
     head_vol = vol16 if use_mlp else vol32
-    total_ms = head["total_ms"]
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = W * H * args.steps * world / (total_ms / 1e3) / 1e6
+    total_ms = max_over_ranks(head["total_ms"], world)
+    value = replica_rate(W * H, args.steps, world, total_ms)
 
     def mpix(ms):
         return W * H / (ms / 1e3) / 1e6
@@ -422,7 +450,7 @@ def run_ours(args):
         t1 = time.perf_counter()
         if k > 0:
             e2e_ms.append((t1 - t0) * 1e3)
-    e2e_val = W * H / (float(np.median(e2e_ms)) / 1e3) / 1e6 * world
+    e2e_val = replica_rate(W * H, 1, world, max_over_ranks(float(np.median(e2e_ms)), world))
 
     if use_mlp:
         roofline = {"bound": "tensor", "kernel": "k_shade_mlp_tc", "achieved": round(mlp_tflops, 2),

@@ -2,6 +2,7 @@
 // inference, the fused training step (forward + backward, tensor cores) and
 // the gradient reduction with Adam.
 #include <atomic>
+
 #include "cg_mlp.cuh"
 
 namespace {
