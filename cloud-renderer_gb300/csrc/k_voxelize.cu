@@ -365,17 +365,18 @@ __device__ __forceinline__ float4 box8(float4 c000, float4 c100, float4 c010, fl
     return make_float4(s.x * 0.125f, s.y * 0.125f, s.z * 0.125f, s.w * 0.125f);
 }
 
-// One CTA per 8^3 brick, 256 threads, two voxels per thread (z and z + 4,
-// so that each staged board is tested against both with one set of shared
-// memory reads).  Boards of the brick's bin are staged through shared memory;
-// each voxel tests its centre against each board's ball on the Q20 grid
-// (int64 squared distance) and sums count and Q16.16 density.
+// One CTA per 8^3 brick, 128 threads, four voxels per thread (z, z + 2,
+// z + 4, z + 6 of one (x, y) column, so that each staged board is tested
+// against all four with one set of shared-memory reads and one dx^2 + dy^2).
+// Boards of the brick's bin are staged through shared memory; each voxel
+// tests its centre against each board's ball on the Q20 grid (int64 squared
+// distance) and sums count and Q16.16 density.
 // COV = false (voxelize): level 0 is assembled in registers, the next
 // `fused_levels` mip levels are reduced in shared memory, raw occupancy is
 // flagged.  COV = true: only the integer coverage (count, dq) is written
 // (the coverage readback and the active-voxel statistic compute it on demand).
 template <bool COV>
-__global__ void __launch_bounds__(256) k_splat(BoardsDev b, Bins bins, const uint8_t* mask,
+__global__ void __launch_bounds__(128) k_splat(BoardsDev b, Bins bins, const uint8_t* mask,
                                                VolDesc vd, void* pyr, uint32_t* count,
                                                uint32_t* dqout, int fused_levels,
                                                OccRaw occ_raw) {
@@ -392,19 +393,20 @@ __global__ void __launch_bounds__(256) k_splat(BoardsDev b, Bins bins, const uin
     const int by = (brick / bins.nbx) % bins.nby;
     const int bz = brick / (bins.nbx * bins.nby);
     const int tid = threadIdx.x;
-    const int lx = tid & 7, ly = (tid >> 3) & 7, lz = tid >> 6;  // lz in 0..3, second voxel lz + 4
+    // voxel k of the thread: (lx, ly, lz + 2k), tile index tid + 128 k
+    const int lx = tid & 7, ly = (tid >> 3) & 7, lz = tid >> 6;  // lz in 0..1
     const int D = vd.D;
     const int x = bx * CG_BRICK + lx, y = by * CG_BRICK + ly;
-    const int z0 = bz * CG_BRICK + lz, z1 = z0 + 4;
-    const bool in0 = (x < D && y < D && z0 < D), in1 = (x < D && y < D && z1 < D);
+    const int z0 = bz * CG_BRICK + lz;
+    const bool inxy = x < D && y < D;
     const int vx = (2 * x + 1) * (int)CG_HALF_Q20;
     const int vy = (2 * y + 1) * (int)CG_HALF_Q20;
     const int vz0 = (2 * z0 + 1) * (int)CG_HALF_Q20;
-    const int vz1 = vz0 + 8 * (int)CG_HALF_Q20;
+    constexpr int DZ = 4 * (int)CG_HALF_Q20;  // two voxels along z
 
     const uint32_t beg = bins.offset[brick];
     const uint32_t n = bins.offset[brick + 1] - beg;
-    uint32_t cnt0 = 0, dsum0 = 0, cnt1 = 0, dsum1 = 0;
+    uint32_t cnt[4] = {0u, 0u, 0u, 0u}, dsum[4] = {0u, 0u, 0u, 0u};
     const int w = tid >> 5;
     for (uint32_t base = 0; base < n; base += CG_SPLAT_CHUNK) {
         const uint32_t m = min((uint32_t)CG_SPLAT_CHUNK, n - base);
@@ -423,49 +425,39 @@ __global__ void __launch_bounds__(256) k_splat(BoardsDev b, Bins bins, const uin
             const int dx = vx - q.x, dy = vy - q.y;
             const unsigned long long dxy = (unsigned long long)((long long)dx * dx) +
                                            (unsigned long long)((long long)dy * dy);
-            const int dz0 = vz0 - q.z, dz1 = vz1 - q.z;
-            const unsigned long long d0 = dxy + (unsigned long long)((long long)dz0 * dz0);
-            const unsigned long long d1 = dxy + (unsigned long long)((long long)dz1 * dz1);
-            if (d0 <= thr) {
-                cnt0 += 1u;
-                dsum0 += dq;
+            if (dxy > thr) continue;  // the column misses the ball
+            int dz = vz0 - q.z;
+#pragma unroll
+            for (int j = 0; j < 4; ++j, dz += DZ) {
+                const unsigned long long d = dxy + (unsigned long long)((long long)dz * dz);
+                if (d <= thr) {
+                    cnt[j] += 1u;
+                    dsum[j] += dq;
+                }
             }
-            if (d1 <= thr) {
-                cnt1 += 1u;
-                dsum1 += dq;
-            }
         }
     }
-    const size_t i0 = ((size_t)z0 * D + y) * D + x;
-    const size_t i1 = i0 + (size_t)4 * D * D;
-    if (COV) {
-        if (in0) {
-            count[i0] = cnt0;
-            dqout[i0] = dsum0;
+    float4 v[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int z = z0 + 2 * j;
+        const bool in = inxy && z < D;
+        const size_t i = ((size_t)z * D + y) * D + x;
+        v[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (!in) continue;
+        if (COV) {
+            count[i] = cnt[j];
+            dqout[i] = dsum[j];
+            continue;
         }
-        if (in1) {
-            count[i1] = cnt1;
-            dqout[i1] = dsum1;
-        }
-        return;
+        const uint8_t mk = mask[i];
+        v[j].x = __uint2float_rn(dsum[j]) * (1.0f / 65536.0f);
+        v[j].y = mk ? 1.0f : 0.0f;
+        v[j].z = __uint2float_rn(cnt[j]);
+        v[j].w = (cnt[j] > 0u || mk) ? 1.0f : 0.0f;
+        store_voxel(vd, pyr, 0, x, y, z, v[j]);
     }
-    float4 v0 = make_float4(0.f, 0.f, 0.f, 0.f), v1 = v0;
-    if (in0) {
-        const uint8_t mk = mask[i0];
-        v0.x = __uint2float_rn(dsum0) * (1.0f / 65536.0f);
-        v0.y = mk ? 1.0f : 0.0f;
-        v0.z = __uint2float_rn(cnt0);
-        v0.w = (cnt0 > 0u || mk) ? 1.0f : 0.0f;
-        store_voxel(vd, pyr, 0, x, y, z0, v0);
-    }
-    if (in1) {
-        const uint8_t mk = mask[i1];
-        v1.x = __uint2float_rn(dsum1) * (1.0f / 65536.0f);
-        v1.y = mk ? 1.0f : 0.0f;
-        v1.z = __uint2float_rn(cnt1);
-        v1.w = (cnt1 > 0u || mk) ? 1.0f : 0.0f;
-        store_voxel(vd, pyr, 0, x, y, z1, v1);
-    }
+    if (COV) return;
     // Raw occupancy (4^3 cells, every level): the brick's eight level-0 cells
     // from its voxels, and at level l >= 1 the one cell holding the brick
     // (level-l cell = brick >> (l - 1)).  Idempotent byte stores into grids
@@ -473,16 +465,18 @@ __global__ void __launch_bounds__(256) k_splat(BoardsDev b, Bins bins, const uin
     if (tid == 0) s_cells = 0u;
     __syncthreads();
     {
-        // the warp's voxels lie in cell y = w & 1, z = 0 (first voxel) or 1
-        // (second), x = lane bit 2 (lanes 0-3 of each row in x cell 0)
-        const unsigned b0 = __ballot_sync(0xffffffffu, in0 && v0.x > 0.f);
-        const unsigned b1 = __ballot_sync(0xffffffffu, in1 && v1.x > 0.f);
+        // the warp's voxels lie in cell y = w & 1; voxel j in cell z = j >> 1;
+        // lanes 0-3 of each row of 8 in x cell 0, lanes 4-7 in x cell 1
         const int cy = 2 * (w & 1);
         unsigned bits = 0u;
-        if (b0 & 0x0F0F0F0Fu) bits |= 1u << cy;
-        if (b0 & 0xF0F0F0F0u) bits |= 1u << (cy + 1);
-        if (b1 & 0x0F0F0F0Fu) bits |= 1u << (cy + 4);
-        if (b1 & 0xF0F0F0F0u) bits |= 1u << (cy + 5);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const bool in = inxy && z0 + 2 * j < D;
+            const unsigned bal = __ballot_sync(0xffffffffu, in && v[j].x > 0.f);
+            const int cz = 4 * (j >> 1);
+            if (bal & 0x0F0F0F0Fu) bits |= 1u << (cy + cz);
+            if (bal & 0xF0F0F0F0u) bits |= 1u << (cy + cz + 1);
+        }
         if ((tid & 31) == 0 && bits) atomicOr(&s_cells, bits);
     }
     __syncthreads();
@@ -513,8 +507,8 @@ __global__ void __launch_bounds__(256) k_splat(BoardsDev b, Bins bins, const uin
         }
     }
     if (fused_levels <= 0) return;
-    tile[tid] = v0;        // voxel (lx, ly, lz)
-    tile[tid + 256] = v1;  // voxel (lx, ly, lz + 4)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) tile[tid + 128 * j] = v[j];  // voxel (lx, ly, lz + 2j)
     __syncthreads();
     // level 1: 4^3 parents
     if (tid < 64) {
@@ -650,10 +644,10 @@ cudaError_t launch_splat(const BoardsDev& b, Bins bins, const uint8_t* mask, Vol
                          void* pyr, uint32_t* count, uint32_t* dq, int fused_levels,
                          OccRaw occ, bool coverage_only, cudaStream_t st) {
     if (coverage_only)
-        k_splat<true><<<bins.nbricks, 256, 0, st>>>(b, bins, mask, vd, pyr, count, dq,
+        k_splat<true><<<bins.nbricks, 128, 0, st>>>(b, bins, mask, vd, pyr, count, dq,
                                                     fused_levels, occ);
     else
-        k_splat<false><<<bins.nbricks, 256, 0, st>>>(b, bins, mask, vd, pyr, count, dq,
+        k_splat<false><<<bins.nbricks, 128, 0, st>>>(b, bins, mask, vd, pyr, count, dq,
                                                      fused_levels, occ);
     return cudaGetLastError();
 }
