@@ -365,9 +365,10 @@ __device__ __forceinline__ float4 box8(float4 c000, float4 c100, float4 c010, fl
     return make_float4(s.x * 0.125f, s.y * 0.125f, s.z * 0.125f, s.w * 0.125f);
 }
 
-// One CTA per 8^3 brick, 128 threads, four voxels per thread (z, z + 2,
-// z + 4, z + 6 of one (x, y) column, so that each staged board is tested
-// against all four with one set of shared-memory reads and one dx^2 + dy^2).
+// One CTA per 8^3 brick, 64 threads, one (x, y) column of eight voxels per
+// thread (each staged board is tested against all eight with one set of
+// shared-memory reads and one dx^2 + dy^2; a column that misses the ball
+// skips its eight tests).
 // Boards of the brick's bin are staged through shared memory; each voxel
 // tests its centre against each board's ball on the Q20 grid (int64 squared
 // distance) and sums count and Q16.16 density.
@@ -376,7 +377,7 @@ __device__ __forceinline__ float4 box8(float4 c000, float4 c100, float4 c010, fl
 // flagged.  COV = true: only the integer coverage (count, dq) is written
 // (the coverage readback and the active-voxel statistic compute it on demand).
 template <bool COV>
-__global__ void __launch_bounds__(128) k_splat(BoardsDev b, Bins bins, const uint8_t* mask,
+__global__ void __launch_bounds__(64) k_splat(BoardsDev b, Bins bins, const uint8_t* mask,
                                                VolDesc vd, void* pyr, uint32_t* count,
                                                uint32_t* dqout, int fused_levels,
                                                OccRaw occ_raw) {
@@ -393,8 +394,8 @@ __global__ void __launch_bounds__(128) k_splat(BoardsDev b, Bins bins, const uin
     const int by = (brick / bins.nbx) % bins.nby;
     const int bz = brick / (bins.nbx * bins.nby);
     const int tid = threadIdx.x;
-    // voxel k of the thread: (lx, ly, lz + 2k), tile index tid + 128 k
-    const int lx = tid & 7, ly = (tid >> 3) & 7, lz = tid >> 6;  // lz in 0..1
+    // voxel j of the thread: (lx, ly, j), tile index tid + 64 j
+    const int lx = tid & 7, ly = (tid >> 3) & 7, lz = 0;
     const int D = vd.D;
     const int x = bx * CG_BRICK + lx, y = by * CG_BRICK + ly;
     const int z0 = bz * CG_BRICK + lz;
@@ -402,11 +403,11 @@ __global__ void __launch_bounds__(128) k_splat(BoardsDev b, Bins bins, const uin
     const int vx = (2 * x + 1) * (int)CG_HALF_Q20;
     const int vy = (2 * y + 1) * (int)CG_HALF_Q20;
     const int vz0 = (2 * z0 + 1) * (int)CG_HALF_Q20;
-    constexpr int DZ = 4 * (int)CG_HALF_Q20;  // two voxels along z
+    constexpr int DZ = 2 * (int)CG_HALF_Q20;  // one voxel along z
 
     const uint32_t beg = bins.offset[brick];
     const uint32_t n = bins.offset[brick + 1] - beg;
-    uint32_t cnt[4] = {0u, 0u, 0u, 0u}, dsum[4] = {0u, 0u, 0u, 0u};
+    uint32_t cnt[8] = {}, dsum[8] = {};
     const int w = tid >> 5;
     for (uint32_t base = 0; base < n; base += CG_SPLAT_CHUNK) {
         const uint32_t m = min((uint32_t)CG_SPLAT_CHUNK, n - base);
@@ -428,7 +429,7 @@ __global__ void __launch_bounds__(128) k_splat(BoardsDev b, Bins bins, const uin
             if (dxy > thr) continue;  // the column misses the ball
             int dz = vz0 - q.z;
 #pragma unroll
-            for (int j = 0; j < 4; ++j, dz += DZ) {
+            for (int j = 0; j < 8; ++j, dz += DZ) {
                 const unsigned long long d = dxy + (unsigned long long)((long long)dz * dz);
                 if (d <= thr) {
                     cnt[j] += 1u;
@@ -437,10 +438,10 @@ __global__ void __launch_bounds__(128) k_splat(BoardsDev b, Bins bins, const uin
             }
         }
     }
-    float4 v[4];
+    float4 v[8];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const int z = z0 + 2 * j;
+    for (int j = 0; j < 8; ++j) {
+        const int z = z0 + j;
         const bool in = inxy && z < D;
         const size_t i = ((size_t)z * D + y) * D + x;
         v[j] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -465,15 +466,15 @@ __global__ void __launch_bounds__(128) k_splat(BoardsDev b, Bins bins, const uin
     if (tid == 0) s_cells = 0u;
     __syncthreads();
     {
-        // the warp's voxels lie in cell y = w & 1; voxel j in cell z = j >> 1;
+        // the warp's voxels lie in cell y = w & 1; voxel j in cell z = j >> 2;
         // lanes 0-3 of each row of 8 in x cell 0, lanes 4-7 in x cell 1
         const int cy = 2 * (w & 1);
         unsigned bits = 0u;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const bool in = inxy && z0 + 2 * j < D;
+        for (int j = 0; j < 8; ++j) {
+            const bool in = inxy && z0 + j < D;
             const unsigned bal = __ballot_sync(0xffffffffu, in && v[j].x > 0.f);
-            const int cz = 4 * (j >> 1);
+            const int cz = 4 * (j >> 2);
             if (bal & 0x0F0F0F0Fu) bits |= 1u << (cy + cz);
             if (bal & 0xF0F0F0F0u) bits |= 1u << (cy + cz + 1);
         }
@@ -508,7 +509,7 @@ __global__ void __launch_bounds__(128) k_splat(BoardsDev b, Bins bins, const uin
     }
     if (fused_levels <= 0) return;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) tile[tid + 128 * j] = v[j];  // voxel (lx, ly, lz + 2j)
+    for (int j = 0; j < 8; ++j) tile[tid + 64 * j] = v[j];  // voxel (lx, ly, j)
     __syncthreads();
     // level 1: 4^3 parents
     if (tid < 64) {
@@ -644,10 +645,10 @@ cudaError_t launch_splat(const BoardsDev& b, Bins bins, const uint8_t* mask, Vol
                          void* pyr, uint32_t* count, uint32_t* dq, int fused_levels,
                          OccRaw occ, bool coverage_only, cudaStream_t st) {
     if (coverage_only)
-        k_splat<true><<<bins.nbricks, 128, 0, st>>>(b, bins, mask, vd, pyr, count, dq,
+        k_splat<true><<<bins.nbricks, 64, 0, st>>>(b, bins, mask, vd, pyr, count, dq,
                                                     fused_levels, occ);
     else
-        k_splat<false><<<bins.nbricks, 128, 0, st>>>(b, bins, mask, vd, pyr, count, dq,
+        k_splat<false><<<bins.nbricks, 64, 0, st>>>(b, bins, mask, vd, pyr, count, dq,
                                                      fused_levels, occ);
     return cudaGetLastError();
 }
