@@ -389,7 +389,8 @@ extern "C" cg_status cg_volume_create(cg_context* ctx, int dimension, float boun
     }
     v->raw_total = raw_total;
     set_occ_layout(v, 4);  // the autotuner's pick on the batching and 1080p workloads
-    if (e == cudaSuccess) e = v->occ.ensure(2 * (size_t)raw_total);
+    // + the level-0 occupied box (6 ints) after the grids, 16-byte aligned
+    if (e == cudaSuccess) e = v->occ.ensure(occ_box_offset(raw_total) + 32);
     const int nb = (dimension + CG_BRICK - 1) / CG_BRICK;
     v->bins.nbx = v->bins.nby = v->bins.nbz = nb;
     v->bins.nbricks = nb * nb * nb;
@@ -588,6 +589,8 @@ OccRaw raw_of(const cg_volume* v) {
     return r;
 }
 
+size_t occ_box_offset(int raw_total) { return ((2 * (size_t)raw_total) + 15) & ~(size_t)15; }
+
 VolDesc desc_of(const cg_volume* v) {
     VolDesc d;
     d.D = v->D;
@@ -604,6 +607,8 @@ VolDesc desc_of(const cg_volume* v) {
     }
     d.pyr = v->pyr.p;
     d.occ = v->occ.as<const uint8_t>() + v->raw_total;
+    d.occ_box = reinterpret_cast<const int*>(v->occ.as<const uint8_t>() +
+                                             occ_box_offset(v->raw_total));
     d.occ_shift = v->occ_brick == 4 ? 2 : (v->occ_brick == 16 ? 4 : 3);
     for (int l = 0; l < CG_MAX_LEVELS; ++l) d.tex[l] = v->tex_obj[l];
     for (int l = 0; l < CG_MAX_LEVELS; ++l) d.surf[l] = 0;
@@ -734,7 +739,8 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
     CG_CUDA(cudaMemsetAsync(v->keys.p, 0xFF, texels * 8, s));
     CG_CUDA(cudaMemsetAsync(v->mask.p, 0, n0, s));
     CG_CUDA(cudaMemsetAsync(bins.count, 0, (size_t)bins.nbricks * 4, s));
-    CG_CUDA(cudaMemsetAsync(v->occ.p, 0, (size_t)v->raw_total, s));
+    // raw cells, brick grids (rewritten by the dilation) and the occupied box
+    CG_CUDA(cudaMemsetAsync(v->occ.p, 0, occ_box_offset(v->raw_total) + 6 * sizeof(int), s));
     // brick bins
     if (b.n) CG_LAUNCH(ctx, launch_bin_count(b, v->D, bins, s));
     CG_LAUNCH(ctx, launch_bin_scan(bins, s));
@@ -1362,8 +1368,11 @@ extern "C" cg_status cg_volume_set_occupancy_brick(cg_volume* v, int brick) {
     CG_CUDA(cudaDeviceSynchronize());
     set_occ_layout(v, brick);
     if (v->voxelized) {
-        // rebuild the brick grids from the raw cells of the last voxelize
+        // rebuild the brick grids (and the occupied box) from the raw cells of
+        // the last voxelize
         const VolDesc vd = desc_of(v);
+        CG_CUDA(cudaMemsetAsync(const_cast<int*>(vd.occ_box), 0, 6 * sizeof(int),
+                                v->ctx->stream));
         CG_LAUNCH(v->ctx, launch_occ_dilate(vd, raw_of(v), v->occ.as<uint8_t>() + v->raw_total,
                                             v->occ_total, v->ctx->stream));
         CG_CUDA(cudaStreamSynchronize(v->ctx->stream));

@@ -181,6 +181,8 @@ struct cg_volume {
 cg_status ensure_textures(cg_volume* v, cudaStream_t s);
 
 VolDesc desc_of(const cg_volume* v);
+// Byte offset of the level-0 occupied box in the volume's occupancy buffer.
+size_t occ_box_offset(int raw_total);
 OccRaw raw_of(const cg_volume* v);
 void set_occ_layout(cg_volume* v, int brick);
 BoardsDev boards_of(const cg_volume* v);

@@ -38,6 +38,9 @@ struct VolDesc {
     float wmin[3], range[3];
     const void* pyr;                // float4* (RGBA32F) or uint32_t* (BF16_FP16)
     const uint8_t* occ;             // occupancy grids, concatenated by level
+    // level-0 box of the occupied (dilated) bricks, in level-0 voxels:
+    // [0..2] = D - lo, [3..5] = hi (exclusive); lo >= hi when nothing is occupied
+    const int* occ_box;
     int occ_shift;
     int occ_nb[CG_MAX_LEVELS];
     int occ_off[CG_MAX_LEVELS];
@@ -301,6 +304,8 @@ cudaError_t launch_splat(const BoardsDev& b, Bins bins, const uint8_t* mask, Vol
                          OccRaw raw, bool coverage_only, cudaStream_t st);
 cudaError_t launch_mip_level(VolDesc vd, void* pyr, int l, cudaStream_t st);
 // Dilated occupancy grids of brick B = 1 << vd.occ_shift from the raw cells.
+// Builds the brick grids from the raw cells and grows the level-0 occupied
+// box (vd.occ_box, zeroed by the caller).
 cudaError_t launch_occ_dilate(VolDesc vd, OccRaw raw, uint8_t* occ, int total, cudaStream_t st);
 cudaError_t launch_count_active(const uint32_t* count, const uint8_t* mask, size_t n,
                                 unsigned long long* out, cudaStream_t st);

@@ -156,6 +156,40 @@ __device__ __forceinline__ float2 quad_hw(const VolDesc& vd, float px, float py,
     return a;
 }
 
+// View-march steps k (sample at t_k = tin + (k + 1/2) dt along the unit
+// direction d from the eye) that can meet the occupied level-0 box (widened by
+// one voxel, and by one step at either end): [k0, k1], empty (k0 > k1) when
+// the ray misses it.  A step outside it whose sample has lod 0 reads exactly 0
+// (its brick is unoccupied), so marches skip those steps.
+__device__ __forceinline__ void occupied_steps(const VolDesc& vd, const float eye[3], float3 d,
+                                               float tin, float dt, int Nv, int& k0, int& k1) {
+    const int* b = vd.occ_box;
+    const float D = (float)vd.D;
+    const float dd[3] = {d.x, d.y, d.z};
+    float ta = -1e30f, tb = 1e30f;
+    k0 = Nv;
+    k1 = -1;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const int lo = vd.D - __ldg(b + a), hi = __ldg(b + 3 + a);
+        if (lo >= hi) return;  // nothing occupied
+        const float vs = D / vd.range[a];
+        const float ve = (eye[a] - vd.wmin[a]) * vs, dv = dd[a] * vs;
+        const float l = (float)lo - 1.f, h = (float)hi + 1.f;
+        if (dv == 0.f) {
+            if (ve < l || ve > h) return;
+            continue;
+        }
+        const float t0 = (l - ve) / dv, t1 = (h - ve) / dv;
+        ta = fmaxf(ta, fminf(t0, t1));
+        tb = fminf(tb, fmaxf(t0, t1));
+    }
+    if (!(tb >= ta)) return;
+    const float fa = fmaxf((ta - tin) / dt - 0.5f, -1.f), fb = fminf((tb - tin) / dt - 0.5f, (float)Nv);
+    k0 = max(0, (int)floorf(fa) - 1);
+    k1 = min(Nv - 1, (int)ceilf(fb) + 1);
+}
+
 // Neumaier compensated accumulation.
 __device__ __forceinline__ void neumaier(float& sum, float& comp, float term) {
     float t = sum + term;

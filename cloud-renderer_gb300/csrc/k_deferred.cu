@@ -89,11 +89,23 @@ __global__ void __launch_bounds__(256) k_march(VolDesc vd, CamDesc cam, TracePar
     unsigned cnt = 0, nsteps = 0;
     float4* pw = sb.pos_w + (size_t)region * sb.capacity;
     float2* gl = sb.light_lane + (size_t)region * sb.capacity;
-    for (int k = 0; k < Nv; ++k) {
+    // this lane's sampled steps: when every sample has lod 0, steps outside the
+    // occupied box read 0 and are skipped (the warp starts at its first one)
+    int kb = 0, ke = Nv;
+    if (live && tin + ((float)(Nv - 1) + 0.5f) * dt < t_lod1) {
+        int k0, k1;
+        cgs::occupied_steps(vd, cam.eye, d, tin, dt, Nv, k0, k1);
+        kb = k0;
+        ke = k1 + 1;
+        if (kb >= ke) live = false;
+    }
+    const int wkb = __reduce_min_sync(0xffffffffu, live ? kb : Nv);
+    for (int k = wkb; k < Nv; ++k) {
+        if (live && k >= ke) live = false;
         if (!__any_sync(0xffffffffu, live)) break;
         bool emit = false;
         float v0 = 0.f, v1 = 0.f, v2 = 0.f, w = 0.f, G = 0.f;
-        if (live) {
+        if (live && k >= kb) {
             float t = tin + ((float)k + 0.5f) * dt;
             float p0 = cam.eye[0] + t * d.x, p1 = cam.eye[1] + t * d.y, p2 = cam.eye[2] + t * d.z;
             v0 = (p0 - vd.wmin[0]) * vsx;

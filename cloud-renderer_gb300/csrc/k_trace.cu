@@ -69,8 +69,17 @@ __global__ void __launch_bounds__(256) k_trace_fused(VolDesc vd, CamDesc cam, Tr
         const float D = (float)vd.D;
         const float vsx = D / vd.range[0], vsy = D / vd.range[1], vsz = D / vd.range[2];
         const float pixk = cam.tanh / (float)cam.H * vsx;
+        // when every sample has lod 0, steps outside the occupied box read 0
+        int kbeg = 0, kend = Nv;
+        const float tlast = tin + ((float)(Nv - 1) + 0.5f) * dt;
+        if (2.f * tlast * pixk <= 1.f) {
+            int k0, k1;
+            cgs::occupied_steps(vd, cam.eye, d, tin, dt, Nv, k0, k1);
+            kbeg = k0;
+            kend = k1 + 1;
+        }
         float T = 1.f, C = 0.f, Cc = 0.f;
-        for (int k = 0; k < Nv; ++k) {
+        for (int k = kbeg; k < kend; ++k) {
             float t = tin + ((float)k + 0.5f) * dt;
             float p0 = cam.eye[0] + t * d.x, p1 = cam.eye[1] + t * d.y, p2 = cam.eye[2] + t * d.z;
             float v0 = (p0 - vd.wmin[0]) * vsx, v1 = (p1 - vd.wmin[1]) * vsy,

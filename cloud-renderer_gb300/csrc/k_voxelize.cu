@@ -548,25 +548,56 @@ __global__ void __launch_bounds__(64) k_splat(BoardsDev b, Bins bins, const uint
 
 // Dilated occupancy: occ[l][c] = 1 when a raw 4^3 cell of level l inside
 // brick c (B = 1 << occ_shift texels) or one of its 26 neighbours is set; one
-// thread per brick of every level.
-__global__ void k_occ_dilate(VolDesc vd, OccRaw raw, uint8_t* occ, int total) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= total) return;
-    int l = 0;
-    while (l + 1 < vd.L && i >= vd.occ_off[l + 1]) ++l;
-    const int nb = vd.occ_nb[l], r = i - vd.occ_off[l];
-    const int cx = r % nb, cy = (r / nb) % nb, cz = r / (nb * nb);
-    const int k = vd.occ_shift - 2;  // raw cells per brick edge: 1 << k
-    const int rn = raw.nb[l];
-    const uint8_t* g = raw.raw + raw.off[l];
-    const int x0 = max((cx - 1) << k, 0), x1 = min((cx + 2) << k, rn);
-    const int y0 = max((cy - 1) << k, 0), y1 = min((cy + 2) << k, rn);
-    const int z0 = max((cz - 1) << k, 0), z1 = min((cz + 2) << k, rn);
-    uint8_t any = 0;
-    for (int z = z0; z < z1 && !any; ++z)
-        for (int y = y0; y < y1 && !any; ++y)
-            for (int x = x0; x < x1; ++x) any |= g[((size_t)z * rn + y) * rn + x];
-    occ[i] = any ? 1 : 0;
+// thread per brick of every level.  The occupied level-0 bricks also grow the
+// level-0 box (box[0..2] = D - lo, box[3..5] = hi, atomic maxima from zero).
+__global__ void __launch_bounds__(256) k_occ_dilate(VolDesc vd, OccRaw raw, uint8_t* occ,
+                                                    int total, int* box) {
+    __shared__ unsigned s_box[8][6];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned m[6] = {0u, 0u, 0u, 0u, 0u, 0u};  // this brick's box terms (0 = none)
+    if (i < total) {
+        int l = 0;
+        while (l + 1 < vd.L && i >= vd.occ_off[l + 1]) ++l;
+        const int nb = vd.occ_nb[l], r = i - vd.occ_off[l];
+        const int cx = r % nb, cy = (r / nb) % nb, cz = r / (nb * nb);
+        const int k = vd.occ_shift - 2;  // raw cells per brick edge: 1 << k
+        const int rn = raw.nb[l];
+        const uint8_t* g = raw.raw + raw.off[l];
+        const int x0 = max((cx - 1) << k, 0), x1 = min((cx + 2) << k, rn);
+        const int y0 = max((cy - 1) << k, 0), y1 = min((cy + 2) << k, rn);
+        const int z0 = max((cz - 1) << k, 0), z1 = min((cz + 2) << k, rn);
+        uint8_t any = 0;
+        for (int z = z0; z < z1 && !any; ++z)
+            for (int y = y0; y < y1 && !any; ++y)
+                for (int x = x0; x < x1; ++x) any |= g[((size_t)z * rn + y) * rn + x];
+        occ[i] = any ? 1 : 0;
+        if (any && l == 0) {
+            const int B = 1 << vd.occ_shift, D = vd.D;
+            const int c[3] = {cx, cy, cz};
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                m[a] = (unsigned)(D - c[a] * B);
+                m[3 + a] = (unsigned)min(D, (c[a] + 1) * B);
+            }
+        }
+    }
+    // the occupied level-0 box: block maxima (warp reductions, then warp 0),
+    // one atomic per value per block
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int a = 0; a < 6; ++a) m[a] = __reduce_max_sync(0xffffffffu, m[a]);
+    if (lane == 0)
+#pragma unroll
+        for (int a = 0; a < 6; ++a) s_box[w][a] = m[a];
+    __syncthreads();
+    if (w == 0) {
+        const int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int a = 0; a < 6; ++a) {
+            const unsigned v = __reduce_max_sync(0xffffffffu, lane < nw ? s_box[lane][a] : 0u);
+            if (lane == 0 && v > 0u) atomicMax(box + a, (int)v);
+        }
+    }
 }
 
 // Generic 2x2x2 reduction from level l to l+1 (one thread per parent).
@@ -654,7 +685,8 @@ cudaError_t launch_splat(const BoardsDev& b, Bins bins, const uint8_t* mask, Vol
 }
 
 cudaError_t launch_occ_dilate(VolDesc vd, OccRaw raw, uint8_t* occ, int total, cudaStream_t st) {
-    k_occ_dilate<<<(total + 255) / 256, 256, 0, st>>>(vd, raw, occ, total);
+    k_occ_dilate<<<(total + 255) / 256, 256, 0, st>>>(vd, raw, occ, total,
+                                                      const_cast<int*>(vd.occ_box));
     return cudaGetLastError();
 }
 
