@@ -240,6 +240,19 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
+    def extend(self, step, sync, min_samples=3, limit_s=5.0):
+        """A timed region shorter than the 100 ms sampling period holds no
+        sample: after it, keep the GPU on the same step (untimed repeats) until
+        `min_samples` samples cover the window -- the timed region and the
+        repeats that follow it without a gap."""
+        self.padded = 0
+        t0 = time.perf_counter()
+        while self.proc and len(self.lines) < min_samples and time.perf_counter() - t0 < limit_s:
+            for _ in range(8):
+                step()
+                self.padded += 1
+            sync()
+
     def __exit__(self, *exc):
         if self.proc:
             self.proc.terminate()
@@ -263,11 +276,13 @@ class ClockSampler:
             for n, v in zip(names, parts[5:9]):
                 if v.lower().startswith("active"):
                     reasons.add(n)
+        pad = getattr(self, "padded", 0)
         if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0,
+                    "untimed_repeats": pad}
         sm.sort()
         return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "untimed_repeats": pad}
 
 
 def load_peaks():
@@ -361,10 +376,11 @@ def run_ours(args):
                 e2.record(stream)
                 ev.append((e0, e1, e2))
             stream.synchronize()
-            if sampler:
-                sampler.__exit__()
             torch.cuda.synchronize()
             launches = ctx.launch_count - l0
+            if sampler:
+                sampler.extend(lambda: frame(steps - 1), stream.synchronize)
+                sampler.__exit__()
             # per-stage times (untimed pass with stage events on)
             ctx.set_timing(True)
             stages = {}
@@ -565,6 +581,8 @@ def run_batch(args):
             b.record(stream)
             evs.append((a, b))
         stream.synchronize()
+        graph_launches = int(ctx.launch_count - l0)
+        sampler.extend(lambda: graph.launch(stream.cuda_stream), stream.synchronize)
         sampler.__exit__()
     ms = [a.elapsed_time(b) for a, b in evs]
     total_ms = float(sum(ms))
@@ -584,7 +602,7 @@ def run_batch(args):
                        "slowest": [list(order[-1][0]), round(order[-1][1], 3)],
                        "one_ray_per_thread_ms": round(table[(1, 1, 8)], 3),
                        "l2": "256 MiB buffer written between timed steps"},
-            "graph_launches": int(ctx.launch_count - l0),
+            "graph_launches": graph_launches,
             "clocks": sampler.summary()}
     print(json.dumps(line), flush=True)
     graph.close()
@@ -689,8 +707,9 @@ def run_animated(args):
             step(k)
             ev[i][1].record(stream)
         torch.cuda.synchronize()
-        sampler.__exit__()
         launches = ctx.launch_count - l0
+        sampler.extend(lambda: step(frames - 1), torch.cuda.synchronize)
+        sampler.__exit__()
         # wall clock of the same loop without per-step events (host work included)
         host[:] = 0
         torch.cuda.synchronize()
@@ -814,8 +833,9 @@ def run_compat(args):
             frame(k)
             ev[k][1].record(stream)
         torch.cuda.synchronize()
-        sampler.__exit__()
         launches = ctx.launch_count - l0
+        sampler.extend(lambda: frame(args.steps - 1), torch.cuda.synchronize)
+        sampler.__exit__()
         ctx.set_timing(True)
         stages = {}
         for k in range(min(args.steps, 8)):
@@ -935,8 +955,9 @@ def run_precision(args):
                 frame(k)
                 ev[k][1].record(stream)
             torch.cuda.synchronize()
-            sampler.__exit__()
             launches = ctx.launch_count - l0
+            sampler.extend(lambda: frame(args.steps - 1), torch.cuda.synchronize)
+            sampler.__exit__()
             ctx.set_timing(True)
             stages = {}
             for k in range(min(args.steps, 4)):

@@ -72,9 +72,17 @@ __device__ __forceinline__ float4 march_thread(const VolDesc& vd, const CamDesc&
     const float D = (float)vd.D;
     const float vsx = D / vd.range[0], vsy = D / vd.range[1], vsz = D / vd.range[2];
     const float pixk = cam.tanh / (float)cam.H * vsx;
+    // when every sample has lod 0, steps outside the occupied box read 0
+    int kbeg = 0, kend = Nv;
+    if (2.f * (tin + ((float)(Nv - 1) + 0.5f) * dt) * pixk <= 1.f) {
+        int k0, k1;
+        cgs::occupied_steps(vd, cam.eye, d, tin, dt, Nv, k0, k1);
+        kbeg = k0;
+        kend = k1 + 1;
+    }
     float T = 1.f, C = 0.f, Cc = 0.f;
 #pragma unroll UNROLL
-    for (int k = 0; k < Nv; ++k) {
+    for (int k = kbeg; k < kend; ++k) {
         float t = tin + ((float)k + 0.5f) * dt;
         float p0 = cam.eye[0] + t * d.x, p1 = cam.eye[1] + t * d.y, p2 = cam.eye[2] + t * d.z;
         float v0 = (p0 - vd.wmin[0]) * vsx, v1 = (p1 - vd.wmin[1]) * vsy,
@@ -111,15 +119,26 @@ __device__ __forceinline__ float4 march_group(const VolDesc& vd, const CamDesc& 
     const float D = (float)vd.D;
     const float vsx = D / vd.range[0], vsy = D / vd.range[1], vsz = D / vd.range[2];
     const float pixk = cam.tanh / (float)cam.H * vsx;
+    // when every sample has lod 0, steps outside the occupied box read 0: the
+    // group starts at the box's first step (rounded down to whole groups of
+    // steps) and ends after its last
+    int kbeg = 0, kend = Nv;
+    if (hit && 2.f * (tin + ((float)(Nv - 1) + 0.5f) * dt) * pixk <= 1.f) {
+        int k0, k1;
+        cgs::occupied_steps(vd, cam.eye, d, tin, dt, Nv, k0, k1);
+        kbeg = k0;
+        kend = k1 + 1;
+    }
     float T = 1.f, C = 0.f, Cc = 0.f;
-    bool run = hit;  // the group's ray has not terminated
+    bool run = hit && kbeg < kend;  // the group's ray has not terminated
+    const int base0 = __reduce_min_sync(0xffffffffu, run ? kbeg - kbeg % LPR : Nv);
 #pragma unroll UNROLL
-    for (int base = 0; base < Nv; base += LPR) {
+    for (int base = base0; base < Nv; base += LPR) {
         if (!__any_sync(0xffffffffu, run)) break;
         // ---- this lane's step: position, density, noise, opacity
         const int k = base + j;
         float v0 = 0.f, v1 = 0.f, v2 = 0.f, alpha = 0.f, G = 0.f;
-        if (run && k < Nv) {
+        if (run && k < kend) {
             float t = tin + ((float)k + 0.5f) * dt;
             float p0 = cam.eye[0] + t * d.x, p1 = cam.eye[1] + t * d.y, p2 = cam.eye[2] + t * d.z;
             v0 = (p0 - vd.wmin[0]) * vsx;
@@ -169,7 +188,7 @@ __device__ __forceinline__ float4 march_group(const VolDesc& vd, const CamDesc& 
             if (ci) cgs::neumaier(C, Cc, ti);
         }
         T = Tg;
-        run = going && base + LPR < Nv;
+        run = going && base + LPR < kend;
     }
     C += Cc;
     if (!hit) return make_float4(0.f, 0.f, 0.f, 0.f);
