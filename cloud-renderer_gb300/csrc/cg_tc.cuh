@@ -30,10 +30,11 @@ __device__ __forceinline__ uint32_t sw32_offset(int row, int chunk) {
 }
 
 // Descriptor of a 32B-swizzled K-major tile (K = 16 FP16 per row): stride
-// byte offset 256 (one 8-row atom), layout SWIZZLE_32B (6).
-__device__ __forceinline__ uint64_t desc_sw32(uint32_t saddr) {
+// byte offset `sbo` between 8-row atoms (256 for a dense tile; 0 makes every
+// row group read the same atom), layout SWIZZLE_32B (6).
+__device__ __forceinline__ uint64_t desc_sw32(uint32_t saddr, uint32_t sbo = 256u) {
     return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) |
-           ((uint64_t)(256 >> 4) << 32) | ((uint64_t)1 << 46) | ((uint64_t)6 << 61);
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46) | ((uint64_t)6 << 61);
 }
 
 // Shared memory matrix descriptor: start address, leading byte offset (unused

@@ -41,35 +41,32 @@ namespace {
 constexpr uint32_t TC_TMEM_COLS = 64;
 constexpr uint64_t TC_WAIT_NS = 1000000000ull;  // 1 s: a wait longer than this is a fault
 // shared memory map (bytes from the 1024-aligned base)
-constexpr int OFF_ACT = 0;                 // 128 x 128 B activation tile
-constexpr int OFF_W1 = 16384;              // 64 x 128 B (K = 16 used)
-constexpr int OFF_W2 = OFF_W1 + 8192;      // 64 x 128 B
-constexpr int OFF_W3 = OFF_W2 + 8192;      // 64 x 128 B
-constexpr int OFF_ONES = OFF_W3 + 8192;    // 128 x 32 B: each row (1, 1, 0, ...) (SW32)
-constexpr int OFF_BIAS = OFF_ONES + 4096;  // 3 x (64 x 32 B): row n (b_hi[n], b_lo[n], 0, ...)
+constexpr int CTAS_PER_SM = 5;
+constexpr int OFF_ACT = 0;                 // 128 x 128 B activation tile (SW128)
+constexpr int OFF_W2 = 16384;              // 64 x 128 B (SW128)
+constexpr int OFF_W3 = OFF_W2 + 8192;      // 64 x 128 B (SW128)
+constexpr int OFF_W1 = OFF_W3 + 8192;      // 64 x 32 B (K = 16, SW32)
+constexpr int OFF_ONES = OFF_W1 + 2048;    // one 8-row atom: each row (1, 1, 0, ...) (SW32)
+constexpr int OFF_BIAS = OFF_ONES + 256;   // 3 x (64 x 32 B): row n (b_hi[n], b_lo[n], 0, ...)
 constexpr int OFF_BAR = OFF_BIAS + 3 * 2048;  // mbarrier + tensor-memory address
 constexpr int SMEM_USED = OFF_BAR + 32;
 constexpr int SMEM_BYTES = SMEM_USED + 1024;  // + alignment slack
 
 constexpr uint32_t IDESC = tc::idesc_f16_f32(128, 64);
 
-// One FP16 weight row (`chunks` x 8 halves, the rest zero) into row r of a
-// swizzled tile, optionally scaled by 1/2.
-__device__ __forceinline__ void stage_row(uint8_t* tile, int r, const __half* src, int chunks,
-                                          bool half_scale) {
+// One FP16 weight row (`chunks` x 8 halves) into row r of a swizzled tile
+// (128B-swizzled rows of 8 chunks, or 32B-swizzled rows of 2), scaled by 1/2.
+template <int CHUNKS>
+__device__ __forceinline__ void stage_row(uint8_t* tile, int r, const __half* src) {
     const __half2 k = __floats2half2_rn(0.5f, 0.5f);
 #pragma unroll
-    for (int c = 0; c < 8; ++c) {
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (c < chunks) {
-            v = *reinterpret_cast<const uint4*>(src + 8 * c);
-            if (half_scale) {
-                __half2* h = reinterpret_cast<__half2*>(&v);
+    for (int c = 0; c < CHUNKS; ++c) {
+        uint4 v = *reinterpret_cast<const uint4*>(src + 8 * c);
+        __half2* h = reinterpret_cast<__half2*>(&v);
 #pragma unroll
-                for (int q = 0; q < 4; ++q) h[q] = __hmul2(h[q], k);
-            }
-        }
-        *reinterpret_cast<uint4*>(tile + tc::sw128_offset(r, c)) = v;
+        for (int q = 0; q < 4; ++q) h[q] = __hmul2(h[q], k);
+        *reinterpret_cast<uint4*>(tile + (CHUNKS == 8 ? tc::sw128_offset(r, c)
+                                                      : tc::sw32_offset(r, c))) = v;
     }
 }
 
@@ -152,29 +149,36 @@ __device__ __forceinline__ unsigned slot_at(const SampleBuf& sb, unsigned tile, 
 
 // Issue one layer (thread 0) and commit it to the barrier: the K slices of
 // the activations, then one more K = 16 slice that adds the bias (a column of
-// ones against the split bias b_hi + b_lo, exact to ~2^-22 relative).
+// ones against the split bias b_hi + b_lo, exact to ~2^-22 relative).  The
+// ones operand is a single 8-row atom read by all 16 row groups (stride byte
+// offset 0); W1 (K = 16) is a 32B-swizzled tile.
 __device__ __forceinline__ void issue_layer(int layer, uint32_t d_tmem, uint32_t a_addr,
                                             uint32_t w_addr, uint32_t ones_addr,
                                             uint32_t bias_addr, uint64_t* bar) {
-    const int ksteps = layer == 0 ? 1 : 4;
-    for (int k = 0; k < ksteps; ++k)
-        tc::mma_f16(d_tmem, tc::desc_sw128(a_addr + 32u * k), tc::desc_sw128(w_addr + 32u * k),
-                    IDESC, k > 0 ? 1u : 0u);
-    tc::mma_f16(d_tmem, tc::desc_sw32(ones_addr), tc::desc_sw32(bias_addr), IDESC, 1u);
+    if (layer == 0) {
+        tc::mma_f16(d_tmem, tc::desc_sw128(a_addr), tc::desc_sw32(w_addr), IDESC, 0u);
+    } else {
+        for (int k = 0; k < 4; ++k)
+            tc::mma_f16(d_tmem, tc::desc_sw128(a_addr + 32u * k),
+                        tc::desc_sw128(w_addr + 32u * k), IDESC, k > 0 ? 1u : 0u);
+    }
+    tc::mma_f16(d_tmem, tc::desc_sw32(ones_addr, 0u), tc::desc_sw32(bias_addr), IDESC, 1u);
     tc::mma_commit(bar);
 }
 
 // All writes of the CTA to the activation tiles -> visible to the tensor
-// core, then one thread issues.
-__device__ __forceinline__ void sync_for_mma() {
+// core, then one thread issues.  The same barrier agrees on a failed wait of
+// any thread (true: the CTA stops before issuing).
+__device__ __forceinline__ bool sync_for_mma(bool bad) {
     tc::fence_proxy_async();
     tc::fence_before_sync();
-    __syncthreads();
+    const bool any_bad = __syncthreads_or(bad) != 0;
     tc::fence_after_sync();
+    return any_bad;
 }
 
 template <int FMT>
-__global__ void __launch_bounds__(128, 4)
+__global__ void __launch_bounds__(128, CTAS_PER_SM)
     k_shade_mlp_tc(const __grid_constant__ VolDesc vd, const __grid_constant__ TraceParams tp,
                    const __grid_constant__ ConeSchedule cone, const __grid_constant__ MlpDev m,
                    const __grid_constant__ FeatGeom geo, SampleBuf sb,
@@ -190,18 +194,21 @@ __global__ void __launch_bounds__(128, 4)
 
     // ---- stage weights: W1..W3 scaled by 1/2
     for (int r = tid; r < 64; r += blockDim.x) {
-        stage_row(base + OFF_W1, r, m.w16 + MLP_H_W1 + r * 16, 2, true);
-        stage_row(base + OFF_W2, r, m.w16 + MLP_H_W2 + r * 64, 8, true);
-        stage_row(base + OFF_W3, r, m.w16 + MLP_H_W3 + r * 64, 8, true);
+        stage_row<2>(base + OFF_W1, r, m.w16 + MLP_H_W1 + r * 16);
+        stage_row<8>(base + OFF_W2, r, m.w16 + MLP_H_W2 + r * 64);
+        stage_row<8>(base + OFF_W3, r, m.w16 + MLP_H_W3 + r * 64);
     }
-    // the ones column and the split half-scaled biases (32B-swizzled, K = 16)
-    {
+    // the ones column (8 rows) and the split half-scaled biases (32B-swizzled,
+    // K = 16)
+    if (tid < 8) {
         const __half one = __float2half_rn(1.f);
         const uint32_t ones = (uint32_t)__half_as_ushort(one) | ((uint32_t)__half_as_ushort(one) << 16);
         *reinterpret_cast<uint4*>(base + OFF_ONES + tc::sw32_offset(tid, 0)) =
             make_uint4(ones, 0u, 0u, 0u);
         *reinterpret_cast<uint4*>(base + OFF_ONES + tc::sw32_offset(tid, 1)) =
             make_uint4(0u, 0u, 0u, 0u);
+    }
+    {
         for (int i = tid; i < 3 * 64; i += blockDim.x) {
             const int l = i >> 6, n = i & 63;
             const float hb = m.k.hb[i];
@@ -236,7 +243,7 @@ __global__ void __launch_bounds__(128, 4)
     const unsigned total = *sb.flat_total;
     const unsigned ntiles = (total + 127u) / 128u;
     unsigned phase = 0, n_fallback = 0, n_valid = 0;
-    bool failed = false;
+    bool failed = false, bad = false;  // bad: a wait of this warp ran out
 
     // ---- the first tile's inputs
     unsigned tile = blockIdx.x;
@@ -264,7 +271,10 @@ __global__ void __launch_bounds__(128, 4)
         float y = 0.f;
 #pragma unroll
         for (int layer = 0; layer < 3; ++layer) {
-            sync_for_mma();
+            if (sync_for_mma(bad)) {  // a commit of parity `phase` is still pending
+                failed = true;
+                break;
+            }
             if (tid == 0) {
                 issue_layer(layer, tmem, a_addr, w_addr[layer], ones_addr,
                             bias_addr + 2048u * layer, bar);
@@ -280,18 +290,16 @@ __global__ void __launch_bounds__(128, 4)
                 ng = sb.light_lane[nslot].x;
             }
             if (layer == 2) fetch_features(geo, tp, nslot, ns, nf);
-            const bool ok = tc::mbar_wait(bar, phase, TC_WAIT_NS);
-            if (__syncthreads_or(!ok)) {  // the commit of parity `phase` is still pending
-                failed = true;
-                break;
-            }
-            phase ^= 1u;
+            // a warp whose wait ran out skips the epilogue (no tensor-memory
+            // read under a running MMA) and the CTA stops at the next barrier
+            bad = __any_sync(0xffffffffu, !tc::mbar_wait(bar, phase, TC_WAIT_NS));
+            if (!bad) phase ^= 1u;
             tc::fence_after_sync();
             // ---- epilogue: TMEM -> bias + SiLU, 32 columns at a time; the
             // last layer folds the 64 -> 1 output in FP32
             float yy = m.k.b4;
 #pragma unroll
-            for (int half = 0; half < 2; ++half) {
+            for (int half = 0; half < 2 && !bad; ++half) {
                 uint32_t acc[32];
                 tc::tmem_ld32(dw + 32u * half, acc);
                 uint32_t h[16];
@@ -316,7 +324,7 @@ __global__ void __launch_bounds__(128, 4)
         }
         if (failed) break;
         // ---- output
-        if (row.slot != CG_NO_SLOT) {
+        if (row.slot != CG_NO_SLOT && !bad) {
             n_valid++;
             float tau;
             if (row.tau_fb >= 0.f) {
@@ -332,9 +340,11 @@ __global__ void __launch_bounds__(128, 4)
         tile = ntile;
         ntile = *s_claim;  // written at layer 0, two barriers ago
     }
+    if (!failed) failed = sync_for_mma(bad);  // the last tile's waits
     if (failed) {
-        // drain the outstanding commit (bounded), then report
-        tc::mbar_wait(bar, phase, TC_WAIT_NS);
+        // drain the outstanding commit (bounded; only warps whose wait ran out
+        // have one: no MMA is issued after a failed barrier), then report
+        if (bad) tc::mbar_wait(bar, phase, TC_WAIT_NS);
         if (tid == 0) atomicOr(status + 1, 1ull);
     }
     unsigned tot = n_fallback, nv = n_valid;
@@ -383,8 +393,8 @@ cudaError_t launch_shade_mlp_tc(VolDesc vd, CamDesc cam, TraceParams tp, const M
     (void)cam;
     ConeSchedule cone = make_cone_schedule(vd, tp);
     const FeatGeom geo = feat_geom(vd, m);
-    // one persistent wave: 4 CTAs per SM (the register and shared-memory
-    // budgets of __launch_bounds__(128, 4); 4 x 64 tensor-memory columns)
+    // one persistent wave: CTAS_PER_SM CTAs per SM (the register and
+    // shared-memory budgets of __launch_bounds__; 64 tensor-memory columns each)
     // (the per-device launch shape and the shared-memory attribute are
     // configured once; atomics keep concurrent host threads well-defined)
     static std::atomic<int> grid[2][64];
@@ -400,7 +410,7 @@ cudaError_t launch_shade_mlp_tc(VolDesc vd, CamDesc cam, TraceParams tp, const M
         int sms = 0;
         e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (e != cudaSuccess) return e;
-        grid[f][dev].store(sms * 4, std::memory_order_release);
+        grid[f][dev].store(sms * CTAS_PER_SM, std::memory_order_release);
     }
     const int blocks = grid[f][dev].load(std::memory_order_acquire);
     if (f == 0)

@@ -220,9 +220,22 @@ __device__ __forceinline__ void texel_range(float lo, float hi, float c, float r
     b = (int)fb;
 }
 
-// One CTA per board; threads sweep the board's texel box.
+// One CTA per board.  The texel-centre coordinates of the board's box are
+// tabulated once (one division per column and per row instead of two per
+// texel); each warp then takes rows and sweeps, with consecutive lanes on
+// consecutive texels, only the columns of the row's chord through the disc
+// (d^2 <= 1.0001 r^2, widened by one texel each side; the per-texel test
+// below still applies, so the chord only drops texels it would reject).
+constexpr int SUN_TAB = 1024;
+
+__device__ __forceinline__ float sun_x(const SunFrame& fr, const float* tab, bool tabbed, int ia,
+                                       int ti) {
+    return tabbed ? tab[ti - ia] : texel_coord(fr.lo, fr.hi, ti, fr.W);
+}
+
 __global__ void __launch_bounds__(256) k_sunmap(BoardsDev b, SunFrame fr,
                                                 unsigned long long* keys) {
+    __shared__ float s_x[SUN_TAB], s_y[SUN_TAB];
     const int i = blockIdx.x;
     if (i >= b.n) return;
     float4 c = b.cwr[i];
@@ -233,24 +246,46 @@ __global__ void __launch_bounds__(256) k_sunmap(BoardsDev b, SunFrame fr,
     texel_range(fr.lo, fr.hi, cv.y, r, fr.H, ja, jb);
     if (ia > ib || ja > jb) return;
     const int nx = ib - ia + 1, ny = jb - ja + 1;
-    const int total = nx * ny;
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-        int ti = ia + t % nx, tj = ja + t / nx;
-        float xv = texel_coord(fr.lo, fr.hi, ti, fr.W);
-        float yv = texel_coord(fr.lo, fr.hi, tj, fr.H);
-        // texels well outside the disc (d^2 > 1.0001 r^2, where the exact
-        // profile test cannot pass) skip the square roots and the division
-        {
-            const float ex = xv - cv.x, ey = yv - cv.y;
-            if (ex * ex + ey * ey > 1.0001f * (r * r)) continue;
+    const bool tabbed = nx <= SUN_TAB && ny <= SUN_TAB;
+    if (tabbed) {
+        for (int t = threadIdx.x; t < nx; t += blockDim.x)
+            s_x[t] = texel_coord(fr.lo, fr.hi, ia + t, fr.W);
+        for (int t = threadIdx.x; t < ny; t += blockDim.x)
+            s_y[t] = texel_coord(fr.lo, fr.hi, ja + t, fr.H);
+        __syncthreads();
+    }
+    const float r2 = 1.0001f * (r * r);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    const float span = fr.hi - fr.lo;
+    for (int row = warp; row < ny; row += nwarps) {
+        const int tj = ja + row;
+        const float yv = tabbed ? s_y[row] : texel_coord(fr.lo, fr.hi, tj, fr.H);
+        const float ey = yv - cv.y;
+        const float rem = r2 - ey * ey;
+        if (!(rem >= 0.f)) continue;  // the whole row is outside the disc
+        // the chord's texels, one texel of margin each side, within the box
+        const float w = sqrtf(rem);
+        int ca = (int)fmaxf(floorf((cv.x - w - fr.lo) / span * (float)fr.W - 0.5f) - 1.0f,
+                            (float)ia);
+        int cb = (int)fminf(ceilf((cv.x + w - fr.lo) / span * (float)fr.W - 0.5f) + 1.0f,
+                            (float)ib);
+        unsigned long long* krow = keys + (size_t)tj * fr.W;
+        for (int ti = ca + lane; ti <= cb; ti += 32) {
+            const float xv = sun_x(fr, s_x, tabbed, ia, ti);
+            // texels well outside the disc (d^2 > 1.0001 r^2, where the exact
+            // profile test cannot pass) skip the square roots and the division
+            {
+                const float ex = xv - cv.x;
+                if (ex * ex + ey * ey > r2) continue;
+            }
+            float zs, depth;
+            if (!sun_fragment(xv, yv, cv, r, fr.near_z, zs, depth)) continue;
+            unsigned long long key =
+                ((unsigned long long)__float_as_uint(depth) << 32) | (unsigned)i;
+            unsigned long long* k = krow + ti;
+            // values only decrease, so a stale read can only make this test pass
+            if (key < *(volatile unsigned long long*)k) atomicMin(k, key);
         }
-        float zs, depth;
-        if (!sun_fragment(xv, yv, cv, r, fr.near_z, zs, depth)) continue;
-        unsigned long long key =
-            ((unsigned long long)__float_as_uint(depth) << 32) | (unsigned)i;
-        unsigned long long* k = keys + (size_t)tj * fr.W + ti;
-        // values only decrease, so a stale read can only make this test pass
-        if (key < *(volatile unsigned long long*)k) atomicMin(k, key);
     }
 }
 
