@@ -416,11 +416,16 @@ __global__ void __launch_bounds__(64) k_splat(BoardsDev b, Bins bins, const uint
                                                VolDesc vd, void* pyr, uint32_t* count,
                                                uint32_t* dqout, int fused_levels,
                                                OccRaw occ_raw) {
-    __shared__ int4 sq[CG_SPLAT_CHUNK];
+    // the staged boards and, once every thread has left the board loop, the
+    // brick's level-0 tile share one buffer (more resident bricks per SM)
+    static_assert(CG_SPLAT_CHUNK * 28 <= CG_BRICK * CG_BRICK * CG_BRICK * 16,
+                  "board chunk larger than the tile it shares memory with");
+    __shared__ __align__(16) uint8_t s_buf[CG_BRICK * CG_BRICK * CG_BRICK * 16];
+    int4* sq = reinterpret_cast<int4*>(s_buf);
+    unsigned long long* sthr = reinterpret_cast<unsigned long long*>(s_buf + CG_SPLAT_CHUNK * 16);
+    uint32_t* sdq = reinterpret_cast<uint32_t*>(s_buf + CG_SPLAT_CHUNK * 24);
+    float4* tile = reinterpret_cast<float4*>(s_buf);
     __shared__ unsigned s_cells;  // raw occupancy of the brick's eight 4^3 cells
-    __shared__ unsigned long long sthr[CG_SPLAT_CHUNK];
-    __shared__ uint32_t sdq[CG_SPLAT_CHUNK];
-    __shared__ float4 tile[CG_BRICK * CG_BRICK * CG_BRICK];
     __shared__ float4 tile1[64];
     __shared__ float4 tile2[8];
 
@@ -473,33 +478,23 @@ __global__ void __launch_bounds__(64) k_splat(BoardsDev b, Bins bins, const uint
             }
         }
     }
-    float4 v[8];
+    if (COV) {
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        const int z = z0 + j;
-        const bool in = inxy && z < D;
-        const size_t i = ((size_t)z * D + y) * D + x;
-        v[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (!in) continue;
-        if (COV) {
+        for (int j = 0; j < 8; ++j) {
+            const int z = z0 + j;
+            if (!(inxy && z < D)) continue;
+            const size_t i = ((size_t)z * D + y) * D + x;
             count[i] = cnt[j];
             dqout[i] = dsum[j];
-            continue;
         }
-        const uint8_t mk = mask[i];
-        v[j].x = __uint2float_rn(dsum[j]) * (1.0f / 65536.0f);
-        v[j].y = mk ? 1.0f : 0.0f;
-        v[j].z = __uint2float_rn(cnt[j]);
-        v[j].w = (cnt[j] > 0u || mk) ? 1.0f : 0.0f;
-        store_voxel(vd, pyr, 0, x, y, z, v[j]);
+        return;
     }
-    if (COV) return;
     // Raw occupancy (4^3 cells, every level): the brick's eight level-0 cells
     // from its voxels, and at level l >= 1 the one cell holding the brick
     // (level-l cell = brick >> (l - 1)).  Idempotent byte stores into grids
     // cleared before the launch; k_occ_dilate builds the brick grids.
     if (tid == 0) s_cells = 0u;
-    __syncthreads();
+    __syncthreads();  // every thread has left the board loop: the tile may be written
     {
         // the warp's voxels lie in cell y = w & 1; voxel j in cell z = j >> 2;
         // lanes 0-3 of each row of 8 in x cell 0, lanes 4-7 in x cell 1
@@ -507,8 +502,20 @@ __global__ void __launch_bounds__(64) k_splat(BoardsDev b, Bins bins, const uint
         unsigned bits = 0u;
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-            const bool in = inxy && z0 + j < D;
-            const unsigned bal = __ballot_sync(0xffffffffu, in && v[j].x > 0.f);
+            const int z = z0 + j;
+            const bool in = inxy && z < D;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (in) {
+                const uint8_t mk = mask[((size_t)z * D + y) * D + x];
+                v.x = __uint2float_rn(dsum[j]) * (1.0f / 65536.0f);
+                v.y = mk ? 1.0f : 0.0f;
+                v.z = __uint2float_rn(cnt[j]);
+                v.w = (cnt[j] > 0u || mk) ? 1.0f : 0.0f;
+                store_voxel(vd, pyr, 0, x, y, z, v);
+            }
+            if (fused_levels > 0) tile[tid + 64 * j] = v;  // voxel (lx, ly, j)
+            // density v.x > 0 exactly when dsum > 0
+            const unsigned bal = __ballot_sync(0xffffffffu, in && dsum[j] > 0u);
             const int cz = 4 * (j >> 2);
             if (bal & 0x0F0F0F0Fu) bits |= 1u << (cy + cz);
             if (bal & 0xF0F0F0F0u) bits |= 1u << (cy + cz + 1);
@@ -543,9 +550,6 @@ __global__ void __launch_bounds__(64) k_splat(BoardsDev b, Bins bins, const uint
         }
     }
     if (fused_levels <= 0) return;
-#pragma unroll
-    for (int j = 0; j < 8; ++j) tile[tid + 64 * j] = v[j];  // voxel (lx, ly, j)
-    __syncthreads();
     // level 1: 4^3 parents
     if (tid < 64) {
         int px = tid & 3, py = (tid >> 2) & 3, pz = tid >> 4;
