@@ -6,6 +6,8 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <atomic>
+
 #include "cg_internal.h"
 
 namespace {
@@ -85,38 +87,49 @@ __global__ void k_bin_count(BoardsDev b, int D, Bins bins) { bin_walk<false>(b, 
 __global__ void k_bin_fill(BoardsDev b, int D, Bins bins) { bin_walk<true>(b, D, bins); }
 
 // Exclusive scan of the brick counts in one CTA; seeds the cursors.  Each
-// pass covers 1024 x 32 counts: every thread loads its 32 consecutive counts
-// with eight 16-byte loads issued together (one memory latency per pass
-// instead of one per 4096 counts), sums them, and a block scan of the thread
-// sums gives the offsets; a running carry links the passes.  count, offset
-// and cursor are 16-byte aligned.
+// pass covers 1024 x 32 counts staged in shared memory: coalesced 16-byte
+// loads into a padded array (one spare word per 32 counts, so that a
+// thread's 32 consecutive counts fall in 32 different banks), per-thread sums,
+// a block scan of the thread sums, the exclusive offsets written back in
+// place, then coalesced 16-byte stores of offsets and cursors.  A running
+// carry links the passes.  count, offset and cursor are 16-byte aligned.
+constexpr int SCAN_PER = 32;
+constexpr int SCAN_TILE = 1024 * SCAN_PER;
+constexpr int SCAN_SMEM = (SCAN_TILE + SCAN_TILE / 32) * 4;
+
+__device__ __forceinline__ int scan_slot(int e) { return e + (e >> 5); }
+
 __global__ void __launch_bounds__(1024) k_bin_scan(Bins bins) {
-    constexpr int PER = 32;
+    extern __shared__ uint32_t s_cnt[];
     __shared__ uint32_t warp_sums[32];
     __shared__ uint32_t carry_s;
     const int n = bins.nbricks;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     if (tid == 0) carry_s = 0;
-    __syncthreads();
-    for (int base = 0; base < n; base += 1024 * PER) {
-        const int i0 = base + tid * PER;
-        uint32_t c[PER];
-        if (i0 + PER <= n) {
+    for (int base = 0; base < n; base += SCAN_TILE) {
+        const int m = min(SCAN_TILE, n - base);
 #pragma unroll
-            for (int k = 0; k < PER; k += 4) {
-                const uint4 q = *reinterpret_cast<const uint4*>(bins.count + i0 + k);
-                c[k] = q.x;
-                c[k + 1] = q.y;
-                c[k + 2] = q.z;
-                c[k + 3] = q.w;
+        for (int j = 0; j < SCAN_TILE / 4096; ++j) {
+            const int e = 4 * tid + 4096 * j;
+            uint4 q = make_uint4(0u, 0u, 0u, 0u);
+            if (e + 3 < m) {
+                q = *reinterpret_cast<const uint4*>(bins.count + base + e);
+            } else {
+                if (e < m) q.x = bins.count[base + e];
+                if (e + 1 < m) q.y = bins.count[base + e + 1];
+                if (e + 2 < m) q.z = bins.count[base + e + 2];
             }
-        } else {
-#pragma unroll
-            for (int k = 0; k < PER; ++k) c[k] = (i0 + k < n) ? bins.count[i0 + k] : 0u;
+            const int sl = scan_slot(e);
+            s_cnt[sl] = q.x;
+            s_cnt[sl + 1] = q.y;
+            s_cnt[sl + 2] = q.z;
+            s_cnt[sl + 3] = q.w;
         }
+        __syncthreads();
+        uint32_t* mine = s_cnt + tid * (SCAN_PER + 1);
         uint32_t s = 0;
 #pragma unroll
-        for (int k = 0; k < PER; ++k) s += c[k];
+        for (int k = 0; k < SCAN_PER; ++k) s += mine[k];
         uint32_t x = s;
         for (int o = 1; o < 32; o <<= 1) {
             uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
@@ -135,32 +148,30 @@ __global__ void __launch_bounds__(1024) k_bin_scan(Bins bins) {
         __syncthreads();
         const uint32_t carry = carry_s;
         uint32_t run = carry + warp_sums[wid] + x - s;
-        if (i0 + PER <= n) {
 #pragma unroll
-            for (int k = 0; k < PER; k += 4) {
-                uint4 q;
-                q.x = run;
-                run += c[k];
-                q.y = run;
-                run += c[k + 1];
-                q.z = run;
-                run += c[k + 2];
-                q.w = run;
-                run += c[k + 3];
-                *reinterpret_cast<uint4*>(bins.offset + i0 + k) = q;
-                *reinterpret_cast<uint4*>(bins.cursor + i0 + k) = q;
-            }
-        } else {
-#pragma unroll
-            for (int k = 0; k < PER; ++k) {
-                if (i0 + k < n) {
-                    bins.offset[i0 + k] = run;
-                    bins.cursor[i0 + k] = run;
-                }
-                run += c[k];
-            }
+        for (int k = 0; k < SCAN_PER; ++k) {
+            const uint32_t c = mine[k];
+            mine[k] = run;
+            run += c;
         }
         __syncthreads();
+#pragma unroll
+        for (int j = 0; j < SCAN_TILE / 4096; ++j) {
+            const int e = 4 * tid + 4096 * j;
+            if (e >= m) continue;
+            const int sl = scan_slot(e);
+            const uint4 q = make_uint4(s_cnt[sl], s_cnt[sl + 1], s_cnt[sl + 2], s_cnt[sl + 3]);
+            if (e + 3 < m) {
+                *reinterpret_cast<uint4*>(bins.offset + base + e) = q;
+                *reinterpret_cast<uint4*>(bins.cursor + base + e) = q;
+            } else {
+                const uint32_t v[4] = {q.x, q.y, q.z, q.w};
+                for (int k = 0; e + k < m; ++k) {
+                    bins.offset[base + e + k] = v[k];
+                    bins.cursor[base + e + k] = v[k];
+                }
+            }
+        }
         if (tid == 1023) carry_s = carry + warp_sums[wid] + x;
         __syncthreads();
     }
@@ -255,6 +266,14 @@ __global__ void __launch_bounds__(256) k_sunmap(BoardsDev b, SunFrame fr,
         __syncthreads();
     }
     const float r2 = 1.0001f * (r * r);
+    // the surface offset dz = (cv.z + r * prof) + near_z over prof in [0, 1]
+    // spans [dz_lo, dz_hi] (rounded steps are monotone): its smallest square
+    float dz2_min = 0.0f;
+    {
+        const float dz_lo = fadd(cv.z, fr.near_z), dz_hi = fadd(fadd(cv.z, r), fr.near_z);
+        if (dz_lo > 0.0f) dz2_min = fmul(dz_lo, dz_lo);
+        else if (dz_hi < 0.0f) dz2_min = fmul(dz_hi, dz_hi);
+    }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
     const float span = fr.hi - fr.lo;
     for (int row = warp; row < ny; row += nwarps) {
@@ -278,13 +297,25 @@ __global__ void __launch_bounds__(256) k_sunmap(BoardsDev b, SunFrame fr,
                 const float ex = xv - cv.x;
                 if (ex * ex + ey * ey > r2) continue;
             }
+            unsigned long long* k = krow + ti;
+            // values only decrease, so a stale read can only make the tests
+            // below pass (never skip a winner)
+            const unsigned long long cur = *(volatile unsigned long long*)k;
+            // a certain loser skips the square roots and the division: this
+            // board's depth here is at least sqrt(xy2 + dz_min^2) (every step
+            // of the depth is monotone in |dz|), and a current depth whose
+            // square is below that by 2^-20 relative is strictly smaller as a
+            // float; an empty texel (all ones, a NaN) never skips
+            {
+                const float xy2 = fadd(fmul(xv, xv), fmul(yv, yv));
+                const float cd = __uint_as_float((unsigned)(cur >> 32));
+                if (cd * cd < fadd(xy2, dz2_min) * (1.0f - 0x1p-20f)) continue;
+            }
             float zs, depth;
             if (!sun_fragment(xv, yv, cv, r, fr.near_z, zs, depth)) continue;
             unsigned long long key =
                 ((unsigned long long)__float_as_uint(depth) << 32) | (unsigned)i;
-            unsigned long long* k = krow + ti;
-            // values only decrease, so a stale read can only make this test pass
-            if (key < *(volatile unsigned long long*)k) atomicMin(k, key);
+            if (key < cur) atomicMin(k, key);
         }
     }
 }
@@ -675,7 +706,20 @@ cudaError_t launch_bin_count(const BoardsDev& b, int D, Bins bins, cudaStream_t 
 }
 
 cudaError_t launch_bin_scan(Bins bins, cudaStream_t st) {
-    k_bin_scan<<<1, 1024, 0, st>>>(bins);
+    // the shared-memory attribute is set once per device (atomics keep
+    // concurrent host threads well-defined)
+    static std::atomic<bool> configured[64];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if (!configured[dev].load(std::memory_order_acquire)) {
+        e = cudaFuncSetAttribute(k_bin_scan, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 SCAN_SMEM);
+        if (e != cudaSuccess) return e;
+        configured[dev].store(true, std::memory_order_release);
+    }
+    k_bin_scan<<<1, 1024, SCAN_SMEM, st>>>(bins);
     return cudaGetLastError();
 }
 

@@ -82,7 +82,9 @@ def test_voxelize_full_1080p_scene_bit_exact(ctx):
     assert_voxelize_exact(vol, sun, ov)
 
 
-@pytest.mark.parametrize("dim,mips", [(2, 2), (20, 3), (96, 7), (128, 8)])
+# 264^3: 33^3 = 35937 bricks, more than one pass of the brick-count scan
+# (32768 per pass) with a ragged last pass
+@pytest.mark.parametrize("dim,mips", [(2, 2), (20, 3), (96, 7), (128, 8), (264, 4)])
 def test_voxelize_odd_sizes(ctx, dim, mips):
     pos, rad, den = random_scene(dim, 30, rmin=0.05, rmax=0.2)
     vol, sun, ov = make_pair(ctx, dim, mips, pos, rad, den, (-0.4, 0.8, 0.5), (97, 61))
