@@ -763,7 +763,15 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
     CG_LAUNCH(ctx, launch_occ_dilate(vd, raw_of(v), v->occ.as<uint8_t>() + v->raw_total,
                                      v->occ_total, s));
     // remaining mips (glGenerateMipmap, VoxelizeShader.cpp:105)
-    for (int l = fused; l + 1 < v->L; ++l) CG_LAUNCH(ctx, launch_mip_level(vd, v->pyr.p, l, s));
+    {
+        int l = fused;
+        for (; l + 1 < v->L; ++l) {
+            const long long np = v->dims[l + 1];
+            if (np * np * np <= CG_MIP_TAIL_MAX) break;
+            CG_LAUNCH(ctx, launch_mip_level(vd, v->pyr.p, l, s));
+        }
+        if (l + 1 < v->L) CG_LAUNCH(ctx, launch_mip_tail(vd, v->pyr.p, l, s));
+    }
     stage_mark(ctx, s, "mips");
     if (!capturing) {
         CG_CUDA(cudaEventRecord(v->boards_read, s));

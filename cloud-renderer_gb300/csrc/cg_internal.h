@@ -303,6 +303,10 @@ cudaError_t launch_splat(const BoardsDev& b, Bins bins, const uint8_t* mask, Vol
                          void* pyr, uint32_t* count, uint32_t* dq, int fused_levels,
                          OccRaw raw, bool coverage_only, cudaStream_t st);
 cudaError_t launch_mip_level(VolDesc vd, void* pyr, int l, cudaStream_t st);
+// levels l0+1 .. L-1 in one single-CTA launch (for levels of at most
+// CG_MIP_TAIL_MAX parents each)
+#define CG_MIP_TAIL_MAX 32768
+cudaError_t launch_mip_tail(VolDesc vd, void* pyr, int l0, cudaStream_t st);
 // Dilated occupancy grids of brick B = 1 << vd.occ_shift from the raw cells.
 // Builds the brick grids from the raw cells and grows the level-0 occupied
 // box (vd.occ_box, zeroed by the caller).

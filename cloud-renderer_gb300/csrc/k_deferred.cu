@@ -236,9 +236,31 @@ __global__ void __launch_bounds__(128) k_accumulate(CamDesc cam, TraceParams tp,
     const uint2* steps = sb.steps + (size_t)region * view_steps;
     const float4* pw = sb.pos_w + (size_t)region * sb.capacity;
     float acc = 0.f, comp = 0.f;
-    for (unsigned e = 0; e < ns; ++e) {
-        const uint2 st = steps[e];
-        if ((st.y >> lane) & 1u) cgs::neumaier(acc, comp, pw[st.x + __popc(st.y & below)].w);
+    // the step table in coalesced chunks of 32 entries (lane e holds entry e),
+    // broadcast by shuffles; eight steps' contributions are fetched before
+    // any is summed, and the sums run in step order
+    for (unsigned base = 0; base < ns; base += 32u) {
+        const unsigned m = min(32u, ns - base);
+        const uint2 st_l = lane < (int)m ? steps[base + lane] : make_uint2(0u, 0u);
+        for (unsigned e0 = 0; e0 < m; e0 += 8u) {
+            float v[8];
+            unsigned have = 0u;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int src = (int)(e0 + q) & 31;
+                const unsigned sx = __shfl_sync(0xffffffffu, st_l.x, src);
+                const unsigned sy = __shfl_sync(0xffffffffu, st_l.y, src);
+                v[q] = 0.f;
+                // entries past m are (0, 0): no lane emitted there
+                if (e0 + q < m && ((sy >> lane) & 1u)) {
+                    v[q] = pw[sx + __popc(sy & below)].w;
+                    have |= 1u << q;
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if ((have >> q) & 1u) cgs::neumaier(acc, comp, v[q]);
+        }
     }
     int px, py;
     region_pixel(region, lane, tiles_x, px, py);

@@ -670,13 +670,11 @@ __global__ void __launch_bounds__(256) k_occ_dilate(VolDesc vd, OccRaw raw, uint
     }
 }
 
-// Generic 2x2x2 reduction from level l to l+1 (one thread per parent).
-__global__ void k_mip_level(VolDesc vd, void* pyr, int l) {
-    const int Nc = vd.dims[l], Np = vd.dims[l + 1];
-    const long long total = (long long)Np * Np * Np;
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= total) return;
-    int x = (int)(i % Np), y = (int)((i / Np) % Np), z = (int)(i / ((long long)Np * Np));
+// Parent (x, y, z) of level l + 1 as the mean of its 2x2x2 children at level
+// l (clamped at odd edges).
+__device__ __forceinline__ void mip_parent(const VolDesc& vd, void* pyr, int l, int x, int y,
+                                           int z) {
+    const int Nc = vd.dims[l];
     int cx0 = min(2 * x, Nc - 1), cx1 = min(2 * x + 1, Nc - 1);
     int cy0 = min(2 * y, Nc - 1), cy1 = min(2 * y + 1, Nc - 1);
     int cz0 = min(2 * z, Nc - 1), cz1 = min(2 * z + 1, Nc - 1);
@@ -685,6 +683,27 @@ __global__ void k_mip_level(VolDesc vd, void* pyr, int l) {
                     load_voxel(vd, pyr, l, cx0, cy0, cz1), load_voxel(vd, pyr, l, cx1, cy0, cz1),
                     load_voxel(vd, pyr, l, cx0, cy1, cz1), load_voxel(vd, pyr, l, cx1, cy1, cz1));
     store_voxel(vd, pyr, l + 1, x, y, z, m);
+}
+
+// Generic 2x2x2 reduction from level l to l+1 (one thread per parent).
+__global__ void k_mip_level(VolDesc vd, void* pyr, int l) {
+    const int Np = vd.dims[l + 1];
+    const long long total = (long long)Np * Np * Np;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    mip_parent(vd, pyr, l, (int)(i % Np), (int)((i / Np) % Np), (int)(i / ((long long)Np * Np)));
+}
+
+// The small levels l0+1 .. L-1 in one CTA, level after level (a block
+// barrier makes each level's stores visible to the next level's loads).
+__global__ void __launch_bounds__(1024) k_mip_tail(VolDesc vd, void* pyr, int l0) {
+    for (int l = l0; l + 1 < vd.L; ++l) {
+        const int Np = vd.dims[l + 1];
+        const int total = Np * Np * Np;
+        for (int i = threadIdx.x; i < total; i += blockDim.x)
+            mip_parent(vd, pyr, l, i % Np, (i / Np) % Np, i / (Np * Np));
+        __syncthreads();
+    }
 }
 
 __global__ void k_count_active(const uint32_t* count, const uint8_t* mask, size_t n,
@@ -778,6 +797,11 @@ cudaError_t launch_mip_level(VolDesc vd, void* pyr, int l, cudaStream_t st) {
     long long total = np * np * np;
     int blocks = (int)((total + 255) / 256);
     k_mip_level<<<blocks, 256, 0, st>>>(vd, pyr, l);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mip_tail(VolDesc vd, void* pyr, int l0, cudaStream_t st) {
+    k_mip_tail<<<1, 1024, 0, st>>>(vd, pyr, l0);
     return cudaGetLastError();
 }
 
