@@ -234,6 +234,7 @@ void context_release(cg_context* ctx) {
     ctx->noise.release();
     ctx->samples_pw.release();
     ctx->samples_gl.release();
+    ctx->samples_c.release();
     ctx->samples_cnt.release();
     ctx->fallbacks.release();
     ctx->stats_scratch.release();

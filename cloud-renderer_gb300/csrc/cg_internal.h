@@ -140,6 +140,7 @@ struct Bins {
 struct SampleBuf {
     float4* pos_w;
     float2* light_lane;
+    float* contrib;   // per slot: the sample's shaded contribution (surrogate path)
     unsigned* count;  // samples per region
     // flat order (written by the march): each march CTA's 8 regions occupy a
     // contiguous range, padded to 32-sample chunks; slot_of[i] = slot

@@ -12,11 +12,12 @@
 // Exact shading (k_shade_exact): one warp per region, 32 samples at a time,
 // then each pixel sums its own samples in step order (shuffle broadcast),
 // exactly the order of the fused kernel.
-// MLP shading: the region counts are scanned (k_region_scan); a persistent
-// kernel walks all samples in flat chunks of 32 -- every chunk full except
-// the last -- computing features, running the network on the tensor cores and
-// writing each sample's contribution in place (k_shade_mlp); k_accumulate
-// then sums each pixel's contributions in step order.
+// MLP shading: the march also lays the samples out in a flat order (each
+// CTA's regions reserve one contiguous range, padded to whole 32-sample
+// chunks); a persistent tensor-core kernel (k_shade_mlp_tc) walks that order
+// in 128-sample tiles, computing features, running the network and writing
+// each sample's contribution to the compact per-slot array; k_accumulate then
+// sums each pixel's contributions in step order.
 #include "cg_deferred.cuh"
 #include "cg_internal.h"
 #include "cg_mlp.cuh"
@@ -234,7 +235,7 @@ __global__ void __launch_bounds__(128) k_accumulate(CamDesc cam, TraceParams tp,
     const unsigned below = (1u << lane) - 1u;
     const unsigned ns = sb.nsteps[region];
     const uint2* steps = sb.steps + (size_t)region * view_steps;
-    const float4* pw = sb.pos_w + (size_t)region * sb.capacity;
+    const float* cw = sb.contrib + (size_t)region * sb.capacity;
     float acc = 0.f, comp = 0.f;
     // the step table in coalesced chunks of 32 entries (lane e holds entry e),
     // broadcast by shuffles; eight steps' contributions are fetched before
@@ -253,7 +254,7 @@ __global__ void __launch_bounds__(128) k_accumulate(CamDesc cam, TraceParams tp,
                 v[q] = 0.f;
                 // entries past m are (0, 0): no lane emitted there
                 if (e0 + q < m && ((sy >> lane) & 1u)) {
-                    v[q] = pw[sx + __popc(sy & below)].w;
+                    v[q] = cw[sx + __popc(sy & below)];
                     have |= 1u << q;
                 }
             }

@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(128, CTAS_PER_SM)
             } else {
                 tau = m.tau_scale * mlp::softplus(y);
             }
-            sb.pos_w[row.slot].w = row.w * __expf(-tp.sigma * tau) * (amb + (1.f - amb) * row.g);
+            sb.contrib[row.slot] = row.w * __expf(-tp.sigma * tau) * (amb + (1.f - amb) * row.g);
         }
         // ---- the next tile's inputs
         pack_row<FMT>(vd, cone, m, tp, nslot, ns, ng, nf, row, act);
