@@ -18,6 +18,8 @@
 // in 128-sample tiles, computing features, running the network and writing
 // each sample's contribution to the compact per-slot array; k_accumulate then
 // sums each pixel's contributions in step order.
+#include <type_traits>
+
 #include "cg_deferred.cuh"
 #include "cg_internal.h"
 #include "cg_mlp.cuh"
@@ -93,7 +95,8 @@ __global__ void __launch_bounds__(256) k_march(VolDesc vd, CamDesc cam, TracePar
     // this lane's sampled steps: when every sample has lod 0, steps outside the
     // occupied box read 0 and are skipped (the warp starts at its first one)
     int kb = 0, ke = Nv;
-    if (live && tin + ((float)(Nv - 1) + 0.5f) * dt < t_lod1) {
+    const bool lod0 = tin + ((float)(Nv - 1) + 0.5f) * dt < t_lod1;
+    if (live && lod0) {
         int k0, k1;
         cgs::occupied_steps(vd, cam.eye, d, tin, dt, Nv, k0, k1);
         kb = k0;
@@ -101,46 +104,61 @@ __global__ void __launch_bounds__(256) k_march(VolDesc vd, CamDesc cam, TracePar
         if (kb >= ke) live = false;
     }
     const int wkb = __reduce_min_sync(0xffffffffu, live ? kb : Nv);
-    for (int k = wkb; k < Nv; ++k) {
-        if (live && k >= ke) live = false;
-        if (!__any_sync(0xffffffffu, live)) break;
-        bool emit = false;
-        float v0 = 0.f, v1 = 0.f, v2 = 0.f, w = 0.f, G = 0.f;
-        if (live && k >= kb) {
-            float t = tin + ((float)k + 0.5f) * dt;
-            float p0 = cam.eye[0] + t * d.x, p1 = cam.eye[1] + t * d.y, p2 = cam.eye[2] + t * d.z;
-            v0 = (p0 - vd.wmin[0]) * vsx;
-            v1 = (p1 - vd.wmin[1]) * vsy;
-            v2 = (p2 - vd.wmin[2]) * vsz;
-            float lod = t < t_lod1 ? 0.f : log2f(fmaxf(1.f, 2.f * t * pixk));
-            float2 rg = HW ? cgs::quad_hw<true>(vd, v0, v1, v2, lod)
-                           : cgs::quad<FMT, true, true, true>(vd, v0, v1, v2, lod);
-            if (rg.x > 0.f) {
-                float rho = rg.x * (HW ? cgs::fbm_volume(tp, p0, p1, p2)
-                                       : cgs::fbm(tp, p0, p1, p2));
-                if (rho > 0.f) {
-                    float alpha = 1.f - (HW ? __expf(-tp.sigma * rho * dt) : expf(-tp.sigma * rho * dt));
-                    w = T * alpha;
-                    G = rg.y;
-                    emit = true;
-                    T *= 1.f - alpha;
-                    if (T < tp.cutoff) live = false;
+    // the steps, in one of two forms: when every live lane's samples have lod
+    // 0 (the warp-uniform common case), level 0 is sampled directly (the same
+    // texel reads as the lod path at lod 0, without the level arithmetic)
+    auto march = [&](auto lod0_form) {
+        constexpr bool LOD0 = decltype(lod0_form)::value;
+        for (int k = wkb; k < Nv; ++k) {
+            if (live && k >= ke) live = false;
+            if (!__any_sync(0xffffffffu, live)) break;
+            bool emit = false;
+            float v0 = 0.f, v1 = 0.f, v2 = 0.f, w = 0.f, G = 0.f;
+            if (live && k >= kb) {
+                float t = tin + ((float)k + 0.5f) * dt;
+                float p0 = cam.eye[0] + t * d.x, p1 = cam.eye[1] + t * d.y, p2 = cam.eye[2] + t * d.z;
+                v0 = (p0 - vd.wmin[0]) * vsx;
+                v1 = (p1 - vd.wmin[1]) * vsy;
+                v2 = (p2 - vd.wmin[2]) * vsz;
+                float2 rg;
+                if (LOD0) {
+                    rg = cgs::tri_hw<true>(vd, 0, v0, v1, v2);
+                } else {
+                    float lod = t < t_lod1 ? 0.f : log2f(fmaxf(1.f, 2.f * t * pixk));
+                    rg = HW ? cgs::quad_hw<true>(vd, v0, v1, v2, lod)
+                            : cgs::quad<FMT, true, true, true>(vd, v0, v1, v2, lod);
+                }
+                if (rg.x > 0.f) {
+                    float rho = rg.x * (HW ? cgs::fbm_volume(tp, p0, p1, p2)
+                                           : cgs::fbm(tp, p0, p1, p2));
+                    if (rho > 0.f) {
+                        float alpha = 1.f - (HW ? __expf(-tp.sigma * rho * dt) : expf(-tp.sigma * rho * dt));
+                        w = T * alpha;
+                        G = rg.y;
+                        emit = true;
+                        T *= 1.f - alpha;
+                        if (T < tp.cutoff) live = false;
+                    }
                 }
             }
+            const unsigned ballot = __ballot_sync(0xffffffffu, emit);
+            if (emit) {
+                const unsigned slot = cnt + __popc(ballot & ((1u << lane) - 1u));
+                pw[slot] = make_float4(v0, v1, v2, w);
+                gl[slot] = make_float2(G, __int_as_float(lane));
+            }
+            // step table: where this step's samples start and which lanes emitted
+            if (ballot) {
+                if (lane == 0) sb.steps[(size_t)region * Nv + nsteps] = make_uint2(cnt, ballot);
+                nsteps++;
+            }
+            cnt += __popc(ballot);
         }
-        const unsigned ballot = __ballot_sync(0xffffffffu, emit);
-        if (emit) {
-            const unsigned slot = cnt + __popc(ballot & ((1u << lane) - 1u));
-            pw[slot] = make_float4(v0, v1, v2, w);
-            gl[slot] = make_float2(G, __int_as_float(lane));
-        }
-        // step table: where this step's samples start and which lanes emitted
-        if (ballot) {
-            if (lane == 0) sb.steps[(size_t)region * Nv + nsteps] = make_uint2(cnt, ballot);
-            nsteps++;
-        }
-        cnt += __popc(ballot);
-    }
+    };
+    if (HW && __all_sync(0xffffffffu, !live || lod0))
+        march(std::true_type{});
+    else
+        march(std::false_type{});
     if (lane == 0) {
         sb.count[region] = cnt;
         sb.nsteps[region] = nsteps;
