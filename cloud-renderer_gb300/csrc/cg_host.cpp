@@ -398,6 +398,9 @@ extern "C" cg_status cg_volume_create(cg_context* ctx, int dimension, float boun
     if (e == cudaSuccess) e = v->bcount.ensure((size_t)v->bins.nbricks * 4);
     if (e == cudaSuccess) e = v->boff.ensure(((size_t)v->bins.nbricks + 1) * 4);
     if (e == cudaSuccess) e = v->bcursor.ensure((size_t)v->bins.nbricks * 4);
+    // every brick starts dirty: the pyramid's memory is uninitialised
+    if (e == cudaSuccess) e = v->bdirty.ensure((size_t)v->bins.nbricks);
+    if (e == cudaSuccess) e = cudaMemset(v->bdirty.p, 1, (size_t)v->bins.nbricks);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&v->boards_ready, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&v->boards_read, cudaEventDisableTiming);
     if (e != cudaSuccess) {
@@ -415,6 +418,7 @@ extern "C" void cg_volume_destroy(cg_volume* v) {
     cudaStreamSynchronize(v->ctx->stream);
     DevBuf* bufs[] = {&v->pyr, &v->count, &v->dq, &v->mask, &v->cwr, &v->q, &v->thr,
                       &v->dqb, &v->culled, &v->bcount, &v->boff, &v->bcursor, &v->blist,
+                      &v->bdirty,
                       &v->keys, &v->posmap, &v->scratch, &v->occ};
     for (DevBuf* b : bufs) b->release();
     v->h_stage.release();
@@ -722,6 +726,7 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
     bins.offset = v->boff.as<uint32_t>();
     bins.cursor = v->bcursor.as<uint32_t>();
     bins.list = v->blist.as<uint32_t>();
+    bins.dirty = v->bdirty.as<uint8_t>();
     VolDesc vd = desc_of(v);
     // once the surrogate renderer has built the texture copies, keep them
     // current from the voxelize stores instead of a copy pass
@@ -1250,6 +1255,7 @@ static cg_status ensure_coverage(const cg_volume* cv) {
     bins.offset = v->boff.as<uint32_t>();
     bins.cursor = v->bcursor.as<uint32_t>();
     bins.list = v->blist.as<uint32_t>();
+    bins.dirty = v->bdirty.as<uint8_t>();
     CG_LAUNCH(v->ctx, launch_splat(boards_of(v), bins, v->mask.as<uint8_t>(), desc_of(v), v->pyr.p,
                                    v->count.as<uint32_t>(), v->dq.as<uint32_t>(), 0,
                                    raw_of(v), true, s));

@@ -147,7 +147,7 @@ struct cg_volume {
     DevBuf cwr, q, thr, dqb, culled;
     HostBuf h_stage;
     Bins bins{};
-    DevBuf bcount, boff, bcursor, blist;
+    DevBuf bcount, boff, bcursor, blist, bdirty;
     // sun map
     int mapW = 0, mapH = 0;
     DevBuf keys, posmap;

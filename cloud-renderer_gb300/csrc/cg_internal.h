@@ -131,6 +131,10 @@ struct Bins {
     uint32_t* offset;  // nbricks + 1
     uint32_t* cursor;  // nbricks
     uint32_t* list;    // pairs
+    // per brick: 1 when its level-0 voxels (and fused levels 1-3) may hold
+    // non-zero values from an earlier voxelize; a brick without boards or
+    // highlights whose flag is 0 is already all zero and is not rewritten
+    uint8_t* dirty;    // nbricks
 };
 
 // ---- deferred renderer ----------------------------------------------------

@@ -525,7 +525,20 @@ __global__ void __launch_bounds__(64) k_splat(BoardsDev b, Bins bins, const uint
     // (level-l cell = brick >> (l - 1)).  Idempotent byte stores into grids
     // cleared before the launch; k_occ_dilate builds the brick grids.
     if (tid == 0) s_cells = 0u;
-    __syncthreads();  // every thread has left the board loop: the tile may be written
+    // the brick's highlight bits, then one block decision (which is also the
+    // barrier after the board loop: the tile may be written): a brick without
+    // boards or highlights whose voxels are still zero from an earlier
+    // voxelize writes nothing
+    unsigned mkb = 0u;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const int z = z0 + j;
+        if (inxy && z < D && mask[((size_t)z * D + y) * D + x]) mkb |= 1u << j;
+    }
+    const bool keep = n > 0u || __syncthreads_or(mkb != 0u);
+    if (!keep && !bins.dirty[brick]) return;
+    __syncthreads();  // every thread has read the flag
+    if (tid == 0) bins.dirty[brick] = keep ? 1 : 0;
     {
         // the warp's voxels lie in cell y = w & 1; voxel j in cell z = j >> 2;
         // lanes 0-3 of each row of 8 in x cell 0, lanes 4-7 in x cell 1
@@ -537,7 +550,7 @@ __global__ void __launch_bounds__(64) k_splat(BoardsDev b, Bins bins, const uint
             const bool in = inxy && z < D;
             float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
             if (in) {
-                const uint8_t mk = mask[((size_t)z * D + y) * D + x];
+                const bool mk = (mkb >> j) & 1u;
                 v.x = __uint2float_rn(dsum[j]) * (1.0f / 65536.0f);
                 v.y = mk ? 1.0f : 0.0f;
                 v.z = __uint2float_rn(cnt[j]);

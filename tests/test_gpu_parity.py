@@ -118,6 +118,35 @@ def test_empty_volume(ctx):
     assert np.all(img == 0)
 
 
+@pytest.mark.parametrize("fmt", [0, 1])
+def test_revoxelize_rewrites_vacated_bricks(ctx, fmt):
+    # bricks that held a cloud in one voxelize and hold nothing in the next are
+    # rewritten (zeros), bricks empty in both are left alone: the pyramid and
+    # its texture copies equal a fresh volume's after every voxelize
+    sun = cloudgb.Sun((0.3, 1.0, 0.2), 96, 64)
+    scenes = [random_scene(s, 24, spread=0.35) for s in (11, 12)] + [
+        (np.zeros((0, 3), np.float32), np.zeros(0, np.float32), np.zeros(0, np.float32)),
+        random_scene(13, 24, spread=0.35)]
+    reused = cloudgb.CloudVolume(64, configs.VOLUME_BOUNDS, configs.VOLUME_POSITION, 7, fmt=fmt,
+                                 ctx=ctx)
+    cam = cloudgb.Camera((0.5, 0.6, -1.2), (0.5, 0.5, 0.5), width=48, height=40)
+    shader = cloudgb.ConeTraceShader(viewSteps=32, vctSteps=8)
+    for pos, rad, den in scenes:
+        reused.set_billboards(pos, rad, den)
+        reused.update()
+        cloudgb.VoxelizeShader().voxelize(reused, sun)
+        fresh = cloudgb.CloudVolume(64, configs.VOLUME_BOUNDS, configs.VOLUME_POSITION, 7,
+                                    fmt=fmt, ctx=ctx)
+        fresh.set_billboards(pos, rad, den)
+        fresh.update()
+        cloudgb.VoxelizeShader().voxelize(fresh, sun)
+        for l in range(7):
+            assert np.array_equal(reused.read_level(l), fresh.read_level(l)), l
+        assert np.array_equal(shader.coneTrace(reused, cam), shader.coneTrace(fresh, cam))
+        fresh.close()
+    reused.close()
+
+
 def test_error_paths(ctx):
     vol = cloudgb.CloudVolume(16, configs.VOLUME_BOUNDS, configs.VOLUME_POSITION, 5, ctx=ctx)
     cam = cloudgb.Camera((0.5, 0.5, -1.5), (0.5, 0.5, 0.5), width=8, height=8)
