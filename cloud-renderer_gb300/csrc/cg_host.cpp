@@ -61,7 +61,14 @@ extern "C" cg_status cg_context_create(int device, cg_context** out) {
     cg_context* c = new cg_context();
     c->device = device;
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming);
     if (e != cudaSuccess) {
+        if (c->join_ev) cudaEventDestroy(c->join_ev);
+        if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+        if (c->side) cudaStreamDestroy(c->side);
+        if (c->stream) cudaStreamDestroy(c->stream);
         delete c;
         return fail(CG_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
     }
@@ -230,6 +237,7 @@ void context_release(cg_context* ctx) {
     if (--ctx->refs > 0) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    cudaStreamSynchronize(ctx->side);
     ctx->image.release();
     ctx->noise.release();
     ctx->samples_pw.release();
@@ -251,6 +259,9 @@ void context_release(cg_context* ctx) {
     release_noise_textures(ctx);
     for (cudaEvent_t e : ctx->marks)
         if (e) cudaEventDestroy(e);
+    cudaEventDestroy(ctx->fork_ev);
+    cudaEventDestroy(ctx->join_ev);
+    cudaStreamDestroy(ctx->side);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -741,9 +752,21 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
     if (v->ready_pending && s != ctx->stream && !capturing)
         CG_CUDA(cudaStreamWaitEvent(s, v->boards_ready, 0));
     stage_begin(ctx, s);
+    // the sun-view pass does not need the bins: it runs on the side stream
+    // while the binning (latency-bound, a few SMs busy) runs on s
+    cudaStream_t sd = ctx->side;
+    CG_CUDA(cudaEventRecord(ctx->fork_ev, s));
+    CG_CUDA(cudaStreamWaitEvent(sd, ctx->fork_ev, 0));
     // clearGPU (CloudVolume.cpp:96-100) + clearPositionMap (VoxelizeShader.cpp:185-187)
-    CG_CUDA(cudaMemsetAsync(v->keys.p, 0xFF, texels * 8, s));
-    CG_CUDA(cudaMemsetAsync(v->mask.p, 0, n0, s));
+    CG_CUDA(cudaMemsetAsync(v->keys.p, 0xFF, texels * 8, sd));
+    CG_CUDA(cudaMemsetAsync(v->mask.p, 0, n0, sd));
+    // pass 1: sun-view nearest-surface map
+    if (b.n) CG_LAUNCH(ctx, launch_sunmap(b, fr, v->keys.as<uint64_t>(), sd));
+    // pass 2: highlight stores
+    CG_LAUNCH(ctx, launch_highlight(b, fr, v->keys.as<uint64_t>(), v->posmap.as<float4>(), v->D,
+                                    v->wmin, v->range, highlight_offset(v),
+                                    v->mask.as<uint8_t>(), sd));
+    CG_CUDA(cudaEventRecord(ctx->join_ev, sd));
     CG_CUDA(cudaMemsetAsync(bins.count, 0, (size_t)bins.nbricks * 4, s));
     // raw cells, brick grids (rewritten by the dilation) and the occupied box
     CG_CUDA(cudaMemsetAsync(v->occ.p, 0, occ_box_offset(v->raw_total) + 6 * sizeof(int), s));
@@ -752,14 +775,9 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
     CG_LAUNCH(ctx, launch_bin_scan(bins, s));
     if (b.n) CG_LAUNCH(ctx, launch_bin_fill(b, v->D, bins, s));
     stage_mark(ctx, s, "bins");
-    // pass 1: sun-view nearest-surface map
-    if (b.n) CG_LAUNCH(ctx, launch_sunmap(b, fr, v->keys.as<uint64_t>(), s));
-    stage_mark(ctx, s, "sunmap");
-    // pass 2: highlight stores
-    CG_LAUNCH(ctx, launch_highlight(b, fr, v->keys.as<uint64_t>(), v->posmap.as<float4>(), v->D,
-                                    v->wmin, v->range, highlight_offset(v),
-                                    v->mask.as<uint8_t>(), s));
-    stage_mark(ctx, s, "highlight");
+    CG_CUDA(cudaStreamWaitEvent(s, ctx->join_ev, 0));
+    // the sun-view pass's time beyond the binning
+    stage_mark(ctx, s, "sun");
     // coverage splat + level 0 + fused mips
     int fused = (v->D % CG_BRICK == 0) ? std::min(CG_FUSED_MIPS, v->L - 1) : 0;
     CG_LAUNCH(ctx, launch_splat(b, bins, v->mask.as<uint8_t>(), vd, v->pyr.p,

@@ -80,6 +80,10 @@ struct HostBuf {
 struct cg_context {
     int device = 0;
     cudaStream_t stream = nullptr;
+    // voxelize: the sun-view pass (sun map + highlights) runs on `side`,
+    // concurrently with the brick binning, forked and joined by two events
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     uint64_t launches = 0;
     int refs = 1;  // the caller's handle + one per volume / model created on it
     bool shaded_valid = false;  // the status words hold a surrogate render's counters
