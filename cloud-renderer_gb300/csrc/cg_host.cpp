@@ -784,8 +784,13 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
                                 v->count.as<uint32_t>(), v->dq.as<uint32_t>(), fused,
                                 raw_of(v), false, s));
     stage_mark(ctx, s, "splat");
+    // the occupancy dilation (raw cells -> brick grids, occupied box) and the
+    // remaining mips are independent: the dilation runs on the side stream
+    CG_CUDA(cudaEventRecord(ctx->fork_ev, s));
+    CG_CUDA(cudaStreamWaitEvent(sd, ctx->fork_ev, 0));
     CG_LAUNCH(ctx, launch_occ_dilate(vd, raw_of(v), v->occ.as<uint8_t>() + v->raw_total,
-                                     v->occ_total, s));
+                                     v->occ_total, sd));
+    CG_CUDA(cudaEventRecord(ctx->join_ev, sd));
     // remaining mips (glGenerateMipmap, VoxelizeShader.cpp:105)
     {
         int l = fused;
@@ -796,6 +801,7 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
         }
         if (l + 1 < v->L) CG_LAUNCH(ctx, launch_mip_tail(vd, v->pyr.p, l, s));
     }
+    CG_CUDA(cudaStreamWaitEvent(s, ctx->join_ev, 0));
     stage_mark(ctx, s, "mips");
     if (!capturing) {
         CG_CUDA(cudaEventRecord(v->boards_read, s));
