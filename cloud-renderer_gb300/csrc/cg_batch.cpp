@@ -224,7 +224,7 @@ struct cg_frame_graph {
 namespace {
 
 void buffers_of(const cg_volume* v, std::vector<const void*>& out) {
-    const void* p[] = {v->cwr.p, v->q.p, v->thr.p, v->dqb.p, v->culled.p, v->blist.p,
+    const void* p[] = {v->cwr, v->q, v->thr, v->dqb, v->culled, v->blist.p,
                        v->pyr.p, v->keys.p, v->posmap.p, v->mask.p, v->occ.p, v->bdirty.p};
     out.insert(out.end(), p, p + sizeof(p) / sizeof(p[0]));
     out.push_back(reinterpret_cast<const void*>((uintptr_t)v->n));

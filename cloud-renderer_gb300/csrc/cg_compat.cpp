@@ -171,7 +171,7 @@ extern "C" cg_status cg_render_compat(cg_context* ctx, const cg_volume* v, const
     std::memset(&P, 0, sizeof(P));
     P.cam = cd;
     P.n = v->n;
-    P.cwr = v->cwr.as<const float4>();
+    P.cwr = v->cwr;
     P.tiles_x = (cam->width + CG_COMPAT_TILE - 1) / CG_COMPAT_TILE;
     P.tiles_y = (cam->height + CG_COMPAT_TILE - 1) / CG_COMPAT_TILE;
     P.near_z = params->near_plane;

@@ -427,8 +427,8 @@ extern "C" void cg_volume_destroy(cg_volume* v) {
     if (!v) return;
     cudaSetDevice(v->ctx->device);
     cudaStreamSynchronize(v->ctx->stream);
-    DevBuf* bufs[] = {&v->pyr, &v->count, &v->dq, &v->mask, &v->cwr, &v->q, &v->thr,
-                      &v->dqb, &v->culled, &v->bcount, &v->boff, &v->bcursor, &v->blist,
+    DevBuf* bufs[] = {&v->pyr, &v->count, &v->dq, &v->mask, &v->boards,
+                      &v->bcount, &v->boff, &v->bcursor, &v->blist,
                       &v->bdirty,
                       &v->keys, &v->posmap, &v->scratch, &v->occ};
     for (DevBuf* b : bufs) b->release();
@@ -549,20 +549,17 @@ extern "C" cg_status cg_volume_set_billboards(cg_volume* v, const float* positio
     }
     CG_CHECK(pairs < (size_t)0xFFFFFFFFu, CG_ERR_OUT_OF_RANGE,
              "cg_volume_set_billboards: %zu board-brick pairs exceed 2^32", pairs);
-    CG_CUDA(v->cwr.ensure(bytes_cwr));
-    CG_CUDA(v->q.ensure(bytes_q));
-    CG_CUDA(v->thr.ensure(bytes_thr));
-    CG_CUDA(v->dqb.ensure(bytes_dq));
-    CG_CUDA(v->culled.ensure(bytes_cul));
+    // the device records mirror the staging layout: one copy uploads them all
+    CG_CUDA(v->boards.ensure(total));
+    char* dev = v->boards.as<char>();
+    v->cwr = reinterpret_cast<float4*>(dev + o_cwr);
+    v->q = reinterpret_cast<int4*>(dev + o_q);
+    v->thr = reinterpret_cast<uint64_t*>(dev + o_thr);
+    v->dqb = reinterpret_cast<uint32_t*>(dev + o_dq);
+    v->culled = reinterpret_cast<uint8_t*>(dev + o_cul);
     CG_CUDA(v->blist.ensure(pairs * 4));
     cudaStream_t s = v->ctx->stream;
-    if (n) {
-        CG_CUDA(cudaMemcpyAsync(v->cwr.p, cwr, bytes_cwr, cudaMemcpyHostToDevice, s));
-        CG_CUDA(cudaMemcpyAsync(v->q.p, qv, bytes_q, cudaMemcpyHostToDevice, s));
-        CG_CUDA(cudaMemcpyAsync(v->thr.p, thr, bytes_thr, cudaMemcpyHostToDevice, s));
-        CG_CUDA(cudaMemcpyAsync(v->dqb.p, dqv, bytes_dq, cudaMemcpyHostToDevice, s));
-        CG_CUDA(cudaMemcpyAsync(v->culled.p, cul, bytes_cul, cudaMemcpyHostToDevice, s));
-    }
+    if (n) CG_CUDA(cudaMemcpyAsync(dev, st, total, cudaMemcpyHostToDevice, s));
     CG_CUDA(cudaEventRecord(v->boards_ready, s));
     v->ready_pending = true;
     v->n = count;
@@ -574,11 +571,11 @@ extern "C" cg_status cg_volume_set_billboards(cg_volume* v, const float* positio
 BoardsDev boards_of(const cg_volume* v) {
     BoardsDev b;
     b.n = v->n;
-    b.cwr = v->cwr.as<const float4>();
-    b.q = v->q.as<const int4>();
-    b.thr = v->thr.as<const uint64_t>();
-    b.dq = v->dqb.as<const uint32_t>();
-    b.culled = v->culled.as<const uint8_t>();
+    b.cwr = v->cwr;
+    b.q = v->q;
+    b.thr = v->thr;
+    b.dq = v->dqb;
+    b.culled = v->culled;
     return b;
 }
 
@@ -1064,9 +1061,25 @@ extern "C" cg_status cg_render(cg_context* ctx, const cg_volume* v, const cg_cam
     cudaStream_t s = pick_stream(ctx, stream);
     const size_t pixels = (size_t)cam->width * cam->height;
     float4* out = reinterpret_cast<float4*>(rgba_out);
+    // host output: page-locked memory the device can address is written by
+    // the pass that finishes the pixels (the image crosses the host link
+    // while that kernel runs); any other host memory gets one copy at the end
+    float4* dst = out;
+    bool copy_back = false;
     if (!out_on_device) {
         CG_CUDA(ctx->image.ensure(pixels * 16));
         out = ctx->image.as<float4>();
+        dst = out;
+        copy_back = true;
+        const bool finishes_directly =
+            params->use_mlp || params->pipeline != CG_PIPELINE_DEFERRED;
+        cudaPointerAttributes pa;
+        if (finishes_directly && cudaPointerGetAttributes(&pa, rgba_out) == cudaSuccess &&
+            pa.type == cudaMemoryTypeHost && pa.devicePointer) {
+            dst = reinterpret_cast<float4*>(pa.devicePointer);
+            copy_back = false;
+        }
+        (void)cudaGetLastError();  // pageable memory may leave a query error behind
     }
     TraceParams tp = trace_params_of(params, v->sun_dir);
     stage_begin(ctx, s);
@@ -1092,20 +1105,18 @@ extern "C" cg_status cg_render(cg_context* ctx, const cg_volume* v, const cg_cam
             CG_LAUNCH(ctx, launch_shade_mlp_tc(vd, cd, tp, md, sb,
                                                ctx->fallbacks.as<unsigned long long>(), s));
             stage_mark(ctx, s, "shade_mlp");
-            CG_LAUNCH(ctx, launch_accumulate(cd, tp, sb, out, s));
+            CG_LAUNCH(ctx, launch_accumulate(cd, tp, sb, out, dst, s));
             stage_mark(ctx, s, "accumulate");
         } else {
             CG_LAUNCH(ctx, launch_shade_exact(vd, cd, tp, sb, out, s));
             stage_mark(ctx, s, "shade_exact");
         }
     } else {
-        CG_LAUNCH(ctx, launch_trace_fused(vd, cd, tp, out, nullptr, s));
+        CG_LAUNCH(ctx, launch_trace_fused(vd, cd, tp, dst, nullptr, s));
         stage_mark(ctx, s, "trace");
     }
-    if (!out_on_device) {
-        CG_CUDA(cudaMemcpyAsync(rgba_out, out, pixels * 16, cudaMemcpyDeviceToHost, s));
-        CG_CUDA(cudaStreamSynchronize(s));
-    }
+    if (copy_back) CG_CUDA(cudaMemcpyAsync(rgba_out, out, pixels * 16, cudaMemcpyDeviceToHost, s));
+    if (!out_on_device) CG_CUDA(cudaStreamSynchronize(s));
     return CG_OK;
 }
 

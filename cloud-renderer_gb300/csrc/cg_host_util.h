@@ -148,7 +148,15 @@ struct cg_volume {
     // boards
     int n = 0;
     size_t pairs = 0;
-    DevBuf cwr, q, thr, dqb, culled;
+    // board records in one allocation, uploaded with one copy: float4 centre +
+    // radius, int4 Q20 centre + radius, u64 ball threshold, u32 Q16 density,
+    // u8 culled (offsets 0, 16n, 32n, 40n, 44n)
+    DevBuf boards;
+    float4* cwr = nullptr;
+    int4* q = nullptr;
+    uint64_t* thr = nullptr;
+    uint32_t* dqb = nullptr;
+    uint8_t* culled = nullptr;
     HostBuf h_stage;
     Bins bins{};
     DevBuf bcount, boff, bcursor, blist, bdirty;

@@ -276,8 +276,10 @@ cudaError_t launch_shade_mlp_tc(VolDesc vd, CamDesc cam, TraceParams tp, const M
 // One CTA waits on an mbarrier nothing arrives on, bounded by limit_ns
 // (status: [1] |= 1 on the timeout, [3] = nanoseconds waited).
 cudaError_t launch_wait_probe(uint64_t limit_ns, unsigned long long* status, cudaStream_t st);
-cudaError_t launch_accumulate(CamDesc cam, TraceParams tp, SampleBuf sb, float4* out,
-                              cudaStream_t st);
+// img: the march's image (alpha); dst: where the finished pixels go (img, or
+// a device-addressable host image)
+cudaError_t launch_accumulate(CamDesc cam, TraceParams tp, SampleBuf sb, const float4* img,
+                              float4* dst, cudaStream_t st);
 cudaError_t launch_mlp_features(VolDesc vd, const MlpDev& m, const float* pos, int n,
                                 const float dir[3], float* out, cudaStream_t st);
 cudaError_t launch_mlp_infer(const MlpDev& m, const float* feat, int n, float* out,

@@ -200,15 +200,17 @@ __device__ __forceinline__ void scatter_chunk(float c, int lj, int m, float& acc
     }
 }
 
-__device__ __forceinline__ void write_rgb(float4* out, const CamDesc& cam, int px, int py,
-                                          float C, const TraceParams& tp) {
+// The pixel's colour C * sun colour with the alpha the march left in `img`,
+// stored to `dst` (`img` itself, or the caller's page-locked host image).
+__device__ __forceinline__ void write_rgb(const float4* img, float4* dst, const CamDesc& cam,
+                                          int px, int py, float C, const TraceParams& tp) {
     if (px < cam.W && py < cam.H) {
-        float4* o = out + (size_t)py * cam.W + px;
-        float4 v = *o;
+        const size_t i = (size_t)py * cam.W + px;
+        float4 v = img[i];
         v.x = C * tp.sun_color[0];
         v.y = C * tp.sun_color[1];
         v.z = C * tp.sun_color[2];
-        *o = v;
+        dst[i] = v;
     }
 }
 
@@ -239,14 +241,14 @@ __global__ void __launch_bounds__(128) k_shade_exact(VolDesc vd, CamDesc cam, Tr
     }
     int px, py;
     region_pixel(region, lane, tiles_x, px, py);
-    write_rgb(out, cam, px, py, acc + comp, tp);
+    write_rgb(out, out, cam, px, py, acc + comp, tp);
 }
 
 // Per region: each pixel sums the contributions of its own samples in step
 // order, locating them through the march's step table (base slot, ballot).
 __global__ void __launch_bounds__(128) k_accumulate(CamDesc cam, TraceParams tp, SampleBuf sb,
                                                     int regions, int tiles_x, int view_steps,
-                                                    float4* out) {
+                                                    const float4* img, float4* dst) {
     const int region = blockIdx.x * 4 + (threadIdx.x >> 5);
     if (region >= regions) return;
     const int lane = threadIdx.x & 31;
@@ -283,7 +285,7 @@ __global__ void __launch_bounds__(128) k_accumulate(CamDesc cam, TraceParams tp,
     }
     int px, py;
     region_pixel(region, lane, tiles_x, px, py);
-    write_rgb(out, cam, px, py, acc + comp, tp);
+    write_rgb(img, dst, cam, px, py, acc + comp, tp);
 }
 
 }  // namespace
@@ -317,10 +319,10 @@ cudaError_t launch_shade_exact(VolDesc vd, CamDesc cam, TraceParams tp, SampleBu
     return cudaGetLastError();
 }
 
-cudaError_t launch_accumulate(CamDesc cam, TraceParams tp, SampleBuf sb, float4* out,
-                              cudaStream_t st) {
+cudaError_t launch_accumulate(CamDesc cam, TraceParams tp, SampleBuf sb, const float4* img,
+                              float4* dst, cudaStream_t st) {
     const int regions = regions_of(cam), tiles_x = (cam.W + 15) / 16;
     k_accumulate<<<(regions + 3) / 4, 128, 0, st>>>(cam, tp, sb, regions, tiles_x, tp.view_steps,
-                                                    out);
+                                                    img, dst);
     return cudaGetLastError();
 }

@@ -244,6 +244,33 @@ def test_mlp_render_rmse_and_gain(ctx, trained):
     assert t_mlp < t_exact, (t_mlp, t_exact)
 
 
+def test_output_destinations_agree(ctx, trained):
+    # the finished image written straight into page-locked host memory, copied
+    # back into pageable memory, or left on the device: the same bytes, for the
+    # surrogate, the plain fused and the exact deferred renderers
+    mlp, _, _ = trained
+    cfg = configs.PLAIN_1080P
+    wl = workload.build(cfg, width=200, height=120)
+    vol, _, _ = _pair(ctx, cfg, wl, cloudgb.FORMAT_BF16_FP16)
+    cam = workload.make_camera(wl.cameras[1])
+    kw = wl.shader_kwargs()
+    for shader in (cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, **kw),
+                   cloudgb.ConeTraceShader(**kw),
+                   cloudgb.ConeTraceShader(pipeline=_lib.PIPELINE_DEFERRED, **kw)):
+        dev = cloudgb.DeviceBuffer(200 * 120 * 16)
+        shader.coneTrace(vol, cam, out=dev)
+        ctx.synchronize()  # a device-side result is asynchronous
+        on_dev = dev.download((120, 200, 4))
+        pinned = cloudgb.HostBuffer((120, 200, 4))
+        pinned.array[:] = -7.0  # every pixel must be overwritten
+        shader.coneTrace(vol, cam, out=pinned)
+        pageable = shader.coneTrace(vol, cam)
+        assert np.array_equal(pinned.array, on_dev)
+        assert np.array_equal(pageable, on_dev)
+        assert on_dev[..., 3].max() > 0.1
+        pinned.free()
+
+
 def test_mlp_render_with_wind(ctx, trained):
     """The surrogate path's fBm volume follows the wind: renders at run times
     inside and past the noise domain's margin stay within RMSE 1e-2 of the
