@@ -199,7 +199,9 @@ cg_status cg_voxelize(cg_volume* vol, const cg_sun* sun, void* stream);
 
 /* ConeTraceShader::coneTrace(CloudVolume*) (ConeTraceShader.cpp:15-82):
  * per-pixel view march + sun cone.  rgba_out holds width*height*4 floats; it
- * is a host pointer (copied back, call is synchronous) unless out_on_device. */
+ * is a host pointer (the call is synchronous) unless out_on_device.  Page-
+ * locked host memory (cg_host_alloc) is written by the device as the pixels
+ * are finished; other host memory receives one copy after the frame. */
 cg_status cg_render(cg_context* ctx, const cg_volume* vol, const cg_camera* cam,
                     const cg_render_params* params, float* rgba_out,
                     int out_on_device, void* stream);
