@@ -1075,7 +1075,7 @@ extern "C" cg_status cg_render(cg_context* ctx, const cg_volume* v, const cg_cam
             params->use_mlp || params->pipeline != CG_PIPELINE_DEFERRED;
         cudaPointerAttributes pa;
         if (finishes_directly && cudaPointerGetAttributes(&pa, rgba_out) == cudaSuccess &&
-            pa.type == cudaMemoryTypeHost && pa.devicePointer) {
+            pa.type == cudaMemoryTypeHost && pa.devicePointer && pa.device == ctx->device) {
             dst = reinterpret_cast<float4*>(pa.devicePointer);
             copy_back = false;
         }
