@@ -282,8 +282,10 @@ cudaError_t launch_accumulate(CamDesc cam, TraceParams tp, SampleBuf sb, const f
                               float4* dst, cudaStream_t st);
 cudaError_t launch_mlp_features(VolDesc vd, const MlpDev& m, const float* pos, int n,
                                 const float dir[3], float* out, cudaStream_t st);
+// network evaluation on the tensor cores (k_shade_tc.cu); status[1] |= 1 when
+// a tensor-core wait ran out of its time limit
 cudaError_t launch_mlp_infer(const MlpDev& m, const float* feat, int n, float* out,
-                             cudaStream_t st);
+                             unsigned long long* status, cudaStream_t st);
 cudaError_t launch_mlp_train(const TrainArgs& ta, int ctas, cudaStream_t st);
 cudaError_t launch_mlp_adam(const AdamArgs& aa, cudaStream_t st);
 

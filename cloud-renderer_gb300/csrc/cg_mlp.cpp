@@ -363,10 +363,19 @@ extern "C" cg_status cg_mlp_infer(const cg_mlp* m, const float* features, int n,
         CG_CUDA(tout.ensure((size_t)n * 4));
         dout = tout.as<float>();
     }
-    CG_LAUNCH(ctx, launch_mlp_infer(device_view(m), df, n, dout, s));
+    // the tensor-core status block: [1] records a wait that ran out
+    CG_CUDA(ctx->fallbacks.ensure(32));
+    CG_CUDA(cudaMemsetAsync(ctx->fallbacks.p, 0, 32, s));
+    ctx->shaded_valid = false;
+    CG_LAUNCH(ctx, launch_mlp_infer(device_view(m), df, n, dout,
+                                    ctx->fallbacks.as<unsigned long long>(), s));
     if (!on_device) {
         CG_CUDA(cudaMemcpyAsync(out, dout, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+        unsigned long long h[2] = {0, 0};
+        CG_CUDA(cudaMemcpyAsync(h, ctx->fallbacks.p, 16, cudaMemcpyDeviceToHost, s));
         CG_CUDA(cudaStreamSynchronize(s));
+        CG_CHECK(h[1] == 0, CG_ERR_DEVICE_FAULT,
+                 "cg_mlp_infer: a tensor-core wait ran out of its time limit (1 s)");
     }
     return CG_OK;
 }

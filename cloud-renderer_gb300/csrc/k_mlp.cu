@@ -20,45 +20,6 @@ __global__ void k_mlp_features(FeatGeom g, const float* pos, int n, float sx, fl
     for (int j = 0; j < MLP_IN; ++j) out[(size_t)i * MLP_IN + j] = f[j];
 }
 
-// ---- inference -----------------------------------------------------------------
-// One warp per 32 rows; weights staged once per CTA.
-__global__ void __launch_bounds__(128) k_mlp_infer(MlpDev m, const float* feat, int n,
-                                                   float* out) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    __half* sW = reinterpret_cast<__half*>(smem);
-    float* sB = reinterpret_cast<float*>(sW + MLP_SMEM_W_HALFS);  // b1 b2 b3 b4
-    __half* sXall = reinterpret_cast<__half*>(sB + 3 * 64 + 4);
-    load_weights(m.w16, sW);
-    for (int i = threadIdx.x; i < 3 * 64 + 1; i += blockDim.x)
-        sB[i] = i < 64 ? m.params[MLP_B1 + i]
-                       : (i < 128 ? m.params[MLP_B2 + i - 64]
-                                  : (i < 192 ? m.params[MLP_B3 + i - 128] : m.params[MLP_B4]));
-    __syncthreads();
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    __half* sX = sXall + w * 32 * MLP_S16;
-    const int nchunks = (n + 31) / 32;
-    for (int c = blockIdx.x * 4 + w; c < nchunks; c += gridDim.x * 4) {
-        const int row = c * 32 + lane;
-#pragma unroll
-        for (int j = 0; j < MLP_IN; ++j) {
-            float f = row < n ? feat[(size_t)row * MLP_IN + j] : 0.f;
-            sX[lane * MLP_S16 + j] = __float2half_rn((f - m.mu[j]) * m.inv_sd[j]);
-        }
-        __syncwarp();
-#pragma unroll
-        for (int mt = 0; mt < 2; ++mt) {
-            float yg, yg8;
-            forward16(sX + mt * 16 * MLP_S16, sW, sB, sB + 64, sB + 128, sB[192], yg, yg8);
-            if (t == 0) {
-                int r0 = c * 32 + mt * 16 + g, r1 = r0 + 8;
-                if (r0 < n) out[r0] = m.tau_scale * softplus(yg);
-                if (r1 < n) out[r1] = m.tau_scale * softplus(yg8);
-            }
-        }
-        __syncwarp();
-    }
-}
-
 // ---- training step -----------------------------------------------------------------
 // One CTA = 128 rows (4 warps x 2 blocks of 16).  Loss per row:
 //   (exp(-sigma * tau_scale * softplus(y)) - exp(-sigma * tau))^2,
@@ -413,24 +374,6 @@ cudaError_t launch_mlp_features(VolDesc vd, const MlpDev& m, const float* pos, i
     if (n <= 0) return cudaSuccess;
     k_mlp_features<<<(n + 127) / 128, 128, 0, st>>>(feat_geom(vd, m), pos, n, dir[0], dir[1],
                                                     dir[2], out);
-    return cudaGetLastError();
-}
-
-size_t mlp_infer_smem() {
-    return (size_t)MLP_SMEM_W_HALFS * 2 + (3 * 64 + 4) * 4 + 4 * 32 * MLP_S16 * 2;
-}
-
-cudaError_t launch_mlp_infer(const MlpDev& m, const float* feat, int n, float* out,
-                             cudaStream_t st) {
-    if (n <= 0) return cudaSuccess;
-    const size_t sm = mlp_infer_smem();
-    cudaError_t e = cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sm);
-    if (e != cudaSuccess) return e;
-    int chunks = (n + 31) / 32;
-    int blocks = (chunks + 3) / 4;
-    if (blocks > 152 * 8) blocks = 152 * 8;
-    k_mlp_infer<<<blocks, 128, sm, st>>>(m, feat, n, out);
     return cudaGetLastError();
 }
 

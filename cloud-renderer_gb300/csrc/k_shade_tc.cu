@@ -28,6 +28,7 @@
 // memory and returns.
 #include <cuda_fp16.h>
 
+#include <algorithm>
 #include <atomic>
 
 #include "cg_deferred.cuh"
@@ -177,22 +178,9 @@ __device__ __forceinline__ bool sync_for_mma(bool bad) {
     return any_bad;
 }
 
-template <int FMT>
-__global__ void __launch_bounds__(128, CTAS_PER_SM)
-    k_shade_mlp_tc(const __grid_constant__ VolDesc vd, const __grid_constant__ TraceParams tp,
-                   const __grid_constant__ ConeSchedule cone, const __grid_constant__ MlpDev m,
-                   const __grid_constant__ FeatGeom geo, SampleBuf sb,
-                   unsigned long long* status) {
-    extern __shared__ uint8_t smem_raw[];
-    const uint32_t raw = tc::smem_addr(smem_raw);
-    uint8_t* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
-    uint8_t* act = base + OFF_ACT;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(base + OFF_BAR);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(base + OFF_BAR + 8);
-    unsigned* s_claim = reinterpret_cast<unsigned*>(base + OFF_BAR + 12);
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-
-    // ---- stage weights: W1..W3 scaled by 1/2
+// Weights W1..W3 scaled by 1/2, the ones column (8 rows) and the split
+// half-scaled biases (32B-swizzled, K = 16) into the CTA's shared tiles.
+__device__ __forceinline__ void stage_network(uint8_t* base, const MlpDev& m, int tid) {
     for (int r = tid; r < 64; r += blockDim.x) {
         stage_row<2>(base + OFF_W1, r, m.w16 + MLP_H_W1 + r * 16);
         stage_row<8>(base + OFF_W2, r, m.w16 + MLP_H_W2 + r * 64);
@@ -220,6 +208,54 @@ __global__ void __launch_bounds__(128, CTAS_PER_SM)
             *reinterpret_cast<uint4*>(tile + tc::sw32_offset(n, 1)) = make_uint4(0u, 0u, 0u, 0u);
         }
     }
+}
+
+// One layer's epilogue for this thread's row: tensor memory -> SiLU, 32
+// columns at a time, written as the next layer's FP16 activations (layers 0,
+// 1) or folded into the FP32 64 -> 1 output (layer 2, returned with b4).
+__device__ __forceinline__ float layer_epilogue(int layer, uint32_t dw, uint8_t* act, int tid,
+                                                const MlpDev& m) {
+    float yy = m.k.b4;
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+        uint32_t acc[32];
+        tc::tmem_ld32(dw + 32u * half, acc);
+        uint32_t h[16];
+        silu32(acc, h);
+        if (layer < 2) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                *reinterpret_cast<uint4*>(act + tc::sw128_offset(tid, 4 * half + q)) =
+                    make_uint4(h[4 * q], h[4 * q + 1], h[4 * q + 2], h[4 * q + 3]);
+        } else {
+            const float* w4 = m.k.w4 + 32 * half;
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const float2 v = __half22float2(*reinterpret_cast<const __half2*>(&h[q]));
+                yy = fmaf(w4[2 * q], v.x, yy);
+                yy = fmaf(w4[2 * q + 1], v.y, yy);
+            }
+        }
+    }
+    return yy;
+}
+
+template <int FMT>
+__global__ void __launch_bounds__(128, CTAS_PER_SM)
+    k_shade_mlp_tc(const __grid_constant__ VolDesc vd, const __grid_constant__ TraceParams tp,
+                   const __grid_constant__ ConeSchedule cone, const __grid_constant__ MlpDev m,
+                   const __grid_constant__ FeatGeom geo, SampleBuf sb,
+                   unsigned long long* status) {
+    extern __shared__ uint8_t smem_raw[];
+    const uint32_t raw = tc::smem_addr(smem_raw);
+    uint8_t* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+    uint8_t* act = base + OFF_ACT;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(base + OFF_BAR);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(base + OFF_BAR + 8);
+    unsigned* s_claim = reinterpret_cast<unsigned*>(base + OFF_BAR + 12);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    stage_network(base, m, tid);
     if (tid == 0) {
         tc::mbar_init(bar, 1);
         tc::fence_mbar_init();
@@ -297,29 +333,10 @@ __global__ void __launch_bounds__(128, CTAS_PER_SM)
             tc::fence_after_sync();
             // ---- epilogue: TMEM -> bias + SiLU, 32 columns at a time; the
             // last layer folds the 64 -> 1 output in FP32
-            float yy = m.k.b4;
-#pragma unroll
-            for (int half = 0; half < 2 && !bad; ++half) {
-                uint32_t acc[32];
-                tc::tmem_ld32(dw + 32u * half, acc);
-                uint32_t h[16];
-                silu32(acc, h);
-                if (layer < 2) {
-#pragma unroll
-                    for (int q = 0; q < 4; ++q)
-                        *reinterpret_cast<uint4*>(act + tc::sw128_offset(tid, 4 * half + q)) =
-                            make_uint4(h[4 * q], h[4 * q + 1], h[4 * q + 2], h[4 * q + 3]);
-                } else {
-                    const float* w4 = m.k.w4 + 32 * half;
-#pragma unroll
-                    for (int q = 0; q < 16; ++q) {
-                        const float2 v = __half22float2(*reinterpret_cast<const __half2*>(&h[q]));
-                        yy = fmaf(w4[2 * q], v.x, yy);
-                        yy = fmaf(w4[2 * q + 1], v.y, yy);
-                    }
-                }
+            if (!bad) {
+                const float yy = layer_epilogue(layer, dw, act, tid, m);
+                if (layer == 2) y = yy;
             }
-            if (layer == 2) y = yy;
             tc::fence_before_sync();
         }
         if (failed) break;
@@ -361,6 +378,91 @@ __global__ void __launch_bounds__(128, CTAS_PER_SM)
     if (warp == 0) tc::tmem_dealloc(tmem, TC_TMEM_COLS);
 }
 
+// The network alone over n rows of raw features (normalised here):
+// out[i] = tau_scale * softplus(y_i).  The tile pipeline of k_shade_mlp_tc
+// without the sample fetches: 128-row tiles at a static stride, the same
+// staged weights, layers, epilogues and bounded waits.
+__global__ void __launch_bounds__(128, CTAS_PER_SM)
+    k_mlp_infer_tc(const __grid_constant__ MlpDev m, const float* feat, int n, float* out,
+                   unsigned long long* status) {
+    extern __shared__ uint8_t smem_raw[];
+    const uint32_t raw = tc::smem_addr(smem_raw);
+    uint8_t* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+    uint8_t* act = base + OFF_ACT;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(base + OFF_BAR);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(base + OFF_BAR + 8);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    stage_network(base, m, tid);
+    if (tid == 0) {
+        tc::mbar_init(bar, 1);
+        tc::fence_mbar_init();
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(tslot, TC_TMEM_COLS);
+        tc::tmem_relinquish();
+    }
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tslot;
+    const uint32_t dw = tmem + ((uint32_t)(warp * 32) << 16);
+    const uint32_t a_addr = tc::smem_addr(act);
+    const uint32_t w_addr[3] = {tc::smem_addr(base + OFF_W1), tc::smem_addr(base + OFF_W2),
+                                tc::smem_addr(base + OFF_W3)};
+    const uint32_t ones_addr = tc::smem_addr(base + OFF_ONES);
+    const uint32_t bias_addr = tc::smem_addr(base + OFF_BIAS);
+    unsigned phase = 0;
+    bool failed = false, bad = false;  // bad: a wait of this warp ran out
+    const int ntiles = (n + 127) / 128;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int row = tile * 128 + tid;
+        // this row's normalised FP16 features into chunks 0-1 of its tile row
+        // (the previous tile's layer-3 MMA, the last reader, has completed)
+        uint32_t x[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const float f0 = row < n ? feat[(size_t)row * MLP_IN + 2 * q] : m.mu[2 * q];
+            const float f1 = row < n ? feat[(size_t)row * MLP_IN + 2 * q + 1] : m.mu[2 * q + 1];
+            x[q] = mlp::pack_h2((f0 - m.mu[2 * q]) * m.inv_sd[2 * q],
+                                (f1 - m.mu[2 * q + 1]) * m.inv_sd[2 * q + 1]);
+        }
+        *reinterpret_cast<uint4*>(act + tc::sw128_offset(tid, 0)) =
+            make_uint4(x[0], x[1], x[2], x[3]);
+        *reinterpret_cast<uint4*>(act + tc::sw128_offset(tid, 1)) =
+            make_uint4(x[4], x[5], x[6], x[7]);
+        float y = 0.f;
+#pragma unroll
+        for (int layer = 0; layer < 3; ++layer) {
+            if (sync_for_mma(bad)) {  // a commit of parity `phase` is still pending
+                failed = true;
+                break;
+            }
+            if (tid == 0)
+                issue_layer(layer, tmem, a_addr, w_addr[layer], ones_addr,
+                            bias_addr + 2048u * layer, bar);
+            bad = __any_sync(0xffffffffu, !tc::mbar_wait(bar, phase, TC_WAIT_NS));
+            if (!bad) phase ^= 1u;
+            tc::fence_after_sync();
+            if (!bad) {
+                const float yy = layer_epilogue(layer, dw, act, tid, m);
+                if (layer == 2) y = yy;
+            }
+            tc::fence_before_sync();
+        }
+        if (failed) break;
+        if (row < n && !bad) out[row] = m.tau_scale * mlp::softplus(y);
+    }
+    if (!failed) failed = sync_for_mma(bad);  // the last tile's waits
+    if (failed) {
+        if (bad) tc::mbar_wait(bar, phase, TC_WAIT_NS);
+        if (tid == 0) atomicOr(status + 1, 1ull);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, TC_TMEM_COLS);
+}
+
 // The bounded wait on an mbarrier that nothing arrives on: one CTA inits the
 // barrier, waits for its first phase with the time limit, and records the
 // outcome in the status block ([1] |= 1 on a timeout, [3] = nanoseconds
@@ -385,6 +487,30 @@ __global__ void k_wait_probe(uint64_t limit_ns, unsigned long long* status) {
 
 cudaError_t launch_wait_probe(uint64_t limit_ns, unsigned long long* status, cudaStream_t st) {
     k_wait_probe<<<1, 32, 0, st>>>(limit_ns, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_infer(const MlpDev& m, const float* feat, int n, float* out,
+                             unsigned long long* status, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    // the shared-memory attribute and the grid are set once per device
+    static std::atomic<int> grid[64];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if (!grid[dev].load(std::memory_order_acquire)) {
+        e = cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 SMEM_BYTES);
+        if (e != cudaSuccess) return e;
+        int sms = 0;
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return e;
+        grid[dev].store(sms * CTAS_PER_SM, std::memory_order_release);
+    }
+    const int ntiles = (n + 127) / 128;
+    const int blocks = std::min(grid[dev].load(std::memory_order_acquire), ntiles);
+    k_mlp_infer_tc<<<blocks, 128, SMEM_BYTES, st>>>(m, feat, n, out, status);
     return cudaGetLastError();
 }
 

@@ -50,9 +50,11 @@ def oracle_of(m, mu, sd):
     return O.OracleMLP(P, mu, sd, m.config.tau_scale)
 
 
-def test_forward_matches_oracle(ctx):
+# 1000 rows: eight tiles, the last partial; 200003: more tiles than CTAs
+@pytest.mark.parametrize("n", [1000, 200003])
+def test_forward_matches_oracle(ctx, n):
     m, mu, sd, rng = random_model(ctx)
-    f = rng.uniform(-2, 2, (1000, 16)).astype(np.float32) * sd + mu
+    f = rng.uniform(-2, 2, (n, 16)).astype(np.float32) * sd + mu
     got = m.infer(f).astype(np.float64)
     om = oracle_of(m, mu, sd)
     y = om.forward(f.astype(np.float64))
