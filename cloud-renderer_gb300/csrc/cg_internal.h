@@ -286,6 +286,8 @@ cudaError_t launch_mlp_features(VolDesc vd, const MlpDev& m, const float* pos, i
 // a tensor-core wait ran out of its time limit
 cudaError_t launch_mlp_infer(const MlpDev& m, const float* feat, int n, float* out,
                              unsigned long long* status, cudaStream_t st);
+// one training step on the tensor cores (k_train_tc.cu); a tensor-core wait
+// that ran out of its time limit leaves a NaN in the CTA's loss slot
 cudaError_t launch_mlp_train(const TrainArgs& ta, int ctas, cudaStream_t st);
 cudaError_t launch_mlp_adam(const AdamArgs& aa, cudaStream_t st);
 

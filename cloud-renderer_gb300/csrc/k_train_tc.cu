@@ -1,0 +1,424 @@
+// k_train_tc.cu -- one training step of the sun-transmittance surrogate on the
+// fifth-generation tensor cores: forward, loss gradient, backward and the
+// per-CTA gradient partials that k_mlp_adam reduces in a fixed order.
+//
+// One CTA = 128 rows of the batch, 4 warps, thread = row.  Every GEMM is a
+// tcgen05.mma (M = 128, FP16 operands from shared memory, FP32 accumulators
+// in tensor memory) issued by thread 0 and committed to one mbarrier:
+//   forward   z_l = A_l W_l^T + b_l          A_0 = x, A_l = h_l (K = 16, 64)
+//   backward  dh_l = dz_{l+1} W_{l+1}        (A = dz rows, B = W^T rows)
+//             [dW_l | db_l] = dz_l^T [h_l | 1] (A = dz^T, padded to 128 rows;
+//             B = h^T plus a row of ones: the bias gradient is column 64 of
+//             the same product; K = the 128 batch rows)
+// Pre-activations are kept in FP16 (z_h) and SiLU is evaluated in FP32 on
+// them; activations and gradients enter the MMAs as FP16.  The output layer
+// (64 -> 1) and its gradients are FP32 per row (dW4 by deterministic
+// warp-shuffle trees).  Transposed operands (dz^T, h^T, x^T) are written by
+// the threads that own the rows.  Every mbarrier wait is bounded (1 s of the
+// global timer); a timeout sets partial[NPARAM] to NaN (the loss slot) for the
+// host to report, drains and frees tensor memory.
+#include <cuda_fp16.h>
+
+#include <atomic>
+
+#include "cg_internal.h"
+#include "cg_mlp.cuh"
+#include "cg_tc.cuh"
+
+namespace {
+
+constexpr uint32_t TT_COLS = 256;  // [0, 64) forward / dh, [64, 160) dW | db
+constexpr uint64_t TT_WAIT_NS = 1000000000ull;
+constexpr int ZS = 66;  // halves per row of the z stores (conflict-free rows)
+// shared memory map (bytes from the 1024-aligned base)
+constexpr int O_X = 0;             // 128 x 128 B SW128 (K = 16 used)
+constexpr int O_H1 = 16384;        // 128 x 128 B SW128
+constexpr int O_H2 = 32768;        // 128 x 128 B SW128
+constexpr int O_D = 49152;         // 128 x 128 B SW128: dz rows
+constexpr int O_DT = 65536;        // 2 K-atoms x 128 rows x 128 B: dz^T (rows 64-127 zero)
+constexpr int DT_ATOM = 16384;
+constexpr int O_HT = 98304;        // 2 K-atoms x 80 rows x 128 B: h^T / x^T, row 64 = ones
+constexpr int HT_ATOM = 10240;
+constexpr int O_W1 = O_HT + 2 * HT_ATOM;  // 64 x 32 B SW32 (K = 16)
+constexpr int O_W2 = O_W1 + 2048;  // 64 x 128 B SW128
+constexpr int O_W3 = O_W2 + 8192;
+constexpr int O_WT2 = O_W3 + 8192;  // W2^T: row = input, K = output
+constexpr int O_WT3 = O_WT2 + 8192;
+constexpr int O_ONES = O_WT3 + 8192;  // one 8-row SW32 atom: rows (1, 1, 0, ...)
+constexpr int O_BIAS = O_ONES + 256;  // 3 x (64 x 32 B) SW32: (b_hi, b_lo, 0, ...)
+constexpr int O_Z = O_BIAS + 3 * 2048;           // 3 x 128 x ZS halves
+constexpr int O_F = O_Z + 3 * 128 * ZS * 2;      // floats: dy[128], w4[64], red[4][64], misc
+constexpr int O_BAR = O_F + (128 + 64 + 4 * 64 + 16) * 4;
+constexpr int TT_USED = O_BAR + 32;
+constexpr int TT_SMEM = TT_USED + 1024;
+static_assert(O_W2 % 1024 == 0 && O_W3 % 1024 == 0 && O_WT2 % 1024 == 0 && O_WT3 % 1024 == 0 &&
+                  O_HT % 1024 == 0 && O_DT % 1024 == 0 && HT_ATOM % 1024 == 0,
+              "128B-swizzled tiles need 1024-byte alignment");
+static_assert(O_ONES % 256 == 0 && O_BIAS % 256 == 0 && O_W1 % 256 == 0, "SW32 alignment");
+static_assert(TT_SMEM <= 227 * 1024, "shared memory");
+
+constexpr uint32_t ID64 = tc::idesc_f16_f32(128, 64);
+constexpr uint32_t ID80 = tc::idesc_f16_f32(128, 80);
+
+__device__ __forceinline__ uint32_t h2u(__half2 h) { return *reinterpret_cast<uint32_t*>(&h); }
+
+// byte address of element (row, k) of a 128B-swizzled K-major tile whose
+// K-atoms (64 halves each) are `atom` bytes apart
+__device__ __forceinline__ uint32_t kt_addr(int row, int k, int atom) {
+    return (uint32_t)((k >> 6) * atom) + tc::sw128_offset(row, (k & 63) >> 3) + (uint32_t)((k & 7) * 2);
+}
+
+__device__ __forceinline__ void mma_k(uint32_t d, uint32_t a, uint32_t b, uint32_t id, int ksteps,
+                                      int a_atom, int b_atom, bool acc0) {
+    for (int k = 0; k < ksteps; ++k) {
+        const uint32_t off = 32u * (k & 3);
+        tc::mma_f16(d, tc::desc_sw128(a + (uint32_t)((k >> 2) * a_atom) + off),
+                    tc::desc_sw128(b + (uint32_t)((k >> 2) * b_atom) + off), id,
+                    (acc0 || k > 0) ? 1u : 0u);
+    }
+}
+
+__device__ __forceinline__ float silu_f(float z) { return z / (1.f + __expf(-z)); }
+__device__ __forceinline__ float silu_grad_f(float z) {
+    const float s = 1.f / (1.f + __expf(-z));
+    return s * (1.f + z * (1.f - s));
+}
+
+// sync + the CTA's agreement on a failed wait
+__device__ __forceinline__ bool tt_sync(bool bad) {
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    const bool any_bad = __syncthreads_or(bad) != 0;
+    tc::fence_after_sync();
+    return any_bad;
+}
+
+// 64 FP32 columns of this thread's tensor-memory lane
+__device__ __forceinline__ void ld64(uint32_t taddr, float (&v)[64]) {
+    uint32_t r[32];
+    tc::tmem_ld32(taddr, r);
+#pragma unroll
+    for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+    tc::tmem_ld32(taddr + 32u, r);
+#pragma unroll
+    for (int j = 0; j < 32; ++j) v[32 + j] = __uint_as_float(r[j]);
+}
+
+__global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
+    extern __shared__ uint8_t smem_raw[];
+    const uint32_t raw = tc::smem_addr(smem_raw);
+    uint8_t* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+    const uint32_t sb = tc::smem_addr(base);
+    __half* zs = reinterpret_cast<__half*>(base + O_Z);
+    float* fdy = reinterpret_cast<float*>(base + O_F);
+    float* fw4 = fdy + 128;
+    float* fred = fw4 + 64;
+    float* fmisc = fred + 4 * 64;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(base + O_BAR);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(base + O_BAR + 8);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    // ---- weights (FP16 image), their transposes, biases, ones
+    for (int r = tid; r < 64; r += 128) {
+#pragma unroll
+        for (int c = 0; c < 2; ++c)
+            *reinterpret_cast<uint4*>(base + O_W1 + tc::sw32_offset(r, c)) =
+                *reinterpret_cast<const uint4*>(ta.w16 + MLP_H_W1 + r * 16 + 8 * c);
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            *reinterpret_cast<uint4*>(base + O_W2 + tc::sw128_offset(r, c)) =
+                *reinterpret_cast<const uint4*>(ta.w16 + MLP_H_W2 + r * 64 + 8 * c);
+            *reinterpret_cast<uint4*>(base + O_W3 + tc::sw128_offset(r, c)) =
+                *reinterpret_cast<const uint4*>(ta.w16 + MLP_H_W3 + r * 64 + 8 * c);
+            // W^T row r (input r), K = outputs 8c .. 8c+7
+            __align__(16) __half t2[8], t3[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                t2[q] = ta.w16[MLP_H_W2 + (8 * c + q) * 64 + r];
+                t3[q] = ta.w16[MLP_H_W3 + (8 * c + q) * 64 + r];
+            }
+            *reinterpret_cast<uint4*>(base + O_WT2 + tc::sw128_offset(r, c)) =
+                *reinterpret_cast<const uint4*>(t2);
+            *reinterpret_cast<uint4*>(base + O_WT3 + tc::sw128_offset(r, c)) =
+                *reinterpret_cast<const uint4*>(t3);
+        }
+        fw4[r] = __half2float(ta.w16[MLP_H_W4 + r]);
+    }
+    for (int i = tid; i < 3 * 64; i += 128) {
+        const int l = i >> 6, n = i & 63;
+        const int off = l == 0 ? MLP_B1 : (l == 1 ? MLP_B2 : MLP_B3);
+        const float bv = ta.params[off + n];
+        const __half hi = __float2half_rn(bv), lo = __float2half_rn(bv - __half2float(hi));
+        uint8_t* tile = base + O_BIAS + 2048 * l;
+        *reinterpret_cast<uint4*>(tile + tc::sw32_offset(n, 0)) =
+            make_uint4(h2u(__halves2half2(hi, lo)), 0u, 0u, 0u);
+        *reinterpret_cast<uint4*>(tile + tc::sw32_offset(n, 1)) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    if (tid < 8) {
+        const uint32_t ones = h2u(__floats2half2_rn(1.f, 1.f));
+        *reinterpret_cast<uint4*>(base + O_ONES + tc::sw32_offset(tid, 0)) =
+            make_uint4(ones, 0u, 0u, 0u);
+        *reinterpret_cast<uint4*>(base + O_ONES + tc::sw32_offset(tid, 1)) =
+            make_uint4(0u, 0u, 0u, 0u);
+    }
+    // dz^T rows 64-127 stay zero; h^T rows 64-79: row 64 all ones, the rest zero
+    {
+        const uint32_t one2 = h2u(__floats2half2_rn(1.f, 1.f));
+        for (int i = tid; i < 2 * 64 * 8; i += 128) {
+            const int a = i >> 9, r = 64 + ((i >> 3) & 63), c = i & 7;
+            *reinterpret_cast<uint4*>(base + O_DT + a * DT_ATOM + tc::sw128_offset(r, c)) =
+                make_uint4(0u, 0u, 0u, 0u);
+        }
+        for (int i = tid; i < 2 * 16 * 8; i += 128) {
+            const int a = i >> 7, r = 64 + ((i >> 3) & 15), c = i & 7;
+            const uint32_t v = r == 64 ? one2 : 0u;
+            *reinterpret_cast<uint4*>(base + O_HT + a * HT_ATOM + tc::sw128_offset(r, c)) =
+                make_uint4(v, v, v, v);
+        }
+    }
+
+    // ---- this thread's row: features (normalised, FP16) into x and x^T
+    const long long r = (long long)blockIdx.x * 128 + tid;
+    bool valid;
+    long long idx;
+    if (ta.sequential) {
+        idx = ta.offset + r;
+        valid = idx < ta.N;
+    } else {
+        const long long step = ta.step ? *ta.step : 0;
+        const unsigned long long lin = (unsigned long long)(step * ta.batch + r);
+        idx = (long long)((lin * ta.perm_mul) % (unsigned long long)ta.N);
+        valid = true;
+    }
+    __align__(16) __half xh[16];
+#pragma unroll
+    for (int j = 0; j < MLP_IN; ++j) {
+        const float f = valid ? ta.feat[(size_t)idx * MLP_IN + j] : 0.f;
+        xh[j] = __float2half_rn((f - ta.mu[j]) * ta.inv_sd[j]);
+    }
+    const float tau = valid ? ta.tau[idx] : -1.f;  // < 0: padding row
+#pragma unroll
+    for (int c = 0; c < 2; ++c)
+        *reinterpret_cast<uint4*>(base + O_X + tc::sw128_offset(tid, c)) =
+            *reinterpret_cast<const uint4*>(xh + 8 * c);
+
+    if (tid == 0) {
+        tc::mbar_init(bar, 1);
+        tc::fence_mbar_init();
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(tslot, TT_COLS);
+        tc::tmem_relinquish();
+    }
+    bool bad = tt_sync(false);
+    const uint32_t tmem = *tslot;
+    const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+    unsigned phase = 0;
+    bool failed = false;
+    auto wait = [&]() {
+        bad = __any_sync(0xffffffffu, !tc::mbar_wait(bar, phase, TT_WAIT_NS));
+        if (!bad) phase ^= 1u;
+        tc::fence_after_sync();
+    };
+
+    // ---- forward
+    float y = 0.f;
+    for (int l = 0; l < 3 && !failed; ++l) {
+        if (tt_sync(bad)) {
+            failed = true;
+            break;
+        }
+        if (tid == 0) {
+            const uint32_t a = sb + (l == 0 ? O_X : (l == 1 ? O_H1 : O_H2));
+            if (l == 0)
+                tc::mma_f16(tmem, tc::desc_sw128(a), tc::desc_sw32(sb + O_W1), ID64, 0u);
+            else
+                mma_k(tmem, a, sb + (l == 1 ? O_W2 : O_W3), ID64, 4, 0, 0, false);
+            tc::mma_f16(tmem, tc::desc_sw32(sb + O_ONES, 0u), tc::desc_sw32(sb + O_BIAS + 2048u * l),
+                        ID64, 1u);
+            tc::mma_commit(bar);
+        }
+        wait();
+        if (!bad) {
+            float z[64];
+            ld64(tmem + lane_off, z);
+            __half* zrow = zs + (size_t)(l * 128 + tid) * ZS;
+            uint32_t hp[32];
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                const __half2 zh = __floats2half2_rn(z[2 * j], z[2 * j + 1]);
+                *reinterpret_cast<__half2*>(zrow + 2 * j) = zh;
+                const float2 zf = __half22float2(zh);
+                hp[j] = h2u(__floats2half2_rn(silu_f(zf.x), silu_f(zf.y)));
+            }
+            if (l < 2) {
+                uint8_t* ht = base + (l == 0 ? O_H1 : O_H2);
+#pragma unroll
+                for (int c = 0; c < 8; ++c)
+                    *reinterpret_cast<uint4*>(ht + tc::sw128_offset(tid, c)) =
+                        make_uint4(hp[4 * c], hp[4 * c + 1], hp[4 * c + 2], hp[4 * c + 3]);
+            } else {
+                float yy = ta.params[MLP_B4];
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const float2 h = __half22float2(*reinterpret_cast<const __half2*>(&hp[j]));
+                    yy = fmaf(fw4[2 * j], h.x, yy);
+                    yy = fmaf(fw4[2 * j + 1], h.y, yy);
+                }
+                y = yy;
+            }
+        }
+        tc::fence_before_sync();
+    }
+
+    // ---- loss and its gradient (per row), the output layer's gradients
+    float dy = 0.f, loss = 0.f;
+    if (tau >= 0.f) {
+        const float k = ta.sigma * ta.tau_scale;
+        const float Th = __expf(-k * mlp::softplus(y)), T = __expf(-ta.sigma * tau);
+        const float diff = Th - T;
+        loss = diff * diff;
+        dy = 2.f * diff * (-k * mlp::sigmoid(y) * Th);
+    }
+    {
+        // dW4[j] = sum_rows dy h3[j] and db4 = sum_rows dy: shuffle trees per
+        // warp, then the four warps in order
+        const __half* z3 = zs + (size_t)(2 * 128 + tid) * ZS;
+        for (int j = 0; j < 64; ++j) {
+            const float h3 = __half2float(__float2half_rn(silu_f(__half2float(z3[j]))));
+            float v = dy * h3;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) fred[warp * 64 + j] = v;
+        }
+        float vb = dy, vl = loss;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            vb += __shfl_xor_sync(0xffffffffu, vb, o);
+            vl += __shfl_xor_sync(0xffffffffu, vl, o);
+        }
+        if (lane == 0) {
+            fmisc[warp] = vb;
+            fmisc[4 + warp] = vl;
+        }
+    }
+
+    float* part = ta.partial + (size_t)blockIdx.x * (MLP_NPARAM + 1);
+    // dz of the layer below from dh (tensor memory cols [0, 64)) or, for the
+    // last hidden layer, from dy w4: FP16 into the dz rows and dz^T
+    auto write_dz = [&](int l, const float (&dh)[64]) {
+        const __half* zrow = zs + (size_t)(l * 128 + tid) * ZS;
+        uint32_t dp[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const float2 zf = __half22float2(*reinterpret_cast<const __half2*>(zrow + 2 * j));
+            const __half2 d2 = __floats2half2_rn(dh[2 * j] * silu_grad_f(zf.x),
+                                                 dh[2 * j + 1] * silu_grad_f(zf.y));
+            dp[j] = h2u(d2);
+            *reinterpret_cast<__half*>(base + O_DT + kt_addr(2 * j, tid, DT_ATOM)) = __low2half(d2);
+            *reinterpret_cast<__half*>(base + O_DT + kt_addr(2 * j + 1, tid, DT_ATOM)) =
+                __high2half(d2);
+        }
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+            *reinterpret_cast<uint4*>(base + O_D + tc::sw128_offset(tid, c)) =
+                make_uint4(dp[4 * c], dp[4 * c + 1], dp[4 * c + 2], dp[4 * c + 3]);
+    };
+    // h^T (rows 0-63) from a row tile, or x^T (rows 0-15)
+    auto write_ht = [&](const uint8_t* rows, int nfeat) {
+        for (int c = 0; c < nfeat / 8; ++c) {
+            const uint4 q = *reinterpret_cast<const uint4*>(rows + tc::sw128_offset(tid, c));
+            const __half* h = reinterpret_cast<const __half*>(&q);
+#pragma unroll
+            for (int e = 0; e < 8; ++e)
+                *reinterpret_cast<__half*>(base + O_HT + kt_addr(8 * c + e, tid, HT_ATOM)) = h[e];
+        }
+    };
+    // rows 0-63 (warps 0, 1) of tensor-memory cols [64, 160): dW[j][0..nin) and db[j]
+    auto store_dw = [&](int wo, int bo, int nin) {
+        if (warp < 2) {
+            const int j = tid;
+            float v[64];
+            ld64(tmem + lane_off + 64u, v);
+            uint32_t rb[32];
+            tc::tmem_ld32(tmem + lane_off + 128u, rb);
+            for (int i = 0; i < nin; ++i) part[wo + j * nin + i] = v[i];
+            part[bo + j] = __uint_as_float(rb[0]);
+        }
+    };
+
+    if (!failed && !bad) {
+        // layer 3: dz3 = dy w4 * silu'(z3)
+        float dh[64];
+#pragma unroll
+        for (int j = 0; j < 64; ++j) dh[j] = dy * fw4[j];
+        write_dz(2, dh);
+        write_ht(base + O_H2, 64);
+    }
+    // backward: (dW3, dh2), (dW2, dh1), dW1
+    for (int l = 2; l >= 0 && !failed; --l) {
+        if (tt_sync(bad)) {
+            failed = true;
+            break;
+        }
+        if (tid == 0) {
+            mma_k(tmem + 64u, sb + O_DT, sb + O_HT, ID80, 8, DT_ATOM, HT_ATOM, false);
+            if (l > 0) mma_k(tmem, sb + O_D, sb + (l == 2 ? O_WT3 : O_WT2), ID64, 4, 0, 0, false);
+            tc::mma_commit(bar);
+        }
+        wait();
+        float dh[64];
+        if (!bad) {
+            store_dw(l == 0 ? MLP_W1 : (l == 1 ? MLP_W2 : MLP_W3),
+                     l == 0 ? MLP_B1 : (l == 1 ? MLP_B2 : MLP_B3), l == 0 ? 16 : 64);
+            if (l > 0) ld64(tmem + lane_off, dh);
+        }
+        tc::fence_before_sync();
+        if (l > 0) {
+            // every warp's tensor-memory loads are done, and the MMAs that read
+            // dz, dz^T and h^T have completed, before they are rewritten
+            if (tt_sync(bad)) {
+                failed = true;
+                break;
+            }
+            write_dz(l - 1, dh);
+            write_ht(base + (l == 2 ? O_H1 : O_X), l == 2 ? 64 : 16);
+            tc::fence_before_sync();
+        }
+    }
+    if (!failed) failed = tt_sync(bad);
+    if (failed) {
+        if (bad) tc::mbar_wait(bar, phase, TT_WAIT_NS);
+        if (tid == 0) part[MLP_NPARAM] = __int_as_float(0x7fc00000);  // NaN loss: reported
+    } else {
+        if (tid < 64)
+            part[MLP_W4 + tid] =
+                ((fred[tid] + fred[64 + tid]) + fred[128 + tid]) + fred[192 + tid];
+        if (tid == 0) {
+            part[MLP_B4] = ((fmisc[0] + fmisc[1]) + fmisc[2]) + fmisc[3];
+            part[MLP_NPARAM] = ((fmisc[4] + fmisc[5]) + fmisc[6]) + fmisc[7];
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, TT_COLS);
+}
+
+}  // namespace
+
+cudaError_t launch_mlp_train(const TrainArgs& ta, int ctas, cudaStream_t st) {
+    // the attribute is set once per device, outside any stream capture
+    static std::atomic<bool> configured[64];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if (!configured[dev].load(std::memory_order_acquire)) {
+        e = cudaFuncSetAttribute(k_mlp_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 TT_SMEM);
+        if (e != cudaSuccess) return e;
+        configured[dev].store(true, std::memory_order_release);
+    }
+    k_mlp_train_tc<<<ctas, 128, TT_SMEM, st>>>(ta);
+    return cudaGetLastError();
+}
