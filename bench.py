@@ -3,16 +3,21 @@ FP32 vs the BF16 volume + MLP sun-cone surrogate.
 
 One step = one frame = voxelize (clear, sun-view map, highlights, coverage
 splat, mips) + render of one 1920x1080 view, cycling through the 16 seeded
-orbit cameras.  Both paths are timed:
-  plain    -- RGBA32F volume, exact sun cone (fused trace kernel)
-  bf16_mlp -- BF16/FP16 volume, deferred renderer, MLP surrogate trained at
-              start-up on the GPU by the library's own kernels
-`value` is the surrogate path's frame throughput when its image stays within
-RMSE 1e-2 of the plain FP32 image (else the plain path's); the FP64-oracle
-RMSE bound is enforced by the GPU tests.  Device-resident timing with CUDA
-events; `e2e` goes through the public C ABI with host boards in and a pinned
-host image out.  Multi-GPU runs are independent replicas (the path has no
-exchange step): value = pixels of all ranks / max-over-ranks time.
+orbit cameras.  Three paths are timed:
+  plain fused     -- RGBA32F volume, exact sun cone, one trace kernel
+  plain deferred  -- RGBA32F volume, march + exact shading of the recorded
+                     samples in full warps (the faster of the two plain
+                     paths is the baseline of the speed-up)
+  bf16_mlp        -- BF16/FP16 volume, MLP surrogate for the sun cone,
+                     trained at start-up on the GPU by the library's kernels
+`value` is the surrogate path's frame throughput when its images of the 16
+views stay within RMSE 1e-2 of the FP64 oracle (the checker, untimed, on
+sampled 32x32 tiles: the centre and three tiles with alpha > 0 per view),
+else the faster plain path's.  Device-resident timing with CUDA events;
+`e2e` goes through the public C ABI with host boards in and a pinned host
+image out.  The default run also times the batching form and the precision
+form briefly (under `paths`).  Multi-GPU runs are independent replicas (the
+path has no exchange step): value = pixels of all ranks / max-over-ranks time.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -50,6 +55,8 @@ def parse():
                          "compat: the reference's billboard image formation; precision: "
                          "4K over a 512^3 BF16/FP16 volume")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-side-legs", action="store_true",
+                    help="skip the short batching-form and precision-form legs of the default run")
     ap.add_argument("--cpu-budget-s", type=float, default=15.0)
     ap.add_argument("--mlp-steps", type=int, default=20000)
     ap.add_argument("--mlp-samples", type=int, default=4_000_000)
@@ -126,9 +133,40 @@ def config_block(wl, extra=None):
 # ---------------------------------------------------------------------------
 # CPU legs (the oracle's FP32 build: the reference's CPU restatement)
 # ---------------------------------------------------------------------------
+def _oracle_camera(cd):
+    class Cam:
+        pass
+    cam = Cam()
+    cam.eye, cam.target, cam.up = cd["eye"], cd["target"], (0.0, 1.0, 0.0)
+    cam.fov_y_degrees, cam.width, cam.height = cd["fov"], cd["width"], cd["height"]
+    return cam
+
+
+def _oracle_params(c):
+    from oracle import oracle as O
+    return O.make_params(view_steps=c["view_steps"], sun_steps=c["sun_steps"],
+                         cone_half_angle=c["cone_half_angle"], cone_initial_height=c["cone_h0"],
+                         cone_min_radius=c["cone_min_radius"], density_scale=c["density_scale"],
+                         ambient=c["ambient"], noise_octaves=c["noise_octaves"],
+                         noise_seed=c["noise_seed"], noise_frequency=c["noise_frequency"],
+                         noise_lacunarity=c["noise_lacunarity"], noise_gain=c["noise_gain"])
+
+
+def _spread_bands(H, band=8):
+    """Row bands of height `band` in bit-reversed order of their index, so that
+    every prefix of the list samples the image evenly from top to bottom (a
+    time-limited sample is then neither the cloud's dense centre alone nor
+    its empty edges)."""
+    n = (H + band - 1) // band
+    bits = max(1, (n - 1).bit_length())
+    order = sorted(range(n), key=lambda i: int(format(i, f"0{bits}b")[::-1], 2))
+    return [i * band for i in order]
+
+
 def cpu_frame_rate(wl, budget_s, threads):
     """FP32 port on `threads` host cores: voxelize the full scene, then render
-    whole rows of view 0 (centre outward) until the time budget is spent.
+    bands of rows of view 0 (spread over the image) until the time budget is
+    spent.
     Returns (Mpix/s, description, extrapolated frame seconds)."""
     from oracle import oracle as O
     from cloudgb import configs
@@ -138,26 +176,12 @@ def cpu_frame_rate(wl, budget_s, threads):
     t0 = time.perf_counter()
     ov.voxelize(wl.sun_direction, *wl.sun_map, threads=threads)
     t_vox = time.perf_counter() - t0
-
-    class Cam:
-        pass
-    cam = Cam()
-    cd = wl.cameras[0]
-    cam.eye, cam.target, cam.up = cd["eye"], cd["target"], (0.0, 1.0, 0.0)
-    cam.fov_y_degrees, cam.width, cam.height = cd["fov"], cd["width"], cd["height"]
-    P = O.make_params(view_steps=c["view_steps"], sun_steps=c["sun_steps"],
-                      cone_half_angle=c["cone_half_angle"], cone_initial_height=c["cone_h0"],
-                      cone_min_radius=c["cone_min_radius"], density_scale=c["density_scale"],
-                      ambient=c["ambient"], noise_octaves=c["noise_octaves"],
-                      noise_seed=c["noise_seed"], noise_frequency=c["noise_frequency"],
-                      noise_lacunarity=c["noise_lacunarity"], noise_gain=c["noise_gain"])
+    cam = _oracle_camera(wl.cameras[0])
+    P = _oracle_params(c)
     W, H = cam.width, cam.height
     band = 8
-    # bands of rows from the centre outward (the centre holds the cloud)
-    starts = list(range(0, H, band))
-    starts.sort(key=lambda y: abs(y + band // 2 - H // 2))
     rows, t_render = 0, 0.0
-    for y0 in starts:
+    for y0 in _spread_bands(H, band):
         h = min(band, H - y0)
         t0 = time.perf_counter()
         ov.render(cam, P, wl.sun_direction, rect=(0, y0, W, h), threads=threads)
@@ -168,40 +192,129 @@ def cpu_frame_rate(wl, budget_s, threads):
     px = rows * W
     frame_s = t_vox + t_render * (W * H) / px
     desc = (f"FP32 port of the path on {threads} host threads: full 256^3 voxelize "
-            f"({t_vox:.2f} s) + {rows} of {H} rows of view 0 ({px} px, {t_render:.2f} s), "
+            f"({t_vox:.2f} s) + {rows} of {H} rows of view 0 in bands of 8 spread over the "
+            f"image ({px} px, {t_render:.2f} s), "
             f"frame time extrapolated per pixel")
     return (W * H) / frame_s / 1e6, desc, frame_s
 
 
 def run_reference(args):
+    """The reference arm: the reference's path restated on the CPU (the
+    oracle's FP32 build; its GL shaders cannot run here), all host threads.
+    Exactly `steps` timed steps; each step voxelizes the full scene and
+    renders bands of rows of the step's view (spread over the image), their
+    render time extrapolated per pixel to the whole 1080p frame, so that the
+    run ends within about a minute whatever `steps` is."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
+    from oracle import oracle as O
+    from cloudgb import configs
     wl = workload()
+    c = wl.cfg
     threads = os.cpu_count() or 1
-    budget = max(2.0, args.cpu_budget_s)
-    rates, desc = [], ""
-    t0 = time.perf_counter()
-    steps = max(1, min(args.steps, 4))
-    for _ in range(steps):
-        r, desc, _ = cpu_frame_rate(wl, budget / steps + 1.0, threads)
-        rates.append(r)
-    wall = time.perf_counter() - t0
-    value = sorted(rates)[len(rates) // 2]
-    ms = (wl.cfg["camera"]["width"] * wl.cfg["camera"]["height"]) / (value * 1e6) * 1e3
+    ov = O.OracleVolume(c["dim"], configs.VOLUME_BOUNDS, configs.VOLUME_POSITION, c["mips"], bits=32)
+    ov.set_boards(wl.positions, wl.scales, wl.densities)
+    P = _oracle_params(c)
+    cams = [_oracle_camera(cd) for cd in wl.cameras]
+    W, H = cams[0].width, cams[0].height
+    budget = max(2.0, args.cpu_budget_s * 4.0)
+    per_step = budget / max(1, args.steps + args.warmup)
+    band = 8
+    frame_s, rows_total, t_vox_total = [], 0, 0.0
+    t_start = time.perf_counter()
+    for k in range(args.warmup + args.steps):
+        cam = cams[k % len(cams)]
+        t0 = time.perf_counter()
+        ov.voxelize(wl.sun_direction, *wl.sun_map, threads=threads)
+        t_vox = time.perf_counter() - t0
+        rows, t_render = 0, 0.0
+        for y0 in _spread_bands(H, band):
+            h = min(band, H - y0)
+            t0 = time.perf_counter()
+            ov.render(cam, P, wl.sun_direction, rect=(0, y0, W, h), threads=threads)
+            t_render += time.perf_counter() - t0
+            rows += h
+            if t_vox + t_render >= per_step:
+                break
+        if k >= args.warmup:
+            frame_s.append(t_vox + t_render * H / rows)
+            rows_total += rows
+            t_vox_total += t_vox
+    wall = time.perf_counter() - t_start
+    total_s = float(sum(frame_s))
+    value = W * H * args.steps / total_s / 1e6
+    sample = (f"FP32 port of the path on {threads} host threads, {args.steps} steps: each step "
+              f"voxelizes the full 256^3 scene (mean {t_vox_total / args.steps:.3f} s) and "
+              f"renders {rows_total / args.steps:.0f} of {H} rows (bands of 8 spread over the image) "
+              f"of its view, "
+              f"render time extrapolated per pixel to the frame")
     line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": args.gpus,
-            "steps": steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(total_s / args.steps * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded SplitMix64 scene)", "impl": "reference",
-            "config": config_block(wl, {"cpu_wall_s": round(wall, 2),
-                                        "note": "the reference's GL path cannot run here (no "
-                                                "graphics stack); this is the FP32 CPU "
-                                                "restatement of its path, plain method"}),
+            "config": config_block(wl),
+            "reference_note": "the reference's GL path cannot run here (no graphics stack); "
+                              "this is the FP32 CPU restatement of its path, plain method",
+            "cpu_wall_s": round(wall, 2),
             "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": threads,
-                             "kind": "port", "sample": desc},
+                             "kind": "port", "sample": sample},
             "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def oracle_check(wl, views, tiles_per_view=3, tile=32, seed=5, threads=None):
+    """The checker, untimed: FP64 oracle renders of 32x32 tiles of the 1080p
+    views, compared with the GPU images of the same views.  `views` maps a
+    view index to {name: H x W x 4 float32 GPU image}.  Tiles per view: the
+    centre tile plus `tiles_per_view` tiles drawn (seeded) from tiles whose
+    GPU alpha is > 0.  Returns per image name the RMSE and max-abs over all
+    tiles, the worst view's RMSE and the tiles' pixel count."""
+    import numpy as np
+    from oracle import oracle as O
+    from cloudgb import configs
+    c = wl.cfg
+    threads = threads or os.cpu_count() or 1
+    ov = O.OracleVolume(c["dim"], configs.VOLUME_BOUNDS, configs.VOLUME_POSITION, c["mips"])
+    ov.set_boards(wl.positions, wl.scales, wl.densities)
+    ov.voxelize(wl.sun_direction, *wl.sun_map, threads=threads)
+    P = _oracle_params(c)
+    rng = np.random.default_rng(seed)
+    sq, mx, n = {}, {}, 0
+    worst = {}
+    for v, imgs in sorted(views.items()):
+        cd = wl.cameras[v]
+        W, H = cd["width"], cd["height"]
+        a = next(iter(imgs.values()))[..., 3]
+        ty, tx = H // tile, W // tile
+        occ = a[:ty * tile, :tx * tile].reshape(ty, tile, tx, tile).max(axis=(1, 3)) > 0
+        cand = np.argwhere(occ)
+        pick = [((H // 2 - tile // 2), (W // 2 - tile // 2))]
+        if len(cand):
+            for i in rng.choice(len(cand), min(tiles_per_view, len(cand)), replace=False):
+                pick.append((int(cand[i][0]) * tile, int(cand[i][1]) * tile))
+        cam = _oracle_camera(cd)
+        vsq = {}
+        for y0, x0 in pick:
+            ref = ov.render(cam, P, wl.sun_direction, rect=(x0, y0, tile, tile), threads=threads)
+            n += ref.size
+            for name, img in imgs.items():
+                d = img[y0:y0 + tile, x0:x0 + tile].astype(np.float64) - ref
+                sq[name] = sq.get(name, 0.0) + float((d * d).sum())
+                vsq[name] = vsq.get(name, 0.0) + float((d * d).sum())
+                mx[name] = max(mx.get(name, 0.0), float(np.abs(d).max()))
+        for name in vsq:
+            r = float(np.sqrt(vsq[name] / (len(pick) * tile * tile * 4)))
+            worst[name] = max(worst.get(name, 0.0), r)
+    out = {}
+    for name in sq:
+        out[name] = {"rmse": float(np.sqrt(sq[name] / n)), "max_abs": mx[name],
+                     "worst_view_rmse": worst[name]}
+    out["pixels"] = n // 4
+    out["tiles"] = f"{len(views)} views x (centre + {tiles_per_view} tiles with alpha > 0) of {tile}x{tile}"
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -336,6 +449,7 @@ def run_ours(args):
     img = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     hbm_peak, tensor_peak, peak_kind = load_peaks()
+    kw = wl.shader_kwargs()
 
     def make_volume(fmt):
         v = cloudgb.CloudVolume(c["dim"], configs.VOLUME_BOUNDS, configs.VOLUME_POSITION,
@@ -345,6 +459,9 @@ def run_ours(args):
         return v
 
     def run_path(vol, shader, steps, warmup, clocks=None):
+        """Time `steps` frames (voxelize + render of view k % 16); then an
+        untimed pass with per-stage events over the first 16 views, recording
+        each view's stage times and, for the surrogate, its shaded samples."""
         params = shader.params()
 
         def frame(k):
@@ -381,43 +498,62 @@ def run_ours(args):
             if sampler:
                 sampler.extend(lambda: frame(steps - 1), stream.synchronize)
                 sampler.__exit__()
-            # per-stage times (untimed pass with stage events on)
             ctx.set_timing(True)
-            stages = {}
-            for k in range(min(steps, 16)):
+            per_view = []
+            for k in range(min(steps, len(cams))):
                 flush.zero_()
                 _lib.check(lib.cg_voxelize(vol.handle, ctypes.byref(csun), sp), "cg_voxelize")
-                for name, ms in ctx.stage_times().items():
-                    stages.setdefault("voxelize." + name, []).append(ms)
+                st = {"voxelize." + n: ms for n, ms in ctx.stage_times().items()}
                 _lib.check(lib.cg_render(ctx.handle, vol.handle, ctypes.byref(ccams[k % len(ccams)]),
                                          ctypes.byref(params), ctypes.c_void_p(img.data_ptr()), 1,
                                          sp), "cg_render")
-                for name, ms in ctx.stage_times().items():
-                    stages.setdefault(name, []).append(ms)
+                st.update(ctx.stage_times())
+                if shader.useMlp:
+                    st["samples"] = ctx.last_samples()
+                per_view.append(st)
             ctx.set_timing(False)
         step_ms = [a.elapsed_time(b) for a, _, b in ev]
-        res = {"total_ms": float(sum(step_ms)), "vox_ms": float(np.mean([a.elapsed_time(m) for a, m, _ in ev])),
-               "render_ms": float(np.mean([m.elapsed_time(b) for _, m, b in ev])),
-               "launches": launches, "stages": {k: float(np.mean(v)) for k, v in stages.items()},
-               "clocks": sampler.summary() if sampler else None}
-        return res
+        keys = [k for k in per_view[0] if k != "samples"]
+        return {"total_ms": float(sum(step_ms)),
+                "vox_ms": float(np.mean([a.elapsed_time(m) for a, m, _ in ev])),
+                "render_ms": float(np.mean([m.elapsed_time(b) for _, m, b in ev])),
+                "launches": launches, "per_view": per_view,
+                "stages": {k: float(np.mean([v[k] for v in per_view])) for k in keys},
+                "clocks": sampler.summary() if sampler else None}
 
-    def image_of(vol, shader, cam):
-        out = np.empty((H, W, 4), np.float32)
-        shader.coneTrace(vol, cam, out=out)
-        return out
+    def mpix(ms):
+        return W * H / (ms / 1e3) / 1e6
 
-    # ---- plain FP32 path
+    def path_summary(r, extra=None):
+        d = {"frame_mpix_s": round(mpix(r["total_ms"] / args.steps), 2),
+             "render_mpix_s": round(mpix(r["render_ms"]), 2),
+             "voxelize_ms": round(r["vox_ms"], 4), "render_ms": round(r["render_ms"], 4),
+             "frame_ms": round(r["total_ms"] / args.steps, 4),
+             "stages_ms": {k: round(v, 4) for k, v in r["stages"].items()},
+             "launches_per_step": r["launches"] / args.steps}
+        if extra:
+            d.update(extra)
+        return d
+
+    # ---- plain FP32: both exact pipelines (fused trace; deferred march +
+    # exact shading), the faster one is the baseline of the speed-up
     vol32 = make_volume(cloudgb.FORMAT_RGBA32F)
-    plain_shader = cloudgb.ConeTraceShader(**wl.shader_kwargs())
-    plain = run_path(vol32, plain_shader, args.steps, args.warmup)
-    # executed-work counters of the timed views (untimed) -> algorithmic bytes
-    used = sorted({k % len(cams) for k in range(args.steps)})
-    per_view = {v: plain_shader.renderStats(vol32, cams[v]) for v in used}
-    alg_bytes = [(per_view[k % len(cams)]["view_samples"] + per_view[k % len(cams)]["sun_samples"])
-                 * 16 + W * H * 16 for k in range(args.steps)]
-    trace_ms = plain["stages"].get("trace", plain["render_ms"])
-    plain_achieved = float(np.mean(alg_bytes)) / (trace_ms / 1e3) / 1e9
+    plain_shader = cloudgb.ConeTraceShader(**kw)
+    deferred_shader = cloudgb.ConeTraceShader(pipeline=_lib.PIPELINE_DEFERRED, **kw)
+    plain_fused = run_path(vol32, plain_shader, args.steps, args.warmup)
+    plain_def = run_path(vol32, deferred_shader, args.steps, args.warmup)
+    plain = min(plain_fused, plain_def, key=lambda r: r["total_ms"])
+    plain_name = "fused" if plain is plain_fused else "deferred"
+    # executed-work counters of the first 16 views (untimed): algorithmic
+    # bytes of each fused-trace launch, paired with that view's trace time
+    stats = [plain_shader.renderStats(vol32, cams[k]) for k in range(len(plain_fused["per_view"]))]
+    # a view sample reads R and G (8 B of an RGBA32F texel per tap), a sun-cone
+    # sample R only (4 B); one texel's bytes per quadrilinear sample
+    alg = [s_["view_samples"] * 8 + s_["sun_samples"] * 4 + W * H * 16 for s_ in stats]
+    alg16 = [(s_["view_samples"] + s_["sun_samples"]) * 16 + W * H * 16 for s_ in stats]
+    trace_ms = [v["trace"] for v in plain_fused["per_view"]]
+    plain_achieved = float(sum(alg)) / (sum(trace_ms) / 1e3) / 1e9
+    tr_plain = load_traffic("trace_fused_rgba32f")
 
     # ---- BF16 volume + MLP surrogate (trained here, on the GPU)
     t0 = time.perf_counter()
@@ -426,32 +562,39 @@ def run_ours(args):
                                             scenes=16, seed=1000)
     train_s = time.perf_counter() - t0
     vol16 = make_volume(cloudgb.FORMAT_BF16_FP16)
-    mlp_shader = cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, **wl.shader_kwargs())
+    mlp_shader = cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, **kw)
     learned = run_path(vol16, mlp_shader, args.steps, args.warmup, clocks=True)
-    # quality: surrogate image vs the plain FP32 image of the same view
+    mlp_stage = "render_mlp" if "render_mlp" in learned["stages"] else "shade_mlp"
+    samples = [v["samples"] for v in learned["per_view"]]
+    mlp_ms = [v[mlp_stage] for v in learned["per_view"]]
+    mlp_tflops = sum(samples) * MLP_FLOP_PER_SAMPLE / (sum(mlp_ms) / 1e3) / 1e12
+    fallbacks = ctx.mlp_fallbacks()
+
+    # ---- quality (untimed): the production model's 1080p images of the 16
+    # views against the FP64 oracle on sampled tiles, and against the plain
+    # FP32 GPU image in full
     cloudgb.VoxelizeShader().voxelize(vol32, sun)
     cloudgb.VoxelizeShader().voxelize(vol16, sun)
-    ref = image_of(vol32, plain_shader, cams[0])
-    got = image_of(vol16, mlp_shader, cams[0])
-    err = ctx.error_stats(got, ref)  # reduced on the GPU in FP64
-    rmse = float(err["rmse_all"])
-    samples = int(ctypes.c_uint64(0).value)
-    sc = ctypes.c_uint64()
-    _lib.check(lib.cg_context_last_samples(ctx.handle, ctypes.byref(sc)))
-    samples = int(sc.value)
-    fallbacks = ctx.mlp_fallbacks()
-    shade_ms = learned["stages"].get("shade_mlp", float("nan"))
-    mlp_tflops = samples * MLP_FLOP_PER_SAMPLE / (shade_ms / 1e3) / 1e12
+    views, full = {}, []
+    for k in range(len(cams)):
+        ref = np.empty((H, W, 4), np.float32)
+        got = np.empty((H, W, 4), np.float32)
+        plain_shader.coneTrace(vol32, cams[k], out=ref)
+        mlp_shader.coneTrace(vol16, cams[k], out=got)
+        e = ctx.error_stats(got, ref)  # reduced on the GPU in FP64
+        full.append((e["rmse_all"], e["max_abs_all"]))
+        views[k] = {"bf16_mlp": got, "plain_fp32": ref}
+    chk = oracle_check(wl, views) if (rank == 0 or world == 1) else None
+    views = None
+    rmse_oracle = chk["bf16_mlp"]["rmse"] if chk else float(max(r for r, _ in full))
+    use_mlp = (chk is None or max(chk["bf16_mlp"]["rmse"], chk["bf16_mlp"]["worst_view_rmse"])
+               <= 1e-2)
 
-    use_mlp = rmse <= 1e-2
     head = learned if use_mlp else plain
-    head_shader = mlp_shader if use_mlp else plain_shader
+    head_shader = mlp_shader if use_mlp else (plain_shader if plain is plain_fused else deferred_shader)
     head_vol = vol16 if use_mlp else vol32
     total_ms = max_over_ranks(head["total_ms"], world)
     value = replica_rate(W * H, args.steps, world, total_ms)
-
-    def mpix(ms):
-        return W * H / (ms / 1e3) / 1e6
 
     # e2e through the public API: host boards in, pinned host image out
     out = cloudgb.HostBuffer((H, W, 4))
@@ -468,69 +611,105 @@ def run_ours(args):
             e2e_ms.append((t1 - t0) * 1e3)
     e2e_val = replica_rate(W * H, 1, world, max_over_ranks(float(np.median(e2e_ms)), world))
 
-    if use_mlp:
-        roofline = {"bound": "tensor", "kernel": "k_shade_mlp_tc", "achieved": round(mlp_tflops, 2),
+    tr_mlp = load_traffic("render_mlp_bf16" if mlp_stage == "render_mlp" else "shade_mlp_bf16")
+    kname = "k_render_mlp_tc" if mlp_stage == "render_mlp" else "k_shade_mlp_tc"
+    roofline_mlp = {"bound": "tensor", "kernel": kname, "achieved": round(mlp_tflops, 2),
                     "peak": tensor_peak, "peak_kind": peak_kind, "unit": "TFLOP/s",
                     "frac": round(mlp_tflops / tensor_peak, 4),
-                    "traffic": load_traffic("shade_mlp_bf16"),
-                    "flop_per_launch": samples * MLP_FLOP_PER_SAMPLE,
-                    "note": "surrogate inferences x 18,560 FLOP over the kernel's CUDA-event time"}
-    else:
-        roofline = None
+                    "traffic": tr_mlp.get("bytes_per_launch") if tr_mlp else None,
+                    "traffic_note": tr_mlp.get("source") if tr_mlp else None,
+                    "flop_per_sample": MLP_FLOP_PER_SAMPLE,
+                    "samples_per_view": samples, "kernel_ms_per_view": [round(x, 4) for x in mlp_ms],
+                    "limiter": tr_mlp.get("limiter") if tr_mlp else None,
+                    "issue_active": tr_mlp.get("issue_active") if tr_mlp else None,
+                    "tensor_pipe_active": tr_mlp.get("tensor_pipe_active") if tr_mlp else None,
+                    "note": "achieved = sum over the 16 views of (view's surrogate inferences x "
+                            "18,560 FLOP) / sum of the same views' kernel CUDA-event times"}
+    dram_gbs = (tr_plain["bytes_per_launch"] / (np.mean(trace_ms) / 1e3) / 1e9) if tr_plain else None
     roofline_plain = {"bound": "hbm", "kernel": "k_trace_fused", "achieved": round(plain_achieved, 1),
                       "peak": hbm_peak, "peak_kind": peak_kind, "unit": "GB/s",
                       "frac": round(plain_achieved / hbm_peak, 4),
-                      "traffic": load_traffic("trace_fused_rgba32f"),
-                      "alg_bytes_per_launch": int(np.mean(alg_bytes))}
+                      "traffic": tr_plain.get("bytes_per_launch") if tr_plain else None,
+                      "traffic_note": tr_plain.get("source") if tr_plain else None,
+                      "alg_bytes_per_launch": int(np.mean(alg)),
+                      "alg_bytes_per_launch_16B_per_sample": int(np.mean(alg16)),
+                      "dram_gbs": round(dram_gbs, 1) if dram_gbs else None,
+                      "dram_frac": round(dram_gbs / hbm_peak, 4) if dram_gbs else None,
+                      "limiter": tr_plain.get("limiter") if tr_plain else None,
+                      "issue_active": tr_plain.get("issue_active") if tr_plain else None,
+                      "note": "achieved = sum over the 16 views of (view samples x 8 B + sun-cone "
+                              "samples x 4 B + 16 B per pixel) / sum of the views' trace times; "
+                              "dram_gbs = the ncu DRAM bytes of one launch / the mean trace time"}
+    paths = {
+        "plain_fp32": path_summary(plain, {"pipeline": plain_name}),
+        "plain_fp32_fused": path_summary(plain_fused),
+        "plain_fp32_deferred": path_summary(plain_def),
+        "bf16_mlp": path_summary(learned, {
+            "rmse_vs_fp64_oracle": chk["bf16_mlp"]["rmse"] if chk else None,
+            "max_abs_vs_fp64_oracle": chk["bf16_mlp"]["max_abs"] if chk else None,
+            "worst_view_rmse_vs_fp64_oracle": chk["bf16_mlp"]["worst_view_rmse"] if chk else None,
+            "rmse_vs_plain_fp32_full_images": float(max(r for r, _ in full)),
+            "max_abs_vs_plain_fp32_full_images": float(max(m for _, m in full)),
+            "samples_per_frame_mean": float(np.mean(samples)),
+            "fallbacks_last_view": fallbacks, "train_s": round(train_s, 2),
+            "train_steps": args.mlp_steps, "train_samples": args.mlp_samples,
+            "final_loss": float(np.mean(losses[-100:]))}),
+        "speedup_render": round(plain["render_ms"] / learned["render_ms"], 3),
+        "speedup_frame": round(plain["total_ms"] / learned["total_ms"], 3),
+        "oracle_check": ({"sample": chk["tiles"], "pixels": chk["pixels"],
+                          "plain_fp32_max_abs": chk["plain_fp32"]["max_abs"],
+                          "plain_fp32_rmse": chk["plain_fp32"]["rmse"]} if chk else None),
+    }
     line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "bf16" if use_mlp else "f32",
             "data": "synthetic (seeded SplitMix64 scene)",
-            "config": config_block(wl, {
-                "path": "bf16_mlp" if use_mlp else "plain_fp32",
-                "paths": {
-                    "plain_fp32": {"frame_mpix_s": round(mpix(plain["total_ms"] / args.steps), 2),
-                                   "render_mpix_s": round(mpix(plain["render_ms"]), 2),
-                                   "voxelize_ms": round(plain["vox_ms"], 4),
-                                   "render_ms": round(plain["render_ms"], 4),
-                                   "stages_ms": {k: round(v, 4) for k, v in plain["stages"].items()},
-                                   "launches_per_step": plain["launches"] / args.steps},
-                    "bf16_mlp": {"frame_mpix_s": round(mpix(learned["total_ms"] / args.steps), 2),
-                                 "render_mpix_s": round(mpix(learned["render_ms"]), 2),
-                                 "voxelize_ms": round(learned["vox_ms"], 4),
-                                 "render_ms": round(learned["render_ms"], 4),
-                                 "stages_ms": {k: round(v, 4) for k, v in learned["stages"].items()},
-                                 "launches_per_step": learned["launches"] / args.steps,
-                                 "rmse_vs_plain_fp32": rmse,
-                                 "max_abs_vs_plain_fp32": float(err["max_abs_all"]),
-                                 "samples_per_frame": samples,
-                                 "fallbacks": fallbacks, "train_s": round(train_s, 2),
-                                 "train_steps": args.mlp_steps, "train_samples": args.mlp_samples,
-                                 "final_loss": float(np.mean(losses[-100:]))},
-                    "speedup_render": round(plain["render_ms"] / learned["render_ms"], 3),
-                    "speedup_frame": round(plain["total_ms"] / learned["total_ms"], 3)}}),
-            "roofline": roofline if roofline else roofline_plain,
+            "config": config_block(wl),
+            "path": "bf16_mlp" if use_mlp else "plain_fp32_" + plain_name,
+            "rmse_vs_fp64_oracle": rmse_oracle,
+            "paths": paths,
+            "roofline": roofline_mlp if use_mlp else roofline_plain,
             "roofline_plain": roofline_plain,
             "gpu_launches": int(head["launches"]),
             "clocks": learned["clocks"],
             "e2e": {"value": round(e2e_val, 3), "unit": UNIT,
                     "h2d_bytes_per_step": head_vol.count * 45, "d2h_bytes_per_step": W * H * 16}}
+    vol32.close()
+    vol16.close()
+    img = flush = None
+    torch.cuda.empty_cache()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         r, desc, _ = cpu_frame_rate(wl, args.cpu_budget_s, os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": round(r, 4), "unit": UNIT, "cores": os.cpu_count(),
                                 "kind": "port", "sample": desc}
+    if rank == 0 and world == 1 and not args.no_side_legs and args.width is None:
+        # the other workloads, short and separately timed, with their clocks
+        sub = argparse.Namespace(**vars(args))
+        sub.steps, sub.warmup = 10, 3
+        paths["batch"] = _short(run_batch(sub, ctx=ctx, emit=False))
+        sub.steps, sub.warmup = 6, 3
+        paths["precision"] = _short(run_precision(sub, ctx=ctx, emit=False))
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
 
 
-def run_batch(args):
+def _short(line):
+    """A side workload's bench line, kept under paths: its value, time,
+    clocks and own details."""
+    keep = ("metric", "value", "unit", "steps", "warmup", "ms_per_step", "gpu_launches",
+            "graph_launches", "clocks", "config")
+    return {k: line[k] for k in keep if k in line}
+
+
+def run_batch(args, ctx=None, emit=True):
     """The batching form: every frame voxelizes 48 clouds of uneven sizes and
     renders 128 views of uneven resolutions (plain FP32 method) as one CUDA
     graph (the render is one persistent launch); the launch shape is
-    autotuned first.  Metric: pixels of all views / frame time."""
+    autotuned first.  Metric: pixels of all views / frame time.  Returns the
+    bench line (printed when `emit`)."""
     import numpy as np
     import torch
 
@@ -539,7 +718,7 @@ def run_batch(args):
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
-    ctx = cloudgb.Context(local)
+    ctx = ctx or cloudgb.Context(local)
     cfg = configs.BATCH_48x128
     bw = Wm.build_batch(cfg)
     sun = cloudgb.Sun(bw.sun_direction, 1280, 720)
@@ -604,8 +783,14 @@ def run_batch(args):
                        "l2": "256 MiB buffer written between timed steps"},
             "graph_launches": graph_launches,
             "clocks": sampler.summary()}
-    print(json.dumps(line), flush=True)
+    if emit:
+        print(json.dumps(line), flush=True)
     graph.close()
+    for o in outs:
+        o.free()
+    for v in vols:
+        v.close()
+    return line
 
 
 def animated_positions(base, frames, dt, seed=11):
@@ -897,7 +1082,7 @@ def run_compat(args):
     vol.close()
 
 
-def run_precision(args):
+def run_precision(args, ctx=None, emit=True):
     """The precision form: 512^3 volume (16384 boards, 5-octave fBm) rendered at
     3840x2160 (128 view steps, 32-step sun cone), one step = voxelize + render
     of one of the 16 orbit views, with the BF16/FP16 volume (exact cone) and
@@ -911,7 +1096,7 @@ def run_precision(args):
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
-    ctx = cloudgb.Context(local)
+    ctx = ctx or cloudgb.Context(local)
     lib = _lib.load()
     cfg = configs.PRECISION_4K
     wl = Wm.build(cfg, width=args.width, height=args.height)
@@ -997,7 +1182,11 @@ def run_precision(args):
                        "l2": "256 MiB buffer written between timed steps"},
             "gpu_launches": int(head["launches"]),
             "clocks": head["clocks"]}
-    print(json.dumps(line), flush=True)
+    if emit:
+        print(json.dumps(line), flush=True)
+    img = flush = None
+    torch.cuda.empty_cache()
+    return line
 
 
 def main():

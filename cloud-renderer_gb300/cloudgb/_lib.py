@@ -167,6 +167,7 @@ SIGNATURES = [
     ("cg_mlp_infer", I, [P, P, I, P, I, P]),
     ("cg_mlp_gradient", I, [P, P, P, I, F, FP, FP, I]),
     ("cg_mlp_train", I, [P, P, P, ctypes.c_longlong, ctypes.POINTER(cg_train_params), FP]),
+    ("cg_mlp_check_train_timeout", I, [P, P, P, ctypes.c_longlong, I, ctypes.c_uint32]),
     ("cg_mlp_get_params", I, [P, FP, FP, FP, ctypes.POINTER(ctypes.c_int)]),
     ("cg_mlp_set_params", I, [P, FP, FP, FP, I]),
     ("cg_mlp_save", I, [P, ctypes.c_char_p]),

@@ -242,6 +242,13 @@ struct TrainArgs {
     int batch;
     int sequential;   // 1: rows offset + r (gradient evaluation), padding past N
     long long offset;
+    // tensor-core status word (zeroed by the host before the steps): bit 0 =
+    // a bounded wait ran out, bit 1 = the drain after it ran out as well
+    unsigned long long* status;
+    unsigned long long wait_ns;  // limit of every mbarrier wait
+    // failure-detection check only: thread 0 issues no MMA and no commit, so
+    // the layer barrier is never completed and the first wait must run out
+    int stall;
 };
 
 struct AdamArgs {
@@ -259,6 +266,10 @@ struct AdamArgs {
     float* loss_out;     // mean loss; index step - loss_base (or 0)
     int loss_slot_by_step;
     int loss_base;
+    // the training kernel's status word (NULL: none); when it is non-zero the
+    // partials may be stale or half-written, so no update is made and the
+    // step counter does not advance
+    const unsigned long long* status;
 };
 
 cudaError_t launch_march(VolDesc vd, CamDesc cam, TraceParams tp, SampleBuf sb, float4* out,
@@ -287,7 +298,8 @@ cudaError_t launch_mlp_features(VolDesc vd, const MlpDev& m, const float* pos, i
 cudaError_t launch_mlp_infer(const MlpDev& m, const float* feat, int n, float* out,
                              unsigned long long* status, cudaStream_t st);
 // one training step on the tensor cores (k_train_tc.cu); a tensor-core wait
-// that ran out of its time limit leaves a NaN in the CTA's loss slot
+// that ran out of its time limit sets ta.status and leaves a NaN in the CTA's
+// loss slot
 cudaError_t launch_mlp_train(const TrainArgs& ta, int ctas, cudaStream_t st);
 cudaError_t launch_mlp_adam(const AdamArgs& aa, cudaStream_t st);
 

@@ -11,6 +11,7 @@
 struct cg_mlp {
     cg_context* ctx = nullptr;
     DevBuf params, w16, m, v, step, ticket, partial, loss, grad;
+    DevBuf status;  // the training kernels' status word (see TrainArgs)
     cg_mlp_config cfg{};
     int host_step = 0;
     MlpConsts consts{};  // host copy of the biases / output row (see MlpConsts)
@@ -147,6 +148,8 @@ extern "C" cg_status cg_mlp_create(cg_context* ctx, uint64_t seed, cg_mlp** out)
     if (e == cudaSuccess) e = m->step.ensure(16);
     if (e == cudaSuccess) e = m->ticket.ensure(16);
     if (e == cudaSuccess) e = m->grad.ensure((MLP_NPARAM + 1) * 4);
+    if (e == cudaSuccess) e = m->status.ensure(16);
+    if (e == cudaSuccess) e = cudaMemset(m->status.p, 0, 16);
     if (e == cudaSuccess) e = cudaMemset(m->m.p, 0, MLP_NPARAM * 4);
     if (e == cudaSuccess) e = cudaMemset(m->v.p, 0, MLP_NPARAM * 4);
     if (e == cudaSuccess) e = cudaMemset(m->step.p, 0, 16);
@@ -181,7 +184,7 @@ extern "C" void cg_mlp_destroy(cg_mlp* m) {
     cudaSetDevice(m->ctx->device);
     cudaStreamSynchronize(m->ctx->stream);
     DevBuf* bufs[] = {&m->params, &m->w16, &m->m, &m->v, &m->step, &m->ticket,
-                      &m->partial, &m->loss, &m->grad};
+                      &m->partial, &m->loss, &m->grad, &m->status};
     for (DevBuf* b : bufs) b->release();
     cg_context* ctx = m->ctx;
     delete m;
@@ -267,6 +270,9 @@ extern "C" cg_status cg_context_mlp_fallbacks(cg_context* ctx, uint64_t* out) {
     unsigned long long h[2] = {0, 0};
     CG_CUDA(cudaMemcpy(h, ctx->fallbacks.p, 16, cudaMemcpyDeviceToHost));
     *out = h[0];
+    CG_CHECK((h[1] & 2ull) == 0, CG_ERR_DEVICE_FAULT,
+             "surrogate render: a tensor-core wait ran out of its time limit (1 s) and the "
+             "drain after it did not complete; the device must be treated as faulted");
     CG_CHECK(h[1] == 0, CG_ERR_DEVICE_FAULT,
              "surrogate render: a tensor-core wait ran out of its time limit (1 s)");
     return CG_OK;
@@ -380,6 +386,9 @@ extern "C" cg_status cg_mlp_infer(const cg_mlp* m, const float* features, int n,
     return CG_OK;
 }
 
+// the bound of every training-kernel wait (a wait longer than this is a fault)
+static const unsigned long long kTrainWaitNs = 1000000000ull;
+
 static TrainArgs train_args(const cg_mlp* m, const float* feat, const float* tau, long long n,
                             float sigma) {
     TrainArgs ta{};
@@ -396,7 +405,27 @@ static TrainArgs train_args(const cg_mlp* m, const float* feat, const float* tau
     ta.params = m->params.as<const float>();
     ta.w16 = m->w16.as<const __half>();
     ta.partial = m->partial.as<float>();
+    ta.status = m->status.as<unsigned long long>();
+    ta.wait_ns = kTrainWaitNs;
+    ta.stall = 0;
     return ta;
+}
+
+// The training kernels' status word after the stream has drained: CG_OK, or
+// CG_ERR_DEVICE_FAULT naming what stopped (no update was made from the
+// failing step on).
+static cg_status train_status(cg_mlp* m, const char* who) {
+    unsigned long long st = 0;
+    CG_CUDA(cudaMemcpy(&st, m->status.p, 8, cudaMemcpyDeviceToHost));
+    if (st == 0) return CG_OK;
+    if (st & 2ull)
+        return fail(CG_ERR_DEVICE_FAULT,
+                    "%s: a tensor-core wait ran out of its time limit and the drain after it "
+                    "did not complete; no update was made from that step on and the device "
+                    "must be treated as faulted", who);
+    return fail(CG_ERR_DEVICE_FAULT,
+                "%s: a tensor-core wait ran out of its time limit; no update was made from "
+                "that step on", who);
 }
 
 extern "C" cg_status cg_mlp_gradient(cg_mlp* m, const float* features, const float* tau, int n,
@@ -418,6 +447,7 @@ extern "C" cg_status cg_mlp_gradient(cg_mlp* m, const float* features, const flo
     const int ctas = (n + 127) / 128;
     CG_CUDA(cudaStreamSynchronize(s));
     CG_CUDA(m->partial.ensure((size_t)ctas * (MLP_NPARAM + 1) * 4));
+    CG_CUDA(cudaMemsetAsync(m->status.p, 0, 16, s));
     TrainArgs ta = train_args(m, df, dt, n, sigma);
     ta.sequential = 1;
     ta.offset = 0;
@@ -429,10 +459,13 @@ extern "C" cg_status cg_mlp_gradient(cg_mlp* m, const float* features, const flo
     aa.inv_batch = 1.f / (float)n;
     aa.grad_out = m->grad.as<float>();
     aa.loss_out = m->grad.as<float>() + MLP_NPARAM;
+    aa.status = m->status.as<const unsigned long long>();
     CG_LAUNCH(ctx, launch_mlp_adam(aa, s));
     std::vector<float> h(MLP_NPARAM + 1);
     CG_CUDA(cudaMemcpyAsync(h.data(), m->grad.p, (MLP_NPARAM + 1) * 4, cudaMemcpyDeviceToHost, s));
     CG_CUDA(cudaStreamSynchronize(s));
+    st = train_status(m, "cg_mlp_gradient");
+    if (st != CG_OK) return st;
     memcpy(grad, h.data(), MLP_NPARAM * 4);
     *loss = h[MLP_NPARAM];
     return CG_OK;
@@ -465,8 +498,34 @@ extern "C" void cg_train_params_default(cg_train_params* p) {
 // of up to 50 steps.  Batches walk a multiplicative permutation of the
 // dataset.  loss_per_step (host, may be NULL) receives the mean loss of
 // every step.
+static cg_status train_impl(cg_mlp* m, const float* d_features, const float* d_tau, long long n,
+                            const cg_train_params* tp, float* loss_per_step,
+                            unsigned long long wait_ns, int stall);
+
 extern "C" cg_status cg_mlp_train(cg_mlp* m, const float* d_features, const float* d_tau,
                                   long long n, const cg_train_params* tp, float* loss_per_step) {
+    return train_impl(m, d_features, d_tau, n, tp, loss_per_step, kTrainWaitNs, 0);
+}
+
+extern "C" cg_status cg_mlp_check_train_timeout(cg_mlp* m, const float* d_features,
+                                                const float* d_tau, long long n, int steps,
+                                                uint32_t limit_us) {
+    CG_CHECK(m, CG_ERR_INVALID_ARGUMENT, "cg_mlp_check_train_timeout: null pointer");
+    CG_CHECK(limit_us >= 1 && limit_us <= 1000000, CG_ERR_OUT_OF_RANGE,
+             "cg_mlp_check_train_timeout: limit %u us not in [1, 1e6]", limit_us);
+    CG_CHECK(steps >= 1 && steps <= 50, CG_ERR_OUT_OF_RANGE,
+             "cg_mlp_check_train_timeout: steps not in [1, 50]");
+    cg_train_params tp;
+    cg_train_params_default(&tp);
+    tp.steps = steps;
+    tp.batch = 1024;
+    return train_impl(m, d_features, d_tau, n, &tp, nullptr, (unsigned long long)limit_us * 1000ull,
+                      1);
+}
+
+static cg_status train_impl(cg_mlp* m, const float* d_features, const float* d_tau, long long n,
+                            const cg_train_params* tp, float* loss_per_step,
+                            unsigned long long wait_ns, int stall) {
     CG_CHECK(m && d_features && d_tau && tp, CG_ERR_INVALID_ARGUMENT, "cg_mlp_train: null pointer");
     CG_CHECK(n >= 1 && n <= (1ll << 31), CG_ERR_OUT_OF_RANGE, "cg_mlp_train: n not in [1, 2^31]");
     CG_CHECK(tp->steps >= 0 && tp->steps <= 10000000, CG_ERR_OUT_OF_RANGE,
@@ -489,8 +548,12 @@ extern "C" cg_status cg_mlp_train(cg_mlp* m, const float* d_features, const floa
                                                 668265263ull, 374761393ull, 1610612741ull};
     unsigned long long mul = primes[tp->seed % 6];
     while (gcd_u64(mul, (unsigned long long)n) != 1ull) mul += 2;
+    CG_CUDA(cudaMemsetAsync(m->status.p, 0, 16, s));
     TrainArgs ta = train_args(m, d_features, d_tau, n, tp->sigma);
-    ta.perm_mul = mul;
+    ta.wait_ns = wait_ns;
+    ta.stall = stall;
+    // reduced mod n: the kernel's product of two factors below n cannot wrap
+    ta.perm_mul = mul % (unsigned long long)n;
     ta.step = m->step.as<const int>();
     ta.batch = tp->batch;
     ta.sequential = 0;
@@ -511,6 +574,7 @@ extern "C" cg_status cg_mlp_train(cg_mlp* m, const float* d_features, const floa
     aa.loss_out = m->loss.as<float>();
     aa.loss_slot_by_step = 1;
     aa.loss_base = m->host_step;
+    aa.status = m->status.as<const unsigned long long>();
     // one eager step sets the kernels' shared-memory attributes before capture
     CG_LAUNCH(ctx, launch_mlp_train(ta, ctas, s));
     CG_LAUNCH(ctx, launch_mlp_adam(aa, s));
@@ -551,11 +615,16 @@ extern "C" cg_status cg_mlp_train(cg_mlp* m, const float* d_features, const floa
     CG_CUDA(cudaMemcpyAsync(tail.data(), m->params.as<float>() + MLP_B1, tail.size() * 4,
                             cudaMemcpyDeviceToHost, s));
     CG_CUDA(cudaStreamSynchronize(s));
+    const int done_steps = step - m->host_step;
     m->host_step = step;
     const float* t = tail.data();  // flat layout from MLP_B1 on
     set_consts(m, t, t + (MLP_B2 - MLP_B1), t + (MLP_B3 - MLP_B1), t + (MLP_W4 - MLP_B1),
                t[MLP_B4 - MLP_B1]);
-    return CG_OK;
+    cg_status st = train_status(m, "cg_mlp_train");
+    if (st != CG_OK && loss_per_step)
+        for (int i = done_steps < 0 ? 0 : done_steps; i < tp->steps; ++i)
+            loss_per_step[i] = std::nanf("");  // steps that made no update
+    return st;
 }
 
 extern "C" cg_status cg_mlp_get_params(const cg_mlp* m, float* params, float* adam_m,

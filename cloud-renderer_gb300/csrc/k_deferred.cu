@@ -20,7 +20,6 @@
 // sums each pixel's contributions in step order.
 #include <type_traits>
 
-#include "cg_deferred.cuh"
 #include "cg_internal.h"
 #include "cg_mlp.cuh"
 #include "cg_sample.cuh"

@@ -31,9 +31,16 @@ __device__ __forceinline__ int half_index(int p) {
 
 // Sum the CTA gradients in CTA order, scale by 1/batch, Adam update (or just
 // return the gradient).  The last CTA to finish advances the step counter.
+// A training kernel that stopped on a bounded wait (non-zero status) leaves
+// stale or half-written partials: no update then, and the step stays.
 __global__ void k_mlp_adam(AdamArgs aa) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const int step = aa.step ? *aa.step : 0;
+    if (aa.status && *aa.status) {
+        if (p == MLP_NPARAM && aa.loss_out)
+            aa.loss_out[aa.loss_slot_by_step ? step - aa.loss_base : 0] = __int_as_float(0x7fc00000);
+        return;
+    }
     if (p <= MLP_NPARAM) {
         float g = 0.f;
         for (int c = 0; c < aa.nparts; ++c) g += aa.partial[(size_t)c * (MLP_NPARAM + 1) + p];

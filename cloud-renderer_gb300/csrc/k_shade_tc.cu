@@ -31,7 +31,6 @@
 #include <algorithm>
 #include <atomic>
 
-#include "cg_deferred.cuh"
 #include "cg_internal.h"
 #include "cg_mlp.cuh"
 #include "cg_sample.cuh"
@@ -176,6 +175,18 @@ __device__ __forceinline__ bool sync_for_mma(bool bad) {
     const bool any_bad = __syncthreads_or(bad) != 0;
     tc::fence_after_sync();
     return any_bad;
+}
+
+// After a failed barrier (CTA-uniform): drain the outstanding commit, bounded
+// (only warps whose wait ran out have one: no MMA is issued after a failed
+// barrier), agree across the CTA whether every drain completed, and report:
+// status[1] |= 1, and |= 2 when a drain ran out too (tensor memory is then
+// freed with an MMA possibly in flight: the host treats the device as faulted).
+__device__ __forceinline__ void report_failure(uint64_t* bar, unsigned phase, bool bad,
+                                               unsigned long long* status) {
+    const bool drained = !bad || tc::mbar_wait(bar, phase, TC_WAIT_NS);
+    const bool undrained = __syncthreads_or(!drained) != 0;
+    if (threadIdx.x == 0) atomicOr(status + 1, undrained ? 3ull : 1ull);
 }
 
 // Weights W1..W3 scaled by 1/2, the ones column (8 rows) and the split
@@ -358,12 +369,7 @@ __global__ void __launch_bounds__(128, CTAS_PER_SM)
         ntile = *s_claim;  // written at layer 0, two barriers ago
     }
     if (!failed) failed = sync_for_mma(bad);  // the last tile's waits
-    if (failed) {
-        // drain the outstanding commit (bounded; only warps whose wait ran out
-        // have one: no MMA is issued after a failed barrier), then report
-        if (bad) tc::mbar_wait(bar, phase, TC_WAIT_NS);
-        if (tid == 0) atomicOr(status + 1, 1ull);
-    }
+    if (failed) report_failure(bar, phase, bad, status);
     unsigned tot = n_fallback, nv = n_valid;
     for (int o = 16; o > 0; o >>= 1) {
         tot += __shfl_xor_sync(0xffffffffu, tot, o);
@@ -454,10 +460,7 @@ __global__ void __launch_bounds__(128, CTAS_PER_SM)
         if (row < n && !bad) out[row] = m.tau_scale * mlp::softplus(y);
     }
     if (!failed) failed = sync_for_mma(bad);  // the last tile's waits
-    if (failed) {
-        if (bad) tc::mbar_wait(bar, phase, TC_WAIT_NS);
-        if (tid == 0) atomicOr(status + 1, 1ull);
-    }
+    if (failed) report_failure(bar, phase, bad, status);
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tmem, TC_TMEM_COLS);

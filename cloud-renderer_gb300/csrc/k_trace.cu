@@ -1,6 +1,5 @@
 // k_trace.cu -- per-pixel view march with the exact sun cone (one thread per
 // pixel), and the traceCone evaluator.
-#include "cg_deferred.cuh"
 #include "cg_internal.h"
 #include "cg_sample.cuh"
 

@@ -14,9 +14,10 @@
 // them; activations and gradients enter the MMAs as FP16.  The output layer
 // (64 -> 1) and its gradients are FP32 per row (dW4 by deterministic
 // warp-shuffle trees).  Transposed operands (dz^T, h^T, x^T) are written by
-// the threads that own the rows.  Every mbarrier wait is bounded (1 s of the
-// global timer); a timeout sets partial[NPARAM] to NaN (the loss slot) for the
-// host to report, drains and frees tensor memory.
+// the threads that own the rows.  Every mbarrier wait is bounded (ta.wait_ns
+// of the global timer, 1 s in training); a timeout sets the status word (and
+// partial[NPARAM] to NaN), drains, frees tensor memory and returns: k_mlp_adam
+// then makes no update and the host reports CG_ERR_DEVICE_FAULT.
 #include <cuda_fp16.h>
 
 #include <atomic>
@@ -28,7 +29,6 @@
 namespace {
 
 constexpr uint32_t TT_COLS = 256;  // [0, 64) forward / dh, [64, 160) dW | db
-constexpr uint64_t TT_WAIT_NS = 1000000000ull;
 constexpr int ZS = 66;  // halves per row of the z stores (conflict-free rows)
 // shared memory map (bytes from the 1024-aligned base)
 constexpr int O_X = 0;             // 128 x 128 B SW128 (K = 16 used)
@@ -185,9 +185,14 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
         idx = ta.offset + r;
         valid = idx < ta.N;
     } else {
+        // lin * perm_mul mod N with both factors reduced mod N first (perm_mul
+        // < N from the host, N <= 2^31): the product stays below 2^62 for any
+        // step count, so the walk remains a permutation of the rows
         const long long step = ta.step ? *ta.step : 0;
-        const unsigned long long lin = (unsigned long long)(step * ta.batch + r);
-        idx = (long long)((lin * ta.perm_mul) % (unsigned long long)ta.N);
+        const unsigned long long N = (unsigned long long)ta.N;
+        const unsigned long long lin = ((unsigned long long)step * (unsigned long long)ta.batch +
+                                        (unsigned long long)r) % N;
+        idx = (long long)((lin * ta.perm_mul) % N);
         valid = true;
     }
     __align__(16) __half xh[16];
@@ -216,7 +221,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
     unsigned phase = 0;
     bool failed = false;
     auto wait = [&]() {
-        bad = __any_sync(0xffffffffu, !tc::mbar_wait(bar, phase, TT_WAIT_NS));
+        bad = __any_sync(0xffffffffu, !tc::mbar_wait(bar, phase, ta.wait_ns));
         if (!bad) phase ^= 1u;
         tc::fence_after_sync();
     };
@@ -228,7 +233,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
             failed = true;
             break;
         }
-        if (tid == 0) {
+        if (tid == 0 && !ta.stall) {
             const uint32_t a = sb + (l == 0 ? O_X : (l == 1 ? O_H1 : O_H2));
             if (l == 0)
                 tc::mma_f16(tmem, tc::desc_sw128(a), tc::desc_sw32(sb + O_W1), ID64, 0u);
@@ -388,8 +393,17 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
     }
     if (!failed) failed = tt_sync(bad);
     if (failed) {
-        if (bad) tc::mbar_wait(bar, phase, TT_WAIT_NS);
-        if (tid == 0) part[MLP_NPARAM] = __int_as_float(0x7fc00000);  // NaN loss: reported
+        // only warps whose wait ran out have a commit pending (no MMA is
+        // issued after a failed barrier): drain it, bounded, and agree across
+        // the CTA whether every drain completed
+        const bool drained = !bad || tc::mbar_wait(bar, phase, ta.wait_ns);
+        const bool undrained = __syncthreads_or(!drained) != 0;
+        if (tid == 0) {
+            part[MLP_NPARAM] = __int_as_float(0x7fc00000);  // NaN loss
+            // bit 1: tensor memory is freed below with an MMA possibly still
+            // in flight, so the host must treat the device as faulted
+            atomicOr(ta.status, undrained ? 3ull : 1ull);
+        }
     } else {
         if (tid < 64)
             part[MLP_W4 + tid] =

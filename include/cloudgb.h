@@ -303,12 +303,26 @@ cg_status cg_mlp_features(const cg_volume* vol, const cg_mlp* mlp, const float* 
 cg_status cg_mlp_infer(const cg_mlp* mlp, const float* features, int n, float* out,
                        int on_device, void* stream);
 /* Mean loss and its gradient (CG_MLP_PARAMS floats, host) over n rows,
- * without an update: the training step's forward and backward kernels. */
+ * without an update: the training step's forward and backward kernels
+ * (CG_ERR_DEVICE_FAULT when one of their bounded waits ran out). */
 cg_status cg_mlp_gradient(cg_mlp* mlp, const float* features, const float* tau, int n,
                           float sigma, float* grad, float* loss, int on_device);
-/* Train on n device-resident rows (features n*16, exact optical depth n). */
+/* Train on n device-resident rows (features n*16, exact optical depth n).
+ * Every tensor-core wait of the training kernel is bounded (1 s): when one
+ * runs out, no update is made from that step on (parameters, Adam moments and
+ * step stay as the last completed step left them), the remaining entries of
+ * loss_per_step are NaN and the call returns CG_ERR_DEVICE_FAULT. */
 cg_status cg_mlp_train(cg_mlp* mlp, const float* d_features, const float* d_tau, long long n,
                        const cg_train_params* params, float* loss_per_step);
+/* Failure-detection check of the training kernels (no reference counterpart):
+ * `steps` (1 .. 50) training steps of 1024 rows over n device-resident rows in
+ * which the tensor-core layer barrier is never completed (no MMA is issued),
+ * with every bounded wait limited to limit_us (1 .. 1e6).  The waits must run
+ * out: returns CG_ERR_DEVICE_FAULT with no update made (parameters, Adam
+ * moments and step unchanged), and the context stays usable.  CG_OK would
+ * mean the bound did not fire. */
+cg_status cg_mlp_check_train_timeout(cg_mlp* mlp, const float* d_features, const float* d_tau,
+                                     long long n, int steps, uint32_t limit_us);
 /* FP32 parameters (W stored [out][in]: W1 16x64, b1, W2, b2, W3, b3, W4, b4),
  * Adam moments and step; m, v, step may be NULL. */
 cg_status cg_mlp_get_params(const cg_mlp* mlp, float* params, float* adam_m, float* adam_v,

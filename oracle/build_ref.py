@@ -2,7 +2,8 @@
 
 Compiles the reference's own shader sources -- res/billboard_vert_instanced.glsl,
 res/first_voxelize.glsl, res/second_voxelize.glsl and res/conetrace_frag.glsl
-of jaafersheriff/Cloud-Renderer, read where they lie under /root/reference --
+of jaafersheriff/Cloud-Renderer, read where they lie in the reference checkout
+(CLOUD_RENDERER_REFERENCE; by default its mount in the build container) --
 as C++ through oracle/ref_shim/glsl_shim.hpp, together with the driver
 oracle/ref_shim/ref_driver.inc that runs them the way the reference's host
 code does.  The translation unit is assembled in memory and piped to g++:
@@ -21,7 +22,9 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE = "/root/reference"
+# the reference checkout: CLOUD_RENDERER_REFERENCE, else its mount in the
+# build container
+REFERENCE = os.environ.get("CLOUD_RENDERER_REFERENCE", "/root/reference")
 SHIM = os.path.join(HERE, "ref_shim")
 OUT_DIR = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT_DIR, "libref_shaders.so")

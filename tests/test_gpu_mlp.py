@@ -244,6 +244,12 @@ def test_mlp_render_rmse_and_gain(ctx, trained):
     t_mlp = best(learned)
     t_exact = best(exact)
     assert t_mlp < t_exact, (t_mlp, t_exact)
+    # the gain over the method without it at the reduced budget: higher Mpix/s
+    # than the half-step exact cone on either exact pipeline, at lower RMSE
+    cheap_deferred = cloudgb.ConeTraceShader(
+        pipeline=_lib.PIPELINE_DEFERRED, **dict(kw, vctSteps=kw["vctSteps"] // 2))
+    t_cheap = min(best(cheap), best(cheap_deferred))
+    assert t_mlp < t_cheap, (t_mlp, t_cheap)
 
 
 def test_output_destinations_agree(ctx, trained):
