@@ -29,6 +29,7 @@ SOURCES = [
     ("k_mlp.cu", []),
     ("k_textures.cu", []),
     ("k_shade_tc.cu", []),
+    ("k_render_tc.cu", []),
     ("k_train_tc.cu", []),
     ("k_stats.cu", []),
     ("k_batch.cu", []),

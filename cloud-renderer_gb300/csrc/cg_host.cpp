@@ -1092,7 +1092,20 @@ extern "C" cg_status cg_render(cg_context* ctx, const cg_volume* v, const cg_cam
         stage_mark(ctx, s, "textures");
     }
     const VolDesc vd = desc_of(v);
-    if (params->use_mlp || params->pipeline == CG_PIPELINE_DEFERRED) {
+    if (params->use_mlp && params->pipeline != CG_PIPELINE_DEFERRED &&
+        32 * params->view_steps <= 0xFFFF) {
+        // march, network and composite in one persistent kernel
+        float* contrib = nullptr;
+        uint2* steps = nullptr;
+        st = ensure_render_slots(ctx, cam->width, cam->height, params->view_steps, contrib,
+                                 steps);
+        if (st != CG_OK) return st;
+        CG_CUDA(cudaMemsetAsync(ctx->fallbacks.p, 0, 32, s));
+        ctx->shaded_valid = true;
+        CG_LAUNCH(ctx, launch_render_mlp_tc(vd, cd, tp, md, contrib, steps, dst,
+                                            ctx->fallbacks.as<unsigned long long>(), s));
+        stage_mark(ctx, s, "render_mlp");
+    } else if (params->use_mlp || params->pipeline == CG_PIPELINE_DEFERRED) {
         // deferred: march records the contributing samples, shading resolves them
         SampleBuf sb;
         st = ensure_samples(ctx, cam->width, cam->height, params->view_steps, sb);

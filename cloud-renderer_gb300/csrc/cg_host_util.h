@@ -214,6 +214,10 @@ void stage_mark(cg_context* ctx, cudaStream_t s, const char* name);
 struct SampleBuf;
 struct MlpDev;
 cg_status ensure_samples(cg_context* ctx, int width, int height, int view_steps, SampleBuf& sb);
+// Contribution slots and step tables of the fused surrogate renderer
+// (launch_render_mlp_tc's layout), in the context's sample buffers.
+cg_status ensure_render_slots(cg_context* ctx, int width, int height, int view_steps,
+                              float*& contrib, uint2*& steps);
 cg_status mlp_device_for_render(const cg_mlp* m, const cg_volume* v, const cg_render_params* p,
                                 MlpDev& md);
 

@@ -286,6 +286,16 @@ cudaError_t launch_shade_mlp_tc(VolDesc vd, CamDesc cam, TraceParams tp, const M
                                 SampleBuf sb, unsigned long long* status, cudaStream_t st);
 // One CTA waits on an mbarrier nothing arrives on, bounded by limit_ns
 // (status: [1] |= 1 on the timeout, [3] = nanoseconds waited).
+// The fused surrogate renderer (k_render_tc.cu): march, tensor-core MLP and
+// composite in one persistent kernel.  contrib: per 8x4-pixel region
+// (raster order, ceil(W/8) * ceil(H/4) of them) 32 * view_steps floats;
+// steps: per region view_steps (first slot, lane ballot) pairs; dst: the
+// finished image.  status (4 words, zeroed before the launch): [0] +=
+// exact-cone fallbacks, [1] |= 1 when a bounded wait ran out (|= 2: and the
+// drain after it), [2] += samples shaded, [3] region claim counter.
+cudaError_t launch_render_mlp_tc(VolDesc vd, CamDesc cam, TraceParams tp, const MlpDev& m,
+                                 float* contrib, uint2* steps, float4* dst,
+                                 unsigned long long* status, cudaStream_t st);
 cudaError_t launch_wait_probe(uint64_t limit_ns, unsigned long long* status, cudaStream_t st);
 // img: the march's image (alpha); dst: where the finished pixels go (img, or
 // a device-addressable host image)

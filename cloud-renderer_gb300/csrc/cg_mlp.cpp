@@ -261,6 +261,24 @@ cg_status ensure_samples(cg_context* ctx, int width, int height, int view_steps,
     return CG_OK;
 }
 
+cg_status ensure_render_slots(cg_context* ctx, int width, int height, int view_steps,
+                              float*& contrib, uint2*& steps) {
+    const size_t regions = (size_t)((width + 7) / 8) * ((height + 3) / 4);
+    const size_t n = regions * (size_t)32 * view_steps;
+    CG_CHECK(n < (size_t)0xFFFFFFFFu, CG_ERR_OUT_OF_RANGE,
+             "render: %zu sample slots (pixels x view_steps) exceed 2^32", n);
+    const size_t step_words = 2 * regions * (size_t)view_steps;
+    if (ctx->samples_c.bytes < n * 4 || ctx->samples_cnt.bytes < step_words * 4) {
+        CG_CUDA(cudaStreamSynchronize(ctx->stream));
+        CG_CUDA(ctx->samples_c.ensure(n * 4));
+        CG_CUDA(ctx->samples_cnt.ensure(step_words * 4));
+    }
+    CG_CUDA(ctx->fallbacks.ensure(32));
+    contrib = ctx->samples_c.as<float>();
+    steps = reinterpret_cast<uint2*>(ctx->samples_cnt.as<unsigned>());
+    return CG_OK;
+}
+
 extern "C" cg_status cg_context_mlp_fallbacks(cg_context* ctx, uint64_t* out) {
     CG_CHECK(ctx && out, CG_ERR_INVALID_ARGUMENT, "cg_context_mlp_fallbacks: null pointer");
     *out = 0;

@@ -33,6 +33,7 @@
 
 #include "cg_internal.h"
 #include "cg_mlp.cuh"
+#include "cg_mlp_tc.cuh"
 #include "cg_sample.cuh"
 #include "cg_tc.cuh"
 
@@ -42,48 +43,11 @@ constexpr uint32_t TC_TMEM_COLS = 64;
 constexpr uint64_t TC_WAIT_NS = 1000000000ull;  // 1 s: a wait longer than this is a fault
 // shared memory map (bytes from the 1024-aligned base)
 constexpr int CTAS_PER_SM = 5;
-constexpr int OFF_ACT = 0;                 // 128 x 128 B activation tile (SW128)
-constexpr int OFF_W2 = 16384;              // 64 x 128 B (SW128)
-constexpr int OFF_W3 = OFF_W2 + 8192;      // 64 x 128 B (SW128)
-constexpr int OFF_W1 = OFF_W3 + 8192;      // 64 x 32 B (K = 16, SW32)
-constexpr int OFF_ONES = OFF_W1 + 2048;    // one 8-row atom: each row (1, 1, 0, ...) (SW32)
-constexpr int OFF_BIAS = OFF_ONES + 256;   // 3 x (64 x 32 B): row n (b_hi[n], b_lo[n], 0, ...)
-constexpr int OFF_BAR = OFF_BIAS + 3 * 2048;  // mbarrier + tensor-memory address
+constexpr int OFF_ACT = 0;                     // 128 x 128 B activation tile (SW128)
+constexpr int OFF_NET = 16384;                 // the network tiles (cg_mlp_tc.cuh)
+constexpr int OFF_BAR = OFF_NET + mlptc::NET_BYTES;  // mbarrier + tensor-memory address
 constexpr int SMEM_USED = OFF_BAR + 32;
 constexpr int SMEM_BYTES = SMEM_USED + 1024;  // + alignment slack
-
-constexpr uint32_t IDESC = tc::idesc_f16_f32(128, 64);
-
-// One FP16 weight row (`chunks` x 8 halves) into row r of a swizzled tile
-// (128B-swizzled rows of 8 chunks, or 32B-swizzled rows of 2), scaled by 1/2.
-template <int CHUNKS>
-__device__ __forceinline__ void stage_row(uint8_t* tile, int r, const __half* src) {
-    const __half2 k = __floats2half2_rn(0.5f, 0.5f);
-#pragma unroll
-    for (int c = 0; c < CHUNKS; ++c) {
-        uint4 v = *reinterpret_cast<const uint4*>(src + 8 * c);
-        __half2* h = reinterpret_cast<__half2*>(&v);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) h[q] = __hmul2(h[q], k);
-        *reinterpret_cast<uint4*>(tile + (CHUNKS == 8 ? tc::sw128_offset(r, c)
-                                                      : tc::sw32_offset(r, c))) = v;
-    }
-}
-
-// SiLU of 32 half-scaled accumulators (the bias is already in them) -> 16
-// FP16 pairs: with h = z/2, silu(z) = h + h * tanh(h), evaluated in FP32 and
-// rounded once.
-__device__ __forceinline__ void silu32(const uint32_t (&acc)[32], uint32_t (&out)[16]) {
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-        const float a = __uint_as_float(acc[2 * j]);
-        const float b = __uint_as_float(acc[2 * j + 1]);
-        float ta, tb;
-        asm("tanh.approx.f32 %0, %1;" : "=f"(ta) : "f"(a));
-        asm("tanh.approx.f32 %0, %1;" : "=f"(tb) : "f"(b));
-        out[j] = mlp::pack_h2(fmaf(a, ta, a), fmaf(b, tb, b));
-    }
-}
 
 // The exact cone for a sample whose features left the trained range (rare):
 // kept out of line so that the hot loop's registers are not sized for it.
@@ -121,49 +85,19 @@ __device__ __forceinline__ void pack_row(const VolDesc& vd, const ConeSchedule& 
                                          const MlpDev& m, const TraceParams& tp, unsigned slot,
                                          const float4& s, float g, const float (&f)[MLP_IN],
                                          Row& r, uint8_t* act) {
-    uint32_t x[8];
     r.slot = slot;
     r.w = s.w;
     r.g = g;
     r.tau_fb = -1.f;
-    if (slot != CG_NO_SLOT) {
-        if (!mlp::in_range(m, f)) r.tau_fb = exact_tau<FMT>(vd, cone, s.x, s.y, s.z, tp.sun);
-#pragma unroll
-        for (int q = 0; q < 8; ++q)
-            x[q] = mlp::pack_h2((f[2 * q] - m.mu[2 * q]) * m.inv_sd[2 * q],
-                                (f[2 * q + 1] - m.mu[2 * q + 1]) * m.inv_sd[2 * q + 1]);
-    } else {
-#pragma unroll
-        for (int q = 0; q < 8; ++q) x[q] = 0u;
-    }
-    const int tid = threadIdx.x;
-    *reinterpret_cast<uint4*>(act + tc::sw128_offset(tid, 0)) = make_uint4(x[0], x[1], x[2], x[3]);
-    *reinterpret_cast<uint4*>(act + tc::sw128_offset(tid, 1)) = make_uint4(x[4], x[5], x[6], x[7]);
+    if (slot != CG_NO_SLOT && !mlp::in_range(m, f))
+        r.tau_fb = exact_tau<FMT>(vd, cone, s.x, s.y, s.z, tp.sun);
+    mlptc::write_inputs(act, threadIdx.x, m, f, slot != CG_NO_SLOT);
 }
 
 __device__ __forceinline__ unsigned slot_at(const SampleBuf& sb, unsigned tile, unsigned ntiles,
                                             unsigned total) {
     const unsigned i = tile * 128u + threadIdx.x;
     return (tile < ntiles && i < total) ? sb.slot_of[i] : CG_NO_SLOT;
-}
-
-// Issue one layer (thread 0) and commit it to the barrier: the K slices of
-// the activations, then one more K = 16 slice that adds the bias (a column of
-// ones against the split bias b_hi + b_lo, exact to ~2^-22 relative).  The
-// ones operand is a single 8-row atom read by all 16 row groups (stride byte
-// offset 0); W1 (K = 16) is a 32B-swizzled tile.
-__device__ __forceinline__ void issue_layer(int layer, uint32_t d_tmem, uint32_t a_addr,
-                                            uint32_t w_addr, uint32_t ones_addr,
-                                            uint32_t bias_addr, uint64_t* bar) {
-    if (layer == 0) {
-        tc::mma_f16(d_tmem, tc::desc_sw128(a_addr), tc::desc_sw32(w_addr), IDESC, 0u);
-    } else {
-        for (int k = 0; k < 4; ++k)
-            tc::mma_f16(d_tmem, tc::desc_sw128(a_addr + 32u * k),
-                        tc::desc_sw128(w_addr + 32u * k), IDESC, k > 0 ? 1u : 0u);
-    }
-    tc::mma_f16(d_tmem, tc::desc_sw32(ones_addr, 0u), tc::desc_sw32(bias_addr), IDESC, 1u);
-    tc::mma_commit(bar);
 }
 
 // All writes of the CTA to the activation tiles -> visible to the tensor
@@ -189,68 +123,6 @@ __device__ __forceinline__ void report_failure(uint64_t* bar, unsigned phase, bo
     if (threadIdx.x == 0) atomicOr(status + 1, undrained ? 3ull : 1ull);
 }
 
-// Weights W1..W3 scaled by 1/2, the ones column (8 rows) and the split
-// half-scaled biases (32B-swizzled, K = 16) into the CTA's shared tiles.
-__device__ __forceinline__ void stage_network(uint8_t* base, const MlpDev& m, int tid) {
-    for (int r = tid; r < 64; r += blockDim.x) {
-        stage_row<2>(base + OFF_W1, r, m.w16 + MLP_H_W1 + r * 16);
-        stage_row<8>(base + OFF_W2, r, m.w16 + MLP_H_W2 + r * 64);
-        stage_row<8>(base + OFF_W3, r, m.w16 + MLP_H_W3 + r * 64);
-    }
-    // the ones column (8 rows) and the split half-scaled biases (32B-swizzled,
-    // K = 16)
-    if (tid < 8) {
-        const __half one = __float2half_rn(1.f);
-        const uint32_t ones = (uint32_t)__half_as_ushort(one) | ((uint32_t)__half_as_ushort(one) << 16);
-        *reinterpret_cast<uint4*>(base + OFF_ONES + tc::sw32_offset(tid, 0)) =
-            make_uint4(ones, 0u, 0u, 0u);
-        *reinterpret_cast<uint4*>(base + OFF_ONES + tc::sw32_offset(tid, 1)) =
-            make_uint4(0u, 0u, 0u, 0u);
-    }
-    {
-        for (int i = tid; i < 3 * 64; i += blockDim.x) {
-            const int l = i >> 6, n = i & 63;
-            const float hb = m.k.hb[i];
-            const __half hi = __float2half_rn(hb);
-            const __half lo = __float2half_rn(hb - __half2float(hi));
-            uint8_t* tile = base + OFF_BIAS + 2048 * l;
-            *reinterpret_cast<uint4*>(tile + tc::sw32_offset(n, 0)) = make_uint4(
-                (uint32_t)__half_as_ushort(hi) | ((uint32_t)__half_as_ushort(lo) << 16), 0u, 0u, 0u);
-            *reinterpret_cast<uint4*>(tile + tc::sw32_offset(n, 1)) = make_uint4(0u, 0u, 0u, 0u);
-        }
-    }
-}
-
-// One layer's epilogue for this thread's row: tensor memory -> SiLU, 32
-// columns at a time, written as the next layer's FP16 activations (layers 0,
-// 1) or folded into the FP32 64 -> 1 output (layer 2, returned with b4).
-__device__ __forceinline__ float layer_epilogue(int layer, uint32_t dw, uint8_t* act, int tid,
-                                                const MlpDev& m) {
-    float yy = m.k.b4;
-#pragma unroll
-    for (int half = 0; half < 2; ++half) {
-        uint32_t acc[32];
-        tc::tmem_ld32(dw + 32u * half, acc);
-        uint32_t h[16];
-        silu32(acc, h);
-        if (layer < 2) {
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-                *reinterpret_cast<uint4*>(act + tc::sw128_offset(tid, 4 * half + q)) =
-                    make_uint4(h[4 * q], h[4 * q + 1], h[4 * q + 2], h[4 * q + 3]);
-        } else {
-            const float* w4 = m.k.w4 + 32 * half;
-#pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                const float2 v = __half22float2(*reinterpret_cast<const __half2*>(&h[q]));
-                yy = fmaf(w4[2 * q], v.x, yy);
-                yy = fmaf(w4[2 * q + 1], v.y, yy);
-            }
-        }
-    }
-    return yy;
-}
-
 template <int FMT>
 __global__ void __launch_bounds__(128, CTAS_PER_SM)
     k_shade_mlp_tc(const __grid_constant__ VolDesc vd, const __grid_constant__ TraceParams tp,
@@ -266,7 +138,7 @@ __global__ void __launch_bounds__(128, CTAS_PER_SM)
     unsigned* s_claim = reinterpret_cast<unsigned*>(base + OFF_BAR + 12);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-    stage_network(base, m, tid);
+    mlptc::stage_network(base + OFF_NET, m, tid, blockDim.x);
     if (tid == 0) {
         tc::mbar_init(bar, 1);
         tc::fence_mbar_init();
@@ -282,10 +154,7 @@ __global__ void __launch_bounds__(128, CTAS_PER_SM)
     const uint32_t tmem = *tslot;
     const uint32_t dw = tmem + ((uint32_t)(warp * 32) << 16);
     const uint32_t a_addr = tc::smem_addr(act);
-    const uint32_t w_addr[3] = {tc::smem_addr(base + OFF_W1), tc::smem_addr(base + OFF_W2),
-                                tc::smem_addr(base + OFF_W3)};
-    const uint32_t ones_addr = tc::smem_addr(base + OFF_ONES);
-    const uint32_t bias_addr = tc::smem_addr(base + OFF_BIAS);
+    const uint32_t net_addr = tc::smem_addr(base + OFF_NET);
     const float amb = tp.ambient;
     const unsigned total = *sb.flat_total;
     const unsigned ntiles = (total + 127u) / 128u;
@@ -323,8 +192,7 @@ __global__ void __launch_bounds__(128, CTAS_PER_SM)
                 break;
             }
             if (tid == 0) {
-                issue_layer(layer, tmem, a_addr, w_addr[layer], ones_addr,
-                            bias_addr + 2048u * layer, bar);
+                mlptc::issue_layer(layer, tmem, a_addr, net_addr, bar);
                 // claim the tile after next (read by all after the next sync)
                 if (layer == 0)
                     *s_claim = 2u * gridDim.x +
@@ -345,7 +213,7 @@ __global__ void __launch_bounds__(128, CTAS_PER_SM)
             // ---- epilogue: TMEM -> bias + SiLU, 32 columns at a time; the
             // last layer folds the 64 -> 1 output in FP32
             if (!bad) {
-                const float yy = layer_epilogue(layer, dw, act, tid, m);
+                const float yy = mlptc::layer_epilogue(layer, dw, act, tid, m);
                 if (layer == 2) y = yy;
             }
             tc::fence_before_sync();
@@ -398,7 +266,7 @@ __global__ void __launch_bounds__(128, CTAS_PER_SM)
     uint64_t* bar = reinterpret_cast<uint64_t*>(base + OFF_BAR);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(base + OFF_BAR + 8);
     const int tid = threadIdx.x, warp = tid >> 5;
-    stage_network(base, m, tid);
+    mlptc::stage_network(base + OFF_NET, m, tid, blockDim.x);
     if (tid == 0) {
         tc::mbar_init(bar, 1);
         tc::fence_mbar_init();
@@ -414,10 +282,7 @@ __global__ void __launch_bounds__(128, CTAS_PER_SM)
     const uint32_t tmem = *tslot;
     const uint32_t dw = tmem + ((uint32_t)(warp * 32) << 16);
     const uint32_t a_addr = tc::smem_addr(act);
-    const uint32_t w_addr[3] = {tc::smem_addr(base + OFF_W1), tc::smem_addr(base + OFF_W2),
-                                tc::smem_addr(base + OFF_W3)};
-    const uint32_t ones_addr = tc::smem_addr(base + OFF_ONES);
-    const uint32_t bias_addr = tc::smem_addr(base + OFF_BIAS);
+    const uint32_t net_addr = tc::smem_addr(base + OFF_NET);
     unsigned phase = 0;
     bool failed = false, bad = false;  // bad: a wait of this warp ran out
     const int ntiles = (n + 127) / 128;
@@ -445,13 +310,12 @@ __global__ void __launch_bounds__(128, CTAS_PER_SM)
                 break;
             }
             if (tid == 0)
-                issue_layer(layer, tmem, a_addr, w_addr[layer], ones_addr,
-                            bias_addr + 2048u * layer, bar);
+                mlptc::issue_layer(layer, tmem, a_addr, net_addr, bar);
             bad = __any_sync(0xffffffffu, !tc::mbar_wait(bar, phase, TC_WAIT_NS));
             if (!bad) phase ^= 1u;
             tc::fence_after_sync();
             if (!bad) {
-                const float yy = layer_epilogue(layer, dw, act, tid, m);
+                const float yy = mlptc::layer_epilogue(layer, dw, act, tid, m);
                 if (layer == 2) y = yy;
             }
             tc::fence_before_sync();

@@ -117,14 +117,20 @@ typedef struct cg_render_params {
     cg_noise noise;
     int use_mlp;               /* 1: sun cone replaced by the MLP surrogate */
     const cg_mlp* mlp;         /* required when use_mlp != 0 */
-    int pipeline;              /* cg_pipeline (exact cone only; the MLP is always deferred) */
+    int pipeline;              /* cg_pipeline */
 } cg_render_params;
 
 /* Kernel organisation of an exact-cone render.  Both give the same image
  * (same samples, same per-pixel summation order). */
 typedef enum cg_pipeline {
-    CG_PIPELINE_FUSED = 0,   /* one thread per pixel marches and traces its cones */
-    CG_PIPELINE_DEFERRED = 1 /* march records contributing samples; cones in full warps */
+    /* exact cone: one thread per pixel marches and traces its cones;
+     * MLP surrogate: one persistent kernel marches, runs the network on the
+     * tensor cores and composites (view_steps <= 2047; above, deferred) */
+    CG_PIPELINE_FUSED = 0,
+    /* march records the contributing samples; the sun term is evaluated for
+     * them in full warps (exact cone) or 128-row tensor-core tiles (MLP),
+     * then each pixel sums its samples in step order */
+    CG_PIPELINE_DEFERRED = 1
 } cg_pipeline;
 
 /* Snapshot of a volume's layout, for readback. */

@@ -252,6 +252,67 @@ def test_mlp_render_rmse_and_gain(ctx, trained):
     assert t_mlp < t_cheap, (t_mlp, t_cheap)
 
 
+@pytest.mark.parametrize("size", [(1920, 1080), (333, 197)])
+def test_fused_render_matches_deferred(ctx, trained, size):
+    """The fused surrogate renderer (march, tensor-core network and composite
+    in one persistent kernel) computes the same samples, network outputs and
+    step-order sums as the deferred form (march, shading tiles, accumulate):
+    images within 1e-6, the same sample and fallback counts.  333 x 197 has
+    ragged 8x4 regions on the right and bottom edges."""
+    mlp, _, _ = trained
+    cfg = configs.PLAIN_1080P
+    W, H = size
+    wl = workload.build(cfg, width=W, height=H)
+    vol = cloudgb.CloudVolume(cfg["dim"], configs.VOLUME_BOUNDS, configs.VOLUME_POSITION,
+                              cfg["mips"], fmt=cloudgb.FORMAT_BF16_FP16, ctx=ctx)
+    vol.set_billboards(wl.positions, wl.scales, wl.densities)
+    vol.update()
+    cloudgb.VoxelizeShader().voxelize(vol, cloudgb.Sun(wl.sun_direction, *wl.sun_map))
+    kw = wl.shader_kwargs()
+    fused = cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, **kw)
+    deferred = cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, pipeline=_lib.PIPELINE_DEFERRED, **kw)
+    for v in (0, 5, 11):
+        cam = workload.make_camera(wl.cameras[v])
+        a = fused.coneTrace(vol, cam)
+        na, fa = ctx.last_samples(), ctx.mlp_fallbacks()
+        b = deferred.coneTrace(vol, cam)
+        nb, fb = ctx.last_samples(), ctx.mlp_fallbacks()
+        assert na == nb and na > 1000, (na, nb)
+        assert fa == fb
+        assert np.abs(a - b).max() <= 1e-6, float(np.abs(a - b).max())
+        assert a[..., 3].max() > 0.1
+        # deterministic: the same image again
+        assert np.array_equal(a, fused.coneTrace(vol, cam))
+    vol.close()
+
+
+def test_fused_render_edge_cases(ctx, trained):
+    """No sample at all (the camera looks away from the box), a single 8x4
+    region (most CTAs get no work), and 1 x 1 pixels: the kernel's end
+    protocol completes and the images equal the deferred form's."""
+    mlp, _, _ = trained
+    cfg = configs.PLAIN_1080P
+    wl = workload.build(cfg, width=64, height=64)
+    vol = cloudgb.CloudVolume(cfg["dim"], configs.VOLUME_BOUNDS, configs.VOLUME_POSITION,
+                              cfg["mips"], fmt=cloudgb.FORMAT_BF16_FP16, ctx=ctx)
+    vol.set_billboards(wl.positions, wl.scales, wl.densities)
+    vol.update()
+    cloudgb.VoxelizeShader().voxelize(vol, cloudgb.Sun(wl.sun_direction, *wl.sun_map))
+    kw = wl.shader_kwargs()
+    fused = cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, **kw)
+    deferred = cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, pipeline=_lib.PIPELINE_DEFERRED, **kw)
+    away = cloudgb.Camera((0.5, 0.5, -1.5), (0.5, 0.5, -3.0), width=200, height=100)
+    img = fused.coneTrace(vol, away)
+    assert ctx.last_samples() == 0 and not img.any()
+    for w, h in ((8, 4), (1, 1), (7, 3)):
+        cam = cloudgb.Camera((0.5, 0.5, -1.5), (0.5, 0.5, 0.5), fov_y_degrees=2.0, width=w,
+                             height=h)
+        a = fused.coneTrace(vol, cam)
+        b = deferred.coneTrace(vol, cam)
+        assert np.abs(a - b).max() <= 1e-6
+    vol.close()
+
+
 def test_output_destinations_agree(ctx, trained):
     # the finished image written straight into page-locked host memory, copied
     # back into pageable memory, or left on the device: the same bytes, for the
@@ -263,6 +324,8 @@ def test_output_destinations_agree(ctx, trained):
     cam = workload.make_camera(wl.cameras[1])
     kw = wl.shader_kwargs()
     for shader in (cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, **kw),
+                   cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, pipeline=_lib.PIPELINE_DEFERRED,
+                                           **kw),
                    cloudgb.ConeTraceShader(**kw),
                    cloudgb.ConeTraceShader(pipeline=_lib.PIPELINE_DEFERRED, **kw)):
         dev = cloudgb.DeviceBuffer(200 * 120 * 16)
