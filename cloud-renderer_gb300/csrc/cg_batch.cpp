@@ -123,6 +123,7 @@ extern "C" cg_status cg_context_get_trace_config(const cg_context* ctx, cg_trace
 extern "C" cg_status cg_render_batch(cg_context* ctx, const cg_batch_view* views, int n,
                                      const cg_render_params* params,
                                      const cg_trace_config* config, void* stream) {
+    NvtxRange nvtx_("cg_render_batch");
     CG_CHECK(ctx, CG_ERR_INVALID_ARGUMENT, "cg_render_batch: context is NULL");
     const cg_trace_config cfg = config ? *config : ctx->trace_cfg;
     CG_CHECK(config_ok(&cfg), CG_ERR_OUT_OF_RANGE,
@@ -144,6 +145,7 @@ extern "C" cg_status cg_render_batch(cg_context* ctx, const cg_batch_view* views
 extern "C" cg_status cg_autotune(cg_context* ctx, const cg_batch_view* views, int n,
                                  const cg_render_params* params, int repeats,
                                  cg_trace_config* best, float* ms) {
+    NvtxRange nvtx_("cg_autotune");
     CG_CHECK(ctx && best, CG_ERR_INVALID_ARGUMENT, "cg_autotune: null pointer");
     CG_CHECK(repeats >= 1 && repeats <= 1000, CG_ERR_OUT_OF_RANGE,
              "cg_autotune: repeats %d not in [1, 1000]", repeats);
@@ -349,6 +351,7 @@ extern "C" cg_status cg_frame_graph_create(cg_context* ctx, cg_volume* const* vo
 }
 
 extern "C" cg_status cg_frame_graph_launch(cg_frame_graph* g, void* stream) {
+    NvtxRange nvtx_("cg_frame_graph_launch");
     CG_CHECK(g && g->exec, CG_ERR_INVALID_ARGUMENT, "cg_frame_graph_launch: no graph");
     CG_CUDA(cudaSetDevice(g->ctx->device));
     // a billboard upload that reallocated a volume's buffers invalidates the

@@ -133,6 +133,7 @@ extern "C" cg_status cg_compat_noise_map(uint32_t seed, float* out) {
 extern "C" cg_status cg_render_compat(cg_context* ctx, const cg_volume* v, const cg_camera* cam,
                                       const cg_compat_params* params, float* rgba_out,
                                       int out_on_device, void* stream) {
+    NvtxRange nvtx_("cg_render_compat");
     CG_CHECK(ctx && v && cam && params && rgba_out, CG_ERR_INVALID_ARGUMENT,
              "cg_render_compat: null pointer");
     CG_CHECK(v->ctx == ctx, CG_ERR_INVALID_ARGUMENT,

@@ -702,6 +702,7 @@ static float highlight_offset(const cg_volume* v) {
 
 
 extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) {
+    NvtxRange nvtx_("cg_voxelize");
     CG_CHECK(v && sun, CG_ERR_INVALID_ARGUMENT, "cg_voxelize: null pointer");
     CG_CHECK(sun->map_width >= 1 && sun->map_height >= 1 && sun->map_width <= 16384 &&
                  sun->map_height <= 16384,
@@ -757,29 +758,38 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
     // clearGPU (CloudVolume.cpp:96-100) + clearPositionMap (VoxelizeShader.cpp:185-187)
     CG_CUDA(cudaMemsetAsync(v->keys.p, 0xFF, texels * 8, sd));
     CG_CUDA(cudaMemsetAsync(v->mask.p, 0, n0, sd));
-    // pass 1: sun-view nearest-surface map
-    if (b.n) CG_LAUNCH(ctx, launch_sunmap(b, fr, v->keys.as<uint64_t>(), sd));
-    // pass 2: highlight stores
-    CG_LAUNCH(ctx, launch_highlight(b, fr, v->keys.as<uint64_t>(), v->posmap.as<float4>(), v->D,
-                                    v->wmin, v->range, highlight_offset(v),
-                                    v->mask.as<uint8_t>(), sd));
-    CG_CUDA(cudaEventRecord(ctx->join_ev, sd));
-    CG_CUDA(cudaMemsetAsync(bins.count, 0, (size_t)bins.nbricks * 4, s));
-    // raw cells, brick grids (rewritten by the dilation) and the occupied box
-    CG_CUDA(cudaMemsetAsync(v->occ.p, 0, occ_box_offset(v->raw_total) + 6 * sizeof(int), s));
-    // brick bins
-    if (b.n) CG_LAUNCH(ctx, launch_bin_count(b, v->D, bins, s));
-    CG_LAUNCH(ctx, launch_bin_scan(bins, s));
-    if (b.n) CG_LAUNCH(ctx, launch_bin_fill(b, v->D, bins, s));
+    {
+        NvtxRange r("voxelize.sun_pass");
+        // pass 1: sun-view nearest-surface map
+        if (b.n) CG_LAUNCH(ctx, launch_sunmap(b, fr, v->keys.as<uint64_t>(), sd));
+        // pass 2: highlight stores
+        CG_LAUNCH(ctx, launch_highlight(b, fr, v->keys.as<uint64_t>(), v->posmap.as<float4>(),
+                                        v->D, v->wmin, v->range, highlight_offset(v),
+                                        v->mask.as<uint8_t>(), sd));
+        CG_CUDA(cudaEventRecord(ctx->join_ev, sd));
+    }
+    {
+        NvtxRange r("voxelize.bins");
+        CG_CUDA(cudaMemsetAsync(bins.count, 0, (size_t)bins.nbricks * 4, s));
+        // raw cells, brick grids (rewritten by the dilation) and the occupied box
+        CG_CUDA(cudaMemsetAsync(v->occ.p, 0, occ_box_offset(v->raw_total) + 6 * sizeof(int), s));
+        // brick bins
+        if (b.n) CG_LAUNCH(ctx, launch_bin_count(b, v->D, bins, s));
+        CG_LAUNCH(ctx, launch_bin_scan(bins, s));
+        if (b.n) CG_LAUNCH(ctx, launch_bin_fill(b, v->D, bins, s));
+    }
     stage_mark(ctx, s, "bins");
     CG_CUDA(cudaStreamWaitEvent(s, ctx->join_ev, 0));
     // the sun-view pass's time beyond the binning
     stage_mark(ctx, s, "sun");
     // coverage splat + level 0 + fused mips
     int fused = (v->D % CG_BRICK == 0) ? std::min(CG_FUSED_MIPS, v->L - 1) : 0;
-    CG_LAUNCH(ctx, launch_splat(b, bins, v->mask.as<uint8_t>(), vd, v->pyr.p,
-                                v->count.as<uint32_t>(), v->dq.as<uint32_t>(), fused,
-                                raw_of(v), false, s));
+    {
+        NvtxRange r("voxelize.splat");
+        CG_LAUNCH(ctx, launch_splat(b, bins, v->mask.as<uint8_t>(), vd, v->pyr.p,
+                                    v->count.as<uint32_t>(), v->dq.as<uint32_t>(), fused,
+                                    raw_of(v), false, s));
+    }
     stage_mark(ctx, s, "splat");
     // the occupancy dilation (raw cells -> brick grids, occupied box) and the
     // remaining mips are independent: the dilation runs on the side stream
@@ -1043,6 +1053,7 @@ cg_status ensure_noise(cg_context* ctx, const cg_volume* v, TraceParams& tp,
 extern "C" cg_status cg_render(cg_context* ctx, const cg_volume* v, const cg_camera* cam,
                                const cg_render_params* params, float* rgba_out,
                                int out_on_device, void* stream) {
+    NvtxRange nvtx_("cg_render");
     CG_CHECK(ctx && v && cam && params && rgba_out, CG_ERR_INVALID_ARGUMENT,
              "cg_render: null pointer");
     CG_CHECK(v->ctx == ctx, CG_ERR_INVALID_ARGUMENT, "cg_render: volume of another context");

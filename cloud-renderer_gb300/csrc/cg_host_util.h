@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cmath>
 #include <cstdarg>
@@ -209,6 +210,16 @@ void context_release(cg_context* ctx);
 // end of a named stage (no-ops unless timing is on).
 void stage_begin(cg_context* ctx, cudaStream_t s);
 void stage_mark(cg_context* ctx, cudaStream_t s, const char* name);
+
+// NVTX range over a scope: profilers (ncu --nvtx, nsys) attribute the launches
+// enqueued inside it to `name`.  Without an attached tool the calls return at
+// once (NVTX v3 is header-only and loads a tool library only when one is set).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // cg_mlp.cpp
 struct SampleBuf;

@@ -544,6 +544,7 @@ extern "C" cg_status cg_mlp_check_train_timeout(cg_mlp* m, const float* d_featur
 static cg_status train_impl(cg_mlp* m, const float* d_features, const float* d_tau, long long n,
                             const cg_train_params* tp, float* loss_per_step,
                             unsigned long long wait_ns, int stall) {
+    NvtxRange nvtx_("cg_mlp_train");
     CG_CHECK(m && d_features && d_tau && tp, CG_ERR_INVALID_ARGUMENT, "cg_mlp_train: null pointer");
     CG_CHECK(n >= 1 && n <= (1ll << 31), CG_ERR_OUT_OF_RANGE, "cg_mlp_train: n not in [1, 2^31]");
     CG_CHECK(tp->steps >= 0 && tp->steps <= 10000000, CG_ERR_OUT_OF_RANGE,

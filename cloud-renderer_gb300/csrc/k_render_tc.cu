@@ -439,7 +439,8 @@ __global__ void __launch_bounds__(RT_THREADS, RT_CTAS_PER_SM)
 
     mlptc::stage_network(S.net, m, tid, RT_THREADS);
     for (int i = tid; i < RT_PRODUCERS * RT_RECS; i += RT_THREADS) S.rec[i].busy = 0u;
-    if (tid < W_COUNT) S.w[tid] = tid == W_END ? 0xFFFFFFFFu : 0u;
+    // the shared words (not W_TMEM: the allocation below writes it)
+    if (tid < W_COUNT && tid != W_TMEM) S.w[tid] = tid == W_END ? 0xFFFFFFFFu : 0u;
     if (tid == 0) {
         for (int i = 0; i < RT_RING; ++i) tc::mbar_init(S.full + i, 128);
         tc::mbar_init(S.act_ready, RT_EPI_WARPS);
