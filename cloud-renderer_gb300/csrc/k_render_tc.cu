@@ -17,8 +17,8 @@
 //               epilogue has written the activations, issues the layer's
 //               tcgen05.mma (M = 128, N = 64, FP16 operands, FP32 tensor-memory
 //               accumulators) and commits it to an mbarrier;
-//   warps 5-9   producers: march their region exactly as k_march<0, true>
-//               does (same samples, same (step, lane) order), append every
+//   warps 5-9   producers: march their region with k_march's texture-filtered
+//               march (cg_march.cuh: same samples, same (step, lane) order), append every
 //               contributing sample (voxel position, weight T*alpha, light G,
 //               record and slot) to a ring of RT_RING 128-row staging tiles in
 //               shared memory, record the region's step table, and once all of
@@ -43,6 +43,7 @@
 #include <type_traits>
 
 #include "cg_internal.h"
+#include "cg_march.cuh"
 #include "cg_mlp.cuh"
 #include "cg_mlp_tc.cuh"
 #include "cg_sample.cuh"
@@ -172,34 +173,6 @@ __device__ __forceinline__ bool spin_until(const Shared& S, P pred, unsigned lon
     return true;
 }
 
-__device__ __forceinline__ bool pixel_ray(const CamDesc& cam, const VolDesc& vd, int px, int py,
-                                          float3& d, float& tin, float& tout) {
-    float ndx = (2.f * ((float)px + 0.5f) / (float)cam.W - 1.f) * cam.tanh * cam.aspect;
-    float ndy = (1.f - 2.f * ((float)py + 0.5f) / (float)cam.H) * cam.tanh;
-    float dx = cam.f[0] + ndx * cam.s[0] + ndy * cam.u[0];
-    float dy = cam.f[1] + ndx * cam.s[1] + ndy * cam.u[1];
-    float dz = cam.f[2] + ndx * cam.s[2] + ndy * cam.u[2];
-    float inv = rsqrtf(dx * dx + dy * dy + dz * dz);
-    d = make_float3(dx * inv, dy * inv, dz * inv);
-    float dd[3] = {d.x, d.y, d.z};
-    float tmin = -1e30f, tmax = 1e30f;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        float lo = vd.wmin[a], hi = vd.wmin[a] + vd.range[a];
-        if (dd[a] == 0.f) {
-            if (cam.eye[a] < lo || cam.eye[a] > hi) return false;
-            continue;
-        }
-        float iv = 1.f / dd[a];
-        float t0 = (lo - cam.eye[a]) * iv, t1 = (hi - cam.eye[a]) * iv;
-        tmin = fmaxf(tmin, fminf(t0, t1));
-        tmax = fminf(tmax, fmaxf(t0, t1));
-    }
-    tin = fmaxf(tmin, 0.f);
-    tout = tmax;
-    return tout > tin;
-}
-
 // ---- producers ---------------------------------------------------------------
 
 struct RenderArgs {
@@ -297,106 +270,46 @@ __device__ bool finish_region(const Shared& S, Rec& rc, const RenderArgs& ra,
     return true;
 }
 
-// March region `region` (the steps of k_march<0, true>), appending every
-// contributing sample to the staging ring; fills record `rc` (index `ri`).
+// March region `region` (cg_march.cuh: the samples and order of k_march's
+// texture-filtered form), appending every contributing sample to the staging
+// ring; fills record `rc` (index `ri`).
 __device__ bool march_region(const Shared& S, Rec& rc, unsigned ri, unsigned region,
                              const VolDesc& vd, const CamDesc& cam, const TraceParams& tp,
                              const RenderArgs& ra, unsigned long long* status) {
     const int lane = threadIdx.x & 31;
     const int px = (int)(region % (unsigned)ra.tiles_x) * 8 + (lane & 7);
     const int py = (int)(region / (unsigned)ra.tiles_x) * 4 + (lane >> 3);
-    const bool valid = px < cam.W && py < cam.H;
-    float3 d = make_float3(0.f, 0.f, 0.f);
-    float tin = 0.f, tout = 0.f;
-    bool live = valid && pixel_ray(cam, vd, px, py, d, tin, tout);
-    const int Nv = tp.view_steps;
-    const float dt = (tout - tin) / (float)Nv;
-    const float D = (float)vd.D;
-    const float vsx = D / vd.range[0], vsy = D / vd.range[1], vsz = D / vd.range[2];
-    const float pixk = cam.tanh / (float)cam.H * vsx;
-    const float t_lod1 = 0.5f / pixk;
-    float T = 1.f;
     unsigned cnt = 0, nsteps = 0, last_row = 0;
-    uint2* steps = ra.steps + (size_t)region * Nv;
-    int kb = 0, ke = Nv;
-    const bool lod0 = tin + ((float)(Nv - 1) + 0.5f) * dt < t_lod1;
-    if (live && lod0) {
-        int k0, k1;
-        cgs::occupied_steps(vd, cam.eye, d, tin, dt, Nv, k0, k1);
-        kb = k0;
-        ke = k1 + 1;
-        if (kb >= ke) live = false;
-    }
-    const int wkb = __reduce_min_sync(0xffffffffu, live ? kb : Nv);
-    bool ok = true;
-    auto march = [&](auto lod0_form) {
-        constexpr bool LOD0 = decltype(lod0_form)::value;
-        for (int k = wkb; k < Nv; ++k) {
-            if (live && k >= ke) live = false;
-            if (!__any_sync(0xffffffffu, live)) break;
-            bool emit = false;
-            float v0 = 0.f, v1 = 0.f, v2 = 0.f, w = 0.f, G = 0.f;
-            if (live && k >= kb) {
-                float t = tin + ((float)k + 0.5f) * dt;
-                float p0 = cam.eye[0] + t * d.x, p1 = cam.eye[1] + t * d.y, p2 = cam.eye[2] + t * d.z;
-                v0 = (p0 - vd.wmin[0]) * vsx;
-                v1 = (p1 - vd.wmin[1]) * vsy;
-                v2 = (p2 - vd.wmin[2]) * vsz;
-                float2 rg;
-                if (LOD0) {
-                    rg = cgs::tri_hw<true>(vd, 0, v0, v1, v2);
-                } else {
-                    float lod = t < t_lod1 ? 0.f : log2f(fmaxf(1.f, 2.f * t * pixk));
-                    rg = cgs::quad_hw<true>(vd, v0, v1, v2, lod);
-                }
-                if (rg.x > 0.f) {
-                    float rho = rg.x * cgs::fbm_volume(tp, p0, p1, p2);
-                    if (rho > 0.f) {
-                        float alpha = 1.f - __expf(-tp.sigma * rho * dt);
-                        w = T * alpha;
-                        G = rg.y;
-                        emit = true;
-                        T *= 1.f - alpha;
-                        if (T < tp.cutoff) live = false;
-                    }
-                }
+    uint2* steps = ra.steps + (size_t)region * tp.view_steps;
+    float T = 1.f;
+    const bool ok = cgm::march_region(
+        vd, cam, tp, px, py, T,
+        [&](bool emit, unsigned ballot, float v0, float v1, float v2, float w, float G) {
+            const unsigned n = __popc(ballot);
+            unsigned base = 0;
+            if (lane == 0) base = atomicAdd(S.w + W_TAIL, n);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            const unsigned t_last = (base + n - 1u) / 128u;
+            // the ring slots of rows [base, base + n) must have been read
+            bool free_ok = true;
+            if (lane == 0)
+                free_ok = spin_until(
+                    S, [&] { return ld_volatile(S.w + W_RELEASED) + RT_RING > t_last; }, status);
+            if (!__shfl_sync(0xffffffffu, free_ok, 0)) return false;
+            if (emit) {
+                const unsigned rank = __popc(ballot & ((1u << lane) - 1u));
+                const unsigned row = base + rank;
+                const unsigned at = row % (RT_RING * 128u);
+                S.pos[at] = make_float4(v0, v1, v2, w);
+                S.meta[at] = make_uint2(__float_as_uint(G), (ri << 16) | (cnt + rank));
+                mbar_arrive(S.full + (row / 128u) % RT_RING, 1u);
             }
-            const unsigned ballot = __ballot_sync(0xffffffffu, emit);
-            if (ballot) {
-                const unsigned n = __popc(ballot);
-                unsigned base = 0;
-                if (lane == 0) base = atomicAdd(S.w + W_TAIL, n);
-                base = __shfl_sync(0xffffffffu, base, 0);
-                const unsigned t_last = (base + n - 1u) / 128u;
-                // the ring slots of rows [base, base + n) must have been read
-                bool free_ok = true;
-                if (lane == 0)
-                    free_ok = spin_until(
-                        S, [&] { return ld_volatile(S.w + W_RELEASED) + RT_RING > t_last; },
-                        status);
-                if (!__shfl_sync(0xffffffffu, free_ok, 0)) {
-                    ok = false;
-                    return;
-                }
-                if (emit) {
-                    const unsigned rank = __popc(ballot & ((1u << lane) - 1u));
-                    const unsigned row = base + rank;
-                    const unsigned at = row % (RT_RING * 128u);
-                    S.pos[at] = make_float4(v0, v1, v2, w);
-                    S.meta[at] = make_uint2(__float_as_uint(G), (ri << 16) | (cnt + rank));
-                    mbar_arrive(S.full + (row / 128u) % RT_RING, 1u);
-                }
-                if (lane == 0) steps[nsteps] = make_uint2(cnt, ballot);
-                nsteps++;
-                cnt += n;
-                last_row = base + n - 1u;
-            }
-        }
-    };
-    if (__all_sync(0xffffffffu, !live || lod0))
-        march(std::true_type{});
-    else
-        march(std::false_type{});
+            if (lane == 0) steps[nsteps] = make_uint2(cnt, ballot);
+            nsteps++;
+            cnt += n;
+            last_row = base + n - 1u;
+            return true;
+        });
     if (!ok) return false;
     rc.T[lane] = T;
     __syncwarp();
