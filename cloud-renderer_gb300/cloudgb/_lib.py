@@ -60,6 +60,7 @@ class cg_render_params(ctypes.Structure):
 
 PIPELINE_FUSED = 0
 PIPELINE_DEFERRED = 1
+PIPELINE_PERSISTENT = 2
 MLP_FEATURES = 16
 MLP_PARAMS = 9473
 

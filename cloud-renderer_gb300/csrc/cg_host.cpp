@@ -849,6 +849,11 @@ cg_status check_params(const cg_render_params* p) {
              CG_ERR_OUT_OF_RANGE, "render params: transmittance_cutoff not in [0, 1)");
     CG_CHECK(p->cone_mode == CG_CONE_TRANSMITTANCE || p->cone_mode == CG_CONE_REFERENCE,
              CG_ERR_INVALID_ARGUMENT, "render params: unknown cone_mode %d", p->cone_mode);
+    CG_CHECK(p->pipeline == CG_PIPELINE_FUSED || p->pipeline == CG_PIPELINE_DEFERRED ||
+                 p->pipeline == CG_PIPELINE_PERSISTENT,
+             CG_ERR_INVALID_ARGUMENT, "render params: unknown pipeline %d", p->pipeline);
+    CG_CHECK(p->pipeline != CG_PIPELINE_PERSISTENT || p->use_mlp, CG_ERR_UNSUPPORTED,
+             "render params: the persistent pipeline renders the MLP surrogate only");
     CG_CHECK(p->noise.octaves >= 0 && p->noise.octaves <= 16, CG_ERR_OUT_OF_RANGE,
              "render params: noise octaves %d not in [0, 16]", p->noise.octaves);
     CG_CHECK(std::isfinite(p->noise.frequency) && std::isfinite(p->noise.lacunarity) &&
@@ -1103,7 +1108,7 @@ extern "C" cg_status cg_render(cg_context* ctx, const cg_volume* v, const cg_cam
         stage_mark(ctx, s, "textures");
     }
     const VolDesc vd = desc_of(v);
-    if (params->use_mlp && params->pipeline != CG_PIPELINE_DEFERRED &&
+    if (params->use_mlp && params->pipeline == CG_PIPELINE_PERSISTENT &&
         32 * params->view_steps <= 0xFFFF) {
         // march, network and composite in one persistent kernel
         float* contrib = nullptr;

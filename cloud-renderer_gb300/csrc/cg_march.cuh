@@ -1,16 +1,18 @@
 // cg_march.cuh -- the view march of the surrogate renderer (texture-filtered
-// view samples and fBm), shared by the deferred march kernel (k_march) and the
-// fused renderer's producer warps (k_render_mlp_tc) so that both emit the same
-// samples in the same (step, lane) order.
+// view samples and fBm) for the persistent renderer's producer warps
+// (k_render_mlp_tc).  It emits the samples of k_march's texture-filtered form
+// in the same (step, lane) order, so the two renderers' images agree bit for
+// bit.
 //
 // One warp marches one 8x4-pixel region, one ray per lane, the lanes in
 // lockstep over the view steps.  A step's inputs -- the occupancy byte of its
 // brick, the density/light texel and the fBm texel -- are fetched one step
 // ahead of their use, and the two texels of a step together, so that a warp
 // waits for one texture latency per step at most instead of the dependent
-// chain occupancy -> density -> fBm.  The arithmetic (positions, lod, alpha,
-// the transmittance update) is that of the per-step form it replaces, so the
-// emitted samples are unchanged.
+// chain occupancy -> density -> fBm (the producers are few: each must hide its
+// own latency).  The arithmetic (positions, lod, alpha, the transmittance
+// update) is k_march's.  k_march keeps its per-step form: with a full grid of
+// warps it is faster (0.145 vs 0.174 ms at 1080p, measured).
 #pragma once
 
 #include <type_traits>

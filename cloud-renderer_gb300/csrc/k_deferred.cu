@@ -21,7 +21,6 @@
 #include <type_traits>
 
 #include "cg_internal.h"
-#include "cg_march.cuh"
 #include "cg_mlp.cuh"
 #include "cg_sample.cuh"
 
@@ -104,26 +103,6 @@ __global__ void __launch_bounds__(256) k_march(VolDesc vd, CamDesc cam, TracePar
         if (kb >= ke) live = false;
     }
     const int wkb = __reduce_min_sync(0xffffffffu, live ? kb : Nv);
-    if constexpr (HW) {
-        // texture-filtered samples: the shared pipelined march (cg_march.cuh)
-        (void)wkb;
-        cgm::march_region(vd, cam, tp, px, py, T,
-                          [&](bool emit, unsigned ballot, float v0, float v1, float v2, float w,
-                              float G) {
-                              if (emit) {
-                                  const unsigned slot =
-                                      cnt + __popc(ballot & ((1u << lane) - 1u));
-                                  pw[slot] = make_float4(v0, v1, v2, w);
-                                  gl[slot] = make_float2(G, __int_as_float(lane));
-                              }
-                              if (lane == 0)
-                                  sb.steps[(size_t)region * Nv + nsteps] =
-                                      make_uint2(cnt, ballot);
-                              nsteps++;
-                              cnt += __popc(ballot);
-                              return true;
-                          });
-    } else {
     // the steps, in one of two forms: when every live lane's samples have lod
     // 0 (the warp-uniform common case), level 0 is sampled directly (the same
     // texel reads as the lod path at lod 0, without the level arithmetic)
@@ -179,7 +158,6 @@ __global__ void __launch_bounds__(256) k_march(VolDesc vd, CamDesc cam, TracePar
         march(std::true_type{});
     else
         march(std::false_type{});
-    }
     if (lane == 0) {
         sb.count[region] = cnt;
         sb.nsteps[region] = nsteps;

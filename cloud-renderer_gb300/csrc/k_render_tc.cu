@@ -5,8 +5,8 @@
 // writes 24-byte records of every contributing sample and reads them back).
 //
 // Work unit: a region = one 8x4-pixel tile of the image (one ray per lane),
-// regions numbered in raster order and claimed dynamically.  Per CTA (two per
-// SM, 320 threads):
+// regions numbered in raster order and claimed dynamically.  Per CTA (three
+// per SM, 256 threads; the fastest of the shapes measured):
 //   warps 0-3   epilogue: one thread per row of a 128-sample tile; features
 //               (12 texture taps), FP16 inputs into the activation tile, the
 //               SiLU epilogues of the three layers (tensor memory -> FP16
@@ -17,7 +17,7 @@
 //               epilogue has written the activations, issues the layer's
 //               tcgen05.mma (M = 128, N = 64, FP16 operands, FP32 tensor-memory
 //               accumulators) and commits it to an mbarrier;
-//   warps 5-9   producers: march their region with k_march's texture-filtered
+//   warps 5-7   producers: march their region with k_march's texture-filtered
 //               march (cg_march.cuh: same samples, same (step, lane) order), append every
 //               contributing sample (voxel position, weight T*alpha, light G,
 //               record and slot) to a ring of RT_RING 128-row staging tiles in
@@ -53,11 +53,11 @@ namespace {
 
 constexpr int RT_EPI_WARPS = 4;
 constexpr int RT_MMA_WARP = 4;
-constexpr int RT_PRODUCERS = 5;
+constexpr int RT_PRODUCERS = 3;
 constexpr int RT_FIRST_PRODUCER = RT_EPI_WARPS + 1;
 constexpr int RT_THREADS = 32 * (RT_EPI_WARPS + 1 + RT_PRODUCERS);
-constexpr int RT_CTAS_PER_SM = 2;
-constexpr int RT_RING = 16;   // staging tiles of 128 rows
+constexpr int RT_CTAS_PER_SM = 3;
+constexpr int RT_RING = 8;    // staging tiles of 128 rows
 constexpr int RT_RECS = 4;    // region records per producer warp
 constexpr uint32_t RT_TMEM_COLS = 64;
 constexpr uint64_t RT_WAIT_NS = 1000000000ull;  // 1 s: a wait longer than this is a fault

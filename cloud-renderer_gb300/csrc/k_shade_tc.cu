@@ -84,19 +84,19 @@ template <int FMT>
 __device__ __forceinline__ void pack_row(const VolDesc& vd, const ConeSchedule& cone,
                                          const MlpDev& m, const TraceParams& tp, unsigned slot,
                                          const float4& s, float g, const float (&f)[MLP_IN],
-                                         Row& r, uint8_t* act) {
+                                         Row& r, uint8_t* act, int row) {
     r.slot = slot;
     r.w = s.w;
     r.g = g;
     r.tau_fb = -1.f;
     if (slot != CG_NO_SLOT && !mlp::in_range(m, f))
         r.tau_fb = exact_tau<FMT>(vd, cone, s.x, s.y, s.z, tp.sun);
-    mlptc::write_inputs(act, threadIdx.x, m, f, slot != CG_NO_SLOT);
+    mlptc::write_inputs(act, row, m, f, slot != CG_NO_SLOT);
 }
 
 __device__ __forceinline__ unsigned slot_at(const SampleBuf& sb, unsigned tile, unsigned ntiles,
-                                            unsigned total) {
-    const unsigned i = tile * 128u + threadIdx.x;
+                                            unsigned total, int row) {
+    const unsigned i = tile * 128u + (unsigned)row;
     return (tile < ntiles && i < total) ? sb.slot_of[i] : CG_NO_SLOT;
 }
 
@@ -123,8 +123,44 @@ __device__ __forceinline__ void report_failure(uint64_t* bar, unsigned phase, bo
     if (threadIdx.x == 0) atomicOr(status + 1, undrained ? 3ull : 1ull);
 }
 
+// ---- the shade kernel: SHADE_GROUPS independent 4-warp groups per CTA, each
+// with its own activation tile, tensor-memory columns, mbarrier and tile
+// stream, sharing one copy of the network tiles (so that more groups fit an
+// SM's shared memory than CTAs of one group would).
+constexpr int SHADE_GROUPS = 1;
+constexpr int SHADE_CTAS_PER_SM = CTAS_PER_SM;
+constexpr uint32_t SHADE_TMEM_COLS = SHADE_GROUPS == 1 ? 64u : (SHADE_GROUPS == 2 ? 128u : 256u);
+constexpr int SH_OFF_NET = SHADE_GROUPS * mlptc::ACT_BYTES;
+constexpr int SH_OFF_BAR = SH_OFF_NET + mlptc::NET_BYTES;  // bar[G], tmem slot, claim[G]
+constexpr int SH_SMEM_BYTES = SH_OFF_BAR + 8 * SHADE_GROUPS + 4 + 4 * SHADE_GROUPS + 1024;
+static_assert(SH_SMEM_BYTES * SHADE_CTAS_PER_SM <= 227 * 1024, "shade kernel shared memory");
+
+// The group's barrier (named barrier 1 + g, 128 threads) that also agrees on
+// a failed wait of any of its threads.
+__device__ __forceinline__ bool group_sync_or(int g, bool v) {
+    if (SHADE_GROUPS == 1) return __syncthreads_or(v) != 0;
+    uint32_t r;
+    asm volatile(
+        "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n"
+        " bar.red.or.pred p, %2, 128, q;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(1 + g)
+        : "memory");
+    return r != 0;
+}
+
+// All writes of the group to its activation tile -> visible to the tensor
+// core, then its first thread issues; true when a wait of the group ran out.
+__device__ __forceinline__ bool group_sync_for_mma(int g, bool bad) {
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    const bool any_bad = group_sync_or(g, bad);
+    tc::fence_after_sync();
+    return any_bad;
+}
+
 template <int FMT>
-__global__ void __launch_bounds__(128, CTAS_PER_SM)
+__global__ void __launch_bounds__(128 * SHADE_GROUPS, SHADE_CTAS_PER_SM)
     k_shade_mlp_tc(const __grid_constant__ VolDesc vd, const __grid_constant__ TraceParams tp,
                    const __grid_constant__ ConeSchedule cone, const __grid_constant__ MlpDev m,
                    const __grid_constant__ FeatGeom geo, SampleBuf sb,
@@ -132,53 +168,56 @@ __global__ void __launch_bounds__(128, CTAS_PER_SM)
     extern __shared__ uint8_t smem_raw[];
     const uint32_t raw = tc::smem_addr(smem_raw);
     uint8_t* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
-    uint8_t* act = base + OFF_ACT;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(base + OFF_BAR);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(base + OFF_BAR + 8);
-    unsigned* s_claim = reinterpret_cast<unsigned*>(base + OFF_BAR + 12);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int g = tid >> 7, r = tid & 127;  // group, row of the group's tile
+    uint8_t* act = base + g * mlptc::ACT_BYTES;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(base + SH_OFF_BAR) + g;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(base + SH_OFF_BAR + 8 * SHADE_GROUPS);
+    unsigned* s_claim = reinterpret_cast<unsigned*>(base + SH_OFF_BAR + 8 * SHADE_GROUPS + 4) + g;
 
-    mlptc::stage_network(base + OFF_NET, m, tid, blockDim.x);
-    if (tid == 0) {
+    mlptc::stage_network(base + SH_OFF_NET, m, tid, blockDim.x);
+    if (r == 0) {
         tc::mbar_init(bar, 1);
         tc::fence_mbar_init();
     }
     if (warp == 0) {
-        tc::tmem_alloc(tslot, TC_TMEM_COLS);
+        tc::tmem_alloc(tslot, SHADE_TMEM_COLS);
         tc::tmem_relinquish();
     }
     tc::fence_proxy_async();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    const uint32_t tmem = *tslot;
-    const uint32_t dw = tmem + ((uint32_t)(warp * 32) << 16);
+    const uint32_t tmem = *tslot + 64u * (uint32_t)g;
+    const uint32_t dw = tmem + ((uint32_t)((warp & 3) * 32) << 16);
     const uint32_t a_addr = tc::smem_addr(act);
-    const uint32_t net_addr = tc::smem_addr(base + OFF_NET);
+    const uint32_t net_addr = tc::smem_addr(base + SH_OFF_NET);
     const float amb = tp.ambient;
     const unsigned total = *sb.flat_total;
     const unsigned ntiles = (total + 127u) / 128u;
+    const unsigned streams = gridDim.x * SHADE_GROUPS;
     unsigned phase = 0, n_fallback = 0, n_valid = 0;
     bool failed = false, bad = false;  // bad: a wait of this warp ran out
 
     // ---- the first tile's inputs
-    unsigned tile = blockIdx.x;
+    unsigned tile = blockIdx.x * SHADE_GROUPS + g;
     Row row;
     {
-        const unsigned slot = slot_at(sb, tile, ntiles, total);
+        const unsigned slot = slot_at(sb, tile, ntiles, total, r);
         float4 sp = make_float4(0.f, 0.f, 0.f, 0.f);
-        float g = 0.f;
+        float gl = 0.f;
         if (slot != CG_NO_SLOT) {
             sp = sb.pos_w[slot];
-            g = sb.light_lane[slot].x;
+            gl = sb.light_lane[slot].x;
         }
         float f[MLP_IN];
         fetch_features(geo, tp, slot, sp, f);
-        pack_row<FMT>(vd, cone, m, tp, slot, sp, g, f, row, act);
+        pack_row<FMT>(vd, cone, m, tp, slot, sp, gl, f, row, act, r);
     }
 
-    // the first two tiles are static, later ones are claimed from status[3]
-    unsigned ntile = tile + gridDim.x;
+    // the first two tiles of a group are static, later ones are claimed from
+    // status[3]
+    unsigned ntile = tile + streams;
     for (; tile < ntiles;) {
         unsigned nslot = CG_NO_SLOT;
         float4 ns = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -187,33 +226,31 @@ __global__ void __launch_bounds__(128, CTAS_PER_SM)
         float y = 0.f;
 #pragma unroll
         for (int layer = 0; layer < 3; ++layer) {
-            if (sync_for_mma(bad)) {  // a commit of parity `phase` is still pending
+            if (group_sync_for_mma(g, bad)) {  // a commit of parity `phase` is still pending
                 failed = true;
                 break;
             }
-            if (tid == 0) {
+            if (r == 0) {
                 mlptc::issue_layer(layer, tmem, a_addr, net_addr, bar);
-                // claim the tile after next (read by all after the next sync)
-                if (layer == 0)
-                    *s_claim = 2u * gridDim.x +
-                               (unsigned)atomicAdd(status + 3, 1ull);
+                // claim the tile after next (read by the group after the next sync)
+                if (layer == 0) *s_claim = 2u * streams + (unsigned)atomicAdd(status + 3, 1ull);
             }
             // ---- the next tile, in stages
-            if (layer == 0) nslot = slot_at(sb, ntile, ntiles, total);
+            if (layer == 0) nslot = slot_at(sb, ntile, ntiles, total, r);
             if (layer == 1 && nslot != CG_NO_SLOT) {
                 ns = sb.pos_w[nslot];
                 ng = sb.light_lane[nslot].x;
             }
             if (layer == 2) fetch_features(geo, tp, nslot, ns, nf);
             // a warp whose wait ran out skips the epilogue (no tensor-memory
-            // read under a running MMA) and the CTA stops at the next barrier
+            // read under a running MMA) and the group stops at the next barrier
             bad = __any_sync(0xffffffffu, !tc::mbar_wait(bar, phase, TC_WAIT_NS));
             if (!bad) phase ^= 1u;
             tc::fence_after_sync();
             // ---- epilogue: TMEM -> bias + SiLU, 32 columns at a time; the
             // last layer folds the 64 -> 1 output in FP32
             if (!bad) {
-                const float yy = mlptc::layer_epilogue(layer, dw, act, tid, m);
+                const float yy = mlptc::layer_epilogue(layer, dw, act, r, m);
                 if (layer == 2) y = yy;
             }
             tc::fence_before_sync();
@@ -232,12 +269,20 @@ __global__ void __launch_bounds__(128, CTAS_PER_SM)
             sb.contrib[row.slot] = row.w * __expf(-tp.sigma * tau) * (amb + (1.f - amb) * row.g);
         }
         // ---- the next tile's inputs
-        pack_row<FMT>(vd, cone, m, tp, nslot, ns, ng, nf, row, act);
+        pack_row<FMT>(vd, cone, m, tp, nslot, ns, ng, nf, row, act, r);
         tile = ntile;
         ntile = *s_claim;  // written at layer 0, two barriers ago
     }
-    if (!failed) failed = sync_for_mma(bad);  // the last tile's waits
-    if (failed) report_failure(bar, phase, bad, status);
+    if (!failed) failed = group_sync_for_mma(g, bad);  // the last tile's waits
+    if (failed) {
+        // drain the outstanding commit (bounded; only warps whose wait ran
+        // out have one), agree within the group whether every drain
+        // completed, and report (|= 2: tensor memory is freed below with an
+        // MMA possibly in flight; the host treats the device as faulted)
+        const bool drained = !bad || tc::mbar_wait(bar, phase, TC_WAIT_NS);
+        const bool undrained = group_sync_or(g, !drained);
+        if (r == 0) atomicOr(status + 1, undrained ? 3ull : 1ull);
+    }
     unsigned tot = n_fallback, nv = n_valid;
     for (int o = 16; o > 0; o >>= 1) {
         tot += __shfl_xor_sync(0xffffffffu, tot, o);
@@ -249,7 +294,7 @@ __global__ void __launch_bounds__(128, CTAS_PER_SM)
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, TC_TMEM_COLS);
+    if (warp == 0) tc::tmem_dealloc(*tslot, SHADE_TMEM_COLS);
 }
 
 // The network alone over n rows of raw features (normalised here):
@@ -398,17 +443,17 @@ cudaError_t launch_shade_mlp_tc(VolDesc vd, CamDesc cam, TraceParams tp, const M
     const int f = vd.fmt == 0 ? 0 : 1;
     if (!grid[f][dev].load(std::memory_order_acquire)) {
         const void* fn = f == 0 ? (const void*)k_shade_mlp_tc<0> : (const void*)k_shade_mlp_tc<1>;
-        e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, SH_SMEM_BYTES);
         if (e != cudaSuccess) return e;
         int sms = 0;
         e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (e != cudaSuccess) return e;
-        grid[f][dev].store(sms * CTAS_PER_SM, std::memory_order_release);
+        grid[f][dev].store(sms * SHADE_CTAS_PER_SM, std::memory_order_release);
     }
     const int blocks = grid[f][dev].load(std::memory_order_acquire);
     if (f == 0)
-        k_shade_mlp_tc<0><<<blocks, 128, SMEM_BYTES, st>>>(vd, tp, cone, m, geo, sb, status);
+        k_shade_mlp_tc<0><<<blocks, 128 * SHADE_GROUPS, SH_SMEM_BYTES, st>>>(vd, tp, cone, m, geo, sb, status);
     else
-        k_shade_mlp_tc<1><<<blocks, 128, SMEM_BYTES, st>>>(vd, tp, cone, m, geo, sb, status);
+        k_shade_mlp_tc<1><<<blocks, 128 * SHADE_GROUPS, SH_SMEM_BYTES, st>>>(vd, tp, cone, m, geo, sb, status);
     return cudaGetLastError();
 }

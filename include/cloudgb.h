@@ -124,13 +124,19 @@ typedef struct cg_render_params {
  * (same samples, same per-pixel summation order). */
 typedef enum cg_pipeline {
     /* exact cone: one thread per pixel marches and traces its cones;
-     * MLP surrogate: one persistent kernel marches, runs the network on the
-     * tensor cores and composites (view_steps <= 2047; above, deferred) */
+     * MLP surrogate: the deferred form below (its fastest on GB300) */
     CG_PIPELINE_FUSED = 0,
     /* march records the contributing samples; the sun term is evaluated for
      * them in full warps (exact cone) or 128-row tensor-core tiles (MLP),
      * then each pixel sums its samples in step order */
-    CG_PIPELINE_DEFERRED = 1
+    CG_PIPELINE_DEFERRED = 1,
+    /* MLP surrogate only (CG_ERR_UNSUPPORTED for the exact cone): one
+     * persistent warp-specialised kernel marches, runs the network on the
+     * tensor cores and composites, with no sample records in global memory;
+     * the same images as the deferred form, bit for bit, but slower on GB300
+     * (the network's epilogue needs the warps the march takes).
+     * view_steps <= 2047 (above, the deferred form) */
+    CG_PIPELINE_PERSISTENT = 2
 } cg_pipeline;
 
 /* Snapshot of a volume's layout, for readback. */

@@ -253,9 +253,9 @@ def test_mlp_render_rmse_and_gain(ctx, trained):
 
 
 @pytest.mark.parametrize("size", [(1920, 1080), (333, 197)])
-def test_fused_render_matches_deferred(ctx, trained, size):
-    """The fused surrogate renderer (march, tensor-core network and composite
-    in one persistent kernel) computes the same samples, network outputs and
+def test_persistent_render_matches_deferred(ctx, trained, size):
+    """The persistent surrogate renderer (march, tensor-core network and
+    composite in one kernel) computes the same samples, network outputs and
     step-order sums as the deferred form (march, shading tiles, accumulate):
     images within 1e-6, the same sample and fallback counts.  333 x 197 has
     ragged 8x4 regions on the right and bottom edges."""
@@ -269,7 +269,8 @@ def test_fused_render_matches_deferred(ctx, trained, size):
     vol.update()
     cloudgb.VoxelizeShader().voxelize(vol, cloudgb.Sun(wl.sun_direction, *wl.sun_map))
     kw = wl.shader_kwargs()
-    fused = cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, **kw)
+    fused = cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, pipeline=_lib.PIPELINE_PERSISTENT,
+                                    **kw)
     deferred = cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, pipeline=_lib.PIPELINE_DEFERRED, **kw)
     for v in (0, 5, 11):
         cam = workload.make_camera(wl.cameras[v])
@@ -286,7 +287,7 @@ def test_fused_render_matches_deferred(ctx, trained, size):
     vol.close()
 
 
-def test_fused_render_edge_cases(ctx, trained):
+def test_persistent_render_edge_cases(ctx, trained):
     """No sample at all (the camera looks away from the box), a single 8x4
     region (most CTAs get no work), and 1 x 1 pixels: the kernel's end
     protocol completes and the images equal the deferred form's."""
@@ -299,7 +300,8 @@ def test_fused_render_edge_cases(ctx, trained):
     vol.update()
     cloudgb.VoxelizeShader().voxelize(vol, cloudgb.Sun(wl.sun_direction, *wl.sun_map))
     kw = wl.shader_kwargs()
-    fused = cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, **kw)
+    fused = cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, pipeline=_lib.PIPELINE_PERSISTENT,
+                                    **kw)
     deferred = cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, pipeline=_lib.PIPELINE_DEFERRED, **kw)
     away = cloudgb.Camera((0.5, 0.5, -1.5), (0.5, 0.5, -3.0), width=200, height=100)
     img = fused.coneTrace(vol, away)
@@ -324,7 +326,7 @@ def test_output_destinations_agree(ctx, trained):
     cam = workload.make_camera(wl.cameras[1])
     kw = wl.shader_kwargs()
     for shader in (cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, **kw),
-                   cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, pipeline=_lib.PIPELINE_DEFERRED,
+                   cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, pipeline=_lib.PIPELINE_PERSISTENT,
                                            **kw),
                    cloudgb.ConeTraceShader(**kw),
                    cloudgb.ConeTraceShader(pipeline=_lib.PIPELINE_DEFERRED, **kw)):
