@@ -479,6 +479,7 @@ class ConeTraceShader:
         self.useMlp = False
         self.mlp = None
         self.pipeline = p.pipeline
+        self.coneLanes = p.cone_lanes
         for k, v in kw.items():
             if not hasattr(self, k):
                 raise AttributeError(f"ConeTraceShader has no parameter {k!r}")
@@ -507,6 +508,7 @@ class ConeTraceShader:
         p.use_mlp = 1 if self.useMlp else 0
         p.mlp = self.mlp.handle if (self.useMlp and self.mlp is not None) else None
         p.pipeline = int(self.pipeline)
+        p.cone_lanes = int(self.coneLanes)
         return p
 
     def coneTrace(self, volume, camera, out=None, stream=None):

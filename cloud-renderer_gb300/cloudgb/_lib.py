@@ -55,7 +55,7 @@ class cg_render_params(ctypes.Structure):
                 ("ambient", ctypes.c_float), ("sun_color", ctypes.c_float * 3),
                 ("transmittance_cutoff", ctypes.c_float), ("cone_mode", ctypes.c_int),
                 ("noise", cg_noise), ("use_mlp", ctypes.c_int), ("mlp", ctypes.c_void_p),
-                ("pipeline", ctypes.c_int)]
+                ("pipeline", ctypes.c_int), ("cone_lanes", ctypes.c_int)]
 
 
 PIPELINE_FUSED = 0

@@ -852,6 +852,8 @@ cg_status check_params(const cg_render_params* p) {
     CG_CHECK(p->pipeline == CG_PIPELINE_FUSED || p->pipeline == CG_PIPELINE_DEFERRED ||
                  p->pipeline == CG_PIPELINE_PERSISTENT,
              CG_ERR_INVALID_ARGUMENT, "render params: unknown pipeline %d", p->pipeline);
+    CG_CHECK(p->cone_lanes >= 0 && p->cone_lanes <= 32, CG_ERR_OUT_OF_RANGE,
+             "render params: cone_lanes %d not in [0, 32]", p->cone_lanes);
     CG_CHECK(p->pipeline != CG_PIPELINE_PERSISTENT || p->use_mlp, CG_ERR_UNSUPPORTED,
              "render params: the persistent pipeline renders the MLP surrogate only");
     CG_CHECK(p->noise.octaves >= 0 && p->noise.octaves <= 16, CG_ERR_OUT_OF_RANGE,
@@ -873,6 +875,7 @@ TraceParams trace_params_of(const cg_render_params* p, const float sun_dir[3]) {
     tp.view_steps = p->view_steps;
     tp.sun_steps = p->sun_steps;
     tp.cone_mode = p->cone_mode;
+    tp.cone_lanes = p->cone_lanes;
     tp.tan_half = (float)std::tan((double)p->cone_half_angle);
     tp.h0 = p->cone_initial_height;
     tp.rmin = p->cone_min_radius;

@@ -81,6 +81,7 @@ struct CamDesc {
 // Render parameters resolved for the device.
 struct TraceParams {
     int view_steps, sun_steps, cone_mode;
+    int cone_lanes;  // warp-cooperative sun cones in the fused trace (0: off)
     float tan_half, h0, rmin, lod_offset, down_scaling;
     float sigma, ambient, cutoff;
     float sun_color[3];

@@ -118,6 +118,12 @@ typedef struct cg_render_params {
     int use_mlp;               /* 1: sun cone replaced by the MLP surrogate */
     const cg_mlp* mlp;         /* required when use_mlp != 0 */
     int pipeline;              /* cg_pipeline */
+    /* exact cone, fused pipeline: 0 (default) = each thread traces the sun
+     * cones of its own ray's samples; N in 1..32 = the warp marches its 32
+     * rays in lockstep and, at a view step where at most N of them
+     * contribute, traces each of those cones with its lanes over the cone's
+     * steps (a shuffle-tree sum; images within 1e-6 of the default) */
+    int cone_lanes;
 } cg_render_params;
 
 /* Kernel organisation of an exact-cone render.  Both give the same image

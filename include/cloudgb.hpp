@@ -279,6 +279,7 @@ class ConeTraceShader {
         freqStep = p.noise.lacunarity;
         persStep = p.noise.gain;
         pipeline = p.pipeline;
+        coneLanes = p.cone_lanes;
     }
 
     int viewSteps, vctSteps;
@@ -295,6 +296,7 @@ class ConeTraceShader {
     bool useMlp = false;
     const cg_mlp* mlp = nullptr;
     int pipeline;
+    int coneLanes;
     Camera camera;
 
     cg_render_params params() const {
@@ -325,6 +327,7 @@ class ConeTraceShader {
         p.use_mlp = useMlp ? 1 : 0;
         p.mlp = useMlp ? mlp : nullptr;
         p.pipeline = pipeline;
+        p.cone_lanes = coneLanes;
         return p;
     }
 
