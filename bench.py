@@ -535,15 +535,18 @@ def run_ours(args):
             d.update(extra)
         return d
 
-    # ---- plain FP32: both exact pipelines (fused trace; deferred march +
-    # exact shading), the faster one is the baseline of the speed-up
+    # ---- plain FP32: every exact form (fused trace with warp-cooperative
+    # cones -- the default --, fused trace with one thread per cone, deferred
+    # march + exact shading); the fastest is the baseline of the speed-up
     vol32 = make_volume(cloudgb.FORMAT_RGBA32F)
     plain_shader = cloudgb.ConeTraceShader(**kw)
+    serial_shader = cloudgb.ConeTraceShader(coneLanes=0, **kw)
     deferred_shader = cloudgb.ConeTraceShader(pipeline=_lib.PIPELINE_DEFERRED, **kw)
     plain_fused = run_path(vol32, plain_shader, args.steps, args.warmup)
+    plain_serial = run_path(vol32, serial_shader, args.steps, args.warmup)
     plain_def = run_path(vol32, deferred_shader, args.steps, args.warmup)
-    plain = min(plain_fused, plain_def, key=lambda r: r["total_ms"])
-    plain_name = "fused" if plain is plain_fused else "deferred"
+    plain, plain_name = min(((plain_fused, "fused"), (plain_serial, "fused_serial_cones"),
+                             (plain_def, "deferred")), key=lambda r: r[0]["total_ms"])
     # executed-work counters of the first 16 views (untimed): algorithmic
     # bytes of each fused-trace launch, paired with that view's trace time
     stats = [plain_shader.renderStats(vol32, cams[k]) for k in range(len(plain_fused["per_view"]))]
@@ -564,6 +567,10 @@ def run_ours(args):
     vol16 = make_volume(cloudgb.FORMAT_BF16_FP16)
     mlp_shader = cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, **kw)
     learned = run_path(vol16, mlp_shader, args.steps, args.warmup, clocks=True)
+    # the same surrogate renderer as one persistent kernel (A/B, same images)
+    persistent = run_path(vol16, cloudgb.ConeTraceShader(useMlp=True, mlp=mlp,
+                                                         pipeline=_lib.PIPELINE_PERSISTENT, **kw),
+                          args.steps, args.warmup)
     mlp_stage = "render_mlp" if "render_mlp" in learned["stages"] else "shade_mlp"
     samples = [v["samples"] for v in learned["per_view"]]
     mlp_ms = [v[mlp_stage] for v in learned["per_view"]]
@@ -591,7 +598,8 @@ def run_ours(args):
                <= 1e-2)
 
     head = learned if use_mlp else plain
-    head_shader = mlp_shader if use_mlp else (plain_shader if plain is plain_fused else deferred_shader)
+    head_shader = mlp_shader if use_mlp else {"fused": plain_shader, "fused_serial_cones": serial_shader,
+                                               "deferred": deferred_shader}[plain_name]
     head_vol = vol16 if use_mlp else vol32
     total_ms = max_over_ranks(head["total_ms"], world)
     value = replica_rate(W * H, args.steps, world, total_ms)
@@ -626,7 +634,7 @@ def run_ours(args):
                     "note": "achieved = sum over the 16 views of (view's surrogate inferences x "
                             "18,560 FLOP) / sum of the same views' kernel CUDA-event times"}
     dram_gbs = (tr_plain["bytes_per_launch"] / (np.mean(trace_ms) / 1e3) / 1e9) if tr_plain else None
-    roofline_plain = {"bound": "hbm", "kernel": "k_trace_fused", "achieved": round(plain_achieved, 1),
+    roofline_plain = {"bound": "hbm", "kernel": "k_trace_coop (the fused trace, cooperative cones)", "achieved": round(plain_achieved, 1),
                       "peak": hbm_peak, "peak_kind": peak_kind, "unit": "GB/s",
                       "frac": round(plain_achieved / hbm_peak, 4),
                       "traffic": tr_plain.get("bytes_per_launch") if tr_plain else None,
@@ -643,7 +651,9 @@ def run_ours(args):
     paths = {
         "plain_fp32": path_summary(plain, {"pipeline": plain_name}),
         "plain_fp32_fused": path_summary(plain_fused),
+        "plain_fp32_fused_serial_cones": path_summary(plain_serial),
         "plain_fp32_deferred": path_summary(plain_def),
+        "bf16_mlp_persistent": path_summary(persistent),
         "bf16_mlp": path_summary(learned, {
             "rmse_vs_fp64_oracle": chk["bf16_mlp"]["rmse"] if chk else None,
             "max_abs_vs_fp64_oracle": chk["bf16_mlp"]["max_abs"] if chk else None,

@@ -13,8 +13,11 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "cloudgb")
-BUILD_DIR = os.path.join(PKG, "_build")
-LIB = os.path.join(OUT_DIR, "libcloudgb.so")
+# CG_BOUNDS_CHECK=1: the bounds-check build (csrc/cg_check.cuh), a separate
+# library with its own objects
+CHECK = os.environ.get("CG_BOUNDS_CHECK") == "1"
+BUILD_DIR = os.path.join(PKG, "_build_check" if CHECK else "_build")
+LIB = os.path.join(OUT_DIR, "libcloudgb_check.so" if CHECK else "libcloudgb.so")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -60,6 +63,8 @@ def build_library(force=False, verbose=False):
     headers.append(os.path.join(ROOT, "include", "cloudgb.h"))
     common = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
               "-I", CSRC, "-I", os.path.join(ROOT, "include")] + ARCH
+    if CHECK:
+        common.append("-DCG_BOUNDS_CHECK=1")
     objs, jobs = [], []
     for src, extra in SOURCES:
         path = os.path.join(CSRC, src)

@@ -6,7 +6,10 @@ import ctypes
 import os
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "libcloudgb.so")
+# the bounds-check build (CG_BOUNDS_CHECK=1 at build time) is loaded instead
+# when CG_BOUNDS_CHECK=1 is set at run time
+LIB_PATH = os.path.join(_HERE, "libcloudgb_check.so" if os.environ.get("CG_BOUNDS_CHECK") == "1"
+                        else "libcloudgb.so")
 
 CG_OK = 0
 STATUS_NAMES = {
@@ -189,6 +192,8 @@ SIGNATURES = [
     ("cg_frame_graph_destroy", None, [P]),
     ("cg_compat_params_default", None, [ctypes.POINTER(cg_compat_params)]),
     ("cg_context_check_wait_timeout", I, [P, ctypes.c_uint32, U64P]),
+    ("cg_bounds_check_build", I, []),
+    ("cg_context_bounds_violations", I, [P, U64P, ctypes.c_char_p, I]),
     ("cg_compat_noise_map", I, [ctypes.c_uint32, FP]),
     ("cg_render_compat", I, [P, P, ctypes.POINTER(cg_camera), ctypes.POINTER(cg_compat_params), P,
                              I, P]),

@@ -91,6 +91,50 @@ void stage_mark(cg_context* ctx, cudaStream_t s, const char* name) {
     ctx->n_marks = i + 1;
 }
 
+// ---- bounds-check build -------------------------------------------------
+// Each kernel translation unit keeps its own error word (cg_check.cuh).
+#define CG_TU_LIST(X)                                                                     \
+    X(k_trace) X(k_deferred) X(k_shade_tc) X(k_render_tc) X(k_voxelize) X(k_batch)        \
+    X(k_compat) X(k_mlp) X(k_textures) X(k_train_tc) X(k_noalloc) X(k_stats)
+#define CG_TU_DECL(name) cudaError_t cg_oob_take_##name(unsigned long long out[2]);
+CG_TU_LIST(CG_TU_DECL)
+
+unsigned long long cg_bounds_take(char* site, int site_len, cudaError_t* err) {
+    unsigned long long total = 0;
+    *err = cudaSuccess;
+    if (site && site_len > 0) site[0] = 0;
+#define CG_TU_TAKE(name)                                                               \
+    {                                                                                  \
+        unsigned long long w[2] = {0ull, 0ull};                                        \
+        const cudaError_t e = cg_oob_take_##name(w);                                   \
+        if (e != cudaSuccess && *err == cudaSuccess) *err = e;                         \
+        if (w[0] && !total && site && site_len > 0)                                    \
+            snprintf(site, (size_t)site_len, "%s.cu (or a header it includes):%u index %u", \
+                     #name, (unsigned)(w[1] >> 32), (unsigned)(w[1] & 0xFFFFFFFFu));    \
+        total += w[0];                                                                 \
+    }
+    CG_TU_LIST(CG_TU_TAKE)
+#undef CG_TU_TAKE
+    return total;
+}
+
+extern "C" int cg_bounds_check_build(void) { return CG_BOUNDS_CHECK; }
+
+extern "C" cg_status cg_context_bounds_violations(cg_context* ctx, uint64_t* count, char* site,
+                                                  int site_len) {
+    CG_CHECK(ctx && count, CG_ERR_INVALID_ARGUMENT,
+             "cg_context_bounds_violations: null pointer");
+    *count = 0;
+    CG_CHECK(CG_BOUNDS_CHECK, CG_ERR_UNSUPPORTED,
+             "cg_context_bounds_violations: not a bounds-check build");
+    CG_CUDA(cudaSetDevice(ctx->device));
+    CG_CUDA(cudaDeviceSynchronize());
+    cudaError_t e = cudaSuccess;
+    *count = cg_bounds_take(site, site_len, &e);
+    CG_CUDA(e);
+    return CG_OK;
+}
+
 extern "C" cg_status cg_context_last_samples(cg_context* ctx, uint64_t* samples) {
     CG_CHECK(ctx && samples, CG_ERR_INVALID_ARGUMENT, "cg_context_last_samples: null pointer");
     *samples = 0;
@@ -309,6 +353,10 @@ extern "C" void cg_render_params_default(cg_render_params* p) {
     p->noise.offset[0] = p->noise.offset[1] = p->noise.offset[2] = 0.0f;
     p->use_mlp = 0;
     p->mlp = nullptr;
+    p->pipeline = CG_PIPELINE_FUSED;
+    // warp-cooperative cones at steps where at most 8 rays of a warp
+    // contribute: the fastest threshold measured at 1080p over 256^3
+    p->cone_lanes = 8;
 }
 
 extern "C" cg_status cg_host_alloc(size_t bytes, void** out) {
@@ -629,6 +677,9 @@ VolDesc desc_of(const cg_volume* v) {
         d.occ_nb[l] = v->occ_nb[l];
         d.occ_off[l] = v->occ_off[l];
     }
+    d.nvox = (long long)v->offs[v->L - 1] +
+             (long long)v->dims[v->L - 1] * v->dims[v->L - 1] * v->dims[v->L - 1];
+    d.occ_total = (int)v->occ_total;
     return d;
 }
 

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "cg_check.cuh"
+
 #define CG_MAX_LEVELS 16
 #define CG_Q20 1048576LL
 #define CG_HALF_Q20 524288LL
@@ -50,6 +52,10 @@ struct VolDesc {
     // surfaces of the same arrays (cudaSurfaceObject_t): when set, voxelize
     // writes each stored voxel there too, so the copies never need a pass
     unsigned long long surf[CG_MAX_LEVELS];
+    // voxels of all levels and bytes of all occupancy grids (the bounds of
+    // the bounds-check build)
+    long long nvox;
+    int occ_total;
 };
 
 // Hash-noise lattice values tabulated per octave over the world box: octave
@@ -156,6 +162,7 @@ struct SampleBuf {
     uint2* steps;     // per region, per emitting step: (first slot, lane ballot)
     unsigned* nsteps; // emitting steps per region
     int capacity;     // 32 * view_steps
+    unsigned long long nslots;  // regions * capacity
 };
 
 // ---- MLP surrogate ----------------------------------------------------------

@@ -258,6 +258,7 @@ cg_status ensure_samples(cg_context* ctx, int width, int height, int view_steps,
     sb.steps = reinterpret_cast<uint2*>(ctx->samples_cnt.as<unsigned>() + at);
     sb.slot_of = ctx->samples_cnt.as<unsigned>() + at + 2 * regions * (size_t)view_steps;
     sb.capacity = (int)cap;
+    sb.nslots = n;
     return CG_OK;
 }
 

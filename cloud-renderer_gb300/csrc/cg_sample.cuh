@@ -27,6 +27,14 @@ __device__ __forceinline__ float2 fetch(const void* pyr, int idx) {
     return make_float2(bf16_lo(t), WANT_G ? fp16_hi(t) : 0.f);
 }
 
+// fetch() at a flat index of the whole pyramid, checked in the bounds-check
+// build (an index past the last level reads 0).
+template <int FMT, bool WANT_G>
+__device__ __forceinline__ float2 fetch_vd(const VolDesc& vd, int idx) {
+    if (!CG_IN_BOUNDS(idx, vd.nvox)) return make_float2(0.f, 0.f);
+    return fetch<FMT, WANT_G>(vd.pyr, idx);
+}
+
 __device__ __forceinline__ float lerp3(const float c[8], float wx, float wy, float wz) {
     float x00 = c[0] + wx * (c[1] - c[0]);
     float x10 = c[2] + wx * (c[3] - c[2]);
@@ -43,7 +51,9 @@ __device__ __forceinline__ bool occupied(const VolDesc& vd, int l, int ix, int i
     int bx = min(max(ix >> sh, 0), nb - 1);
     int by = min(max(iy >> sh, 0), nb - 1);
     int bz = min(max(iz >> sh, 0), nb - 1);
-    return __ldg(vd.occ + vd.occ_off[l] + (bz * nb + by) * nb + bx) != 0;
+    const int at = vd.occ_off[l] + (bz * nb + by) * nb + bx;
+    if (!CG_IN_BOUNDS(at, vd.occ_total)) return false;
+    return __ldg(vd.occ + at) != 0;
 }
 
 // Trilinear at level l of channel R (and G when WANT_G), level-0 voxel-space
@@ -70,7 +80,7 @@ __device__ __forceinline__ float2 tri(const VolDesc& vd, int l, float px, float 
         const int o[8] = {0, 1, N, N + 1, NN, NN + 1, NN + N, NN + N + 1};
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-            float2 t = fetch<FMT, WANT_G>(vd.pyr, i0 + o[k]);
+            float2 t = fetch_vd<FMT, WANT_G>(vd, i0 + o[k]);
             r[k] = t.x;
             g[k] = t.y;
         }
@@ -94,7 +104,7 @@ __device__ __forceinline__ float2 tri(const VolDesc& vd, int l, float px, float 
                 for (int a = 0; a < 2; ++a) {
                     const int k = c * 4 + b * 2 + a;
                     const bool ok = !BORDER || (vx[a] && vy[b] && vz[c]);
-                    float2 t = fetch<FMT, WANT_G>(vd.pyr, base + (zs[c] * N + ys[b]) * N + xs[a]);
+                    float2 t = fetch_vd<FMT, WANT_G>(vd, base + (zs[c] * N + ys[b]) * N + xs[a]);
                     r[k] = ok ? t.x : 0.f;
                     g[k] = ok ? t.y : 0.f;
                 }

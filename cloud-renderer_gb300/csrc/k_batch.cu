@@ -304,3 +304,5 @@ cudaError_t launch_trace_batch(int fmt, int lanes_per_ray, int unroll, const Bat
     return fmt == 0 ? launch_lpr<0>(lanes_per_ray, unroll, views, n, total_tiles, counter, blocks, st)
                     : launch_lpr<1>(lanes_per_ray, unroll, views, n, total_tiles, counter, blocks, st);
 }
+
+CG_OOB_TU(k_batch)

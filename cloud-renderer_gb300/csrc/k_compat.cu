@@ -370,3 +370,5 @@ cudaError_t launch_compat_tiles(const VolDesc& vd, const ConeSchedule& cs, const
         k_compat_tiles<1><<<tiles, 256, 0, st>>>(vd, cs, P, offset, list, out);
     return cudaGetLastError();
 }
+
+CG_OOB_TU(k_compat)

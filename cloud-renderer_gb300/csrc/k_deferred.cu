@@ -143,8 +143,10 @@ __global__ void __launch_bounds__(256) k_march(VolDesc vd, CamDesc cam, TracePar
             const unsigned ballot = __ballot_sync(0xffffffffu, emit);
             if (emit) {
                 const unsigned slot = cnt + __popc(ballot & ((1u << lane) - 1u));
-                pw[slot] = make_float4(v0, v1, v2, w);
-                gl[slot] = make_float2(G, __int_as_float(lane));
+                if (CG_IN_BOUNDS((size_t)region * sb.capacity + slot, sb.nslots)) {
+                    pw[slot] = make_float4(v0, v1, v2, w);
+                    gl[slot] = make_float2(G, __int_as_float(lane));
+                }
             }
             // step table: where this step's samples start and which lanes emitted
             if (ballot) {
@@ -272,7 +274,9 @@ __global__ void __launch_bounds__(128) k_accumulate(CamDesc cam, TraceParams tp,
                 const unsigned sy = __shfl_sync(0xffffffffu, st_l.y, src);
                 v[q] = 0.f;
                 // entries past m are (0, 0): no lane emitted there
-                if (e0 + q < m && ((sy >> lane) & 1u)) {
+                if (e0 + q < m && ((sy >> lane) & 1u) &&
+                    CG_IN_BOUNDS((size_t)region * sb.capacity + sx + __popc(sy & below),
+                                 sb.nslots)) {
                     v[q] = cw[sx + __popc(sy & below)];
                     have |= 1u << q;
                 }
@@ -325,3 +329,5 @@ cudaError_t launch_accumulate(CamDesc cam, TraceParams tp, SampleBuf sb, const f
                                                     img, dst);
     return cudaGetLastError();
 }
+
+CG_OOB_TU(k_deferred)

@@ -88,3 +88,5 @@ cudaError_t launch_mlp_adam(const AdamArgs& aa, cudaStream_t st) {
     k_mlp_adam<<<(MLP_NPARAM + 1 + 255) / 256, 256, 0, st>>>(aa);
     return cudaGetLastError();
 }
+
+CG_OOB_TU(k_mlp)

@@ -111,3 +111,5 @@ extern "C" cg_status cg_sun_map_noalloc(int dimension, float bound_min, float bo
     if (e != cudaSuccess) return noalloc_fail(CG_ERR_CUDA, cudaGetErrorString(e));
     return CG_OK;
 }
+
+CG_OOB_TU(k_noalloc)

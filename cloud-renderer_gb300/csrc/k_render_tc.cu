@@ -423,8 +423,10 @@ __global__ void __launch_bounds__(RT_THREADS, RT_CTAS_PER_SM)
                     tau = m.tau_scale * mlp::softplus(y);
                 }
                 const Rec& rc = S.rec[ri];
-                ra.contrib[(size_t)rc.region * ra.cap + (mt.y & 0xFFFFu)] =
-                    sp.w * __expf(-tp.sigma * tau) * (amb + (1.f - amb) * __uint_as_float(mt.x));
+                const size_t at = (size_t)rc.region * ra.cap + (mt.y & 0xFFFFu);
+                if (CG_IN_BOUNDS(at, (size_t)ra.regions * ra.cap))
+                    ra.contrib[at] = sp.w * __expf(-tp.sigma * tau) *
+                                     (amb + (1.f - amb) * __uint_as_float(mt.x));
             }
             // count the shaded samples per record (rows of one record share
             // one atomic)
@@ -560,3 +562,5 @@ cudaError_t launch_render_mlp_tc(VolDesc vd, CamDesc cam, TraceParams tp, const 
                                                                        status);
     return cudaGetLastError();
 }
+
+CG_OOB_TU(k_render_tc)

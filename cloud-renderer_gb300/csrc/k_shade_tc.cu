@@ -97,7 +97,8 @@ __device__ __forceinline__ void pack_row(const VolDesc& vd, const ConeSchedule& 
 __device__ __forceinline__ unsigned slot_at(const SampleBuf& sb, unsigned tile, unsigned ntiles,
                                             unsigned total, int row) {
     const unsigned i = tile * 128u + (unsigned)row;
-    return (tile < ntiles && i < total) ? sb.slot_of[i] : CG_NO_SLOT;
+    const unsigned s = (tile < ntiles && i < total) ? sb.slot_of[i] : CG_NO_SLOT;
+    return (s == CG_NO_SLOT || CG_IN_BOUNDS(s, sb.nslots)) ? s : CG_NO_SLOT;
 }
 
 // All writes of the CTA to the activation tiles -> visible to the tensor
@@ -266,7 +267,9 @@ __global__ void __launch_bounds__(128 * SHADE_GROUPS, SHADE_CTAS_PER_SM)
             } else {
                 tau = m.tau_scale * mlp::softplus(y);
             }
-            sb.contrib[row.slot] = row.w * __expf(-tp.sigma * tau) * (amb + (1.f - amb) * row.g);
+            if (CG_IN_BOUNDS(row.slot, sb.nslots))
+                sb.contrib[row.slot] =
+                    row.w * __expf(-tp.sigma * tau) * (amb + (1.f - amb) * row.g);
         }
         // ---- the next tile's inputs
         pack_row<FMT>(vd, cone, m, tp, nslot, ns, ng, nf, row, act, r);
@@ -457,3 +460,5 @@ cudaError_t launch_shade_mlp_tc(VolDesc vd, CamDesc cam, TraceParams tp, const M
         k_shade_mlp_tc<1><<<blocks, 128 * SHADE_GROUPS, SH_SMEM_BYTES, st>>>(vd, tp, cone, m, geo, sb, status);
     return cudaGetLastError();
 }
+
+CG_OOB_TU(k_shade_tc)

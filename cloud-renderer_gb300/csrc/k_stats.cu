@@ -90,3 +90,5 @@ cudaError_t launch_err_stats(const float4* a, const void* ref, int ref_f64, size
     k_err_final<<<1, STATS_THREADS, 0, st>>>(scratch, STATS_CTAS, out);
     return cudaGetLastError();
 }
+
+CG_OOB_TU(k_stats)

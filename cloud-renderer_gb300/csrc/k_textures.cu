@@ -78,3 +78,5 @@ cudaError_t launch_pack_level(VolDesc vd, int l, cudaSurfaceObject_t surf, cudaS
         k_pack_level<1><<<blocks, 256, 0, st>>>(vd, l, surf);
     return cudaGetLastError();
 }
+
+CG_OOB_TU(k_textures)

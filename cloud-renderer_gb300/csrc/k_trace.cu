@@ -340,3 +340,5 @@ cudaError_t launch_trace_cones(VolDesc vd, TraceParams tp, const float* pos, int
         k_trace_cones<1><<<blocks, 128, 0, st>>>(vd, tp, cs, pos, n, out);
     return cudaGetLastError();
 }
+
+CG_OOB_TU(k_trace)

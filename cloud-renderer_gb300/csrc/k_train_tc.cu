@@ -436,3 +436,5 @@ cudaError_t launch_mlp_train(const TrainArgs& ta, int ctas, cudaStream_t st) {
     k_mlp_train_tc<<<ctas, 128, TT_SMEM, st>>>(ta);
     return cudaGetLastError();
 }
+
+CG_OOB_TU(k_train_tc)

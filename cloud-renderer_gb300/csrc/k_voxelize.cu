@@ -369,13 +369,13 @@ __global__ void k_highlight(BoardsDev b, SunFrame fr, const unsigned long long* 
     posmap[idx] = make_float4(p[0], p[1], p[2], 1.0f);
     const float o = hp.offset;
     int vi;
-    if (voxel_index(hp, p[0], p[1], p[2], vi)) mask[vi] = 1;
+    if (voxel_index(hp, p[0], p[1], p[2], vi) && CG_IN_BOUNDS(vi, (size_t)hp.D * hp.D * hp.D)) mask[vi] = 1;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
         float x = (k & 4) ? fsub(p[0], o) : fadd(p[0], o);
         float y = (k & 2) ? fsub(p[1], o) : fadd(p[1], o);
         float z = (k & 1) ? fsub(p[2], o) : fadd(p[2], o);
-        if (voxel_index(hp, x, y, z, vi)) mask[vi] = 1;
+        if (voxel_index(hp, x, y, z, vi) && CG_IN_BOUNDS(vi, (size_t)hp.D * hp.D * hp.D)) mask[vi] = 1;
     }
 }
 
@@ -397,6 +397,7 @@ __device__ __forceinline__ void store_voxel(const VolDesc& vd, void* pyr, int l,
                                             int z, float4 v) {
     const int N = vd.dims[l];
     size_t idx = (size_t)vd.offs[l] + ((size_t)z * N + y) * N + x;
+    if (!CG_IN_BOUNDS(idx, vd.nvox)) return;
     __half2 h;
     if (vd.fmt == 0) {
         reinterpret_cast<float4*>(pyr)[idx] = v;
@@ -826,3 +827,5 @@ cudaError_t launch_count_active(const uint32_t* count, const uint8_t* mask, size
     k_count_active<<<blocks, 256, 0, st>>>(count, mask, n, out);
     return cudaGetLastError();
 }
+
+CG_OOB_TU(k_voxelize)

@@ -118,11 +118,13 @@ typedef struct cg_render_params {
     int use_mlp;               /* 1: sun cone replaced by the MLP surrogate */
     const cg_mlp* mlp;         /* required when use_mlp != 0 */
     int pipeline;              /* cg_pipeline */
-    /* exact cone, fused pipeline: 0 (default) = each thread traces the sun
-     * cones of its own ray's samples; N in 1..32 = the warp marches its 32
-     * rays in lockstep and, at a view step where at most N of them
-     * contribute, traces each of those cones with its lanes over the cone's
-     * steps (a shuffle-tree sum; images within 1e-6 of the default) */
+    /* exact cone, fused pipeline: 0 = each thread traces the sun cones of
+     * its own ray's samples; N in 1..32 = the warp marches its 32 rays in
+     * lockstep and, at a view step where at most N of them contribute,
+     * traces each of those cones with its lanes over the cone's steps (a
+     * shuffle-tree sum; images within 1e-6 of N = 0).  Default 8 (the
+     * fastest measured: 1080p over 256^3, 3 % faster than 0, while 32 is
+     * six times slower) */
     int cone_lanes;
 } cg_render_params;
 
@@ -372,6 +374,17 @@ cg_status cg_context_last_samples(cg_context* ctx, uint64_t* samples);
  * out: returns CG_ERR_DEVICE_FAULT with *waited_us = the time waited, and the
  * context stays usable.  CG_OK would mean the bound did not fire. */
 cg_status cg_context_check_wait_timeout(cg_context* ctx, uint32_t limit_us, uint64_t* waited_us);
+
+/* Bounds-check build (no reference counterpart; the stand-in for a memory
+ * checker): cg_bounds_check_build() is 1 when the library was built with
+ * CG_BOUNDS_CHECK=1, whose kernels test their global gather and scatter
+ * indexes, skip an out-of-range access and count it instead of faulting.
+ * cg_context_bounds_violations returns the count since its last call
+ * (clearing it) and, in site (may be NULL), the first one's source line and
+ * index; CG_ERR_UNSUPPORTED in the normal build.  Synchronises the device. */
+int cg_bounds_check_build(void);
+cg_status cg_context_bounds_violations(cg_context* ctx, uint64_t* count, char* site,
+                                       int site_len);
 
 /* ---- allocation-free variant ------------------------------------------- */
 

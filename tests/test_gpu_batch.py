@@ -131,3 +131,30 @@ def test_frame_graph_replay(ctx):
         assert np.abs(a - r).max() <= TOL
     assert any(np.abs(a - b).max() > 1e-3 for a, b in zip(moved, first))
     g.close()
+
+
+@pytest.mark.parametrize("lanes", [1, 32])
+def test_batch_matches_oracle(ctx, lanes):
+    """Every view of a batch against the FP64 oracle directly (not only
+    through the single-view renderer): max-abs <= 1e-4 per RGBA channel."""
+    from oracle import oracle as O
+    bw, sun, vols, cams, outs, views, shader = make_batch(ctx)
+    ctx.render_batch(views, shader, config=(lanes, 1, 0))
+    ctx.synchronize()
+    oracles = {}
+    P = O.params_from_shader(shader)
+    seen = 0.0
+    for i, vd in enumerate(bw.views):
+        k = vd["cloud"]
+        if k not in oracles:
+            c = bw.clouds[k]
+            ov = O.OracleVolume(c["dim"], configs.VOLUME_BOUNDS, configs.VOLUME_POSITION, c["mips"])
+            ov.set_boards(c["positions"], c["scales"], c["densities"])
+            ov.voxelize(sun.direction, sun.map_width, sun.map_height)
+            oracles[k] = ov
+        ref = oracles[k].render(cams[i], P, sun.direction)
+        got = read(outs[i], cams[i]).astype(np.float64)
+        err = np.abs(got - ref).max(axis=(0, 1))
+        assert np.all(err <= 1e-4), (i, err)
+        seen = max(seen, float(ref[..., 3].max()))
+    assert seen > 0.1

@@ -231,7 +231,7 @@ def test_cooperative_cones_match_fused_and_oracle(ctx, cone_mode):
                              wl.sun_direction, wl.sun_map)
     kw = dict(wl.shader_kwargs(), coneMode=cone_mode)
     cam = workload.make_camera(wl.cameras[2])
-    base = cloudgb.ConeTraceShader(**kw).coneTrace(vol, cam)
+    base = cloudgb.ConeTraceShader(coneLanes=0, **kw).coneTrace(vol, cam)
     ref = _oracle_image(ov, cloudgb.ConeTraceShader(**kw), cam, sun.direction)
     assert base[..., 3].max() > 0.2
     for lanes in (1, 8, 32):
@@ -240,7 +240,7 @@ def test_cooperative_cones_match_fused_and_oracle(ctx, cone_mode):
         err = np.abs(img.astype(np.float64) - ref).max()
         assert err <= IMAGE_TOL, (lanes, err)
     big = workload.make_camera(dict(wl.cameras[2], width=1920, height=1080))
-    a = cloudgb.ConeTraceShader(**kw).coneTrace(vol, big)
+    a = cloudgb.ConeTraceShader(coneLanes=0, **kw).coneTrace(vol, big)
     b = cloudgb.ConeTraceShader(coneLanes=32, **kw).coneTrace(vol, big)
     assert np.abs(a - b).max() <= 1e-6
     with pytest.raises(cloudgb.CloudError):
