@@ -460,6 +460,7 @@ extern "C" cg_status cg_volume_create(cg_context* ctx, int dimension, float boun
     // every brick starts dirty: the pyramid's memory is uninitialised
     if (e == cudaSuccess) e = v->bdirty.ensure((size_t)v->bins.nbricks);
     if (e == cudaSuccess) e = cudaMemset(v->bdirty.p, 1, (size_t)v->bins.nbricks);
+    if (e == cudaSuccess) e = v->bhl.ensure((size_t)v->bins.nbricks);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&v->boards_ready, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&v->boards_read, cudaEventDisableTiming);
     if (e != cudaSuccess) {
@@ -477,7 +478,7 @@ extern "C" void cg_volume_destroy(cg_volume* v) {
     cudaStreamSynchronize(v->ctx->stream);
     DevBuf* bufs[] = {&v->pyr, &v->count, &v->dq, &v->mask, &v->boards,
                       &v->bcount, &v->boff, &v->bcursor, &v->blist,
-                      &v->bdirty,
+                      &v->bdirty, &v->bhl,
                       &v->keys, &v->posmap, &v->scratch, &v->occ};
     for (DevBuf* b : bufs) b->release();
     v->h_stage.release();
@@ -787,6 +788,7 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
     bins.cursor = v->bcursor.as<uint32_t>();
     bins.list = v->blist.as<uint32_t>();
     bins.dirty = v->bdirty.as<uint8_t>();
+    bins.hl = v->bhl.as<const uint8_t>();
     VolDesc vd = desc_of(v);
     // once the surrogate renderer has built the texture copies, keep them
     // current from the voxelize stores instead of a copy pass
@@ -809,6 +811,7 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
     // clearGPU (CloudVolume.cpp:96-100) + clearPositionMap (VoxelizeShader.cpp:185-187)
     CG_CUDA(cudaMemsetAsync(v->keys.p, 0xFF, texels * 8, sd));
     CG_CUDA(cudaMemsetAsync(v->mask.p, 0, n0, sd));
+    CG_CUDA(cudaMemsetAsync(v->bhl.p, 0, (size_t)bins.nbricks, sd));
     {
         NvtxRange r("voxelize.sun_pass");
         // pass 1: sun-view nearest-surface map
@@ -816,7 +819,7 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
         // pass 2: highlight stores
         CG_LAUNCH(ctx, launch_highlight(b, fr, v->keys.as<uint64_t>(), v->posmap.as<float4>(),
                                         v->D, v->wmin, v->range, highlight_offset(v),
-                                        v->mask.as<uint8_t>(), sd));
+                                        v->mask.as<uint8_t>(), v->bhl.as<uint8_t>(), sd));
         CG_CUDA(cudaEventRecord(ctx->join_ev, sd));
     }
     {
@@ -1374,6 +1377,7 @@ static cg_status ensure_coverage(const cg_volume* cv) {
     bins.cursor = v->bcursor.as<uint32_t>();
     bins.list = v->blist.as<uint32_t>();
     bins.dirty = v->bdirty.as<uint8_t>();
+    bins.hl = nullptr;  // the coverage-only splat reads no mask
     CG_LAUNCH(v->ctx, launch_splat(boards_of(v), bins, v->mask.as<uint8_t>(), desc_of(v), v->pyr.p,
                                    v->count.as<uint32_t>(), v->dq.as<uint32_t>(), 0,
                                    raw_of(v), true, s));

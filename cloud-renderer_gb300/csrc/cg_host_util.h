@@ -161,6 +161,7 @@ struct cg_volume {
     HostBuf h_stage;
     Bins bins{};
     DevBuf bcount, boff, bcursor, blist, bdirty;
+    DevBuf bhl;  // per-brick highlight flags of the current voxelize
     // sun map
     int mapW = 0, mapH = 0;
     DevBuf keys, posmap;

@@ -142,6 +142,9 @@ struct Bins {
     // non-zero values from an earlier voxelize; a brick without boards or
     // highlights whose flag is 0 is already all zero and is not rewritten
     uint8_t* dirty;    // nbricks
+    // per brick: 1 when a highlight store of this voxelize marked one of its
+    // voxels (written by the highlight pass; NULL: the splat reads the mask)
+    const uint8_t* hl;
 };
 
 // ---- deferred renderer ----------------------------------------------------
@@ -335,10 +338,12 @@ cudaError_t launch_bin_scan(Bins bins, cudaStream_t st);
 cudaError_t launch_bin_fill(const BoardsDev& b, int D, Bins bins, cudaStream_t st);
 cudaError_t launch_sunmap(const BoardsDev& b, const SunFrame& fr, uint64_t* keys,
                           cudaStream_t st);
+// hl_brick (may be NULL): per 8^3 brick of the volume, set to 1 beside every
+// mask byte set (cleared by the caller before the launch)
 cudaError_t launch_highlight(const BoardsDev& b, const SunFrame& fr, const uint64_t* keys,
                              float4* posmap, int D, const float wmin[3],
                              const float range[3], float offset, uint8_t* mask,
-                             cudaStream_t st);
+                             uint8_t* hl_brick, cudaStream_t st);
 // coverage_only: write the integer coverage (count, dq) and nothing else
 cudaError_t launch_splat(const BoardsDev& b, Bins bins, const uint8_t* mask, VolDesc vd,
                          void* pyr, uint32_t* count, uint32_t* dq, int fused_levels,

@@ -107,7 +107,7 @@ extern "C" cg_status cg_sun_map_noalloc(int dimension, float bound_min, float bo
     }
     e = launch_highlight(b, fr, reinterpret_cast<const uint64_t*>(keys),
                          reinterpret_cast<float4*>(d_positions), dimension, wmin, range, offset,
-                         d_mask, s);
+                         d_mask, nullptr, s);
     if (e != cudaSuccess) return noalloc_fail(CG_ERR_CUDA, cudaGetErrorString(e));
     return CG_OK;
 }

@@ -326,10 +326,12 @@ struct HiParams {
     float wmin[3], range[3];
     float fD, offset;
     int D;
+    int nb;            // bricks per axis
+    uint8_t* hl;       // per-brick highlight flags (NULL: none)
 };
 
 __device__ __forceinline__ bool voxel_index(const HiParams& hp, float x, float y, float z,
-                                            int& o) {
+                                            int& o, int& brick) {
     float c[3] = {x, y, z};
     int id[3];
 #pragma unroll
@@ -340,7 +342,16 @@ __device__ __forceinline__ bool voxel_index(const HiParams& hp, float x, float y
         id[a] = __float2int_rz(v);  // ivec3(): truncation toward zero
     }
     o = (id[2] * hp.D + id[1]) * hp.D + id[0];
+    brick = ((id[2] / CG_BRICK) * hp.nb + id[1] / CG_BRICK) * hp.nb + id[0] / CG_BRICK;
     return true;
+}
+
+// One highlight store: the voxel's mask byte and, when flags are kept, its
+// brick's flag.
+__device__ __forceinline__ void mark(const HiParams& hp, uint8_t* mask, int vi, int brick) {
+    if (!CG_IN_BOUNDS(vi, (size_t)hp.D * hp.D * hp.D)) return;
+    mask[vi] = 1;
+    if (hp.hl && CG_IN_BOUNDS(brick, (size_t)hp.nb * hp.nb * hp.nb)) hp.hl[brick] = 1;
 }
 
 __global__ void k_highlight(BoardsDev b, SunFrame fr, const unsigned long long* keys,
@@ -368,14 +379,14 @@ __global__ void k_highlight(BoardsDev b, SunFrame fr, const unsigned long long* 
                     fr.eye[a]);
     posmap[idx] = make_float4(p[0], p[1], p[2], 1.0f);
     const float o = hp.offset;
-    int vi;
-    if (voxel_index(hp, p[0], p[1], p[2], vi) && CG_IN_BOUNDS(vi, (size_t)hp.D * hp.D * hp.D)) mask[vi] = 1;
+    int vi, bk;
+    if (voxel_index(hp, p[0], p[1], p[2], vi, bk)) mark(hp, mask, vi, bk);
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
         float x = (k & 4) ? fsub(p[0], o) : fadd(p[0], o);
         float y = (k & 2) ? fsub(p[1], o) : fadd(p[1], o);
         float z = (k & 1) ? fsub(p[2], o) : fadd(p[2], o);
-        if (voxel_index(hp, x, y, z, vi) && CG_IN_BOUNDS(vi, (size_t)hp.D * hp.D * hp.D)) mask[vi] = 1;
+        if (voxel_index(hp, x, y, z, vi, bk)) mark(hp, mask, vi, bk);
     }
 }
 
@@ -530,13 +541,18 @@ __global__ void __launch_bounds__(64) k_splat(BoardsDev b, Bins bins, const uint
     // barrier after the board loop: the tile may be written): a brick without
     // boards or highlights whose voxels are still zero from an earlier
     // voxelize writes nothing
+    // (with per-brick flags, a brick no highlight store touched reads none of
+    // its 512 mask bytes)
+    const bool hl = bins.hl == nullptr || bins.hl[brick] != 0;
     unsigned mkb = 0u;
+    if (hl) {
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        const int z = z0 + j;
-        if (inxy && z < D && mask[((size_t)z * D + y) * D + x]) mkb |= 1u << j;
+        for (int j = 0; j < 8; ++j) {
+            const int z = z0 + j;
+            if (inxy && z < D && mask[((size_t)z * D + y) * D + x]) mkb |= 1u << j;
+        }
     }
-    const bool keep = n > 0u || __syncthreads_or(mkb != 0u);
+    const bool keep = n > 0u || (hl && __syncthreads_or(mkb != 0u));
     if (!keep && !bins.dirty[brick]) return;
     __syncthreads();  // every thread has read the flag
     if (tid == 0) bins.dirty[brick] = keep ? 1 : 0;
@@ -772,8 +788,10 @@ cudaError_t launch_sunmap(const BoardsDev& b, const SunFrame& fr, uint64_t* keys
 cudaError_t launch_highlight(const BoardsDev& b, const SunFrame& fr, const uint64_t* keys,
                              float4* posmap, int D, const float wmin[3],
                              const float range[3], float offset, uint8_t* mask,
-                             cudaStream_t st) {
+                             uint8_t* hl_brick, cudaStream_t st) {
     HiParams hp;
+    hp.nb = (D + CG_BRICK - 1) / CG_BRICK;
+    hp.hl = hl_brick;
     for (int a = 0; a < 3; ++a) {
         hp.wmin[a] = wmin[a];
         hp.range[a] = range[a];
