@@ -478,7 +478,7 @@ extern "C" void cg_volume_destroy(cg_volume* v) {
     cudaStreamSynchronize(v->ctx->stream);
     DevBuf* bufs[] = {&v->pyr, &v->count, &v->dq, &v->mask, &v->boards,
                       &v->bcount, &v->boff, &v->bcursor, &v->blist,
-                      &v->bdirty, &v->bhl, &v->sunext,
+                      &v->bdirty, &v->bhl,
                       &v->keys, &v->posmap, &v->scratch, &v->occ};
     for (DevBuf* b : bufs) b->release();
     v->h_stage.release();
@@ -600,7 +600,6 @@ extern "C" cg_status cg_volume_set_billboards(cg_volume* v, const float* positio
              "cg_volume_set_billboards: %zu board-brick pairs exceed 2^32", pairs);
     // the device records mirror the staging layout: one copy uploads them all
     CG_CUDA(v->boards.ensure(total));
-    CG_CUDA(v->sunext.ensure((size_t)(n > 0 ? n : 1) * sizeof(ushort4)));
     char* dev = v->boards.as<char>();
     v->cwr = reinterpret_cast<float4*>(dev + o_cwr);
     v->q = reinterpret_cast<int4*>(dev + o_q);
@@ -810,13 +809,13 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
     CG_CUDA(cudaEventRecord(ctx->fork_ev, s));
     CG_CUDA(cudaStreamWaitEvent(sd, ctx->fork_ev, 0));
     // clearGPU (CloudVolume.cpp:96-100) + clearPositionMap (VoxelizeShader.cpp:185-187)
+    CG_CUDA(cudaMemsetAsync(v->keys.p, 0xFF, texels * 8, sd));
     CG_CUDA(cudaMemsetAsync(v->mask.p, 0, n0, sd));
     CG_CUDA(cudaMemsetAsync(v->bhl.p, 0, (size_t)bins.nbricks, sd));
     {
         NvtxRange r("voxelize.sun_pass");
-        // pass 1: sun-view nearest-surface map (every texel's key written)
-        CG_LAUNCH(ctx, launch_sunmap_tiles(b, fr, v->sunext.as<ushort4>(),
-                                           v->keys.as<uint64_t>(), sd));
+        // pass 1: sun-view nearest-surface map
+        if (b.n) CG_LAUNCH(ctx, launch_sunmap(b, fr, v->keys.as<uint64_t>(), sd));
         // pass 2: highlight stores
         CG_LAUNCH(ctx, launch_highlight(b, fr, v->keys.as<uint64_t>(), v->posmap.as<float4>(),
                                         v->D, v->wmin, v->range, highlight_offset(v),

@@ -162,7 +162,6 @@ struct cg_volume {
     Bins bins{};
     DevBuf bcount, boff, bcursor, blist, bdirty;
     DevBuf bhl;  // per-brick highlight flags of the current voxelize
-    DevBuf sunext;  // per board: its texel box in the sun map (ushort4)
     // sun map
     int mapW = 0, mapH = 0;
     DevBuf keys, posmap;

@@ -336,10 +336,6 @@ bool sun_frame_for_box(const float position[3], float b0, float b1, const float 
 cudaError_t launch_bin_count(const BoardsDev& b, int D, Bins bins, cudaStream_t st);
 cudaError_t launch_bin_scan(Bins bins, cudaStream_t st);
 cudaError_t launch_bin_fill(const BoardsDev& b, int D, Bins bins, cudaStream_t st);
-// The sun map by texel tiles: every key written (no clearing needed); ext:
-// per-board scratch (n ushort4).
-cudaError_t launch_sunmap_tiles(const BoardsDev& b, const SunFrame& fr, ushort4* ext,
-                                uint64_t* keys, cudaStream_t st);
 cudaError_t launch_sunmap(const BoardsDev& b, const SunFrame& fr, uint64_t* keys,
                           cudaStream_t st);
 // hl_brick (may be NULL): per 8^3 brick of the volume, set to 1 beside every

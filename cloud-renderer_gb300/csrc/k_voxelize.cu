@@ -320,114 +320,6 @@ __global__ void __launch_bounds__(256) k_sunmap(BoardsDev b, SunFrame fr,
     }
 }
 
-// ---- the sun map by texel tiles --------------------------------------------
-// The same keys as k_sunmap without atomics: a CTA owns a 64 x 16 tile of the
-// map, one thread four of its texels (columns lane, lane + 32; rows warp,
-// warp + 8).  The boards whose texel box (texel_range, as k_sunmap) meets the
-// tile are gathered 256 at a time from per-board extents computed once
-// (k_sun_extents); each thread tests its texels against them with k_sunmap's
-// arithmetic -- the 1.0001 r^2 disc pre-test, the certain-loser skip against
-// its own running minimum, the exact profile and depth -- and keeps the
-// minimum (depth bits << 32 | board) in a register.  Every texel's key is
-// written once (all ones where no board reaches it): no clearing pass, no
-// atomics, no reads of the key map.
-constexpr int SMT_W = 64, SMT_H = 16;
-
-__global__ void k_sun_extents(BoardsDev b, SunFrame fr, ushort4* ext) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= b.n) return;
-    const float4 c = b.cwr[i];
-    const float3 cv = sun_view_of(fr, c);
-    int ia, ib, ja, jb;
-    texel_range(fr.lo, fr.hi, cv.x, c.w, fr.W, ia, ib);
-    texel_range(fr.lo, fr.hi, cv.y, c.w, fr.H, ja, jb);
-    // an empty box is stored as ia > ib (texel_range gives 1 > 0)
-    ext[i] = make_ushort4((unsigned short)ia, (unsigned short)ib, (unsigned short)ja,
-                          (unsigned short)jb);
-}
-
-__global__ void __launch_bounds__(256) k_sunmap_tiles(BoardsDev b, SunFrame fr,
-                                                      const ushort4* ext,
-                                                      unsigned long long* keys) {
-    __shared__ float4 s_cv[256];   // sun-view centre, radius
-    __shared__ float s_dz2[256];   // smallest square of the surface offset
-    __shared__ ushort4 s_ext[256];
-    __shared__ int s_idx[256];
-    __shared__ int s_n;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int x0 = blockIdx.x * SMT_W, y0 = blockIdx.y * SMT_H;
-    const int x1 = min(x0 + SMT_W, fr.W) - 1, y1 = min(y0 + SMT_H, fr.H) - 1;
-    int tx[2], ty[2];
-    float xv[2], yv[2];
-    tx[0] = x0 + lane;
-    tx[1] = x0 + lane + 32;
-    ty[0] = y0 + warp;
-    ty[1] = y0 + warp + 8;
-    for (int q = 0; q < 2; ++q) {
-        xv[q] = texel_coord(fr.lo, fr.hi, tx[q], fr.W);
-        yv[q] = texel_coord(fr.lo, fr.hi, ty[q], fr.H);
-    }
-    unsigned long long best[4] = {CG_KEY_EMPTY, CG_KEY_EMPTY, CG_KEY_EMPTY, CG_KEY_EMPTY};
-    for (int base = 0; base < b.n; base += 256) {
-        if (tid == 0) s_n = 0;
-        __syncthreads();
-        const int j = base + tid;
-        if (j < b.n) {
-            const ushort4 e = ext[j];
-            if (e.x <= e.y && e.z <= e.w && (int)e.x <= x1 && (int)e.y >= x0 &&
-                (int)e.z <= y1 && (int)e.w >= y0) {
-                const int k = atomicAdd(&s_n, 1);
-                s_idx[k] = j;
-                s_ext[k] = e;
-            }
-        }
-        __syncthreads();
-        const int m = s_n;
-        if (tid < m) {
-            const float4 c = b.cwr[s_idx[tid]];
-            const float3 cv = sun_view_of(fr, c);
-            s_cv[tid] = make_float4(cv.x, cv.y, cv.z, c.w);
-            float dz2_min = 0.0f;
-            const float dz_lo = fadd(cv.z, fr.near_z), dz_hi = fadd(fadd(cv.z, c.w), fr.near_z);
-            if (dz_lo > 0.0f) dz2_min = fmul(dz_lo, dz_lo);
-            else if (dz_hi < 0.0f) dz2_min = fmul(dz_hi, dz_hi);
-            s_dz2[tid] = dz2_min;
-        }
-        __syncthreads();
-        for (int k = 0; k < m; ++k) {
-            const ushort4 e = s_ext[k];
-            const float4 c4 = s_cv[k];
-            const float3 cv = make_float3(c4.x, c4.y, c4.z);
-            const float r = c4.w;
-            const float r2 = 1.0001f * (r * r);
-            const float dz2_min = s_dz2[k];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int qx = q & 1, qy = q >> 1;
-                if (tx[qx] < (int)e.x || tx[qx] > (int)e.y || ty[qy] < (int)e.z ||
-                    ty[qy] > (int)e.w)
-                    continue;
-                const float ex = xv[qx] - cv.x, ey = yv[qy] - cv.y;
-                if (ex * ex + ey * ey > r2) continue;
-                const float xy2 = fadd(fmul(xv[qx], xv[qx]), fmul(yv[qy], yv[qy]));
-                const float cd = __uint_as_float((unsigned)(best[q] >> 32));
-                if (cd * cd < fadd(xy2, dz2_min) * (1.0f - 0x1p-20f)) continue;
-                float zs, depth;
-                if (!sun_fragment(xv[qx], yv[qy], cv, r, fr.near_z, zs, depth)) continue;
-                const unsigned long long key =
-                    ((unsigned long long)__float_as_uint(depth) << 32) | (unsigned)s_idx[k];
-                if (key < best[q]) best[q] = key;
-            }
-        }
-        __syncthreads();
-    }
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        const int qx = q & 1, qy = q >> 1;
-        if (tx[qx] < fr.W && ty[qy] < fr.H) keys[(size_t)ty[qy] * fr.W + tx[qx]] = best[q];
-    }
-}
-
 // ---- highlight stores (second_voxelize.glsl:34-51) -------------------------
 
 struct HiParams {
@@ -890,14 +782,6 @@ cudaError_t launch_sunmap(const BoardsDev& b, const SunFrame& fr, uint64_t* keys
                           cudaStream_t st) {
     if (b.n == 0) return cudaSuccess;
     k_sunmap<<<b.n, 256, 0, st>>>(b, fr, reinterpret_cast<unsigned long long*>(keys));
-    return cudaGetLastError();
-}
-
-cudaError_t launch_sunmap_tiles(const BoardsDev& b, const SunFrame& fr, ushort4* ext,
-                                uint64_t* keys, cudaStream_t st) {
-    if (b.n > 0) k_sun_extents<<<(b.n + 255) / 256, 256, 0, st>>>(b, fr, ext);
-    dim3 grd((fr.W + SMT_W - 1) / SMT_W, (fr.H + SMT_H - 1) / SMT_H);
-    k_sunmap_tiles<<<grd, 256, 0, st>>>(b, fr, ext, reinterpret_cast<unsigned long long*>(keys));
     return cudaGetLastError();
 }
 
