@@ -64,8 +64,10 @@ extern "C" cg_status cg_context_create(int device, cg_context** out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->clear_ev, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         if (c->join_ev) cudaEventDestroy(c->join_ev);
+        if (c->clear_ev) cudaEventDestroy(c->clear_ev);
         if (c->fork_ev) cudaEventDestroy(c->fork_ev);
         if (c->side) cudaStreamDestroy(c->side);
         if (c->stream) cudaStreamDestroy(c->stream);
@@ -305,6 +307,7 @@ void context_release(cg_context* ctx) {
         if (e) cudaEventDestroy(e);
     cudaEventDestroy(ctx->fork_ev);
     cudaEventDestroy(ctx->join_ev);
+    cudaEventDestroy(ctx->clear_ev);
     cudaStreamDestroy(ctx->side);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -808,15 +811,19 @@ extern "C" cg_status cg_voxelize(cg_volume* v, const cg_sun* sun, void* stream) 
     cudaStream_t sd = ctx->side;
     CG_CUDA(cudaEventRecord(ctx->fork_ev, s));
     CG_CUDA(cudaStreamWaitEvent(sd, ctx->fork_ev, 0));
-    // clearGPU (CloudVolume.cpp:96-100) + clearPositionMap (VoxelizeShader.cpp:185-187)
+    // clearGPU (CloudVolume.cpp:96-100) + clearPositionMap (VoxelizeShader.cpp:185-187):
+    // the highlight mask and its brick flags are cleared on s, where the binning
+    // has time to spare, the key map on the side stream ahead of the sun map
+    CG_CUDA(cudaMemsetAsync(v->mask.p, 0, n0, s));
+    CG_CUDA(cudaMemsetAsync(v->bhl.p, 0, (size_t)bins.nbricks, s));
+    CG_CUDA(cudaEventRecord(ctx->clear_ev, s));
     CG_CUDA(cudaMemsetAsync(v->keys.p, 0xFF, texels * 8, sd));
-    CG_CUDA(cudaMemsetAsync(v->mask.p, 0, n0, sd));
-    CG_CUDA(cudaMemsetAsync(v->bhl.p, 0, (size_t)bins.nbricks, sd));
     {
         NvtxRange r("voxelize.sun_pass");
         // pass 1: sun-view nearest-surface map
         if (b.n) CG_LAUNCH(ctx, launch_sunmap(b, fr, v->keys.as<uint64_t>(), sd));
-        // pass 2: highlight stores
+        // pass 2: highlight stores (after the mask's clearing)
+        CG_CUDA(cudaStreamWaitEvent(sd, ctx->clear_ev, 0));
         CG_LAUNCH(ctx, launch_highlight(b, fr, v->keys.as<uint64_t>(), v->posmap.as<float4>(),
                                         v->D, v->wmin, v->range, highlight_offset(v),
                                         v->mask.as<uint8_t>(), v->bhl.as<uint8_t>(), sd));

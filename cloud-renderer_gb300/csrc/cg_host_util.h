@@ -85,6 +85,7 @@ struct cg_context {
     // concurrently with the brick binning, forked and joined by two events
     cudaStream_t side = nullptr;
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    cudaEvent_t clear_ev = nullptr;  // voxelize: the mask cleared (on the caller's stream)
     uint64_t launches = 0;
     int refs = 1;  // the caller's handle + one per volume / model created on it
     bool shaded_valid = false;  // the status words hold a surrogate render's counters
