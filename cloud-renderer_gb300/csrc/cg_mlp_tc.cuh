@@ -29,14 +29,10 @@ constexpr int NET_W3 = 8192;
 constexpr int NET_W1 = 16384;
 constexpr int NET_ONES = NET_W1 + 2048;
 constexpr int NET_BIAS = NET_ONES + 256;
-// the output layer for the tensor cores: 16 rows x 128 B, 128B-swizzled, row 0 =
-// W4 (FP16, not scaled), rows 1-15 zero (N = 16, the smallest M = 128 allows)
-constexpr int NET_W4 = ((NET_BIAS + 3 * 2048) + 1023) / 1024 * 1024;
-constexpr int NET_BYTES = NET_W4 + 2048;
+constexpr int NET_BYTES = NET_BIAS + 3 * 2048;
 constexpr int ACT_BYTES = 128 * 128;  // one activation tile
 
 constexpr uint32_t IDESC = tc::idesc_f16_f32(128, 64);
-constexpr uint32_t IDESC_OUT = tc::idesc_f16_f32(128, 16);
 
 // One FP16 weight row (`chunks` x 8 halves) into row r of a swizzled tile
 // (128B-swizzled rows of 8 chunks, or 32B-swizzled rows of 2), scaled by 1/2.
@@ -71,14 +67,6 @@ __device__ __forceinline__ void stage_network(uint8_t* net, const MlpDev& m, int
         *reinterpret_cast<uint4*>(net + NET_ONES + tc::sw32_offset(t, 1)) =
             make_uint4(0u, 0u, 0u, 0u);
     }
-    // the output row (FP16 image rows 0-7: row 0 = W4, the rest zero) and 8
-    // more zero rows
-    for (int i = t; i < 16 * 8; i += n) {
-        const int r = i >> 3, c = i & 7;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (r < 8) v = *reinterpret_cast<const uint4*>(m.w16 + MLP_H_W4 + r * 64 + 8 * c);
-        *reinterpret_cast<uint4*>(net + NET_W4 + tc::sw128_offset(r, c)) = v;
-    }
     for (int i = t; i < 3 * 64; i += n) {
         const int l = i >> 6, r = i & 63;
         const float hb = m.k.hb[i];
@@ -110,17 +98,6 @@ __device__ __forceinline__ void issue_layer(int layer, uint32_t d_tmem, uint32_t
     tc::mma_commit(bar);
 }
 
-// The output layer on the tensor cores (one thread): y = h3 . W4 into tensor
-// memory column 0 at d_tmem (K = 64 in four slices of the activation tile,
-// N = 16 with 15 zero rows); b4 is added by the epilogue in FP32.
-__device__ __forceinline__ void issue_output(uint32_t d_tmem, uint32_t a_addr, uint32_t net_addr,
-                                             uint64_t* bar) {
-    for (int k = 0; k < 4; ++k)
-        tc::mma_f16(d_tmem, tc::desc_sw128(a_addr + 32u * k),
-                    tc::desc_sw128(net_addr + NET_W4 + 32u * k), IDESC_OUT, k > 0 ? 1u : 0u);
-    tc::mma_commit(bar);
-}
-
 // SiLU of 32 half-scaled accumulators (the bias is already in them) -> 16
 // FP16 pairs: with h = z/2, silu(z) = h + h * tanh(h), evaluated in FP32 and
 // rounded once.
@@ -139,10 +116,9 @@ __device__ __forceinline__ void silu32(const uint32_t (&acc)[32], uint32_t (&out
 // One layer's epilogue for tile row `row` (this thread's tensor-memory lane,
 // dw = the lane's address of the layer's 64 accumulator columns): SiLU, 32
 // columns at a time, written as the next layer's FP16 activations (layers 0,
-// 1; layer 2 too when the output layer runs on the tensor cores) or folded
-// into the FP32 64 -> 1 output (layer 2, returned with b4).
+// 1) or folded into the FP32 64 -> 1 output (layer 2, returned with b4).
 __device__ __forceinline__ float layer_epilogue(int layer, uint32_t dw, uint8_t* act, int row,
-                                                const MlpDev& m, bool fold_output = true) {
+                                                const MlpDev& m) {
     float yy = m.k.b4;
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
@@ -150,7 +126,7 @@ __device__ __forceinline__ float layer_epilogue(int layer, uint32_t dw, uint8_t*
         tc::tmem_ld32(dw + 32u * half, acc);
         uint32_t h[16];
         silu32(acc, h);
-        if (layer < 2 || !fold_output) {
+        if (layer < 2) {
 #pragma unroll
             for (int q = 0; q < 4; ++q)
                 *reinterpret_cast<uint4*>(act + tc::sw128_offset(row, 4 * half + q)) =

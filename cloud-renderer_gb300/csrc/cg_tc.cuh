@@ -141,18 +141,6 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
         : "memory");
 }
 
-// 32 lanes x 1 column of 32-bit words, waited for in the same statement.
-__device__ __forceinline__ uint32_t tmem_ld1(uint32_t taddr) {
-    uint32_t r;
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];\n"
-        "tcgen05.wait::ld.sync.aligned;"
-        : "=r"(r)
-        : "r"(taddr)
-        : "memory");
-    return r;
-}
-
 // 32 lanes x 64 columns of 32-bit words, waited for in the same statement
 // (so no use of the registers can be scheduled before the wait): thread i of
 // the warp receives lane (taddr.lane + i), columns taddr.col .. +63.

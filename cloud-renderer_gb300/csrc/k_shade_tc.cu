@@ -129,9 +129,6 @@ __device__ __forceinline__ void report_failure(uint64_t* bar, unsigned phase, bo
 // stream, sharing one copy of the network tiles (so that more groups fit an
 // SM's shared memory than CTAs of one group would).
 constexpr int SHADE_GROUPS = 1;
-// the 64 -> 1 output layer as a fourth tcgen05 MMA (true) or as FP32 FMAs in
-// the third layer's epilogue (false)
-constexpr bool SHADE_OUTPUT_MMA = false;
 constexpr int SHADE_CTAS_PER_SM = CTAS_PER_SM;
 constexpr uint32_t SHADE_TMEM_COLS = SHADE_GROUPS == 1 ? 64u : (SHADE_GROUPS == 2 ? 128u : 256u);
 constexpr int SH_OFF_NET = SHADE_GROUPS * mlptc::ACT_BYTES;
@@ -229,16 +226,13 @@ __global__ void __launch_bounds__(128 * SHADE_GROUPS, SHADE_CTAS_PER_SM)
         float nf[MLP_IN];
         float y = 0.f;
 #pragma unroll
-        for (int layer = 0; layer < (SHADE_OUTPUT_MMA ? 4 : 3); ++layer) {
+        for (int layer = 0; layer < 3; ++layer) {
             if (group_sync_for_mma(g, bad)) {  // a commit of parity `phase` is still pending
                 failed = true;
                 break;
             }
             if (r == 0) {
-                if (layer < 3)
-                    mlptc::issue_layer(layer, tmem, a_addr, net_addr, bar);
-                else
-                    mlptc::issue_output(tmem, a_addr, net_addr, bar);
+                mlptc::issue_layer(layer, tmem, a_addr, net_addr, bar);
                 // claim the tile after next (read by the group after the next sync)
                 if (layer == 0) *s_claim = 2u * streams + (unsigned)atomicAdd(status + 3, 1ull);
             }
@@ -257,12 +251,8 @@ __global__ void __launch_bounds__(128 * SHADE_GROUPS, SHADE_CTAS_PER_SM)
             // ---- epilogue: TMEM -> bias + SiLU, 32 columns at a time; the
             // last layer folds the 64 -> 1 output in FP32
             if (!bad) {
-                if (layer == 3) {
-                    y = __uint_as_float(tc::tmem_ld1(dw)) + m.k.b4;
-                } else {
-                    const float yy = mlptc::layer_epilogue(layer, dw, act, r, m, !SHADE_OUTPUT_MMA);
-                    if (layer == 2) y = yy;
-                }
+                const float yy = mlptc::layer_epilogue(layer, dw, act, r, m);
+                if (layer == 2) y = yy;
             }
             tc::fence_before_sync();
         }
