@@ -2,10 +2,12 @@
 
 Tolerances: the network runs with FP16 weights/activations on the tensor
 cores (FP32 accumulation), so forward and gradient are compared with the FP64
-oracle evaluated on the same FP16-rounded weights, within 2 % (forward,
-relative to the output scale) and 5 % relative L2 / cosine >= 0.998
-(gradient).  Renders with the surrogate must stay within RMSE 1e-2 of the FP64
-oracle's exact image.
+oracle evaluated on the same FP16-rounded weights.  Measured on a GB300: forward
+max-abs 4.6e-4 of the output scale, gradient relative L2 1.8e-4 (worst parameter
+block 5.7e-4), loss 2.2e-5 relative; the bars sit about four times above those:
+2e-3 (forward), 1e-3 relative L2 and cosine >= 0.99999 (gradient), 3e-3 per
+parameter block, 2e-4 (loss).  Renders with the surrogate must stay within RMSE
+1e-2 of the FP64 oracle's exact image.
 """
 import ctypes
 import time
@@ -59,8 +61,8 @@ def test_forward_matches_oracle(ctx, n):
     om = oracle_of(m, mu, sd)
     y = om.forward(f.astype(np.float64))
     ref = om.tau_scale * np.logaddexp(0.0, y)
-    assert np.abs(got - ref).max() <= 0.02 * om.tau_scale * max(1.0, np.abs(y).max())
-    assert np.corrcoef(got, ref)[0, 1] > 0.999
+    assert np.abs(got - ref).max() <= 2e-3 * om.tau_scale * max(1.0, np.abs(y).max())
+    assert np.corrcoef(got, ref)[0, 1] > 0.99999
 
 
 def test_gradient_matches_oracle(ctx):
@@ -72,14 +74,14 @@ def test_gradient_matches_oracle(ctx):
     g, loss = m.gradient(f, tau, sigma)
     om = oracle_of(m, mu, sd)
     oloss, og = om.loss_grad(f.astype(np.float64), tau.astype(np.float64), sigma)
-    assert loss == pytest.approx(oloss, rel=2e-2)
+    assert loss == pytest.approx(oloss, rel=2e-4)
     rel = np.linalg.norm(g - og) / np.linalg.norm(og)
     cos = float(g @ og / (np.linalg.norm(g) * np.linalg.norm(og)))
-    assert rel < 0.05 and cos > 0.998, (rel, cos)
+    assert rel < 1e-3 and cos > 0.99999, (rel, cos)
     for a, b in [(0, 1024), (1024, 1088), (1088, 5184), (5184, 5248), (5248, 9344),
                  (9344, 9408), (9408, 9472), (9472, 9473)]:
         seg_rel = np.linalg.norm(g[a:b] - og[a:b]) / max(np.linalg.norm(og[a:b]), 1e-12)
-        assert seg_rel < 0.08, (a, b, seg_rel)
+        assert seg_rel < 3e-3, (a, b, seg_rel)
 
 
 def test_adam_step_matches_torch(ctx):
