@@ -81,7 +81,8 @@ class cg_mlp_config(ctypes.Structure):
 class cg_train_params(ctypes.Structure):
     _fields_ = [("steps", ctypes.c_int), ("batch", ctypes.c_int), ("lr", ctypes.c_float),
                 ("beta1", ctypes.c_float), ("beta2", ctypes.c_float), ("eps", ctypes.c_float),
-                ("sigma", ctypes.c_float), ("seed", ctypes.c_uint64)]
+                ("sigma", ctypes.c_float), ("seed", ctypes.c_uint64),
+                ("separate_adam", ctypes.c_int)]
 
 
 class cg_trace_config(ctypes.Structure):

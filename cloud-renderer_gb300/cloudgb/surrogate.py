@@ -133,8 +133,10 @@ class SunMLP:
         return g, float(loss.value)
 
     def train(self, features, tau, steps, batch=16384, lr=1e-3, sigma=2.0, seed=1,
-              beta1=0.9, beta2=0.999, eps=1e-8):
-        """Train on host arrays (uploaded once) and return the per-step loss."""
+              beta1=0.9, beta2=0.999, eps=1e-8, separate_adam=False):
+        """Train on host arrays (uploaded once) and return the per-step loss.
+        separate_adam: run Adam as its own launch even where it fits in the
+        training launch (identical results)."""
         from . import DeviceBuffer
         f = np.ascontiguousarray(features, np.float32).reshape(-1, N_FEATURES)
         t = np.ascontiguousarray(tau, np.float32).reshape(-1)
@@ -146,6 +148,7 @@ class SunMLP:
         self._lib.cg_train_params_default(ctypes.byref(tp))
         tp.steps, tp.batch, tp.lr, tp.sigma, tp.seed = int(steps), int(batch), lr, sigma, seed
         tp.beta1, tp.beta2, tp.eps = beta1, beta2, eps
+        tp.separate_adam = 1 if separate_adam else 0
         losses = np.empty(max(1, int(steps)), np.float32)
         check(self._lib.cg_mlp_train(self.handle, df.ptr, dt.ptr, f.shape[0], ctypes.byref(tp),
                                      _fp(losses)), "cg_mlp_train")

@@ -239,29 +239,6 @@ inline FeatGeom feat_geom(const VolDesc& vd, const MlpDev& m) {
     return g;
 }
 
-struct TrainArgs {
-    const float* feat;  // [N][16] raw features
-    const float* tau;   // [N] exact optical depth
-    long long N;
-    unsigned long long perm_mul;  // multiplier coprime with N
-    float mu[16], inv_sd[16];
-    float tau_scale, sigma;
-    const float* params;
-    const __half* w16;
-    float* partial;   // [ctas][MLP_NPARAM + 1]
-    const int* step;  // device step counter (NULL: 0)
-    int batch;
-    int sequential;   // 1: rows offset + r (gradient evaluation), padding past N
-    long long offset;
-    // tensor-core status word (zeroed by the host before the steps): bit 0 =
-    // a bounded wait ran out, bit 1 = the drain after it ran out as well
-    unsigned long long* status;
-    unsigned long long wait_ns;  // limit of every mbarrier wait
-    // failure-detection check only: thread 0 issues no MMA and no commit, so
-    // the layer barrier is never completed and the first wait must run out
-    int stall;
-};
-
 struct AdamArgs {
     const float* partial;
     int nparts;
@@ -281,6 +258,37 @@ struct AdamArgs {
     // partials may be stale or half-written, so no update is made and the
     // step counter does not advance
     const unsigned long long* status;
+};
+
+struct TrainArgs {
+    const float* feat;  // [N][16] raw features
+    const float* tau;   // [N] exact optical depth
+    long long N;
+    unsigned long long perm_mul;  // multiplier coprime with N
+    float mu[16], inv_sd[16];
+    float tau_scale, sigma;
+    const float* params;
+    const __half* w16;
+    float* partial;   // [ctas][MLP_NPARAM + 1]
+    const int* step;  // device step counter (NULL: 0)
+    int batch;
+    int sequential;   // 1: rows offset + r (gradient evaluation), padding past N
+    long long offset;
+    // tensor-core status word (zeroed by the host before the steps): bit 0 =
+    // a bounded wait ran out, bit 1 = the drain after it ran out as well,
+    // bit 2 = the fused optimiser's grid barrier ran out
+    unsigned long long* status;
+    unsigned long long wait_ns;  // limit of every mbarrier wait
+    // failure-detection check only: thread 0 issues no MMA and no commit, so
+    // the layer barrier is never completed and the first wait must run out
+    int stall;
+    // optimiser in the same launch (cooperative: every CTA resident).  After
+    // its partials each CTA meets the others at a bounded grid barrier on
+    // grid_bar (an arrival counter the host zeroes before the launches), then
+    // reduces and updates its slice of the parameters with `adam`; CTA 0
+    // advances adam.step.  NULL: partials only, k_mlp_adam follows.
+    unsigned* grid_bar;
+    AdamArgs adam;
 };
 
 cudaError_t launch_march(VolDesc vd, CamDesc cam, TraceParams tp, SampleBuf sb, float4* out,
@@ -321,7 +329,11 @@ cudaError_t launch_mlp_infer(const MlpDev& m, const float* feat, int n, float* o
 // one training step on the tensor cores (k_train_tc.cu); a tensor-core wait
 // that ran out of its time limit sets ta.status and leaves a NaN in the CTA's
 // loss slot
+// One training step: partials only (ta.grid_bar NULL), or with the optimiser
+// fused (cooperative launch; cudaErrorCooperativeLaunchTooLarge when ctas
+// exceeds mlp_train_resident_ctas()).
 cudaError_t launch_mlp_train(const TrainArgs& ta, int ctas, cudaStream_t st);
+int mlp_train_resident_ctas();
 cudaError_t launch_mlp_adam(const AdamArgs& aa, cudaStream_t st);
 
 // Message returned by cg_last_error() on this thread (cg_host.cpp).

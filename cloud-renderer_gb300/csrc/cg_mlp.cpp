@@ -437,6 +437,10 @@ static cg_status train_status(cg_mlp* m, const char* who) {
     unsigned long long st = 0;
     CG_CUDA(cudaMemcpy(&st, m->status.p, 8, cudaMemcpyDeviceToHost));
     if (st == 0) return CG_OK;
+    if (st & 4ull)
+        return fail(CG_ERR_DEVICE_FAULT,
+                    "%s: the fused optimiser's grid barrier ran out of its time limit; the "
+                    "update of that step may be partial", who);
     if (st & 2ull)
         return fail(CG_ERR_DEVICE_FAULT,
                     "%s: a tensor-core wait ran out of its time limit and the drain after it "
@@ -595,35 +599,57 @@ static cg_status train_impl(cg_mlp* m, const float* d_features, const float* d_t
     aa.loss_slot_by_step = 1;
     aa.loss_base = m->host_step;
     aa.status = m->status.as<const unsigned long long>();
+    // the optimiser fused into the training launch when every CTA of the
+    // batch can be resident at once (its grid barrier: status word 1)
+    const int resident = mlp_train_resident_ctas();
+    CG_CHECK(resident > 0, CG_ERR_CUDA, "cg_mlp_train: cannot size the training kernel");
+    const bool fused = !tp->separate_adam && ctas <= resident;
+    if (fused) {
+        ta.grid_bar = reinterpret_cast<unsigned*>(m->status.as<unsigned long long>() + 1);
+        ta.adam = aa;
+    }
+    const int per_step = fused ? 1 : 2;
+    auto one_step = [&]() -> cudaError_t {
+        cudaError_t e = launch_mlp_train(ta, ctas, s);
+        if (e == cudaSuccess && !fused) e = launch_mlp_adam(aa, s);
+        return e;
+    };
     // one eager step sets the kernels' shared-memory attributes before capture
-    CG_LAUNCH(ctx, launch_mlp_train(ta, ctas, s));
-    CG_LAUNCH(ctx, launch_mlp_adam(aa, s));
+    cudaError_t e = one_step();
+    if (e != cudaSuccess) return fail(CG_ERR_CUDA, "cg_mlp_train: %s", cudaGetErrorString(e));
+    ctx->launches += per_step;
     int done = 1;
     const int G = 50;
     if (tp->steps - done >= G) {
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
         CG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        cudaError_t e = cudaSuccess;
-        for (int i = 0; i < G && e == cudaSuccess; ++i) {
-            e = launch_mlp_train(ta, ctas, s);
-            if (e == cudaSuccess) e = launch_mlp_adam(aa, s);
-        }
+        for (int i = 0; i < G && e == cudaSuccess; ++i) e = one_step();
         cudaError_t e2 = cudaStreamEndCapture(s, &graph);
         if (e == cudaSuccess) e = e2;
         if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
-        while (e == cudaSuccess && tp->steps - done >= G) {
+        if (e != cudaSuccess) {
+            // not capturable here: the steps run as direct launches
+            if (exec) cudaGraphExecDestroy(exec);
+            if (graph) cudaGraphDestroy(graph);
+            exec = nullptr;
+            graph = nullptr;
+            (void)cudaGetLastError();
+            e = cudaSuccess;
+        }
+        while (exec && e == cudaSuccess && tp->steps - done >= G) {
             e = cudaGraphLaunch(exec, s);
             done += G;
-            ctx->launches += 2 * G;
+            ctx->launches += (uint64_t)per_step * G;
         }
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
         if (e != cudaSuccess) return fail(CG_ERR_CUDA, "cg_mlp_train: %s", cudaGetErrorString(e));
     }
     for (; done < tp->steps; ++done) {
-        CG_LAUNCH(ctx, launch_mlp_train(ta, ctas, s));
-        CG_LAUNCH(ctx, launch_mlp_adam(aa, s));
+        e = one_step();
+        if (e != cudaSuccess) return fail(CG_ERR_CUDA, "cg_mlp_train: %s", cudaGetErrorString(e));
+        ctx->launches += per_step;
     }
     if (loss_per_step)
         CG_CUDA(cudaMemcpyAsync(loss_per_step, m->loss.p, (size_t)tp->steps * 4,

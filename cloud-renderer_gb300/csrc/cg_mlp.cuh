@@ -56,4 +56,55 @@ __device__ __forceinline__ bool in_range(const MlpDev& m, const float f[MLP_IN])
     return ok;
 }
 
+// Index of parameter p in the FP16 weight image (-1 for biases).
+__device__ __forceinline__ int half_index(int p) {
+    if (p < MLP_B1) return MLP_H_W1 + p;
+    if (p >= MLP_W2 && p < MLP_B2) return MLP_H_W2 + (p - MLP_W2);
+    if (p >= MLP_W3 && p < MLP_B3) return MLP_H_W3 + (p - MLP_W3);
+    if (p >= MLP_W4 && p < MLP_B4) return MLP_H_W4 + (p - MLP_W4);
+    return -1;
+}
+
+// Parameter p (p == MLP_NPARAM: the loss) of one optimiser step: the CTA
+// partials summed in CTA order and scaled by 1/batch, then the loss slot, the
+// returned gradient, or the Adam update of the FP32 master, its moments and
+// its FP16 copy.  The separate optimiser kernel and the training kernel's
+// fused tail both call it, so the two give bit-identical steps.  stopped: a
+// training kernel stopped on a bounded wait (non-zero status) and left stale
+// or half-written partials -- the loss slot is NaN and nothing is updated.
+// The partials are read past L1 (other SMs wrote them in the same launch when
+// the optimiser is fused).
+__device__ __forceinline__ void adam_param(const AdamArgs& aa, int p, int step, bool stopped) {
+    if (stopped) {
+        if (p == MLP_NPARAM && aa.loss_out)
+            aa.loss_out[aa.loss_slot_by_step ? step - aa.loss_base : 0] = __int_as_float(0x7fc00000);
+        return;
+    }
+    // explicit roundings (no FMA contraction left to the compiler): the two
+    // kernels that inline this must issue the same operations
+    float g = 0.f;
+    for (int c = 0; c < aa.nparts; ++c)
+        g = __fadd_rn(g, __ldcg(aa.partial + (size_t)c * (MLP_NPARAM + 1) + p));
+    g = __fmul_rn(g, aa.inv_batch);
+    if (p == MLP_NPARAM) {
+        if (aa.loss_out) aa.loss_out[aa.loss_slot_by_step ? step - aa.loss_base : 0] = g;
+    } else if (aa.grad_out) {
+        aa.grad_out[p] = g;
+    } else {
+        const float t1 = (float)(step + 1);
+        const float m = __fmaf_rn(aa.beta1, aa.m[p], __fmul_rn(__fsub_rn(1.f, aa.beta1), g));
+        const float v = __fmaf_rn(aa.beta2, aa.v[p],
+                                  __fmul_rn(__fmul_rn(__fsub_rn(1.f, aa.beta2), g), g));
+        aa.m[p] = m;
+        aa.v[p] = v;
+        const float mh = __fdiv_rn(m, __fsub_rn(1.f, powf(aa.beta1, t1)));
+        const float vh = __fdiv_rn(v, __fsub_rn(1.f, powf(aa.beta2, t1)));
+        const float w = __fsub_rn(aa.params[p], __fdiv_rn(__fmul_rn(aa.lr, mh),
+                                                          __fadd_rn(__fsqrt_rn(vh), aa.eps)));
+        aa.params[p] = w;
+        const int hi = half_index(p);
+        if (hi >= 0) aa.w16[hi] = __float2half_rn(w);
+    }
+}
+
 }  // namespace mlp

@@ -18,6 +18,11 @@
 // of the global timer, 1 s in training); a timeout sets the status word (and
 // partial[NPARAM] to NaN), drains, frees tensor memory and returns: k_mlp_adam
 // then makes no update and the host reports CG_ERR_DEVICE_FAULT.
+//
+// Fused optimiser (ta.grid_bar set, cooperative launch): the step is one
+// launch.  After its partials every CTA arrives at a grid barrier and each
+// then reduces and updates a slice of the parameters with the same function,
+// in the same CTA order, as k_mlp_adam -- the two paths give identical bits.
 #include <cuda_fp16.h>
 
 #include <atomic>
@@ -91,6 +96,46 @@ __device__ __forceinline__ bool tt_sync(bool bad) {
     const bool any_bad = __syncthreads_or(bad) != 0;
     tc::fence_after_sync();
     return any_bad;
+}
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// The optimiser tail of a fused step.  Each CTA's partials, its reads of the
+// step counter and of the weights all come before its arrival at the grid
+// barrier, every update after the last arrival.  The barrier is a monotonic
+// arrival counter: a completed step leaves it at a multiple of gridDim.x, so
+// the generation of an arrival is its ticket / gridDim.x.  Its wait is bounded
+// by four mbarrier limits -- longer than the slowest CTA that still arrives
+// (a wait that ran out plus its drain) -- and sets status bit 2 when it runs
+// out; a CTA that failed a wait set its bit before arriving, so after the
+// barrier every CTA sees it and no slice is updated.
+__device__ void fused_adam(const TrainArgs& ta, int step, int* flag) {
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned ticket = atomicAdd(ta.grid_bar, 1u);
+        const unsigned target = (ticket / gridDim.x + 1u) * gridDim.x;
+        const uint64_t limit = 4ull * ta.wait_ns, t0 = tc::global_ns();
+        bool met = true;
+        while (ld_acquire(ta.grid_bar) < target) {
+            if (tc::global_ns() - t0 > limit) {
+                met = false;
+                break;
+            }
+            __nanosleep(32);
+        }
+        if (!met) atomicOr(ta.status, 4ull);
+        __threadfence();
+        *flag = *reinterpret_cast<volatile unsigned long long*>(ta.status) != 0ull ? 1 : 0;
+    }
+    __syncthreads();
+    const bool stopped = *flag != 0;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p <= MLP_NPARAM; p += gridDim.x * blockDim.x)
+        mlp::adam_param(ta.adam, p, step, stopped);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && !stopped) *ta.adam.step = step + 1;
 }
 
 // 64 FP32 columns of this thread's tensor-memory lane
@@ -178,6 +223,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
     }
 
     // ---- this thread's row: features (normalised, FP16) into x and x^T
+    const int step0 = ta.step ? *ta.step : 0;
     const long long r = (long long)blockIdx.x * 128 + tid;
     bool valid;
     long long idx;
@@ -188,9 +234,8 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
         // lin * perm_mul mod N with both factors reduced mod N first (perm_mul
         // < N from the host, N <= 2^31): the product stays below 2^62 for any
         // step count, so the walk remains a permutation of the rows
-        const long long step = ta.step ? *ta.step : 0;
         const unsigned long long N = (unsigned long long)ta.N;
-        const unsigned long long lin = ((unsigned long long)step * (unsigned long long)ta.batch +
+        const unsigned long long lin = ((unsigned long long)step0 * (unsigned long long)ta.batch +
                                         (unsigned long long)r) % N;
         idx = (long long)((lin * ta.perm_mul) % N);
         valid = true;
@@ -416,25 +461,53 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tmem, TT_COLS);
+    if (ta.grid_bar) fused_adam(ta, step0, reinterpret_cast<int*>(fmisc + 8));
 }
 
 }  // namespace
 
-cudaError_t launch_mlp_train(const TrainArgs& ta, int ctas, cudaStream_t st) {
-    // the attribute is set once per device, outside any stream capture
-    static std::atomic<bool> configured[64];
+// CTAs of the training kernel resident at once on the current device (set
+// up once per device, outside any stream capture; 0 on an error).
+int mlp_train_resident_ctas() {
+    static std::atomic<int> resident[64];
     int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-    if (!configured[dev].load(std::memory_order_acquire)) {
-        e = cudaFuncSetAttribute(k_mlp_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 TT_SMEM);
-        if (e != cudaSuccess) return e;
-        configured[dev].store(true, std::memory_order_release);
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+    int r = resident[dev].load(std::memory_order_acquire);
+    if (r > 0) return r;
+    if (cudaFuncSetAttribute(k_mlp_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             TT_SMEM) != cudaSuccess)
+        return 0;
+    int per_sm = 0, sms = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlp_train_tc, 128, TT_SMEM) !=
+            cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return 0;
+    r = per_sm * sms;
+    resident[dev].store(r, std::memory_order_release);
+    return r;
+}
+
+cudaError_t launch_mlp_train(const TrainArgs& ta, int ctas, cudaStream_t st) {
+    const int resident = mlp_train_resident_ctas();
+    if (resident <= 0) return cudaErrorInvalidConfiguration;
+    if (!ta.grid_bar) {
+        k_mlp_train_tc<<<ctas, 128, TT_SMEM, st>>>(ta);
+        return cudaGetLastError();
     }
-    k_mlp_train_tc<<<ctas, 128, TT_SMEM, st>>>(ta);
-    return cudaGetLastError();
+    // the fused optimiser's grid barrier needs every CTA resident: a
+    // cooperative launch, refused when the grid does not fit
+    if (ctas > resident) return cudaErrorCooperativeLaunchTooLarge;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)ctas);
+    cfg.blockDim = dim3(128);
+    cfg.dynamicSmemBytes = TT_SMEM;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_mlp_train_tc, ta);
 }
 
 CG_OOB_TU(k_train_tc)

@@ -306,6 +306,10 @@ typedef struct cg_train_params {
     float lr, beta1, beta2, eps; /* Adam */
     float sigma;      /* extinction of the loss (exp(-sigma tau_pred) - exp(-sigma tau))^2 */
     uint64_t seed;    /* batch permutation */
+    int separate_adam; /* 0 (default): Adam runs inside the training launch when the
+                          batch's CTAs fit on the GPU at once (batch <= 128 x the
+                          resident CTAs, 19456 rows on 152 SMs), else as a second
+                          launch; 1: always the second launch.  Same results. */
 } cg_train_params;
 
 void cg_mlp_config_default(cg_mlp_config* c);

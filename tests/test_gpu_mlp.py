@@ -149,6 +149,35 @@ def test_checkpoint_resume_is_bit_identical(ctx, tmp_path):
         surrogate.SunMLP.load(ctx, bad)
 
 
+@pytest.mark.parametrize("batch", [2048, 19584])
+def test_fused_adam_matches_separate_launch(ctx, batch):
+    """Adam inside the training launch (a grid barrier, one launch per step)
+    and Adam as its own launch give identical bits: parameters, moments, step
+    and per-step losses, over graph-replayed and direct steps.  19584 rows are
+    153 CTAs, more than a 152-SM GPU holds at once: the fused request then
+    falls back to two launches per step."""
+    torch = pytest.importorskip("torch")
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    f, tau = synthetic_set(40000, seed=4)
+    steps = 75  # one direct step, a 50-step graph replay, 24 direct steps
+    runs = []
+    for separate in (False, True):
+        m = surrogate.SunMLP(ctx, seed=21)
+        m.fit_normalization(f, tau)
+        n0 = ctx.launch_count
+        losses = m.train(f, tau, steps=steps, batch=batch, lr=1e-3, sigma=2.0,
+                         separate_adam=separate)
+        runs.append((ctx.launch_count - n0, losses, m.get_params()))
+    fused_fits = batch // 128 <= sms
+    assert runs[0][0] == (steps if fused_fits else 2 * steps)
+    assert runs[1][0] == 2 * steps
+    assert np.isfinite(runs[0][1]).all()
+    assert np.array_equal(runs[0][1], runs[1][1])
+    for x, y in zip(runs[0][2][:3], runs[1][2][:3]):
+        assert np.array_equal(x, y)
+    assert runs[0][2][3] == runs[1][2][3] == steps
+
+
 def _pair(ctx, cfg, wl, fmt):
     vol = cloudgb.CloudVolume(cfg["dim"], configs.VOLUME_BOUNDS, configs.VOLUME_POSITION,
                               cfg["mips"], fmt=fmt, ctx=ctx)
