@@ -38,7 +38,9 @@ for p in (PKG, ROOT):
 
 METRIC = "Mpix/s 1080p @256³ volume: plain FP32 vs BF16+MLP surrogate at RMSE≤1e-2"
 UNIT = "Mpix/s"
-MLP_FLOP_PER_SAMPLE = 2 * (16 * 64 + 64 * 64 + 64 * 64 + 64)
+def mlp_flop_per_sample(layers):
+    """Multiply-adds x 2 of one inference: 16 -> 64, (layers - 1) x 64 -> 64, 64 -> 1."""
+    return 2 * (16 * 64 + (layers - 1) * 64 * 64 + 64)
 
 
 def parse():
@@ -558,15 +560,29 @@ def run_ours(args):
     plain_achieved = float(sum(alg)) / (sum(trace_ms) / 1e3) / 1e9
     tr_plain = load_traffic("trace_fused_rgba32f")
 
-    # ---- BF16 volume + MLP surrogate (trained here, on the GPU)
+    # ---- BF16 volume + MLP surrogate (trained here, on the GPU): the default
+    # depth, and a three-hidden-layer model on the same data for comparison
     t0 = time.perf_counter()
-    mlp, losses = surrogate.train_surrogate(ctx, plain_shader, samples=args.mlp_samples,
-                                            steps=args.mlp_steps, batch=16384, lr=1e-3,
-                                            scenes=16, seed=1000)
+    feats, taus, mlp = surrogate.training_set(ctx, plain_shader, samples=args.mlp_samples,
+                                              scenes=16, seed=1000)
+    data_s = time.perf_counter() - t0
+    mlp.fit_normalization(feats, taus)
+    t0 = time.perf_counter()
+    losses = mlp.train(feats, taus, args.mlp_steps, batch=16384, lr=1e-3,
+                       sigma=plain_shader.densityScale, seed=1000)
     train_s = time.perf_counter() - t0
+    mlp3 = surrogate.SunMLP(ctx, hidden_layers=3)
+    mlp3.copy_config(mlp)
+    t0 = time.perf_counter()
+    losses3 = mlp3.train(feats, taus, args.mlp_steps, batch=16384, lr=1e-3,
+                         sigma=plain_shader.densityScale, seed=1000)
+    train3_s = time.perf_counter() - t0
+    feats = taus = None
     vol16 = make_volume(cloudgb.FORMAT_BF16_FP16)
     mlp_shader = cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, **kw)
     learned = run_path(vol16, mlp_shader, args.steps, args.warmup, clocks=True)
+    mlp3_shader = cloudgb.ConeTraceShader(useMlp=True, mlp=mlp3, **kw)
+    learned3 = run_path(vol16, mlp3_shader, args.steps, args.warmup)
     # the same surrogate renderer as one persistent kernel (A/B, same images)
     persistent = run_path(vol16, cloudgb.ConeTraceShader(useMlp=True, mlp=mlp,
                                                          pipeline=_lib.PIPELINE_PERSISTENT, **kw),
@@ -574,7 +590,8 @@ def run_ours(args):
     mlp_stage = "render_mlp" if "render_mlp" in learned["stages"] else "shade_mlp"
     samples = [v["samples"] for v in learned["per_view"]]
     mlp_ms = [v[mlp_stage] for v in learned["per_view"]]
-    mlp_tflops = sum(samples) * MLP_FLOP_PER_SAMPLE / (sum(mlp_ms) / 1e3) / 1e12
+    flop_per_sample = mlp_flop_per_sample(mlp.hidden_layers)
+    mlp_tflops = sum(samples) * flop_per_sample / (sum(mlp_ms) / 1e3) / 1e12
     fallbacks = ctx.mlp_fallbacks()
 
     # ---- quality (untimed): the production model's 1080p images of the 16
@@ -586,11 +603,13 @@ def run_ours(args):
     for k in range(len(cams)):
         ref = np.empty((H, W, 4), np.float32)
         got = np.empty((H, W, 4), np.float32)
+        got3 = np.empty((H, W, 4), np.float32)
         plain_shader.coneTrace(vol32, cams[k], out=ref)
         mlp_shader.coneTrace(vol16, cams[k], out=got)
+        mlp3_shader.coneTrace(vol16, cams[k], out=got3)
         e = ctx.error_stats(got, ref)  # reduced on the GPU in FP64
         full.append((e["rmse_all"], e["max_abs_all"]))
-        views[k] = {"bf16_mlp": got, "plain_fp32": ref}
+        views[k] = {"bf16_mlp": got, "plain_fp32": ref, "bf16_mlp_3_layers": got3}
     chk = oracle_check(wl, views) if (rank == 0 or world == 1) else None
     views = None
     rmse_oracle = chk["bf16_mlp"]["rmse"] if chk else float(max(r for r, _ in full))
@@ -626,13 +645,13 @@ def run_ours(args):
                     "frac": round(mlp_tflops / tensor_peak, 4),
                     "traffic": tr_mlp.get("bytes_per_launch") if tr_mlp else None,
                     "traffic_note": tr_mlp.get("source") if tr_mlp else None,
-                    "flop_per_sample": MLP_FLOP_PER_SAMPLE,
+                    "flop_per_sample": flop_per_sample, "hidden_layers": mlp.hidden_layers,
                     "samples_per_view": samples, "kernel_ms_per_view": [round(x, 4) for x in mlp_ms],
                     "limiter": tr_mlp.get("limiter") if tr_mlp else None,
                     "issue_active": tr_mlp.get("issue_active") if tr_mlp else None,
                     "tensor_pipe_active": tr_mlp.get("tensor_pipe_active") if tr_mlp else None,
                     "note": "achieved = sum over the 16 views of (view's surrogate inferences x "
-                            "18,560 FLOP) / sum of the same views' kernel CUDA-event times"}
+                            "flop_per_sample) / sum of the same views' kernel CUDA-event times"}
     dram_gbs = (tr_plain["bytes_per_launch"] / (np.mean(trace_ms) / 1e3) / 1e9) if tr_plain else None
     roofline_plain = {"bound": "hbm", "kernel": "k_trace_coop (the fused trace, cooperative cones)", "achieved": round(plain_achieved, 1),
                       "peak": hbm_peak, "peak_kind": peak_kind, "unit": "GB/s",
@@ -661,9 +680,17 @@ def run_ours(args):
             "rmse_vs_plain_fp32_full_images": float(max(r for r, _ in full)),
             "max_abs_vs_plain_fp32_full_images": float(max(m for _, m in full)),
             "samples_per_frame_mean": float(np.mean(samples)),
-            "fallbacks_last_view": fallbacks, "train_s": round(train_s, 2),
+            "fallbacks_last_view": fallbacks, "hidden_layers": mlp.hidden_layers,
+            "data_s": round(data_s, 2), "train_s": round(train_s, 2),
             "train_steps": args.mlp_steps, "train_samples": args.mlp_samples,
             "final_loss": float(np.mean(losses[-100:]))}),
+        "bf16_mlp_3_layers": path_summary(learned3, {
+            "hidden_layers": 3,
+            "rmse_vs_fp64_oracle": chk["bf16_mlp_3_layers"]["rmse"] if chk else None,
+            "max_abs_vs_fp64_oracle": chk["bf16_mlp_3_layers"]["max_abs"] if chk else None,
+            "worst_view_rmse_vs_fp64_oracle":
+                chk["bf16_mlp_3_layers"]["worst_view_rmse"] if chk else None,
+            "train_s": round(train3_s, 2), "final_loss": float(np.mean(losses3[-100:]))}),
         "speedup_render": round(plain["render_ms"] / learned["render_ms"], 3),
         "speedup_frame": round(plain["total_ms"] / learned["total_ms"], 3),
         "oracle_check": ({"sample": chk["tiles"], "pixels": chk["pixels"],

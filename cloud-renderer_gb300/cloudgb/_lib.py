@@ -66,6 +66,8 @@ PIPELINE_DEFERRED = 1
 PIPELINE_PERSISTENT = 2
 MLP_FEATURES = 16
 MLP_PARAMS = 9473
+MLP_MAX_LAYERS = 3
+MLP_DEFAULT_LAYERS = 2
 
 
 class cg_mlp_config(ctypes.Structure):
@@ -165,6 +167,8 @@ SIGNATURES = [
     ("cg_train_params_default", None, [ctypes.POINTER(cg_train_params)]),
     ("cg_mlp_param_count", I, []),
     ("cg_mlp_create", I, [P, ctypes.c_uint64, PP]),
+    ("cg_mlp_create_layers", I, [P, ctypes.c_uint64, I, PP]),
+    ("cg_mlp_hidden_layers", I, [P]),
     ("cg_mlp_destroy", None, [P]),
     ("cg_mlp_configure", I, [P, ctypes.POINTER(cg_mlp_config)]),
     ("cg_mlp_get_config", I, [P, ctypes.POINTER(cg_mlp_config)]),

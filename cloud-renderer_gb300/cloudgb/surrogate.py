@@ -27,17 +27,32 @@ def _fp(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
 
 
-class SunMLP:
-    """cg_mlp handle (16 -> 64 -> 64 -> 64 -> 1, SiLU)."""
+DEFAULT_LAYERS = _lib.MLP_DEFAULT_LAYERS
 
-    def __init__(self, ctx, seed=1, handle=None):
+
+class SunMLP:
+    """cg_mlp handle: 16 -> 64 [-> 64 [-> 64]] -> 1, SiLU, with 1, 2 (default)
+    or 3 hidden layers."""
+
+    def __init__(self, ctx, seed=1, handle=None, hidden_layers=None):
         self.ctx = ctx
         self._lib = load()
         if handle is None:
             h = ctypes.c_void_p()
-            check(self._lib.cg_mlp_create(ctx.handle, int(seed), ctypes.byref(h)), "cg_mlp_create")
+            layers = DEFAULT_LAYERS if hidden_layers is None else int(hidden_layers)
+            check(self._lib.cg_mlp_create_layers(ctx.handle, int(seed), layers, ctypes.byref(h)),
+                  "cg_mlp_create_layers")
             handle = h
         self.handle = handle
+
+    @property
+    def hidden_layers(self):
+        return int(self._lib.cg_mlp_hidden_layers(self.handle))
+
+    def copy_config(self, other):
+        """Take another model's configuration (features, normalisation, cone)."""
+        c = other.config
+        check(self._lib.cg_mlp_configure(self.handle, ctypes.byref(c)), "cg_mlp_configure")
 
     @classmethod
     def load(cls, ctx, path):
@@ -185,9 +200,11 @@ def march_samples(volume, shader, camera, capacity=4 << 20):
 
 
 def training_set(ctx, shader, samples=4_000_000, scenes=16, dim=256, mips=8, fmt=None,
-                 views_per_scene=4, view_size=(480, 270), seed=1000, mlp=None):
-    """(features, tau) drawn from the renderer's view samples over training
-    scenes (seeds seed .. seed + scenes - 1, disjoint from evaluation seeds)."""
+                 views_per_scene=4, view_size=(480, 270), seed=1000, mlp=None,
+                 hidden_layers=None):
+    """(features, tau, model) drawn from the renderer's view samples over
+    training scenes (seeds seed .. seed + scenes - 1, disjoint from evaluation
+    seeds); a new model (hidden_layers deep) is created unless one is given."""
     import cloudgb
     fmt = cloudgb.FORMAT_BF16_FP16 if fmt is None else fmt
     rng = scene.SplitMix64(seed)
@@ -212,7 +229,7 @@ def training_set(ctx, shader, samples=4_000_000, scenes=16, dim=256, mips=8, fmt
         sun = cloudgb.Sun(tuple(sd), *configs.PLAIN_1080P["sun_map"])
         cloudgb.VoxelizeShader().voxelize(vol, sun)
         if mlp is None:
-            mlp = SunMLP(ctx)
+            mlp = SunMLP(ctx, hidden_layers=hidden_layers)
             mlp.configure_for(vol, shader)
         eyes = scene.orbit_cameras(seed + 101 + k, views_per_scene)
         P, Wt = [], []
@@ -241,11 +258,11 @@ def training_set(ctx, shader, samples=4_000_000, scenes=16, dim=256, mips=8, fmt
 
 
 def train_surrogate(ctx, shader, samples=4_000_000, steps=20000, batch=16384, lr=1e-3,
-                    scenes=16, seed=1000, dim=256, mips=8):
+                    scenes=16, seed=1000, dim=256, mips=8, hidden_layers=None):
     """Generate the training set, fit the normalisation and train; returns
     (model, per-step loss)."""
     f, tau, mlp = training_set(ctx, shader, samples=samples, scenes=scenes, dim=dim, mips=mips,
-                               seed=seed)
+                               seed=seed, hidden_layers=hidden_layers)
     mlp.fit_normalization(f, tau)
     losses = mlp.train(f, tau, steps, batch=batch, lr=lr, sigma=shader.densityScale, seed=seed)
     return mlp, losses

@@ -171,6 +171,11 @@ struct SampleBuf {
 // ---- MLP surrogate ----------------------------------------------------------
 #define MLP_IN 16
 #define MLP_H 64
+// hidden layers: 1, 2 or 3 of width 64 (a model's depth is fixed when it is
+// created); the parameter vector always has room for three, and the blocks of
+// the layers a model does not use stay zero and are never updated
+#define MLP_MAX_LAYERS 3
+#define MLP_DEFAULT_LAYERS 2
 // flat FP32 parameter vector: W stored [out][in]
 #define MLP_W1 0
 #define MLP_B1 1024
@@ -212,8 +217,16 @@ struct MlpDev {
     float tau_scale;
     float h0;
     int lb;
+    int layers;           // hidden layers in use (1 .. MLP_MAX_LAYERS)
     MlpConsts k;          // copy of the current biases (for inference)
 };
+
+// Parameters [lo, hi) of the hidden layers a model of `layers` does not use
+// (W2 .. b3 for one layer, W3 .. b3 for two, none for three).
+inline void mlp_frozen_range(int layers, int& lo, int& hi) {
+    lo = layers <= 1 ? MLP_W2 : (layers == 2 ? MLP_W3 : 0);
+    hi = layers >= MLP_MAX_LAYERS ? 0 : MLP_W4;
+}
 
 // Feature-tap geometry of a (model, volume) pair, precomputed on the host:
 // tap 3i+k reads level l_i (tex[i]) at texel coordinate v * sc[i] + dsc[3i+k] * s.
@@ -258,6 +271,9 @@ struct AdamArgs {
     // partials may be stale or half-written, so no update is made and the
     // step counter does not advance
     const unsigned long long* status;
+    // parameters of unused hidden layers (mlp_frozen_range): no partials are
+    // written for them; their gradient reads 0 and they are never updated
+    int frozen_lo, frozen_hi;
 };
 
 struct TrainArgs {
@@ -271,6 +287,7 @@ struct TrainArgs {
     const __half* w16;
     float* partial;   // [ctas][MLP_NPARAM + 1]
     const int* step;  // device step counter (NULL: 0)
+    int layers;       // hidden layers (1 .. MLP_MAX_LAYERS)
     int batch;
     int sequential;   // 1: rows offset + r (gradient evaluation), padding past N
     long long offset;

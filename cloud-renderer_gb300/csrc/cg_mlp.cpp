@@ -12,6 +12,7 @@ struct cg_mlp {
     cg_context* ctx = nullptr;
     DevBuf params, w16, m, v, step, ticket, partial, loss, grad;
     DevBuf status;  // the training kernels' status word (see TrainArgs)
+    int layers = MLP_DEFAULT_LAYERS;  // hidden layers, fixed at creation
     cg_mlp_config cfg{};
     int host_step = 0;
     MlpConsts consts{};  // host copy of the biases / output row (see MlpConsts)
@@ -71,11 +72,20 @@ void set_consts(cg_mlp* m, const float* b1, const float* b2, const float* b3, co
     m->consts.b4 = b4;
 }
 
-cg_status upload_params(cg_mlp* m, const float* p) {
+// Zero the blocks of the hidden layers a model of `layers` does not use.
+void zero_frozen(int layers, float* p) {
+    int lo, hi;
+    mlp_frozen_range(layers, lo, hi);
+    for (int i = lo; i < hi; ++i) p[i] = 0.f;
+}
+
+cg_status upload_params(cg_mlp* m, const float* src) {
+    std::vector<float> p(src, src + MLP_NPARAM);
+    zero_frozen(m->layers, p.data());
     std::vector<__half> h;
-    half_image(p, h);
-    set_consts(m, p + MLP_B1, p + MLP_B2, p + MLP_B3, p + MLP_W4, p[MLP_B4]);
-    CG_CUDA(cudaMemcpy(m->params.p, p, MLP_NPARAM * 4, cudaMemcpyHostToDevice));
+    half_image(p.data(), h);
+    set_consts(m, &p[MLP_B1], &p[MLP_B2], &p[MLP_B3], &p[MLP_W4], p[MLP_B4]);
+    CG_CUDA(cudaMemcpy(m->params.p, p.data(), MLP_NPARAM * 4, cudaMemcpyHostToDevice));
     CG_CUDA(cudaMemcpy(m->w16.p, h.data(), MLP_NHALF * 2, cudaMemcpyHostToDevice));
     return CG_OK;
 }
@@ -93,6 +103,7 @@ MlpDev device_view(const cg_mlp* m) {
     d.tau_scale = m->cfg.tau_scale;
     d.h0 = m->cfg.initial_height;
     d.lb = m->cfg.base_level;
+    d.layers = m->layers;
     d.k = m->consts;
     return d;
 }
@@ -133,11 +144,21 @@ extern "C" void cg_mlp_config_default(cg_mlp_config* c) {
 extern "C" int cg_mlp_param_count(void) { return MLP_NPARAM; }
 
 extern "C" cg_status cg_mlp_create(cg_context* ctx, uint64_t seed, cg_mlp** out) {
+    return cg_mlp_create_layers(ctx, seed, MLP_DEFAULT_LAYERS, out);
+}
+
+extern "C" int cg_mlp_hidden_layers(const cg_mlp* m) { return m ? m->layers : 0; }
+
+extern "C" cg_status cg_mlp_create_layers(cg_context* ctx, uint64_t seed, int hidden_layers,
+                                          cg_mlp** out) {
     CG_CHECK(ctx && out, CG_ERR_INVALID_ARGUMENT, "cg_mlp_create: null pointer");
     *out = nullptr;
+    CG_CHECK(hidden_layers >= 1 && hidden_layers <= MLP_MAX_LAYERS, CG_ERR_OUT_OF_RANGE,
+             "cg_mlp_create: hidden_layers %d not in [1, %d]", hidden_layers, MLP_MAX_LAYERS);
     CG_CUDA(cudaSetDevice(ctx->device));
     cg_mlp* m = new cg_mlp();
     m->ctx = ctx;
+    m->layers = hidden_layers;
     context_retain(ctx);
     cg_mlp_config_default(&m->cfg);
     cudaError_t e = cudaSuccess;
@@ -166,6 +187,8 @@ extern "C" cg_status cg_mlp_create(cg_context* ctx, uint64_t seed, cg_mlp** out)
         const double b = std::sqrt(gain / fan_in);
         for (int i = 0; i < n; ++i) p[off + i] = (float)((2.0 * r.uniform() - 1.0) * b);
     };
+    // (the stream draws all three hidden layers, so a layer's initial weights
+    // do not depend on the depth; the unused ones are zeroed on upload)
     fill(MLP_W1, 1024, 16, 6.0);
     fill(MLP_W2, 4096, 64, 6.0);
     fill(MLP_W3, 4096, 64, 6.0);
@@ -427,6 +450,7 @@ static TrainArgs train_args(const cg_mlp* m, const float* feat, const float* tau
     ta.status = m->status.as<unsigned long long>();
     ta.wait_ns = kTrainWaitNs;
     ta.stall = 0;
+    ta.layers = m->layers;
     return ta;
 }
 
@@ -483,6 +507,7 @@ extern "C" cg_status cg_mlp_gradient(cg_mlp* m, const float* features, const flo
     aa.grad_out = m->grad.as<float>();
     aa.loss_out = m->grad.as<float>() + MLP_NPARAM;
     aa.status = m->status.as<const unsigned long long>();
+    mlp_frozen_range(m->layers, aa.frozen_lo, aa.frozen_hi);
     CG_LAUNCH(ctx, launch_mlp_adam(aa, s));
     std::vector<float> h(MLP_NPARAM + 1);
     CG_CUDA(cudaMemcpyAsync(h.data(), m->grad.p, (MLP_NPARAM + 1) * 4, cudaMemcpyDeviceToHost, s));
@@ -599,6 +624,7 @@ static cg_status train_impl(cg_mlp* m, const float* d_features, const float* d_t
     aa.loss_slot_by_step = 1;
     aa.loss_base = m->host_step;
     aa.status = m->status.as<const unsigned long long>();
+    mlp_frozen_range(m->layers, aa.frozen_lo, aa.frozen_hi);
     // the optimiser fused into the training launch when every CTA of the
     // batch can be resident at once (its grid barrier: status word 1)
     const int resident = mlp_train_resident_ctas();
@@ -696,19 +722,26 @@ extern "C" cg_status cg_mlp_set_params(cg_mlp* m, const float* params, const flo
     CG_CUDA(cudaStreamSynchronize(m->ctx->stream));
     cg_status st = upload_params(m, params);
     if (st != CG_OK) return st;
-    if (adam_m) CG_CUDA(cudaMemcpy(m->m.p, adam_m, MLP_NPARAM * 4, cudaMemcpyHostToDevice));
-    else CG_CUDA(cudaMemset(m->m.p, 0, MLP_NPARAM * 4));
-    if (adam_v) CG_CUDA(cudaMemcpy(m->v.p, adam_v, MLP_NPARAM * 4, cudaMemcpyHostToDevice));
-    else CG_CUDA(cudaMemset(m->v.p, 0, MLP_NPARAM * 4));
+    // moments (zero when not given; zero for the unused layers either way)
+    for (int k = 0; k < 2; ++k) {
+        const float* src = k == 0 ? adam_m : adam_v;
+        std::vector<float> h(MLP_NPARAM, 0.f);
+        if (src) h.assign(src, src + MLP_NPARAM);
+        zero_frozen(m->layers, h.data());
+        CG_CUDA(cudaMemcpy((k == 0 ? m->m : m->v).p, h.data(), MLP_NPARAM * 4,
+                           cudaMemcpyHostToDevice));
+    }
     CG_CUDA(cudaMemcpy(m->step.p, &step, 4, cudaMemcpyHostToDevice));
     m->host_step = step;
     return CG_OK;
 }
 
 // ---- checkpoint: "CGMLPCK1", u32 version, u32 nparam, u32 nin, u32 nhidden,
-// i32 step, cg_mlp_config, f32 params/m/v [nparam], u32 CRC32 of all before.
+// [version 2: u32 hidden layers], i32 step, cg_mlp_config, f32 params/m/v
+// [nparam], u32 CRC32 of all before.  Version 1 files (three hidden layers,
+// no layer count) still load.
 static const char kMagic[8] = {'C', 'G', 'M', 'L', 'P', 'C', 'K', '1'};
-static const uint32_t kVersion = 1;
+static const uint32_t kVersion = 2;
 
 extern "C" cg_status cg_mlp_save(const cg_mlp* m, const char* path) {
     CG_CHECK(m && path, CG_ERR_INVALID_ARGUMENT, "cg_mlp_save: null pointer");
@@ -721,7 +754,7 @@ extern "C" cg_status cg_mlp_save(const cg_mlp* m, const char* path) {
         const uint8_t* b = reinterpret_cast<const uint8_t*>(d);
         buf.insert(buf.end(), b, b + n);
     };
-    uint32_t hdr[4] = {kVersion, MLP_NPARAM, MLP_IN, MLP_H};
+    uint32_t hdr[5] = {kVersion, MLP_NPARAM, MLP_IN, MLP_H, (uint32_t)m->layers};
     put(kMagic, 8);
     put(hdr, sizeof(hdr));
     put(&step, 4);
@@ -749,19 +782,27 @@ extern "C" cg_status cg_mlp_load(cg_context* ctx, const char* path, cg_mlp** out
     size_t r;
     while ((r = fread(tmp, 1, sizeof(tmp), f)) > 0) buf.insert(buf.end(), tmp, tmp + r);
     fclose(f);
-    const size_t expect = 8 + 16 + 4 + sizeof(cg_mlp_config) + 3 * MLP_NPARAM * 4 + 4;
+    CG_CHECK(buf.size() >= 12 && memcmp(buf.data(), kMagic, 8) == 0, CG_ERR_BAD_CHECKPOINT,
+             "cg_mlp_load: bad magic");
+    uint32_t version;
+    memcpy(&version, buf.data() + 8, 4);
+    CG_CHECK(version == 1 || version == 2, CG_ERR_BAD_CHECKPOINT,
+             "cg_mlp_load: unknown version %u", version);
+    const size_t hdr_words = version == 1 ? 4 : 5;
+    const size_t expect =
+        8 + 4 * hdr_words + 4 + sizeof(cg_mlp_config) + 3 * MLP_NPARAM * 4 + 4;
     CG_CHECK(buf.size() == expect, CG_ERR_BAD_CHECKPOINT,
              "cg_mlp_load: %s has %zu bytes, expected %zu", path, buf.size(), expect);
-    CG_CHECK(memcmp(buf.data(), kMagic, 8) == 0, CG_ERR_BAD_CHECKPOINT, "cg_mlp_load: bad magic");
-    uint32_t hdr[4];
-    memcpy(hdr, buf.data() + 8, 16);
-    CG_CHECK(hdr[0] == kVersion && hdr[1] == MLP_NPARAM && hdr[2] == MLP_IN && hdr[3] == MLP_H,
-             CG_ERR_BAD_CHECKPOINT, "cg_mlp_load: version/shape mismatch");
+    uint32_t hdr[5] = {0, 0, 0, 0, 3};  // version 1: three hidden layers
+    memcpy(hdr, buf.data() + 8, 4 * hdr_words);
+    CG_CHECK(hdr[1] == MLP_NPARAM && hdr[2] == MLP_IN && hdr[3] == MLP_H && hdr[4] >= 1 &&
+                 hdr[4] <= MLP_MAX_LAYERS,
+             CG_ERR_BAD_CHECKPOINT, "cg_mlp_load: shape mismatch");
     uint32_t crc;
     memcpy(&crc, buf.data() + buf.size() - 4, 4);
     CG_CHECK(crc32_update(0, buf.data(), buf.size() - 4) == crc, CG_ERR_BAD_CHECKPOINT,
              "cg_mlp_load: CRC mismatch");
-    size_t off = 24;
+    size_t off = 8 + 4 * hdr_words;
     int step;
     memcpy(&step, buf.data() + off, 4);
     off += 4;
@@ -775,7 +816,7 @@ extern "C" cg_status cg_mlp_load(cg_context* ctx, const char* path, cg_mlp** out
     off += MLP_NPARAM * 4;
     memcpy(vv.data(), buf.data() + off, MLP_NPARAM * 4);
     cg_mlp* m = nullptr;
-    cg_status st = cg_mlp_create(ctx, 0, &m);
+    cg_status st = cg_mlp_create_layers(ctx, 0, (int)hdr[4], &m);
     if (st != CG_OK) return st;
     st = cg_mlp_configure(m, &cfg);
     if (st == CG_OK) st = cg_mlp_set_params(m, p.data(), mm.data(), vv.data(), step);

@@ -1,8 +1,9 @@
 // cg_mlp.cuh -- the sun-transmittance surrogate's shared device helpers: the
-// 16 input features of a sample, their trained range, FP16 packing and the
-// output link.  The network itself (16 -> 3 x 64 SiLU -> 1, FP16 operands,
-// FP32 accumulation) runs on the tensor cores in k_shade_tc.cu (inference)
-// and k_train_tc.cu (training); FP32 master weights live with Adam.
+// 16 input features of a sample, their trained range, FP16 packing, the
+// output link and the per-parameter optimiser step.  The network itself
+// (16 -> 1..3 x 64 SiLU -> 1, FP16 operands, FP32 accumulation) runs on the
+// tensor cores in k_shade_tc.cu / k_render_tc.cu (inference) and
+// k_train_tc.cu (training); FP32 master weights live with Adam.
 #pragma once
 
 #include <cuda_fp16.h>
@@ -78,6 +79,10 @@ __device__ __forceinline__ void adam_param(const AdamArgs& aa, int p, int step, 
     if (stopped) {
         if (p == MLP_NPARAM && aa.loss_out)
             aa.loss_out[aa.loss_slot_by_step ? step - aa.loss_base : 0] = __int_as_float(0x7fc00000);
+        return;
+    }
+    if (p >= aa.frozen_lo && p < aa.frozen_hi) {  // a hidden layer the model does not use
+        if (aa.grad_out) aa.grad_out[p] = 0.f;
         return;
     }
     // explicit roundings (no FMA contraction left to the compiler): the two

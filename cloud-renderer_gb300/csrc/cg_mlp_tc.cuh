@@ -1,8 +1,8 @@
-// cg_mlp_tc.cuh -- the surrogate network (16 -> 64 -> 64 -> 64 SiLU -> 1) on
-// the fifth-generation tensor cores, shared by the shade kernel, the
-// standalone inference kernel (k_shade_tc.cu) and the fused renderer
-// (k_render_tc.cu): the weight tiles a CTA stages in shared memory, one
-// layer's MMA issue, and one layer's epilogue for a thread's row.
+// cg_mlp_tc.cuh -- the surrogate network (16 -> 64 [-> 64 [-> 64]] SiLU -> 1:
+// one to three hidden layers) on the fifth-generation tensor cores, shared by
+// the shade kernel, the standalone inference kernel (k_shade_tc.cu) and the
+// fused renderer (k_render_tc.cu): the weight tiles a CTA stages in shared
+// memory, one layer's MMA issue, and one layer's epilogue for a thread's row.
 //
 // Network tiles (bytes from a 1024-aligned base, NET_BYTES in all):
 //   W2, W3   64 x 128 B, 128B-swizzled K-major (K = 64)
@@ -50,13 +50,14 @@ __device__ __forceinline__ void stage_row(uint8_t* tile, int r, const __half* sr
     }
 }
 
-// Weights W1..W3 scaled by 1/2, the ones column (8 rows) and the split
-// half-scaled biases into the network tiles at `net`; threads t = 0 .. n-1.
+// The model's hidden-layer weights (W1 .. W_layers) scaled by 1/2, the ones
+// column (8 rows) and the split half-scaled biases into the network tiles at
+// `net`; threads t = 0 .. n-1.
 __device__ __forceinline__ void stage_network(uint8_t* net, const MlpDev& m, int t, int n) {
     for (int r = t; r < 64; r += n) {
         stage_row<2>(net + NET_W1, r, m.w16 + MLP_H_W1 + r * 16);
-        stage_row<8>(net + NET_W2, r, m.w16 + MLP_H_W2 + r * 64);
-        stage_row<8>(net + NET_W3, r, m.w16 + MLP_H_W3 + r * 64);
+        if (m.layers >= 2) stage_row<8>(net + NET_W2, r, m.w16 + MLP_H_W2 + r * 64);
+        if (m.layers >= 3) stage_row<8>(net + NET_W3, r, m.w16 + MLP_H_W3 + r * 64);
     }
     if (t < 8) {
         const __half one = __float2half_rn(1.f);
@@ -67,7 +68,7 @@ __device__ __forceinline__ void stage_network(uint8_t* net, const MlpDev& m, int
         *reinterpret_cast<uint4*>(net + NET_ONES + tc::sw32_offset(t, 1)) =
             make_uint4(0u, 0u, 0u, 0u);
     }
-    for (int i = t; i < 3 * 64; i += n) {
+    for (int i = t; i < m.layers * 64; i += n) {
         const int l = i >> 6, r = i & 63;
         const float hb = m.k.hb[i];
         const __half hi = __float2half_rn(hb);
@@ -115,9 +116,9 @@ __device__ __forceinline__ void silu32(const uint32_t (&acc)[32], uint32_t (&out
 
 // One layer's epilogue for tile row `row` (this thread's tensor-memory lane,
 // dw = the lane's address of the layer's 64 accumulator columns): SiLU, 32
-// columns at a time, written as the next layer's FP16 activations (layers 0,
-// 1) or folded into the FP32 64 -> 1 output (layer 2, returned with b4).
-__device__ __forceinline__ float layer_epilogue(int layer, uint32_t dw, uint8_t* act, int row,
+// columns at a time, written as the next layer's FP16 activations, or, for
+// the last hidden layer, folded into the FP32 64 -> 1 output (returned with b4).
+__device__ __forceinline__ float layer_epilogue(bool last, uint32_t dw, uint8_t* act, int row,
                                                 const MlpDev& m) {
     float yy = m.k.b4;
 #pragma unroll
@@ -126,7 +127,7 @@ __device__ __forceinline__ float layer_epilogue(int layer, uint32_t dw, uint8_t*
         tc::tmem_ld32(dw + 32u * half, acc);
         uint32_t h[16];
         silu32(acc, h);
-        if (layer < 2) {
+        if (!last) {
 #pragma unroll
             for (int q = 0; q < 4; ++q)
                 *reinterpret_cast<uint4*>(act + tc::sw128_offset(row, 4 * half + q)) =

@@ -9,7 +9,7 @@
 // per SM, 256 threads; the fastest of the shapes measured):
 //   warps 0-3   epilogue: one thread per row of a 128-sample tile; features
 //               (12 texture taps), FP16 inputs into the activation tile, the
-//               SiLU epilogues of the three layers (tensor memory -> FP16
+//               SiLU epilogues of the hidden layers (tensor memory -> FP16
 //               activations in place), the 64 -> 1 output, the sample's
 //               contribution w * exp(-sigma tau) * (ambient + (1 - ambient) G)
 //               into the region's contribution slots;
@@ -399,7 +399,7 @@ __global__ void __launch_bounds__(RT_THREADS, RT_CTAS_PER_SM)
             mlptc::write_inputs(S.act, tid, m, f, valid);
             float y = 0.f;
 #pragma unroll 1
-            for (int layer = 0; layer < 3 && !bad; ++layer) {
+            for (int layer = 0; layer < m.layers && !bad; ++layer) {
                 // this warp's activation rows -> visible to the tensor core
                 tc::fence_proxy_async();
                 tc::fence_before_sync();
@@ -409,8 +409,9 @@ __global__ void __launch_bounds__(RT_THREADS, RT_CTAS_PER_SM)
                 if (bad) break;
                 mphase ^= 1u;
                 tc::fence_after_sync();
-                const float yy = mlptc::layer_epilogue(layer, dw, S.act, tid, m);
-                if (layer == 2) y = yy;
+                const bool last = layer == m.layers - 1;
+                const float yy = mlptc::layer_epilogue(last, dw, S.act, tid, m);
+                if (last) y = yy;
             }
             if (bad) continue;  // leaves at the next tile's joint decision
             if (valid) {
@@ -449,7 +450,7 @@ __global__ void __launch_bounds__(RT_THREADS, RT_CTAS_PER_SM)
             if (nv) atomicAdd(status + 2, (unsigned long long)nv);
         }
     } else if (warp == RT_MMA_WARP) {
-        // ---- tensor-core issue: three layers per tile until told to stop
+        // ---- tensor-core issue: m.layers layers per tile until told to stop
         const uint32_t a_addr = tc::smem_addr(S.act), net_addr = tc::smem_addr(S.net);
         unsigned aphase = 0, issued = 0;
         for (;;) {
@@ -460,7 +461,9 @@ __global__ void __launch_bounds__(RT_THREADS, RT_CTAS_PER_SM)
             aphase ^= 1u;
             if (ld_volatile(S.w + W_STOP) || ld_volatile(S.w + W_ABORT)) break;
             tc::fence_after_sync();
-            if (lane == 0) mlptc::issue_layer((int)(issued % 3u), tmem, a_addr, net_addr, S.mma_done);
+            if (lane == 0)
+                mlptc::issue_layer((int)(issued % (unsigned)m.layers), tmem, a_addr, net_addr,
+                                   S.mma_done);
             issued++;
             __syncwarp();
         }
@@ -528,6 +531,7 @@ __global__ void __launch_bounds__(RT_THREADS, RT_CTAS_PER_SM)
 cudaError_t launch_render_mlp_tc(VolDesc vd, CamDesc cam, TraceParams tp, const MlpDev& m,
                                  float* contrib, uint2* steps, float4* dst,
                                  unsigned long long* status, cudaStream_t st) {
+    if (m.layers < 1 || m.layers > MLP_MAX_LAYERS) return cudaErrorInvalidValue;
     const ConeSchedule cone = make_cone_schedule(vd, tp);
     const FeatGeom geo = feat_geom(vd, m);
     RenderArgs ra;

@@ -1,6 +1,7 @@
 // k_shade_tc.cu -- the surrogate's inference on the fifth-generation tensor
 // cores: sun transmittance of every recorded view sample through the MLP
-// (16 -> 64 -> 64 -> 64 SiLU -> 1, FP16 operands, FP32 accumulation).
+// (16 -> NL x 64 SiLU -> 1 with NL = 1, 2 or 3 hidden layers, a template
+// parameter; FP16 operands, FP32 accumulation).
 //
 // One CTA = 4 warps (thread = row of a 128-row tile), persistent over tiles.
 // Per tile:
@@ -9,20 +10,21 @@
 //   2. thread 0 issues layer 1 (one tcgen05.mma, M=128 N=64 K=16) into tensor
 //      memory and commits it to an mbarrier;
 //   3. each warp reads its 32 rows back (tcgen05.ld), applies SiLU and writes
-//      the next activation tile in place as FP16; layers 2 and 3 are 4 MMAs
-//      each (K = 64); every layer ends with one more K = 16 MMA that adds the
-//      bias (a column of ones against the bias split into two FP16 halves);
+//      the next activation tile in place as FP16; hidden layers 2 and 3 are 4
+//      MMAs each (K = 64); every layer ends with one more K = 16 MMA that adds
+//      the bias (a column of ones against the bias split into two FP16 halves);
 //   4. the last epilogue folds the 64 -> 1 output layer into FP32 FMAs, then
 //      the softplus link, the transmittance and the sample's contribution;
 //      the next tile's inputs go into the tile.
 // The next tile is fetched in stages while this one runs, so that no load is
-// consumed in the phase that issued it: its slot (layer 1), its sample
-// (layer 2), its 12 texture taps (layer 3), its inputs (output).  Tiles are
+// consumed in the phase that issued it: its slot (during the tile before),
+// its sample (layer 1), its 12 texture taps (the last layer), its inputs
+// (output); with one layer slot, sample and taps share the one phase.  Tiles are
 // claimed dynamically (an atomic counter, two tiles ahead of the one being
 // shaded): CTAs on slower SMs (the far die's L2, texture misses) take fewer
 // tiles instead of setting the kernel's tail.
-// Layers 1-3 run on weights and biases pre-scaled by 1/2 (exact in FP16 and
-// FP32), so the accumulator holds z/2 and SiLU is z/2 * (1 + tanh(z/2)).
+// Hidden layers run on weights and biases pre-scaled by 1/2 (exact in FP16
+// and FP32), so the accumulator holds z/2 and SiLU is z/2 * (1 + tanh(z/2)).
 // Every mbarrier wait is bounded (1 s of the global timer): on a timeout the
 // CTA records an error, waits (bounded) for its MMA to drain, frees its tensor
 // memory and returns.
@@ -160,7 +162,7 @@ __device__ __forceinline__ bool group_sync_for_mma(int g, bool bad) {
     return any_bad;
 }
 
-template <int FMT>
+template <int FMT, int NL>
 __global__ void __launch_bounds__(128 * SHADE_GROUPS, SHADE_CTAS_PER_SM)
     k_shade_mlp_tc(const __grid_constant__ VolDesc vd, const __grid_constant__ TraceParams tp,
                    const __grid_constant__ ConeSchedule cone, const __grid_constant__ MlpDev m,
@@ -219,14 +221,17 @@ __global__ void __launch_bounds__(128 * SHADE_GROUPS, SHADE_CTAS_PER_SM)
     // the first two tiles of a group are static, later ones are claimed from
     // status[3]
     unsigned ntile = tile + streams;
+    // with two or more layers a tile's slot is fetched one tile ahead (at
+    // layer 1 of the tile before, from the claim made at its layer 0)
+    unsigned nslot = NL >= 2 ? slot_at(sb, ntile, ntiles, total, r) : CG_NO_SLOT;
     for (; tile < ntiles;) {
-        unsigned nslot = CG_NO_SLOT;
+        unsigned nnslot = CG_NO_SLOT, nntile = 0u;
         float4 ns = make_float4(0.f, 0.f, 0.f, 0.f);
         float ng = 0.f;
         float nf[MLP_IN];
         float y = 0.f;
 #pragma unroll
-        for (int layer = 0; layer < 3; ++layer) {
+        for (int layer = 0; layer < NL; ++layer) {
             if (group_sync_for_mma(g, bad)) {  // a commit of parity `phase` is still pending
                 failed = true;
                 break;
@@ -236,13 +241,19 @@ __global__ void __launch_bounds__(128 * SHADE_GROUPS, SHADE_CTAS_PER_SM)
                 // claim the tile after next (read by the group after the next sync)
                 if (layer == 0) *s_claim = 2u * streams + (unsigned)atomicAdd(status + 3, 1ull);
             }
-            // ---- the next tile, in stages
-            if (layer == 0) nslot = slot_at(sb, ntile, ntiles, total, r);
-            if (layer == 1 && nslot != CG_NO_SLOT) {
+            // ---- the next tile, in stages: its sample (layer 0), the slot of
+            // the tile after it (layer 1), its texture taps (last layer); one
+            // layer: slot, sample and taps in the same phase
+            if (NL == 1) nslot = slot_at(sb, ntile, ntiles, total, r);
+            if (layer == 0 && nslot != CG_NO_SLOT) {
                 ns = sb.pos_w[nslot];
                 ng = sb.light_lane[nslot].x;
             }
-            if (layer == 2) fetch_features(geo, tp, nslot, ns, nf);
+            if (NL >= 2 && layer == 1) {
+                nntile = *s_claim;  // written at layer 0, one barrier ago
+                nnslot = slot_at(sb, nntile, ntiles, total, r);
+            }
+            if (layer == NL - 1) fetch_features(geo, tp, nslot, ns, nf);
             // a warp whose wait ran out skips the epilogue (no tensor-memory
             // read under a running MMA) and the group stops at the next barrier
             bad = __any_sync(0xffffffffu, !tc::mbar_wait(bar, phase, TC_WAIT_NS));
@@ -251,8 +262,8 @@ __global__ void __launch_bounds__(128 * SHADE_GROUPS, SHADE_CTAS_PER_SM)
             // ---- epilogue: TMEM -> bias + SiLU, 32 columns at a time; the
             // last layer folds the 64 -> 1 output in FP32
             if (!bad) {
-                const float yy = mlptc::layer_epilogue(layer, dw, act, r, m);
-                if (layer == 2) y = yy;
+                const float yy = mlptc::layer_epilogue(layer == NL - 1, dw, act, r, m);
+                if (layer == NL - 1) y = yy;
             }
             tc::fence_before_sync();
         }
@@ -274,7 +285,12 @@ __global__ void __launch_bounds__(128 * SHADE_GROUPS, SHADE_CTAS_PER_SM)
         // ---- the next tile's inputs
         pack_row<FMT>(vd, cone, m, tp, nslot, ns, ng, nf, row, act, r);
         tile = ntile;
-        ntile = *s_claim;  // written at layer 0, two barriers ago
+        if (NL >= 2) {
+            ntile = nntile;
+            nslot = nnslot;
+        } else {
+            ntile = *s_claim;  // written at layer 0, one barrier ago
+        }
     }
     if (!failed) failed = group_sync_for_mma(g, bad);  // the last tile's waits
     if (failed) {
@@ -304,6 +320,7 @@ __global__ void __launch_bounds__(128 * SHADE_GROUPS, SHADE_CTAS_PER_SM)
 // out[i] = tau_scale * softplus(y_i).  The tile pipeline of k_shade_mlp_tc
 // without the sample fetches: 128-row tiles at a static stride, the same
 // staged weights, layers, epilogues and bounded waits.
+template <int NL>
 __global__ void __launch_bounds__(128, CTAS_PER_SM)
     k_mlp_infer_tc(const __grid_constant__ MlpDev m, const float* feat, int n, float* out,
                    unsigned long long* status) {
@@ -337,7 +354,7 @@ __global__ void __launch_bounds__(128, CTAS_PER_SM)
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int row = tile * 128 + tid;
         // this row's normalised FP16 features into chunks 0-1 of its tile row
-        // (the previous tile's layer-3 MMA, the last reader, has completed)
+        // (the previous tile's last MMA, the last reader, has completed)
         uint32_t x[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
@@ -352,7 +369,7 @@ __global__ void __launch_bounds__(128, CTAS_PER_SM)
             make_uint4(x[4], x[5], x[6], x[7]);
         float y = 0.f;
 #pragma unroll
-        for (int layer = 0; layer < 3; ++layer) {
+        for (int layer = 0; layer < NL; ++layer) {
             if (sync_for_mma(bad)) {  // a commit of parity `phase` is still pending
                 failed = true;
                 break;
@@ -363,8 +380,8 @@ __global__ void __launch_bounds__(128, CTAS_PER_SM)
             if (!bad) phase ^= 1u;
             tc::fence_after_sync();
             if (!bad) {
-                const float yy = mlptc::layer_epilogue(layer, dw, act, tid, m);
-                if (layer == 2) y = yy;
+                const float yy = mlptc::layer_epilogue(layer == NL - 1, dw, act, tid, m);
+                if (layer == NL - 1) y = yy;
             }
             tc::fence_before_sync();
         }
@@ -408,16 +425,21 @@ cudaError_t launch_wait_probe(uint64_t limit_ns, unsigned long long* status, cud
 cudaError_t launch_mlp_infer(const MlpDev& m, const float* feat, int n, float* out,
                              unsigned long long* status, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    // the shared-memory attribute and the grid are set once per device
+    if (m.layers < 1 || m.layers > MLP_MAX_LAYERS) return cudaErrorInvalidValue;
+    // the shared-memory attributes and the grid are set once per device
     static std::atomic<int> grid[64];
+    const void* fns[MLP_MAX_LAYERS] = {(const void*)k_mlp_infer_tc<1>,
+                                       (const void*)k_mlp_infer_tc<2>,
+                                       (const void*)k_mlp_infer_tc<3>};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
     if (!grid[dev].load(std::memory_order_acquire)) {
-        e = cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 SMEM_BYTES);
-        if (e != cudaSuccess) return e;
+        for (const void* fn : fns) {
+            e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+            if (e != cudaSuccess) return e;
+        }
         int sms = 0;
         e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (e != cudaSuccess) return e;
@@ -425,7 +447,11 @@ cudaError_t launch_mlp_infer(const MlpDev& m, const float* feat, int n, float* o
     }
     const int ntiles = (n + 127) / 128;
     const int blocks = std::min(grid[dev].load(std::memory_order_acquire), ntiles);
-    k_mlp_infer_tc<<<blocks, 128, SMEM_BYTES, st>>>(m, feat, n, out, status);
+    switch (m.layers) {
+        case 1: k_mlp_infer_tc<1><<<blocks, 128, SMEM_BYTES, st>>>(m, feat, n, out, status); break;
+        case 2: k_mlp_infer_tc<2><<<blocks, 128, SMEM_BYTES, st>>>(m, feat, n, out, status); break;
+        default: k_mlp_infer_tc<3><<<blocks, 128, SMEM_BYTES, st>>>(m, feat, n, out, status); break;
+    }
     return cudaGetLastError();
 }
 
@@ -438,26 +464,32 @@ cudaError_t launch_shade_mlp_tc(VolDesc vd, CamDesc cam, TraceParams tp, const M
     // shared-memory budgets of __launch_bounds__; 64 tensor-memory columns each)
     // (the per-device launch shape and the shared-memory attribute are
     // configured once; atomics keep concurrent host threads well-defined)
-    static std::atomic<int> grid[2][64];
+    if (m.layers < 1 || m.layers > MLP_MAX_LAYERS) return cudaErrorInvalidValue;
+    static std::atomic<int> grid[64];
+    using ShadeFn = void (*)(VolDesc, TraceParams, ConeSchedule, MlpDev, FeatGeom, SampleBuf,
+                             unsigned long long*);
+    const ShadeFn fns[2][MLP_MAX_LAYERS] = {
+        {k_shade_mlp_tc<0, 1>, k_shade_mlp_tc<0, 2>, k_shade_mlp_tc<0, 3>},
+        {k_shade_mlp_tc<1, 1>, k_shade_mlp_tc<1, 2>, k_shade_mlp_tc<1, 3>}};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-    const int f = vd.fmt == 0 ? 0 : 1;
-    if (!grid[f][dev].load(std::memory_order_acquire)) {
-        const void* fn = f == 0 ? (const void*)k_shade_mlp_tc<0> : (const void*)k_shade_mlp_tc<1>;
-        e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, SH_SMEM_BYTES);
-        if (e != cudaSuccess) return e;
+    if (!grid[dev].load(std::memory_order_acquire)) {
+        for (const auto& row : fns)
+            for (ShadeFn fn : row) {
+                e = cudaFuncSetAttribute((const void*)fn,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, SH_SMEM_BYTES);
+                if (e != cudaSuccess) return e;
+            }
         int sms = 0;
         e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (e != cudaSuccess) return e;
-        grid[f][dev].store(sms * SHADE_CTAS_PER_SM, std::memory_order_release);
+        grid[dev].store(sms * SHADE_CTAS_PER_SM, std::memory_order_release);
     }
-    const int blocks = grid[f][dev].load(std::memory_order_acquire);
-    if (f == 0)
-        k_shade_mlp_tc<0><<<blocks, 128 * SHADE_GROUPS, SH_SMEM_BYTES, st>>>(vd, tp, cone, m, geo, sb, status);
-    else
-        k_shade_mlp_tc<1><<<blocks, 128 * SHADE_GROUPS, SH_SMEM_BYTES, st>>>(vd, tp, cone, m, geo, sb, status);
+    const int blocks = grid[dev].load(std::memory_order_acquire);
+    fns[vd.fmt == 0 ? 0 : 1][m.layers - 1]<<<blocks, 128 * SHADE_GROUPS, SH_SMEM_BYTES, st>>>(
+        vd, tp, cone, m, geo, sb, status);
     return cudaGetLastError();
 }
 

@@ -2,7 +2,8 @@
 // fifth-generation tensor cores: forward, loss gradient, backward and the
 // per-CTA gradient partials that k_mlp_adam reduces in a fixed order.
 //
-// One CTA = 128 rows of the batch, 4 warps, thread = row.  Every GEMM is a
+// One CTA = 128 rows of the batch, 4 warps, thread = row.  The network has NL
+// = 1, 2 or 3 hidden layers (a template parameter).  Every GEMM is a
 // tcgen05.mma (M = 128, FP16 operands from shared memory, FP32 accumulators
 // in tensor memory) issued by thread 0 and committed to one mbarrier:
 //   forward   z_l = A_l W_l^T + b_l          A_0 = x, A_l = h_l (K = 16, 64)
@@ -25,6 +26,7 @@
 // in the same CTA order, as k_mlp_adam -- the two paths give identical bits.
 #include <cuda_fp16.h>
 
+#include <algorithm>
 #include <atomic>
 
 #include "cg_internal.h"
@@ -149,6 +151,7 @@ __device__ __forceinline__ void ld64(uint32_t taddr, float (&v)[64]) {
     for (int j = 0; j < 32; ++j) v[32 + j] = __uint_as_float(r[j]);
 }
 
+template <int NL>
 __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
     extern __shared__ uint8_t smem_raw[];
     const uint32_t raw = tc::smem_addr(smem_raw);
@@ -163,33 +166,33 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
     uint32_t* tslot = reinterpret_cast<uint32_t*>(base + O_BAR + 8);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-    // ---- weights (FP16 image), their transposes, biases, ones
+    // ---- weights (FP16 image) of the NL hidden layers, the transposes of
+    // layers 2 .. NL, biases, ones
     for (int r = tid; r < 64; r += 128) {
 #pragma unroll
         for (int c = 0; c < 2; ++c)
             *reinterpret_cast<uint4*>(base + O_W1 + tc::sw32_offset(r, c)) =
                 *reinterpret_cast<const uint4*>(ta.w16 + MLP_H_W1 + r * 16 + 8 * c);
 #pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            *reinterpret_cast<uint4*>(base + O_W2 + tc::sw128_offset(r, c)) =
-                *reinterpret_cast<const uint4*>(ta.w16 + MLP_H_W2 + r * 64 + 8 * c);
-            *reinterpret_cast<uint4*>(base + O_W3 + tc::sw128_offset(r, c)) =
-                *reinterpret_cast<const uint4*>(ta.w16 + MLP_H_W3 + r * 64 + 8 * c);
-            // W^T row r (input r), K = outputs 8c .. 8c+7
-            __align__(16) __half t2[8], t3[8];
+        for (int l = 1; l < NL; ++l) {
+            const int src = l == 1 ? MLP_H_W2 : MLP_H_W3;
+            uint8_t* w = base + (l == 1 ? O_W2 : O_W3);
+            uint8_t* wt = base + (l == 1 ? O_WT2 : O_WT3);
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                t2[q] = ta.w16[MLP_H_W2 + (8 * c + q) * 64 + r];
-                t3[q] = ta.w16[MLP_H_W3 + (8 * c + q) * 64 + r];
+            for (int c = 0; c < 8; ++c) {
+                *reinterpret_cast<uint4*>(w + tc::sw128_offset(r, c)) =
+                    *reinterpret_cast<const uint4*>(ta.w16 + src + r * 64 + 8 * c);
+                // W^T row r (input r), K = outputs 8c .. 8c+7
+                __align__(16) __half t[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) t[q] = ta.w16[src + (8 * c + q) * 64 + r];
+                *reinterpret_cast<uint4*>(wt + tc::sw128_offset(r, c)) =
+                    *reinterpret_cast<const uint4*>(t);
             }
-            *reinterpret_cast<uint4*>(base + O_WT2 + tc::sw128_offset(r, c)) =
-                *reinterpret_cast<const uint4*>(t2);
-            *reinterpret_cast<uint4*>(base + O_WT3 + tc::sw128_offset(r, c)) =
-                *reinterpret_cast<const uint4*>(t3);
         }
         fw4[r] = __half2float(ta.w16[MLP_H_W4 + r]);
     }
-    for (int i = tid; i < 3 * 64; i += 128) {
+    for (int i = tid; i < NL * 64; i += 128) {
         const int l = i >> 6, n = i & 63;
         const int off = l == 0 ? MLP_B1 : (l == 1 ? MLP_B2 : MLP_B3);
         const float bv = ta.params[off + n];
@@ -273,7 +276,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
 
     // ---- forward
     float y = 0.f;
-    for (int l = 0; l < 3 && !failed; ++l) {
+    for (int l = 0; l < NL && !failed; ++l) {
         if (tt_sync(bad)) {
             failed = true;
             break;
@@ -301,7 +304,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
                 const float2 zf = __half22float2(zh);
                 hp[j] = h2u(__floats2half2_rn(silu_f(zf.x), silu_f(zf.y)));
             }
-            if (l < 2) {
+            if (l < NL - 1) {
                 uint8_t* ht = base + (l == 0 ? O_H1 : O_H2);
 #pragma unroll
                 for (int c = 0; c < 8; ++c)
@@ -331,12 +334,13 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
         dy = 2.f * diff * (-k * mlp::sigmoid(y) * Th);
     }
     {
-        // dW4[j] = sum_rows dy h3[j] and db4 = sum_rows dy: shuffle trees per
-        // warp, then the four warps in order
-        const __half* z3 = zs + (size_t)(2 * 128 + tid) * ZS;
+        // dW4[j] = sum_rows dy h[j] (h: the last hidden layer's activations)
+        // and db4 = sum_rows dy: shuffle trees per warp, then the four warps in
+        // order
+        const __half* zl = zs + (size_t)((NL - 1) * 128 + tid) * ZS;
         for (int j = 0; j < 64; ++j) {
-            const float h3 = __half2float(__float2half_rn(silu_f(__half2float(z3[j]))));
-            float v = dy * h3;
+            const float hl = __half2float(__float2half_rn(silu_f(__half2float(zl[j]))));
+            float v = dy * hl;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
             if (lane == 0) fred[warp * 64 + j] = v;
@@ -397,16 +401,18 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
         }
     };
 
+    // the input tile of hidden layer l (x, h1 or h2) and its width
+    auto input_of = [&](int l) { return base + (l == 0 ? O_X : (l == 1 ? O_H1 : O_H2)); };
     if (!failed && !bad) {
-        // layer 3: dz3 = dy w4 * silu'(z3)
+        // last hidden layer: dz = dy w4 * silu'(z)
         float dh[64];
 #pragma unroll
         for (int j = 0; j < 64; ++j) dh[j] = dy * fw4[j];
-        write_dz(2, dh);
-        write_ht(base + O_H2, 64);
+        write_dz(NL - 1, dh);
+        write_ht(input_of(NL - 1), NL - 1 == 0 ? 16 : 64);
     }
-    // backward: (dW3, dh2), (dW2, dh1), dW1
-    for (int l = 2; l >= 0 && !failed; --l) {
+    // backward, from the last hidden layer down: (dW3, dh2), (dW2, dh1), dW1
+    for (int l = NL - 1; l >= 0 && !failed; --l) {
         if (tt_sync(bad)) {
             failed = true;
             break;
@@ -432,7 +438,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
                 break;
             }
             write_dz(l - 1, dh);
-            write_ht(base + (l == 2 ? O_H1 : O_X), l == 2 ? 64 : 16);
+            write_ht(input_of(l - 1), l - 1 == 0 ? 16 : 64);
             tc::fence_before_sync();
         }
     }
@@ -464,6 +470,10 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
     if (ta.grid_bar) fused_adam(ta, step0, reinterpret_cast<int*>(fmisc + 8));
 }
 
+using TrainFn = void (*)(TrainArgs);
+const TrainFn kTrainFns[MLP_MAX_LAYERS] = {k_mlp_train_tc<1>, k_mlp_train_tc<2>,
+                                           k_mlp_train_tc<3>};
+
 }  // namespace
 
 // CTAs of the training kernel resident at once on the current device (set
@@ -474,24 +484,33 @@ int mlp_train_resident_ctas() {
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
     int r = resident[dev].load(std::memory_order_acquire);
     if (r > 0) return r;
-    if (cudaFuncSetAttribute(k_mlp_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             TT_SMEM) != cudaSuccess)
-        return 0;
-    int per_sm = 0, sms = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mlp_train_tc, 128, TT_SMEM) !=
-            cudaSuccess ||
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-        return 0;
+    for (TrainFn fn : kTrainFns)
+        if (cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 TT_SMEM) != cudaSuccess)
+            return 0;
+    // the fewest resident CTAs over the depths (they share the shared-memory
+    // layout and the launch bounds)
+    int per_sm = 1 << 30, sms = 0;
+    for (TrainFn fn : kTrainFns) {
+        int k = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, (const void*)fn, 128, TT_SMEM) !=
+            cudaSuccess)
+            return 0;
+        per_sm = std::min(per_sm, k);
+    }
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
     r = per_sm * sms;
     resident[dev].store(r, std::memory_order_release);
     return r;
 }
 
 cudaError_t launch_mlp_train(const TrainArgs& ta, int ctas, cudaStream_t st) {
+    if (ta.layers < 1 || ta.layers > MLP_MAX_LAYERS) return cudaErrorInvalidValue;
+    const TrainFn fn = kTrainFns[ta.layers - 1];
     const int resident = mlp_train_resident_ctas();
     if (resident <= 0) return cudaErrorInvalidConfiguration;
     if (!ta.grid_bar) {
-        k_mlp_train_tc<<<ctas, 128, TT_SMEM, st>>>(ta);
+        fn<<<ctas, 128, TT_SMEM, st>>>(ta);
         return cudaGetLastError();
     }
     // the fused optimiser's grid barrier needs every CTA resident: a
@@ -507,7 +526,7 @@ cudaError_t launch_mlp_train(const TrainArgs& ta, int ctas, cudaStream_t st) {
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_mlp_train_tc, ta);
+    return cudaLaunchKernelEx(&cfg, fn, ta);
 }
 
 CG_OOB_TU(k_train_tc)

@@ -274,16 +274,21 @@ cg_status cg_volume_active_voxels(const cg_volume* vol, uint64_t* active);
 
 /* ---- MLP sun-transmittance surrogate ------------------------------------
  * No counterpart in the reference (its traceCone is the exact method).  A
- * 16 -> 64 -> 64 -> 64 -> 1 SiLU network predicts the sun cone's optical
- * depth from 16 features of a view sample:
+ * SiLU network of 1, 2 (default) or 3 hidden layers of width 64 (16 -> 64
+ * [-> 64 [-> 64]] -> 1) predicts the sun cone's optical depth from 16
+ * features of a view sample:
  *   f[3i+k] = density at level base_level+i sampled at
  *             v + (initial_height + (k + 0.5) * 2^(base_level+i)) * s  (i<4, k<3)
  *   f[12..14] = v / dimension,  f[15] = s.y
  * (v: level-0 voxel position, s: unit sun direction).  FP16 weights and
  * activations on the tensor cores, FP32 accumulation and master weights.
- * Training, inference and the render use the project's own kernels. */
+ * Training, inference and the render use the project's own kernels.  The
+ * parameter vector always has the three-layer layout (CG_MLP_PARAMS floats);
+ * a shallower model keeps the blocks of the layers it does not use at zero. */
 #define CG_MLP_FEATURES 16
 #define CG_MLP_PARAMS 9473
+#define CG_MLP_MAX_LAYERS 3
+#define CG_MLP_DEFAULT_LAYERS 2
 
 typedef struct cg_mlp_config {
     int base_level;        /* feature levels base_level .. base_level+3 */
@@ -315,8 +320,13 @@ typedef struct cg_train_params {
 void cg_mlp_config_default(cg_mlp_config* c);
 void cg_train_params_default(cg_train_params* p);
 int cg_mlp_param_count(void);
-/* He-uniform initialisation from a SplitMix64 stream seeded with `seed`. */
+/* He-uniform initialisation from a SplitMix64 stream seeded with `seed`;
+ * CG_MLP_DEFAULT_LAYERS hidden layers. */
 cg_status cg_mlp_create(cg_context* ctx, uint64_t seed, cg_mlp** out);
+/* The same with 1 .. CG_MLP_MAX_LAYERS hidden layers (fixed for the model's
+ * life; checkpoints record it). */
+cg_status cg_mlp_create_layers(cg_context* ctx, uint64_t seed, int hidden_layers, cg_mlp** out);
+int cg_mlp_hidden_layers(const cg_mlp* mlp);
 void cg_mlp_destroy(cg_mlp* mlp);
 cg_status cg_mlp_configure(cg_mlp* mlp, const cg_mlp_config* config);
 cg_status cg_mlp_get_config(const cg_mlp* mlp, cg_mlp_config* config);

@@ -1421,41 +1421,48 @@ static void mlp_layer(const double* W, const double* b, const double* x, int nin
     }
 }
 
-/* Normalised output y of one row of raw features f. */
+/* Hidden layer l (0-based) of the parameter vector: weights, bias, fan-in. */
+static const double* mlp_w(const double* P, int l) { return P + (l == 0 ? M_W1 : (l == 1 ? M_W2 : M_W3)); }
+static const double* mlp_b(const double* P, int l) { return P + (l == 0 ? M_B1 : (l == 1 ? M_B2 : M_B3)); }
+static int mlp_nin(int l) { return l == 0 ? 16 : 64; }
+static int mlp_woff(int l) { return l == 0 ? M_W1 : (l == 1 ? M_W2 : M_W3); }
+static int mlp_boff(int l) { return l == 0 ? M_B1 : (l == 1 ? M_B2 : M_B3); }
+
+/* Normalised output y of one row of raw features f through `layers` (1..3)
+ * hidden layers; the output layer (W4, b4) reads the last one. */
 OR_API double or_mlp_forward(const double* P, const double* mu, const double* sd,
-                             const double f[16]) {
-    double x[16], z[64], h1[64], h2[64], h3[64];
-    for (int j = 0; j < 16; ++j) x[j] = (f[j] - mu[j]) / sd[j];
-    mlp_layer(P + M_W1, P + M_B1, x, 16, z);
-    for (int o = 0; o < 64; ++o) h1[o] = silu_d(z[o]);
-    mlp_layer(P + M_W2, P + M_B2, h1, 64, z);
-    for (int o = 0; o < 64; ++o) h2[o] = silu_d(z[o]);
-    mlp_layer(P + M_W3, P + M_B3, h2, 64, z);
-    for (int o = 0; o < 64; ++o) h3[o] = silu_d(z[o]);
+                             const double f[16], int layers) {
+    double a[64], z[64];
+    for (int j = 0; j < 16; ++j) a[j] = (f[j] - mu[j]) / sd[j];
+    for (int l = 0; l < layers; ++l) {
+        mlp_layer(mlp_w(P, l), mlp_b(P, l), a, mlp_nin(l), z);
+        for (int o = 0; o < 64; ++o) a[o] = silu_d(z[o]);
+    }
     double y = P[M_B4];
-    for (int i = 0; i < 64; ++i) y += P[M_W4 + i] * h3[i];
+    for (int i = 0; i < 64; ++i) y += P[M_W4 + i] * a[i];
     return y;
 }
 
 /* Mean over n rows of (exp(-sigma*scale*softplus(y)) - exp(-sigma*tau))^2 and
- * its gradient with respect to the 9473 parameters (grad, zeroed here).  The
- * predicted optical depth is scale * softplus(y). */
+ * its gradient with respect to the 9473 parameters (grad, zeroed here; the
+ * blocks of unused hidden layers stay 0) for a network of `layers` (1..3)
+ * hidden layers.  The predicted optical depth is scale * softplus(y). */
 OR_API double or_mlp_loss_grad(const double* P, const double* mu, const double* sd,
                                double tau_scale, double sigma, const double* feats,
-                               const double* tau, int n, double* grad) {
+                               const double* tau, int n, double* grad, int layers) {
     for (int i = 0; i < M_NPARAM; ++i) grad[i] = 0.0;
     double loss = 0.0;
     for (int r = 0; r < n; ++r) {
-        double x[16], z1[64], z2[64], z3[64], h1[64], h2[64], h3[64];
-        for (int j = 0; j < 16; ++j) x[j] = (feats[r * 16 + j] - mu[j]) / sd[j];
-        mlp_layer(P + M_W1, P + M_B1, x, 16, z1);
-        for (int o = 0; o < 64; ++o) h1[o] = silu_d(z1[o]);
-        mlp_layer(P + M_W2, P + M_B2, h1, 64, z2);
-        for (int o = 0; o < 64; ++o) h2[o] = silu_d(z2[o]);
-        mlp_layer(P + M_W3, P + M_B3, h2, 64, z3);
-        for (int o = 0; o < 64; ++o) h3[o] = silu_d(z3[o]);
+        /* h[0] = x (16 wide), h[l+1] = silu(z[l]) */
+        double h[4][64], z[3][64];
+        for (int j = 0; j < 16; ++j) h[0][j] = (feats[r * 16 + j] - mu[j]) / sd[j];
+        for (int l = 0; l < layers; ++l) {
+            mlp_layer(mlp_w(P, l), mlp_b(P, l), h[l], mlp_nin(l), z[l]);
+            for (int o = 0; o < 64; ++o) h[l + 1][o] = silu_d(z[l][o]);
+        }
+        const double* hl = h[layers];
         double y = P[M_B4];
-        for (int i = 0; i < 64; ++i) y += P[M_W4 + i] * h3[i];
+        for (int i = 0; i < 64; ++i) y += P[M_W4 + i] * hl[i];
         double k = sigma * tau_scale;
         double sp = (y > 0 ? y : 0.0) + log1p(exp(-fabs(y)));
         double sg = 1.0 / (1.0 + exp(-y));
@@ -1463,33 +1470,27 @@ OR_API double or_mlp_loss_grad(const double* P, const double* mu, const double* 
         double diff = Th - T;
         loss += diff * diff;
         double dy = 2.0 * diff * (-k * sg * Th) / (double)n;
-        double d3[64], d2[64], d1[64];
+        double d[64], dn[64];
         grad[M_B4] += dy;
         for (int i = 0; i < 64; ++i) {
-            grad[M_W4 + i] += dy * h3[i];
-            d3[i] = dy * P[M_W4 + i] * silu_grad_d(z3[i]);
+            grad[M_W4 + i] += dy * hl[i];
+            d[i] = dy * P[M_W4 + i] * silu_grad_d(z[layers - 1][i]);
         }
-        for (int o = 0; o < 64; ++o) {
-            grad[M_B3 + o] += d3[o];
-            for (int i = 0; i < 64; ++i) grad[M_W3 + o * 64 + i] += d3[o] * h2[i];
-        }
-        for (int i = 0; i < 64; ++i) {
-            double s = 0.0;
-            for (int o = 0; o < 64; ++o) s += P[M_W3 + o * 64 + i] * d3[o];
-            d2[i] = s * silu_grad_d(z2[i]);
-        }
-        for (int o = 0; o < 64; ++o) {
-            grad[M_B2 + o] += d2[o];
-            for (int i = 0; i < 64; ++i) grad[M_W2 + o * 64 + i] += d2[o] * h1[i];
-        }
-        for (int i = 0; i < 64; ++i) {
-            double s = 0.0;
-            for (int o = 0; o < 64; ++o) s += P[M_W2 + o * 64 + i] * d2[o];
-            d1[i] = s * silu_grad_d(z1[i]);
-        }
-        for (int o = 0; o < 64; ++o) {
-            grad[M_B1 + o] += d1[o];
-            for (int i = 0; i < 16; ++i) grad[M_W1 + o * 16 + i] += d1[o] * x[i];
+        for (int l = layers - 1; l >= 0; --l) {
+            const int nin = mlp_nin(l);
+            const double* W = mlp_w(P, l);
+            for (int o = 0; o < 64; ++o) {
+                grad[mlp_boff(l) + o] += d[o];
+                for (int i = 0; i < nin; ++i) grad[mlp_woff(l) + o * nin + i] += d[o] * h[l][i];
+            }
+            if (l > 0) {
+                for (int i = 0; i < 64; ++i) {
+                    double s = 0.0;
+                    for (int o = 0; o < 64; ++o) s += W[o * 64 + i] * d[o];
+                    dn[i] = s * silu_grad_d(z[l - 1][i]);
+                }
+                for (int i = 0; i < 64; ++i) d[i] = dn[i];
+            }
         }
     }
     return loss / (double)n;

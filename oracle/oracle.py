@@ -102,9 +102,9 @@ def load(bits=64):
         "or_compat_render": (I, [P, ctypes.POINTER(or_camera), ctypes.POINTER(or_compat_params),
                                  FP, FP, DP, I]),
         "or_mlp_features": (None, [P, DP, DP, I, ctypes.c_double, DP]),
-        "or_mlp_forward": (ctypes.c_double, [DP, DP, DP, DP]),
+        "or_mlp_forward": (ctypes.c_double, [DP, DP, DP, DP, I]),
         "or_mlp_loss_grad": (ctypes.c_double, [DP, DP, DP, ctypes.c_double, ctypes.c_double, DP,
-                                               DP, I, DP]),
+                                               DP, I, DP, I]),
         "or_adam_step": (None, [DP, DP, DP, DP, I, ctypes.c_double, ctypes.c_double,
                                 ctypes.c_double, ctypes.c_double, I]),
     }
@@ -319,21 +319,24 @@ def _dp(a):
 
 
 class OracleMLP:
-    """FP64 forward / loss gradient / Adam of the surrogate (or_mlp_*)."""
+    """FP64 forward / loss gradient / Adam of the surrogate (or_mlp_*) with 1,
+    2 or 3 hidden layers."""
 
     NPARAM = 9473
 
-    def __init__(self, params, mean, stddev, tau_scale):
+    def __init__(self, params, mean, stddev, tau_scale, layers=3):
         self.lib = load(64)
         self.P = np.ascontiguousarray(params, np.float64)
         self.mu = np.ascontiguousarray(mean, np.float64)
         self.sd = np.ascontiguousarray(stddev, np.float64)
         self.tau_scale = float(tau_scale)
+        self.layers = int(layers)
 
     def forward(self, feats):
         f = np.ascontiguousarray(feats, np.float64).reshape(-1, 16)
         return np.array([self.lib.or_mlp_forward(_dp(self.P), _dp(self.mu), _dp(self.sd),
-                                                 _dp(np.ascontiguousarray(row))) for row in f])
+                                                 _dp(np.ascontiguousarray(row)), self.layers)
+                         for row in f])
 
     def loss_grad(self, feats, tau, sigma, params=None):
         P = self.P if params is None else np.ascontiguousarray(params, np.float64)
@@ -341,7 +344,8 @@ class OracleMLP:
         t = np.ascontiguousarray(tau, np.float64).reshape(-1)
         g = np.zeros(self.NPARAM, np.float64)
         loss = self.lib.or_mlp_loss_grad(_dp(P), _dp(self.mu), _dp(self.sd), self.tau_scale,
-                                         float(sigma), _dp(f), _dp(t), f.shape[0], _dp(g))
+                                         float(sigma), _dp(f), _dp(t), f.shape[0], _dp(g),
+                                         self.layers)
         return loss, g
 
 

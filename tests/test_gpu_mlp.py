@@ -26,8 +26,8 @@ def fp16_round(p):
     return p.astype(np.float16).astype(np.float64)
 
 
-def random_model(ctx, seed=3):
-    m = surrogate.SunMLP(ctx, seed=seed)
+def random_model(ctx, seed=3, layers=None):
+    m = surrogate.SunMLP(ctx, seed=seed, hidden_layers=layers)
     rng = np.random.default_rng(seed)
     mu = rng.uniform(-0.5, 0.5, 16)
     sd = rng.uniform(0.5, 2.0, 16)
@@ -49,13 +49,23 @@ def oracle_of(m, mu, sd):
     # the GPU multiplies with FP16 weights; biases stay FP32
     for a, b in [(0, 1024), (1088, 5184), (5248, 9344), (9408, 9472)]:
         P[a:b] = fp16_round(P[a:b])
-    return O.OracleMLP(P, mu, sd, m.config.tau_scale)
+    return O.OracleMLP(P, mu, sd, m.config.tau_scale, layers=m.hidden_layers)
+
+
+# blocks [lo, hi) of the hidden layers a model of `layers` does not use
+FROZEN = {1: (1088, 9408), 2: (5248, 9408), 3: (0, 0)}
+BLOCKS = [(0, 1024), (1024, 1088), (1088, 5184), (5184, 5248), (5248, 9344), (9344, 9408),
+          (9408, 9472), (9472, 9473)]
 
 
 # 1000 rows: eight tiles, the last partial; 200003: more tiles than CTAs
+@pytest.mark.parametrize("layers", [1, 2, 3])
 @pytest.mark.parametrize("n", [1000, 200003])
-def test_forward_matches_oracle(ctx, n):
-    m, mu, sd, rng = random_model(ctx)
+def test_forward_matches_oracle(ctx, n, layers):
+    m, mu, sd, rng = random_model(ctx, layers=layers)
+    assert m.hidden_layers == layers
+    lo, hi = FROZEN[layers]
+    assert not m.get_params()[0][lo:hi].any()  # unused layers are zero
     f = rng.uniform(-2, 2, (n, 16)).astype(np.float32) * sd + mu
     got = m.infer(f).astype(np.float64)
     om = oracle_of(m, mu, sd)
@@ -65,8 +75,9 @@ def test_forward_matches_oracle(ctx, n):
     assert np.corrcoef(got, ref)[0, 1] > 0.99999
 
 
-def test_gradient_matches_oracle(ctx):
-    m, mu, sd, rng = random_model(ctx, seed=5)
+@pytest.mark.parametrize("layers", [1, 2, 3])
+def test_gradient_matches_oracle(ctx, layers):
+    m, mu, sd, rng = random_model(ctx, seed=5, layers=layers)
     n = 600  # not a multiple of 128: padding rows must contribute nothing
     f = (rng.uniform(-2, 2, (n, 16)) * sd + mu).astype(np.float32)
     tau = rng.uniform(0.0, 1.5, n).astype(np.float32)
@@ -78,15 +89,19 @@ def test_gradient_matches_oracle(ctx):
     rel = np.linalg.norm(g - og) / np.linalg.norm(og)
     cos = float(g @ og / (np.linalg.norm(g) * np.linalg.norm(og)))
     assert rel < 1e-3 and cos > 0.99999, (rel, cos)
-    for a, b in [(0, 1024), (1024, 1088), (1088, 5184), (5184, 5248), (5248, 9344),
-                 (9344, 9408), (9408, 9472), (9472, 9473)]:
+    lo, hi = FROZEN[layers]
+    assert not g[lo:hi].any()
+    for a, b in BLOCKS:
+        if lo <= a < hi:
+            continue
         seg_rel = np.linalg.norm(g[a:b] - og[a:b]) / max(np.linalg.norm(og[a:b]), 1e-12)
         assert seg_rel < 3e-3, (a, b, seg_rel)
 
 
-def test_adam_step_matches_torch(ctx):
+@pytest.mark.parametrize("layers", [1, 2, 3])
+def test_adam_step_matches_torch(ctx, layers):
     torch = pytest.importorskip("torch")
-    m, mu, sd, rng = random_model(ctx, seed=7)
+    m, mu, sd, rng = random_model(ctx, seed=7, layers=layers)
     n = 256
     f = (rng.uniform(-2, 2, (n, 16)) * sd + mu).astype(np.float32)
     tau = rng.uniform(0.0, 1.5, n).astype(np.float32)
@@ -103,6 +118,8 @@ def test_adam_step_matches_torch(ctx):
     big = np.abs(g) > 1e-5  # the first Adam step is lr*sign(g) there
     np.testing.assert_allclose(p1[big], ref[big], rtol=0, atol=2e-6)
     np.testing.assert_allclose(m1[big], 0.1 * g[big], rtol=2e-3, atol=1e-9)
+    lo, hi = FROZEN[layers]  # unused layers: never updated, moments stay zero
+    assert not p1[lo:hi].any() and not m1[lo:hi].any() and not v1[lo:hi].any()
 
 
 def synthetic_set(n, seed=11):
@@ -121,18 +138,30 @@ def test_training_reduces_loss(ctx):
     assert losses[-20:].mean() < 0.2 * losses[:20].mean(), (losses[:5], losses[-5:])
 
 
-def test_checkpoint_resume_is_bit_identical(ctx, tmp_path):
-    m = surrogate.SunMLP(ctx, seed=13)
+@pytest.mark.parametrize("layers", [2, 3])
+def test_checkpoint_resume_is_bit_identical(ctx, tmp_path, layers):
+    import zlib
+    m = surrogate.SunMLP(ctx, seed=13, hidden_layers=layers)
     f, tau = synthetic_set(16384, seed=2)
     m.fit_normalization(f, tau)
     m.train(f, tau, steps=120, batch=2048, lr=1e-3, sigma=2.0)
     path = str(tmp_path / "sun.ckpt")
     m.save(path)
     r = surrogate.SunMLP.load(ctx, path)
+    assert r.hidden_layers == layers
     a, b = m.get_params(), r.get_params()
     for x, y in zip(a[:3], b[:3]):
         assert np.array_equal(x, y)
     assert a[3] == b[3] == 120
+    if layers == 3:
+        # a version-1 file (no layer count: three hidden layers) still loads
+        data = open(path, "rb").read()
+        body = data[:8] + (1).to_bytes(4, "little") + data[12:24] + data[28:-4]
+        old = str(tmp_path / "v1.ckpt")
+        open(old, "wb").write(body + zlib.crc32(body).to_bytes(4, "little"))
+        o = surrogate.SunMLP.load(ctx, old)
+        assert o.hidden_layers == 3
+        assert np.array_equal(o.get_params()[0], a[0]) and o.get_params()[3] == 120
     m.train(f, tau, steps=70, batch=2048, lr=1e-3, sigma=2.0)
     r.train(f, tau, steps=70, batch=2048, lr=1e-3, sigma=2.0)
     assert np.array_equal(m.get_params()[0], r.get_params()[0])
@@ -149,8 +178,8 @@ def test_checkpoint_resume_is_bit_identical(ctx, tmp_path):
         surrogate.SunMLP.load(ctx, bad)
 
 
-@pytest.mark.parametrize("batch", [2048, 19584])
-def test_fused_adam_matches_separate_launch(ctx, batch):
+@pytest.mark.parametrize("batch,layers", [(2048, 1), (2048, 2), (2048, 3), (19584, 2)])
+def test_fused_adam_matches_separate_launch(ctx, batch, layers):
     """Adam inside the training launch (a grid barrier, one launch per step)
     and Adam as its own launch give identical bits: parameters, moments, step
     and per-step losses, over graph-replayed and direct steps.  19584 rows are
@@ -162,7 +191,7 @@ def test_fused_adam_matches_separate_launch(ctx, batch):
     steps = 75  # one direct step, a 50-step graph replay, 24 direct steps
     runs = []
     for separate in (False, True):
-        m = surrogate.SunMLP(ctx, seed=21)
+        m = surrogate.SunMLP(ctx, seed=21, hidden_layers=layers)
         m.fit_normalization(f, tau)
         n0 = ctx.launch_count
         losses = m.train(f, tau, steps=steps, batch=batch, lr=1e-3, sigma=2.0,

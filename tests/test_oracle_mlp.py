@@ -6,7 +6,7 @@ import pytest
 from oracle import oracle as O
 
 
-def rand_model(seed=0):
+def rand_model(seed=0, layers=3):
     rng = np.random.default_rng(seed)
     P = np.zeros(O.OracleMLP.NPARAM)
     P[0:1024] = rng.uniform(-0.6, 0.6, 1024)
@@ -19,16 +19,41 @@ def rand_model(seed=0):
     P[9472] = 0.1
     mu = rng.uniform(-1, 1, 16)
     sd = rng.uniform(0.5, 2, 16)
-    return O.OracleMLP(P, mu, sd, tau_scale=0.7), rng
+    return O.OracleMLP(P, mu, sd, tau_scale=0.7, layers=layers), rng
 
 
-def test_gradient_matches_central_differences():
-    m, rng = rand_model()
+# blocks [lo, hi) of the hidden layers a network of `layers` does not use
+FROZEN = {1: (1088, 9408), 2: (5248, 9408), 3: (0, 0)}
+
+
+def numpy_forward(m, f):
+    """Independent restatement: h <- silu(W h + b) per hidden layer, y = W4 h + b4."""
+    P = m.P
+    h = (f - m.mu) / m.sd
+    blocks = [(0, 1024, 1088, 16), (1088, 5184, 5248, 64), (5248, 9344, 9408, 64)]
+    for w0, b0, b1, nin in blocks[:m.layers]:
+        z = h @ P[w0:b0].reshape(64, nin).T + P[b0:b1]
+        h = z / (1.0 + np.exp(-z))
+    return h @ P[9408:9472] + P[9472]
+
+
+@pytest.mark.parametrize("layers", [1, 2, 3])
+def test_forward_matches_numpy(layers):
+    m, rng = rand_model(3, layers)
+    f = rng.uniform(-2, 2, (40, 16))
+    np.testing.assert_allclose(m.forward(f), numpy_forward(m, f), rtol=1e-12, atol=1e-13)
+
+
+@pytest.mark.parametrize("layers", [1, 2, 3])
+def test_gradient_matches_central_differences(layers):
+    m, rng = rand_model(0, layers)
     f = rng.uniform(-2, 2, (24, 16))
     tau = rng.uniform(0, 2, 24)
     sigma = 1.5
     loss, g = m.loss_grad(f, tau, sigma)
     assert loss > 0
+    lo, hi = FROZEN[layers]
+    assert not g[lo:hi].any()  # unused layers: exactly zero
     idx = list(rng.choice(9473, 60, replace=False)) + [0, 1024, 1088, 5248, 9408, 9472]
     h = 1e-6
     for i in idx:
@@ -40,8 +65,9 @@ def test_gradient_matches_central_differences():
         assert g[i] == pytest.approx(num, rel=1e-5, abs=1e-9), i
 
 
-def test_forward_consistent_with_loss():
-    m, rng = rand_model(1)
+@pytest.mark.parametrize("layers", [1, 2, 3])
+def test_forward_consistent_with_loss(layers):
+    m, rng = rand_model(1, layers)
     f = rng.uniform(-2, 2, (5, 16))
     y = m.forward(f)
     sigma = 2.0
