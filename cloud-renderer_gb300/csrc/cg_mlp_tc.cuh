@@ -4,11 +4,12 @@
 // fused renderer (k_render_tc.cu): the weight tiles a CTA stages in shared
 // memory, one layer's MMA issue, and one layer's epilogue for a thread's row.
 //
-// Network tiles (bytes from a 1024-aligned base, NET_BYTES in all):
-//   W2, W3   64 x 128 B, 128B-swizzled K-major (K = 64)
+// Network tiles of a layout for up to NL hidden layers (Net<NL>; bytes from
+// a 1024-aligned base, Net<NL>::BYTES in all):
+//   W2, W3   64 x 128 B, 128B-swizzled K-major (K = 64), present for NL >= 2, 3
 //   W1       64 x 32 B, 32B-swizzled (K = 16)
 //   ONES     one 8-row 32B-swizzled atom, every row (1, 1, 0, ...)
-//   BIAS     3 x (64 x 32 B) 32B-swizzled: row n = (b_hi[n], b_lo[n], 0, ...)
+//   BIAS     NL x (64 x 32 B) 32B-swizzled: row n = (b_hi[n], b_lo[n], 0, ...)
 // Layers 1-3 run on weights and biases pre-scaled by 1/2 (exact in FP16 and
 // FP32), so the accumulator holds z/2 and SiLU is z/2 * (1 + tanh(z/2)).  The
 // bias enters as one more K = 16 MMA: the ones column against the bias split
@@ -24,12 +25,17 @@
 
 namespace mlptc {
 
-constexpr int NET_W2 = 0;
-constexpr int NET_W3 = 8192;
-constexpr int NET_W1 = 16384;
-constexpr int NET_ONES = NET_W1 + 2048;
-constexpr int NET_BIAS = NET_ONES + 256;
-constexpr int NET_BYTES = NET_BIAS + 3 * 2048;
+template <int NL>
+struct Net {
+    static constexpr int W2 = 0;
+    static constexpr int W3 = 8192;
+    static constexpr int W1 = 8192 * (NL - 1);
+    static constexpr int ONES = W1 + 2048;
+    static constexpr int BIAS = ONES + 256;
+    static constexpr int BYTES = BIAS + NL * 2048;
+    static_assert(NL >= 1 && NL <= MLP_MAX_LAYERS, "hidden layers");
+    static_assert(W1 % 256 == 0 && ONES % 256 == 0 && BIAS % 256 == 0, "SW32 alignment");
+};
 constexpr int ACT_BYTES = 128 * 128;  // one activation tile
 
 constexpr uint32_t IDESC = tc::idesc_f16_f32(128, 64);
@@ -50,22 +56,24 @@ __device__ __forceinline__ void stage_row(uint8_t* tile, int r, const __half* sr
     }
 }
 
-// The model's hidden-layer weights (W1 .. W_layers) scaled by 1/2, the ones
-// column (8 rows) and the split half-scaled biases into the network tiles at
-// `net`; threads t = 0 .. n-1.
+// The model's hidden-layer weights (W1 .. W_layers, m.layers <= NL) scaled by
+// 1/2, the ones column (8 rows) and the split half-scaled biases into the
+// Net<NL> tiles at `net`; threads t = 0 .. n-1.
+template <int NL>
 __device__ __forceinline__ void stage_network(uint8_t* net, const MlpDev& m, int t, int n) {
+    using L = Net<NL>;
     for (int r = t; r < 64; r += n) {
-        stage_row<2>(net + NET_W1, r, m.w16 + MLP_H_W1 + r * 16);
-        if (m.layers >= 2) stage_row<8>(net + NET_W2, r, m.w16 + MLP_H_W2 + r * 64);
-        if (m.layers >= 3) stage_row<8>(net + NET_W3, r, m.w16 + MLP_H_W3 + r * 64);
+        stage_row<2>(net + L::W1, r, m.w16 + MLP_H_W1 + r * 16);
+        if (NL >= 2 && m.layers >= 2) stage_row<8>(net + L::W2, r, m.w16 + MLP_H_W2 + r * 64);
+        if (NL >= 3 && m.layers >= 3) stage_row<8>(net + L::W3, r, m.w16 + MLP_H_W3 + r * 64);
     }
     if (t < 8) {
         const __half one = __float2half_rn(1.f);
         const uint32_t ones =
             (uint32_t)__half_as_ushort(one) | ((uint32_t)__half_as_ushort(one) << 16);
-        *reinterpret_cast<uint4*>(net + NET_ONES + tc::sw32_offset(t, 0)) =
+        *reinterpret_cast<uint4*>(net + L::ONES + tc::sw32_offset(t, 0)) =
             make_uint4(ones, 0u, 0u, 0u);
-        *reinterpret_cast<uint4*>(net + NET_ONES + tc::sw32_offset(t, 1)) =
+        *reinterpret_cast<uint4*>(net + L::ONES + tc::sw32_offset(t, 1)) =
             make_uint4(0u, 0u, 0u, 0u);
     }
     for (int i = t; i < m.layers * 64; i += n) {
@@ -73,7 +81,7 @@ __device__ __forceinline__ void stage_network(uint8_t* net, const MlpDev& m, int
         const float hb = m.k.hb[i];
         const __half hi = __float2half_rn(hb);
         const __half lo = __float2half_rn(hb - __half2float(hi));
-        uint8_t* tile = net + NET_BIAS + 2048 * l;
+        uint8_t* tile = net + L::BIAS + 2048 * l;
         *reinterpret_cast<uint4*>(tile + tc::sw32_offset(r, 0)) = make_uint4(
             (uint32_t)__half_as_ushort(hi) | ((uint32_t)__half_as_ushort(lo) << 16), 0u, 0u, 0u);
         *reinterpret_cast<uint4*>(tile + tc::sw32_offset(r, 1)) = make_uint4(0u, 0u, 0u, 0u);
@@ -82,20 +90,22 @@ __device__ __forceinline__ void stage_network(uint8_t* net, const MlpDev& m, int
 
 // Issue one layer (one thread) into tensor memory at d_tmem and commit it to
 // `bar`: the K slices of the activation tile at a_addr against the layer's
-// weights, then the bias slice.  The ones operand is a single 8-row atom read
-// by all 16 row groups (stride byte offset 0).
+// weights (Net<NL> tiles at net_addr), then the bias slice.  The ones operand
+// is a single 8-row atom read by all 16 row groups (stride byte offset 0).
+template <int NL>
 __device__ __forceinline__ void issue_layer(int layer, uint32_t d_tmem, uint32_t a_addr,
                                             uint32_t net_addr, uint64_t* bar) {
+    using L = Net<NL>;
     if (layer == 0) {
-        tc::mma_f16(d_tmem, tc::desc_sw128(a_addr), tc::desc_sw32(net_addr + NET_W1), IDESC, 0u);
+        tc::mma_f16(d_tmem, tc::desc_sw128(a_addr), tc::desc_sw32(net_addr + L::W1), IDESC, 0u);
     } else {
-        const uint32_t w_addr = net_addr + (layer == 1 ? NET_W2 : NET_W3);
+        const uint32_t w_addr = net_addr + (layer == 1 ? L::W2 : L::W3);
         for (int k = 0; k < 4; ++k)
             tc::mma_f16(d_tmem, tc::desc_sw128(a_addr + 32u * k),
                         tc::desc_sw128(w_addr + 32u * k), IDESC, k > 0 ? 1u : 0u);
     }
-    tc::mma_f16(d_tmem, tc::desc_sw32(net_addr + NET_ONES, 0u),
-                tc::desc_sw32(net_addr + NET_BIAS + 2048u * layer), IDESC, 1u);
+    tc::mma_f16(d_tmem, tc::desc_sw32(net_addr + L::ONES, 0u),
+                tc::desc_sw32(net_addr + L::BIAS + 2048u * layer), IDESC, 1u);
     tc::mma_commit(bar);
 }
 

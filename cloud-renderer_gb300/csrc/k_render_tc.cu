@@ -80,7 +80,9 @@ struct Rec {
 // shared memory map (bytes from the 1024-aligned base)
 constexpr int OFF_ACT = 0;
 constexpr int OFF_NET = OFF_ACT + mlptc::ACT_BYTES;
-constexpr int OFF_POS = OFF_NET + mlptc::NET_BYTES;          // float4 [RING * 128]
+// the three-layer network layout (a model of any depth runs in it)
+using RtNet = mlptc::Net<MLP_MAX_LAYERS>;
+constexpr int OFF_POS = OFF_NET + RtNet::BYTES;              // float4 [RING * 128]
 constexpr int OFF_META = OFF_POS + RT_RING * 128 * 16;        // uint2 [RING * 128]
 constexpr int OFF_REC = OFF_META + RT_RING * 128 * 8;         // Rec [PRODUCERS][RECS]
 constexpr int OFF_BAR = OFF_REC + RT_PRODUCERS * RT_RECS * (int)sizeof(Rec);
@@ -350,7 +352,7 @@ __global__ void __launch_bounds__(RT_THREADS, RT_CTAS_PER_SM)
     S.w = reinterpret_cast<unsigned*>(base + OFF_WORDS);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-    mlptc::stage_network(S.net, m, tid, RT_THREADS);
+    mlptc::stage_network<MLP_MAX_LAYERS>(S.net, m, tid, RT_THREADS);
     for (int i = tid; i < RT_PRODUCERS * RT_RECS; i += RT_THREADS) S.rec[i].busy = 0u;
     // the shared words (not W_TMEM: the allocation below writes it)
     if (tid < W_COUNT && tid != W_TMEM) S.w[tid] = tid == W_END ? 0xFFFFFFFFu : 0u;
@@ -462,7 +464,8 @@ __global__ void __launch_bounds__(RT_THREADS, RT_CTAS_PER_SM)
             if (ld_volatile(S.w + W_STOP) || ld_volatile(S.w + W_ABORT)) break;
             tc::fence_after_sync();
             if (lane == 0)
-                mlptc::issue_layer((int)(issued % (unsigned)m.layers), tmem, a_addr, net_addr,
+                mlptc::issue_layer<MLP_MAX_LAYERS>((int)(issued % (unsigned)m.layers), tmem, a_addr,
+                                                   net_addr,
                                    S.mma_done);
             issued++;
             __syncwarp();

@@ -43,13 +43,21 @@ namespace {
 
 constexpr uint32_t TC_TMEM_COLS = 64;
 constexpr uint64_t TC_WAIT_NS = 1000000000ull;  // 1 s: a wait longer than this is a fault
-// shared memory map (bytes from the 1024-aligned base)
-constexpr int CTAS_PER_SM = 5;
-constexpr int OFF_ACT = 0;                     // 128 x 128 B activation tile (SW128)
-constexpr int OFF_NET = 16384;                 // the network tiles (cg_mlp_tc.cuh)
-constexpr int OFF_BAR = OFF_NET + mlptc::NET_BYTES;  // mbarrier + tensor-memory address
-constexpr int SMEM_USED = OFF_BAR + 32;
-constexpr int SMEM_BYTES = SMEM_USED + 1024;  // + alignment slack
+// CTAs per SM by depth: the register budget (__launch_bounds__) and the
+// shared memory (the network tiles of the model's layers) allow five for
+// three hidden layers and SHALLOW_CTAS_PER_SM for fewer
+constexpr int SHALLOW_CTAS_PER_SM = 6;
+template <int NL>
+constexpr int ctas_per_sm() { return NL >= 3 ? 5 : SHALLOW_CTAS_PER_SM; }
+// shared memory map of k_mlp_infer_tc (bytes from the 1024-aligned base)
+constexpr int OFF_ACT = 0;      // 128 x 128 B activation tile (SW128)
+constexpr int OFF_NET = 16384;  // the network tiles (cg_mlp_tc.cuh)
+template <int NL>
+struct InferSmem {
+    static constexpr int OFF_BAR = OFF_NET + mlptc::Net<NL>::BYTES;  // mbarrier + TMEM address
+    static constexpr int BYTES = OFF_BAR + 32 + 1024;                // + alignment slack
+    static_assert((BYTES + 1024) * ctas_per_sm<NL>() <= 228 * 1024, "infer shared memory");
+};
 
 // The exact cone for a sample whose features left the trained range (rare):
 // kept out of line so that the hot loop's registers are not sized for it.
@@ -131,12 +139,15 @@ __device__ __forceinline__ void report_failure(uint64_t* bar, unsigned phase, bo
 // stream, sharing one copy of the network tiles (so that more groups fit an
 // SM's shared memory than CTAs of one group would).
 constexpr int SHADE_GROUPS = 1;
-constexpr int SHADE_CTAS_PER_SM = CTAS_PER_SM;
 constexpr uint32_t SHADE_TMEM_COLS = SHADE_GROUPS == 1 ? 64u : (SHADE_GROUPS == 2 ? 128u : 256u);
 constexpr int SH_OFF_NET = SHADE_GROUPS * mlptc::ACT_BYTES;
-constexpr int SH_OFF_BAR = SH_OFF_NET + mlptc::NET_BYTES;  // bar[G], tmem slot, claim[G]
-constexpr int SH_SMEM_BYTES = SH_OFF_BAR + 8 * SHADE_GROUPS + 4 + 4 * SHADE_GROUPS + 1024;
-static_assert(SH_SMEM_BYTES * SHADE_CTAS_PER_SM <= 227 * 1024, "shade kernel shared memory");
+template <int NL>
+struct ShadeSmem {
+    static constexpr int OFF_BAR = SH_OFF_NET + mlptc::Net<NL>::BYTES;  // bar[G], tmem slot, claim[G]
+    static constexpr int BYTES = OFF_BAR + 8 * SHADE_GROUPS + 4 + 4 * SHADE_GROUPS + 1024;
+    static_assert((BYTES + 1024) * ctas_per_sm<NL>() <= 228 * 1024, "shade shared memory");
+    static_assert(SHADE_TMEM_COLS * ctas_per_sm<NL>() <= 512, "tensor memory");
+};
 
 // The group's barrier (named barrier 1 + g, 128 threads) that also agrees on
 // a failed wait of any of its threads.
@@ -163,7 +174,7 @@ __device__ __forceinline__ bool group_sync_for_mma(int g, bool bad) {
 }
 
 template <int FMT, int NL>
-__global__ void __launch_bounds__(128 * SHADE_GROUPS, SHADE_CTAS_PER_SM)
+__global__ void __launch_bounds__(128 * SHADE_GROUPS, ctas_per_sm<NL>())
     k_shade_mlp_tc(const __grid_constant__ VolDesc vd, const __grid_constant__ TraceParams tp,
                    const __grid_constant__ ConeSchedule cone, const __grid_constant__ MlpDev m,
                    const __grid_constant__ FeatGeom geo, SampleBuf sb,
@@ -174,11 +185,12 @@ __global__ void __launch_bounds__(128 * SHADE_GROUPS, SHADE_CTAS_PER_SM)
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int g = tid >> 7, r = tid & 127;  // group, row of the group's tile
     uint8_t* act = base + g * mlptc::ACT_BYTES;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(base + SH_OFF_BAR) + g;
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(base + SH_OFF_BAR + 8 * SHADE_GROUPS);
-    unsigned* s_claim = reinterpret_cast<unsigned*>(base + SH_OFF_BAR + 8 * SHADE_GROUPS + 4) + g;
+    constexpr int OB = ShadeSmem<NL>::OFF_BAR;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(base + OB) + g;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(base + OB + 8 * SHADE_GROUPS);
+    unsigned* s_claim = reinterpret_cast<unsigned*>(base + OB + 8 * SHADE_GROUPS + 4) + g;
 
-    mlptc::stage_network(base + SH_OFF_NET, m, tid, blockDim.x);
+    mlptc::stage_network<NL>(base + SH_OFF_NET, m, tid, blockDim.x);
     if (r == 0) {
         tc::mbar_init(bar, 1);
         tc::fence_mbar_init();
@@ -237,7 +249,7 @@ __global__ void __launch_bounds__(128 * SHADE_GROUPS, SHADE_CTAS_PER_SM)
                 break;
             }
             if (r == 0) {
-                mlptc::issue_layer(layer, tmem, a_addr, net_addr, bar);
+                mlptc::issue_layer<NL>(layer, tmem, a_addr, net_addr, bar);
                 // claim the tile after next (read by the group after the next sync)
                 if (layer == 0) *s_claim = 2u * streams + (unsigned)atomicAdd(status + 3, 1ull);
             }
@@ -321,17 +333,17 @@ __global__ void __launch_bounds__(128 * SHADE_GROUPS, SHADE_CTAS_PER_SM)
 // without the sample fetches: 128-row tiles at a static stride, the same
 // staged weights, layers, epilogues and bounded waits.
 template <int NL>
-__global__ void __launch_bounds__(128, CTAS_PER_SM)
+__global__ void __launch_bounds__(128, ctas_per_sm<NL>())
     k_mlp_infer_tc(const __grid_constant__ MlpDev m, const float* feat, int n, float* out,
                    unsigned long long* status) {
     extern __shared__ uint8_t smem_raw[];
     const uint32_t raw = tc::smem_addr(smem_raw);
     uint8_t* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
     uint8_t* act = base + OFF_ACT;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(base + OFF_BAR);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(base + OFF_BAR + 8);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(base + InferSmem<NL>::OFF_BAR);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(base + InferSmem<NL>::OFF_BAR + 8);
     const int tid = threadIdx.x, warp = tid >> 5;
-    mlptc::stage_network(base + OFF_NET, m, tid, blockDim.x);
+    mlptc::stage_network<NL>(base + OFF_NET, m, tid, blockDim.x);
     if (tid == 0) {
         tc::mbar_init(bar, 1);
         tc::fence_mbar_init();
@@ -375,7 +387,7 @@ __global__ void __launch_bounds__(128, CTAS_PER_SM)
                 break;
             }
             if (tid == 0)
-                mlptc::issue_layer(layer, tmem, a_addr, net_addr, bar);
+                mlptc::issue_layer<NL>(layer, tmem, a_addr, net_addr, bar);
             bad = __any_sync(0xffffffffu, !tc::mbar_wait(bar, phase, TC_WAIT_NS));
             if (!bad) phase ^= 1u;
             tc::fence_after_sync();
@@ -426,32 +438,32 @@ cudaError_t launch_mlp_infer(const MlpDev& m, const float* feat, int n, float* o
                              unsigned long long* status, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     if (m.layers < 1 || m.layers > MLP_MAX_LAYERS) return cudaErrorInvalidValue;
-    // the shared-memory attributes and the grid are set once per device
-    static std::atomic<int> grid[64];
-    const void* fns[MLP_MAX_LAYERS] = {(const void*)k_mlp_infer_tc<1>,
-                                       (const void*)k_mlp_infer_tc<2>,
-                                       (const void*)k_mlp_infer_tc<3>};
+    // the shared-memory attributes and the SM count are set up once per device
+    static std::atomic<int> sm_count[64];
+    using InferFn = void (*)(MlpDev, const float*, int, float*, unsigned long long*);
+    const InferFn fns[MLP_MAX_LAYERS] = {k_mlp_infer_tc<1>, k_mlp_infer_tc<2>, k_mlp_infer_tc<3>};
+    const int smem[MLP_MAX_LAYERS] = {InferSmem<1>::BYTES, InferSmem<2>::BYTES,
+                                      InferSmem<3>::BYTES};
+    const int per_sm[MLP_MAX_LAYERS] = {ctas_per_sm<1>(), ctas_per_sm<2>(), ctas_per_sm<3>()};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-    if (!grid[dev].load(std::memory_order_acquire)) {
-        for (const void* fn : fns) {
-            e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (!sm_count[dev].load(std::memory_order_acquire)) {
+        for (int i = 0; i < MLP_MAX_LAYERS; ++i) {
+            e = cudaFuncSetAttribute((const void*)fns[i],
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, smem[i]);
             if (e != cudaSuccess) return e;
         }
         int sms = 0;
         e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (e != cudaSuccess) return e;
-        grid[dev].store(sms * CTAS_PER_SM, std::memory_order_release);
+        sm_count[dev].store(sms, std::memory_order_release);
     }
+    const int L = m.layers - 1;
     const int ntiles = (n + 127) / 128;
-    const int blocks = std::min(grid[dev].load(std::memory_order_acquire), ntiles);
-    switch (m.layers) {
-        case 1: k_mlp_infer_tc<1><<<blocks, 128, SMEM_BYTES, st>>>(m, feat, n, out, status); break;
-        case 2: k_mlp_infer_tc<2><<<blocks, 128, SMEM_BYTES, st>>>(m, feat, n, out, status); break;
-        default: k_mlp_infer_tc<3><<<blocks, 128, SMEM_BYTES, st>>>(m, feat, n, out, status); break;
-    }
+    const int blocks = std::min(sm_count[dev].load(std::memory_order_acquire) * per_sm[L], ntiles);
+    fns[L]<<<blocks, 128, smem[L], st>>>(m, feat, n, out, status);
     return cudaGetLastError();
 }
 
@@ -460,36 +472,40 @@ cudaError_t launch_shade_mlp_tc(VolDesc vd, CamDesc cam, TraceParams tp, const M
     (void)cam;
     ConeSchedule cone = make_cone_schedule(vd, tp);
     const FeatGeom geo = feat_geom(vd, m);
-    // one persistent wave: CTAS_PER_SM CTAs per SM (the register and
-    // shared-memory budgets of __launch_bounds__; 64 tensor-memory columns each)
-    // (the per-device launch shape and the shared-memory attribute are
-    // configured once; atomics keep concurrent host threads well-defined)
+    // (the shared-memory attributes and the SM count are configured once per
+    // device; atomics keep concurrent host threads well-defined)
     if (m.layers < 1 || m.layers > MLP_MAX_LAYERS) return cudaErrorInvalidValue;
-    static std::atomic<int> grid[64];
+    static std::atomic<int> sm_count[64];
     using ShadeFn = void (*)(VolDesc, TraceParams, ConeSchedule, MlpDev, FeatGeom, SampleBuf,
                              unsigned long long*);
     const ShadeFn fns[2][MLP_MAX_LAYERS] = {
         {k_shade_mlp_tc<0, 1>, k_shade_mlp_tc<0, 2>, k_shade_mlp_tc<0, 3>},
         {k_shade_mlp_tc<1, 1>, k_shade_mlp_tc<1, 2>, k_shade_mlp_tc<1, 3>}};
+    const int smem[MLP_MAX_LAYERS] = {ShadeSmem<1>::BYTES, ShadeSmem<2>::BYTES,
+                                      ShadeSmem<3>::BYTES};
+    const int per_sm[MLP_MAX_LAYERS] = {ctas_per_sm<1>(), ctas_per_sm<2>(), ctas_per_sm<3>()};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-    if (!grid[dev].load(std::memory_order_acquire)) {
-        for (const auto& row : fns)
-            for (ShadeFn fn : row) {
-                e = cudaFuncSetAttribute((const void*)fn,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, SH_SMEM_BYTES);
+    if (!sm_count[dev].load(std::memory_order_acquire)) {
+        for (int f = 0; f < 2; ++f)
+            for (int i = 0; i < MLP_MAX_LAYERS; ++i) {
+                e = cudaFuncSetAttribute((const void*)fns[f][i],
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem[i]);
                 if (e != cudaSuccess) return e;
             }
         int sms = 0;
         e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (e != cudaSuccess) return e;
-        grid[dev].store(sms * SHADE_CTAS_PER_SM, std::memory_order_release);
+        sm_count[dev].store(sms, std::memory_order_release);
     }
-    const int blocks = grid[dev].load(std::memory_order_acquire);
-    fns[vd.fmt == 0 ? 0 : 1][m.layers - 1]<<<blocks, 128 * SHADE_GROUPS, SH_SMEM_BYTES, st>>>(
-        vd, tp, cone, m, geo, sb, status);
+    // one persistent wave: ctas_per_sm<NL>() CTAs per SM (64 tensor-memory
+    // columns each)
+    const int L = m.layers - 1;
+    const int blocks = sm_count[dev].load(std::memory_order_acquire) * per_sm[L];
+    fns[vd.fmt == 0 ? 0 : 1][L]<<<blocks, 128 * SHADE_GROUPS, smem[L], st>>>(vd, tp, cone, m, geo,
+                                                                            sb, status);
     return cudaGetLastError();
 }
 
