@@ -1190,10 +1190,12 @@ extern "C" cg_status cg_render(cg_context* ctx, const cg_volume* v, const cg_cam
         SampleBuf sb;
         st = ensure_samples(ctx, cam->width, cam->height, params->view_steps, sb);
         if (st != CG_OK) return st;
+        // the shading status block is cleared before the march, so that the
+        // shading kernel directly follows it (a dependent launch)
+        if (params->use_mlp) CG_CUDA(cudaMemsetAsync(ctx->fallbacks.p, 0, 32, s));
         CG_LAUNCH(ctx, launch_march(vd, cd, tp, sb, out, params->use_mlp != 0, s));
         stage_mark(ctx, s, "march");
         if (params->use_mlp) {
-            CG_CUDA(cudaMemsetAsync(ctx->fallbacks.p, 0, 32, s));
             ctx->shaded_valid = true;
             CG_LAUNCH(ctx, launch_shade_mlp_tc(vd, cd, tp, md, sb,
                                                ctx->fallbacks.as<unsigned long long>(), s));

@@ -17,6 +17,35 @@
 #define CG_FUSED_MIPS 3      // levels produced inside the splat kernel
 #define CG_SPLAT_CHUNK 256   // boards staged in shared memory per pass
 
+// ---- programmatic dependent launch: a kernel launched with
+// launch_dependent() may start while the kernel before it on the stream is
+// still running; it runs its independent prologue, then grid_dep_wait()
+// blocks until that kernel has completed and its memory is visible.  A
+// kernel calls grid_dep_trigger() once its dependent may be scheduled (else
+// at its exit).  Both are no-ops for an ordinary launch.
+#ifdef __CUDACC__
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_trigger() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_dependent(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                                    cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+#endif
+
 // Sun-view frame: lookAt basis + ortho window (Sun::update, Sun.hpp:26-43).
 struct SunFrame {
     float eye[3], right[3], up[3], fwd[3], t[3];

@@ -72,6 +72,9 @@ __device__ __forceinline__ bool pixel_ray(const CamDesc& cam, const VolDesc& vd,
 template <int FMT, bool HW>
 __global__ void __launch_bounds__(256) k_march(VolDesc vd, CamDesc cam, TraceParams tp,
                                                SampleBuf sb, float4* out) {
+    // the shading pass may be scheduled once every march CTA has started: its
+    // CTAs stage their network while the last wave of the march runs
+    grid_dep_trigger();
     int px, py;
     tile_pixel(px, py);
     const int lane = threadIdx.x & 31;
@@ -251,6 +254,7 @@ __global__ void __launch_bounds__(128) k_accumulate(CamDesc cam, TraceParams tp,
                                                     int regions, int tiles_x, int view_steps,
                                                     const float4* img, float4* dst) {
     const int region = blockIdx.x * 4 + (threadIdx.x >> 5);
+    grid_dep_wait();  // the contributions of the shading pass
     if (region >= regions) return;
     const int lane = threadIdx.x & 31;
     const unsigned below = (1u << lane) - 1u;
@@ -325,9 +329,8 @@ cudaError_t launch_shade_exact(VolDesc vd, CamDesc cam, TraceParams tp, SampleBu
 cudaError_t launch_accumulate(CamDesc cam, TraceParams tp, SampleBuf sb, const float4* img,
                               float4* dst, cudaStream_t st) {
     const int regions = regions_of(cam), tiles_x = (cam.W + 15) / 16;
-    k_accumulate<<<(regions + 3) / 4, 128, 0, st>>>(cam, tp, sb, regions, tiles_x, tp.view_steps,
-                                                    img, dst);
-    return cudaGetLastError();
+    return launch_dependent(k_accumulate, dim3((regions + 3) / 4), dim3(128), 0, st, cam, tp, sb,
+                            regions, tiles_x, (int)tp.view_steps, img, dst);
 }
 
 CG_OOB_TU(k_deferred)

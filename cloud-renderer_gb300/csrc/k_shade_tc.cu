@@ -203,6 +203,7 @@ __global__ void __launch_bounds__(128 * SHADE_GROUPS, ctas_per_sm<NL>())
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
+    grid_dep_wait();  // the march's samples and flat order
     const uint32_t tmem = *tslot + 64u * (uint32_t)g;
     const uint32_t dw = tmem + ((uint32_t)((warp & 3) * 32) << 16);
     const uint32_t a_addr = tc::smem_addr(act);
@@ -504,9 +505,10 @@ cudaError_t launch_shade_mlp_tc(VolDesc vd, CamDesc cam, TraceParams tp, const M
     // columns each)
     const int L = m.layers - 1;
     const int blocks = sm_count[dev].load(std::memory_order_acquire) * per_sm[L];
-    fns[vd.fmt == 0 ? 0 : 1][L]<<<blocks, 128 * SHADE_GROUPS, smem[L], st>>>(vd, tp, cone, m, geo,
-                                                                            sb, status);
-    return cudaGetLastError();
+    // launched as a dependent of the march: the prologue (network tiles,
+    // barrier, tensor memory) overlaps the march's last wave
+    return launch_dependent(fns[vd.fmt == 0 ? 0 : 1][L], dim3(blocks), dim3(128 * SHADE_GROUPS),
+                            (size_t)smem[L], st, vd, tp, cone, m, geo, sb, status);
 }
 
 CG_OOB_TU(k_shade_tc)
