@@ -290,6 +290,7 @@ void context_release(cg_context* ctx) {
     ctx->samples_gl.release();
     ctx->samples_c.release();
     ctx->samples_cnt.release();
+    ctx->samples_alpha.release();
     ctx->fallbacks.release();
     ctx->stats_scratch.release();
     ctx->stats_a.release();
@@ -1193,14 +1194,14 @@ extern "C" cg_status cg_render(cg_context* ctx, const cg_volume* v, const cg_cam
         // the shading status block is cleared before the march, so that the
         // shading kernel directly follows it (a dependent launch)
         if (params->use_mlp) CG_CUDA(cudaMemsetAsync(ctx->fallbacks.p, 0, 32, s));
-        CG_LAUNCH(ctx, launch_march(vd, cd, tp, sb, out, params->use_mlp != 0, s));
+        CG_LAUNCH(ctx, launch_march(vd, cd, tp, sb, params->use_mlp != 0, s));
         stage_mark(ctx, s, "march");
         if (params->use_mlp) {
             ctx->shaded_valid = true;
             CG_LAUNCH(ctx, launch_shade_mlp_tc(vd, cd, tp, md, sb,
                                                ctx->fallbacks.as<unsigned long long>(), s));
             stage_mark(ctx, s, "shade_mlp");
-            CG_LAUNCH(ctx, launch_accumulate(cd, tp, sb, out, dst, s));
+            CG_LAUNCH(ctx, launch_accumulate(cd, tp, sb, dst, s));
             stage_mark(ctx, s, "accumulate");
         } else {
             CG_LAUNCH(ctx, launch_shade_exact(vd, cd, tp, sb, out, s));
@@ -1273,7 +1274,7 @@ extern "C" cg_status cg_march_samples(cg_context* ctx, const cg_volume* v, const
     SampleBuf sb;
     st = ensure_samples(ctx, cam->width, cam->height, params->view_steps, sb);
     if (st != CG_OK) return st;
-    CG_LAUNCH(ctx, launch_march(desc_of(v), cd, tp, sb, ctx->image.as<float4>(), false, s));
+    CG_LAUNCH(ctx, launch_march(desc_of(v), cd, tp, sb, false, s));
     const size_t regions = (size_t)((cam->width + 15) / 16) * ((cam->height + 15) / 16) * 8;
     std::vector<unsigned> cnt(regions);
     CG_CUDA(cudaMemcpyAsync(cnt.data(), sb.count, regions * 4, cudaMemcpyDeviceToHost, s));

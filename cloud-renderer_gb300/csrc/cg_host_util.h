@@ -108,7 +108,7 @@ struct cg_context {
     float noise_ref[3] = {0, 0, 0}, noise_margin[3] = {0, 0, 0};
     NoiseTab noise_tab{};
     // deferred renderer: recorded view samples and the MLP fallback counter
-    DevBuf samples_pw, samples_gl, samples_cnt, samples_c;
+    DevBuf samples_pw, samples_gl, samples_cnt, samples_c, samples_alpha;
     DevBuf fallbacks;  // surrogate render status (see launch_shade_mlp_tc)
     DevBuf stats_scratch, stats_a, stats_ref;  // cg_image_error_stats staging
     // batch render: launch shape, descriptors (host, pinned staging, device

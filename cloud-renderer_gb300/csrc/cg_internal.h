@@ -193,6 +193,7 @@ struct SampleBuf {
     unsigned* flat_total;
     uint2* steps;     // per region, per emitting step: (first slot, lane ballot)
     unsigned* nsteps; // emitting steps per region
+    float* alpha;     // per pixel (row-major, W x H): 1 - T after the march
     int capacity;     // 32 * view_steps
     unsigned long long nslots;  // regions * capacity
 };
@@ -337,8 +338,9 @@ struct TrainArgs {
     AdamArgs adam;
 };
 
-cudaError_t launch_march(VolDesc vd, CamDesc cam, TraceParams tp, SampleBuf sb, float4* out,
-                         bool hw, cudaStream_t st);
+// The view march (writes the samples, the step tables and sb.alpha).
+cudaError_t launch_march(VolDesc vd, CamDesc cam, TraceParams tp, SampleBuf sb, bool hw,
+                         cudaStream_t st);
 cudaError_t launch_shade_exact(VolDesc vd, CamDesc cam, TraceParams tp, SampleBuf sb,
                                float4* out, cudaStream_t st);
 cudaError_t launch_pack_level(VolDesc vd, int l, cudaSurfaceObject_t surf, cudaStream_t st);
@@ -362,10 +364,10 @@ cudaError_t launch_render_mlp_tc(VolDesc vd, CamDesc cam, TraceParams tp, const 
                                  float* contrib, uint2* steps, float4* dst,
                                  unsigned long long* status, cudaStream_t st);
 cudaError_t launch_wait_probe(uint64_t limit_ns, unsigned long long* status, cudaStream_t st);
-// img: the march's image (alpha); dst: where the finished pixels go (img, or
-// a device-addressable host image)
-cudaError_t launch_accumulate(CamDesc cam, TraceParams tp, SampleBuf sb, const float4* img,
-                              float4* dst, cudaStream_t st);
+// dst: where the finished pixels go (a device image, or a device-addressable
+// host image); their alpha comes from the march (sb.alpha)
+cudaError_t launch_accumulate(CamDesc cam, TraceParams tp, SampleBuf sb, float4* dst,
+                              cudaStream_t st);
 cudaError_t launch_mlp_features(VolDesc vd, const MlpDev& m, const float* pos, int n,
                                 const float dir[3], float* out, cudaStream_t st);
 // network evaluation on the tensor cores (k_shade_tc.cu); status[1] |= 1 when

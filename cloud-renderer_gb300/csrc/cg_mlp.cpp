@@ -260,18 +260,22 @@ cg_status ensure_samples(cg_context* ctx, int width, int height, int view_steps,
     // (the padded flat order has at most 31 padding rows per 8 regions)
     const size_t flat = n + 32 * (regions / 8 + 1);
     const size_t idx_words = 2 * regions + 2 + 2 * regions * view_steps + 2 + flat;
+    const size_t pixels = (size_t)width * height;
     if (ctx->samples_pw.bytes < n * 16 || ctx->samples_gl.bytes < n * 8 ||
-        ctx->samples_c.bytes < n * 4 || ctx->samples_cnt.bytes < idx_words * 4) {
+        ctx->samples_c.bytes < n * 4 || ctx->samples_cnt.bytes < idx_words * 4 ||
+        ctx->samples_alpha.bytes < pixels * 4) {
         CG_CUDA(cudaStreamSynchronize(ctx->stream));
         CG_CUDA(ctx->samples_pw.ensure(n * 16));
         CG_CUDA(ctx->samples_gl.ensure(n * 8));
         CG_CUDA(ctx->samples_c.ensure(n * 4));
         CG_CUDA(ctx->samples_cnt.ensure(idx_words * 4));
+        CG_CUDA(ctx->samples_alpha.ensure(pixels * 4));
     }
     CG_CUDA(ctx->fallbacks.ensure(32));
     sb.pos_w = ctx->samples_pw.as<float4>();
     sb.light_lane = ctx->samples_gl.as<float2>();
     sb.contrib = ctx->samples_c.as<float>();
+    sb.alpha = ctx->samples_alpha.as<float>();
     sb.count = ctx->samples_cnt.as<unsigned>();
     sb.nsteps = sb.count + regions;
     sb.flat_total = sb.nsteps + regions;

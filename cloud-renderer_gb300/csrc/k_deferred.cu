@@ -8,7 +8,7 @@
 // lanes whose sample has alpha > 0 append (voxel position, w = T*alpha,
 // light G, lane) to the warp's region of the sample buffer (capacity 32 *
 // view_steps), in (step, lane) order.  The pixel's alpha 1 - T is final after
-// this pass.
+// this pass (one float per pixel; the shading passes write the RGBA image).
 // Exact shading (k_shade_exact): one warp per region, 32 samples at a time,
 // then each pixel sums its own samples in step order (shuffle broadcast),
 // exactly the order of the fused kernel.
@@ -71,7 +71,7 @@ __device__ __forceinline__ bool pixel_ray(const CamDesc& cam, const VolDesc& vd,
 // HW: view samples and noise filtered by the texture unit (surrogate renderer).
 template <int FMT, bool HW>
 __global__ void __launch_bounds__(256) k_march(VolDesc vd, CamDesc cam, TraceParams tp,
-                                               SampleBuf sb, float4* out) {
+                                               SampleBuf sb) {
     // the shading pass may be scheduled once every march CTA has started: its
     // CTAs stage their network while the last wave of the march runs
     grid_dep_trigger();
@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(256) k_march(VolDesc vd, CamDesc cam, TracePar
         sb.count[region] = cnt;
         sb.nsteps[region] = nsteps;
     }
-    if (valid) out[(size_t)py * cam.W + px] = make_float4(0.f, 0.f, 0.f, 1.f - T);
+    if (valid) sb.alpha[(size_t)py * cam.W + px] = 1.f - T;
     // Flat order for the shading pass: the CTA's 8 regions take one contiguous
     // range (reserved with one atomic, padded to whole 32-sample chunks), and
     // every flat row records its sample's slot.
@@ -204,17 +204,15 @@ __device__ __forceinline__ void scatter_chunk(float c, int lj, int m, float& acc
     }
 }
 
-// The pixel's colour C * sun colour with the alpha the march left in `img`,
-// stored to `dst` (`img` itself, or the caller's page-locked host image).
-__device__ __forceinline__ void write_rgb(const float4* img, float4* dst, const CamDesc& cam,
+// The pixel's colour C * sun colour with the alpha the march left in
+// `alpha`, stored to `dst` (a device image or the caller's page-locked host
+// image).
+__device__ __forceinline__ void write_rgb(const float* alpha, float4* dst, const CamDesc& cam,
                                           int px, int py, float C, const TraceParams& tp) {
     if (px < cam.W && py < cam.H) {
         const size_t i = (size_t)py * cam.W + px;
-        float4 v = img[i];
-        v.x = C * tp.sun_color[0];
-        v.y = C * tp.sun_color[1];
-        v.z = C * tp.sun_color[2];
-        dst[i] = v;
+        dst[i] = make_float4(C * tp.sun_color[0], C * tp.sun_color[1], C * tp.sun_color[2],
+                             alpha[i]);
     }
 }
 
@@ -245,14 +243,14 @@ __global__ void __launch_bounds__(128) k_shade_exact(VolDesc vd, CamDesc cam, Tr
     }
     int px, py;
     region_pixel(region, lane, tiles_x, px, py);
-    write_rgb(out, out, cam, px, py, acc + comp, tp);
+    write_rgb(sb.alpha, out, cam, px, py, acc + comp, tp);
 }
 
 // Per region: each pixel sums the contributions of its own samples in step
 // order, locating them through the march's step table (base slot, ballot).
 __global__ void __launch_bounds__(128) k_accumulate(CamDesc cam, TraceParams tp, SampleBuf sb,
                                                     int regions, int tiles_x, int view_steps,
-                                                    const float4* img, float4* dst) {
+                                                    float4* dst) {
     const int region = blockIdx.x * 4 + (threadIdx.x >> 5);
     grid_dep_wait();  // the contributions of the shading pass
     if (region >= regions) return;
@@ -292,25 +290,25 @@ __global__ void __launch_bounds__(128) k_accumulate(CamDesc cam, TraceParams tp,
     }
     int px, py;
     region_pixel(region, lane, tiles_x, px, py);
-    write_rgb(img, dst, cam, px, py, acc + comp, tp);
+    write_rgb(sb.alpha, dst, cam, px, py, acc + comp, tp);
 }
 
 }  // namespace
 
 static int regions_of(const CamDesc& cam) { return ((cam.W + 15) / 16) * ((cam.H + 15) / 16) * 8; }
 
-cudaError_t launch_march(VolDesc vd, CamDesc cam, TraceParams tp, SampleBuf sb, float4* out,
-                         bool hw, cudaStream_t st) {
+cudaError_t launch_march(VolDesc vd, CamDesc cam, TraceParams tp, SampleBuf sb, bool hw,
+                         cudaStream_t st) {
     // the flat-order reservation counter starts from zero on every launch
     cudaError_t e = cudaMemsetAsync(sb.flat_total, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
     dim3 grd((cam.W + 15) / 16, (cam.H + 15) / 16);
     if (hw)
-        k_march<0, true><<<grd, 256, 0, st>>>(vd, cam, tp, sb, out);
+        k_march<0, true><<<grd, 256, 0, st>>>(vd, cam, tp, sb);
     else if (vd.fmt == 0)
-        k_march<0, false><<<grd, 256, 0, st>>>(vd, cam, tp, sb, out);
+        k_march<0, false><<<grd, 256, 0, st>>>(vd, cam, tp, sb);
     else
-        k_march<1, false><<<grd, 256, 0, st>>>(vd, cam, tp, sb, out);
+        k_march<1, false><<<grd, 256, 0, st>>>(vd, cam, tp, sb);
     return cudaGetLastError();
 }
 
@@ -326,11 +324,11 @@ cudaError_t launch_shade_exact(VolDesc vd, CamDesc cam, TraceParams tp, SampleBu
     return cudaGetLastError();
 }
 
-cudaError_t launch_accumulate(CamDesc cam, TraceParams tp, SampleBuf sb, const float4* img,
-                              float4* dst, cudaStream_t st) {
+cudaError_t launch_accumulate(CamDesc cam, TraceParams tp, SampleBuf sb, float4* dst,
+                              cudaStream_t st) {
     const int regions = regions_of(cam), tiles_x = (cam.W + 15) / 16;
     return launch_dependent(k_accumulate, dim3((regions + 3) / 4), dim3(128), 0, st, cam, tp, sb,
-                            regions, tiles_x, (int)tp.view_steps, img, dst);
+                            regions, tiles_x, (int)tp.view_steps, dst);
 }
 
 CG_OOB_TU(k_deferred)
