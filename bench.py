@@ -560,8 +560,9 @@ def run_ours(args):
     plain_achieved = float(sum(alg)) / (sum(trace_ms) / 1e3) / 1e9
     tr_plain = load_traffic("trace_fused_rgba32f")
 
-    # ---- BF16 volume + MLP surrogate (trained here, on the GPU): the default
-    # depth, and a three-hidden-layer model on the same data for comparison
+    # ---- BF16 volume + MLP surrogate (trained here, on the GPU): the named
+    # model (three hidden layers of 64), and a two-hidden-layer model trained
+    # on the same data, reported beside it
     t0 = time.perf_counter()
     feats, taus, mlp = surrogate.training_set(ctx, plain_shader, samples=args.mlp_samples,
                                               scenes=16, seed=1000)
@@ -571,18 +572,18 @@ def run_ours(args):
     losses = mlp.train(feats, taus, args.mlp_steps, batch=16384, lr=1e-3,
                        sigma=plain_shader.densityScale, seed=1000)
     train_s = time.perf_counter() - t0
-    mlp3 = surrogate.SunMLP(ctx, hidden_layers=3)
-    mlp3.copy_config(mlp)
+    mlp2 = surrogate.SunMLP(ctx, hidden_layers=2)
+    mlp2.copy_config(mlp)
     t0 = time.perf_counter()
-    losses3 = mlp3.train(feats, taus, args.mlp_steps, batch=16384, lr=1e-3,
+    losses2 = mlp2.train(feats, taus, args.mlp_steps, batch=16384, lr=1e-3,
                          sigma=plain_shader.densityScale, seed=1000)
-    train3_s = time.perf_counter() - t0
+    train2_s = time.perf_counter() - t0
     feats = taus = None
     vol16 = make_volume(cloudgb.FORMAT_BF16_FP16)
     mlp_shader = cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, **kw)
     learned = run_path(vol16, mlp_shader, args.steps, args.warmup, clocks=True)
-    mlp3_shader = cloudgb.ConeTraceShader(useMlp=True, mlp=mlp3, **kw)
-    learned3 = run_path(vol16, mlp3_shader, args.steps, args.warmup)
+    mlp2_shader = cloudgb.ConeTraceShader(useMlp=True, mlp=mlp2, **kw)
+    learned2 = run_path(vol16, mlp2_shader, args.steps, args.warmup)
     # the same surrogate renderer as one persistent kernel (A/B, same images)
     persistent = run_path(vol16, cloudgb.ConeTraceShader(useMlp=True, mlp=mlp,
                                                          pipeline=_lib.PIPELINE_PERSISTENT, **kw),
@@ -603,13 +604,13 @@ def run_ours(args):
     for k in range(len(cams)):
         ref = np.empty((H, W, 4), np.float32)
         got = np.empty((H, W, 4), np.float32)
-        got3 = np.empty((H, W, 4), np.float32)
+        got2 = np.empty((H, W, 4), np.float32)
         plain_shader.coneTrace(vol32, cams[k], out=ref)
         mlp_shader.coneTrace(vol16, cams[k], out=got)
-        mlp3_shader.coneTrace(vol16, cams[k], out=got3)
+        mlp2_shader.coneTrace(vol16, cams[k], out=got2)
         e = ctx.error_stats(got, ref)  # reduced on the GPU in FP64
         full.append((e["rmse_all"], e["max_abs_all"]))
-        views[k] = {"bf16_mlp": got, "plain_fp32": ref, "bf16_mlp_3_layers": got3}
+        views[k] = {"bf16_mlp": got, "plain_fp32": ref, "bf16_mlp_2_layers": got2}
     chk = oracle_check(wl, views) if (rank == 0 or world == 1) else None
     views = None
     rmse_oracle = chk["bf16_mlp"]["rmse"] if chk else float(max(r for r, _ in full))
@@ -684,13 +685,16 @@ def run_ours(args):
             "data_s": round(data_s, 2), "train_s": round(train_s, 2),
             "train_steps": args.mlp_steps, "train_samples": args.mlp_samples,
             "final_loss": float(np.mean(losses[-100:]))}),
-        "bf16_mlp_3_layers": path_summary(learned3, {
-            "hidden_layers": 3,
-            "rmse_vs_fp64_oracle": chk["bf16_mlp_3_layers"]["rmse"] if chk else None,
-            "max_abs_vs_fp64_oracle": chk["bf16_mlp_3_layers"]["max_abs"] if chk else None,
+        "bf16_mlp_2_layers": path_summary(learned2, {
+            "hidden_layers": 2,
+            "note": "the same surrogate with two hidden layers, trained on the same data (an "
+                    "option of the library, not the named model)",
+            "rmse_vs_fp64_oracle": chk["bf16_mlp_2_layers"]["rmse"] if chk else None,
+            "max_abs_vs_fp64_oracle": chk["bf16_mlp_2_layers"]["max_abs"] if chk else None,
             "worst_view_rmse_vs_fp64_oracle":
-                chk["bf16_mlp_3_layers"]["worst_view_rmse"] if chk else None,
-            "train_s": round(train3_s, 2), "final_loss": float(np.mean(losses3[-100:]))}),
+                chk["bf16_mlp_2_layers"]["worst_view_rmse"] if chk else None,
+            "speedup_frame": round(plain["total_ms"] / learned2["total_ms"], 3),
+            "train_s": round(train2_s, 2), "final_loss": float(np.mean(losses2[-100:]))}),
         "speedup_render": round(plain["render_ms"] / learned["render_ms"], 3),
         "speedup_frame": round(plain["total_ms"] / learned["total_ms"], 3),
         "oracle_check": ({"sample": chk["tiles"], "pixels": chk["pixels"],

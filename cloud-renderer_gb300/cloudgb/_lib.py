@@ -67,7 +67,7 @@ PIPELINE_PERSISTENT = 2
 MLP_FEATURES = 16
 MLP_PARAMS = 9473
 MLP_MAX_LAYERS = 3
-MLP_DEFAULT_LAYERS = 2
+MLP_DEFAULT_LAYERS = 3
 
 
 class cg_mlp_config(ctypes.Structure):

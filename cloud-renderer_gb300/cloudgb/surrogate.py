@@ -31,8 +31,8 @@ DEFAULT_LAYERS = _lib.MLP_DEFAULT_LAYERS
 
 
 class SunMLP:
-    """cg_mlp handle: 16 -> 64 [-> 64 [-> 64]] -> 1, SiLU, with 1, 2 (default)
-    or 3 hidden layers."""
+    """cg_mlp handle: 16 -> 64 [-> 64 [-> 64]] -> 1, SiLU, with 3 (default), 2
+    or 1 hidden layers."""
 
     def __init__(self, ctx, seed=1, handle=None, hidden_layers=None):
         self.ctx = ctx

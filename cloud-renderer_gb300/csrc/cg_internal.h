@@ -205,7 +205,7 @@ struct SampleBuf {
 // created); the parameter vector always has room for three, and the blocks of
 // the layers a model does not use stay zero and are never updated
 #define MLP_MAX_LAYERS 3
-#define MLP_DEFAULT_LAYERS 2
+#define MLP_DEFAULT_LAYERS 3
 // flat FP32 parameter vector: W stored [out][in]
 #define MLP_W1 0
 #define MLP_B1 1024
