@@ -312,6 +312,45 @@ def test_mlp_render_rmse_and_gain(ctx, trained):
     assert t_mlp < t_cheap, (t_mlp, t_cheap)
 
 
+def test_two_layer_model_render(ctx, trained):
+    """The two-hidden-layer surrogate (a library option) trained the same way:
+    its render stays within RMSE 1e-2 of the FP64 oracle and below the
+    half-step exact cone, and it renders faster than the three-layer model."""
+    mlp3 = trained[0]
+    cfg = configs.PLAIN_1080P
+    sh = cloudgb.ConeTraceShader(**workload.build(cfg, boards=8).shader_kwargs())
+    mlp2, losses = surrogate.train_surrogate(ctx, sh, samples=1_000_000, steps=3000,
+                                             batch=16384, scenes=8, seed=1000, hidden_layers=2)
+    assert mlp2.hidden_layers == 2 and mlp3.hidden_layers == 3
+    assert losses[-50:].mean() < losses[:50].mean()
+    wl = workload.build(cfg, width=480, height=270)
+    vol, sun, ov = _pair(ctx, cfg, wl, cloudgb.FORMAT_BF16_FP16)
+    cam = workload.make_camera(wl.cameras[3])
+    kw = wl.shader_kwargs()
+    ref = ov.render(cam, O.params_from_shader(cloudgb.ConeTraceShader(**kw)), sun.direction)
+    img = cloudgb.ConeTraceShader(useMlp=True, mlp=mlp2, **kw).coneTrace(vol, cam)
+    rmse = float(np.sqrt(((img.astype(np.float64) - ref) ** 2).mean()))
+    cheap = cloudgb.ConeTraceShader(**dict(kw, vctSteps=kw["vctSteps"] // 2))
+    rmse_c = float(np.sqrt(((cheap.coneTrace(vol, cam).astype(np.float64) - ref) ** 2).mean()))
+    assert rmse <= 1e-2 and rmse <= rmse_c, (rmse, rmse_c)
+    big = cloudgb.Camera(cam.eye, cam.target, width=1920, height=1080)
+    out = cloudgb.DeviceBuffer(1920 * 1080 * 16)
+
+    def best(model):
+        shader = cloudgb.ConeTraceShader(useMlp=True, mlp=model, **kw)
+        ts = []
+        for _ in range(5):
+            ctx.synchronize()
+            t0 = time.perf_counter()
+            shader.coneTrace(vol, big, out=out)
+            ctx.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return min(ts)
+
+    t2, t3 = best(mlp2), best(mlp3)
+    assert t2 < t3, (t2, t3)
+
+
 @pytest.mark.parametrize("size", [(1920, 1080), (333, 197)])
 def test_persistent_render_matches_deferred(ctx, trained, size):
     """The persistent surrogate renderer (march, tensor-core network and
