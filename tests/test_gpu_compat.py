@@ -2,10 +2,12 @@
 reference-shader fixtures.
 
 Tolerance: the GPU blends front to back in FP32, the oracle back to front in
-FP64; pixel values agree within 1e-3 except for rare fragments whose discard
+FP64; pixel values agree within 1e-4 except for rare fragments whose discard
 test, quad-edge test or noise step count sits on a threshold and resolves
-differently in the two precisions: at most 0.2 % of the values may differ by
-more.
+differently in the two precisions: at most 0.05 % of the values may differ by
+more, and none by more than 1e-3.  Measured on a GB300 over the six fixture
+cases: at most 0.012 % of the values beyond 1e-4 (max 2.2e-4), 99.9th
+percentile below 4e-6.
 """
 import numpy as np
 import pytest
@@ -46,10 +48,11 @@ def shader_of(P):
     return sh
 
 
-def assert_close(img, ref, tol=1e-3, frac=2e-3, what=""):
+def assert_close(img, ref, tol=1e-4, frac=5e-4, cap=1e-3, what=""):
     err = np.abs(np.asarray(img, np.float64) - np.asarray(ref, np.float64))
     bad = float((err > tol).mean())
     assert bad <= frac, f"{what}: {bad:.4%} of values beyond {tol} (max {err.max():.3g})"
+    assert err.max() <= cap, f"{what}: max error {err.max():.3g} beyond {cap}"
 
 
 @pytest.mark.parametrize("name", list(G.CASES))
