@@ -87,9 +87,19 @@ __device__ __forceinline__ void adam_param(const AdamArgs& aa, int p, int step, 
     }
     // explicit roundings (no FMA contraction left to the compiler): the two
     // kernels that inline this must issue the same operations
+    // CTA order, sixteen loads in flight at a time
+    const float* src = aa.partial + p;
+    constexpr size_t STRIDE = MLP_NPARAM + 1;
     float g = 0.f;
-    for (int c = 0; c < aa.nparts; ++c)
-        g = __fadd_rn(g, __ldcg(aa.partial + (size_t)c * (MLP_NPARAM + 1) + p));
+    int c = 0;
+    for (; c + 16 <= aa.nparts; c += 16) {
+        float v[16];
+#pragma unroll
+        for (int u = 0; u < 16; ++u) v[u] = __ldcg(src + (size_t)(c + u) * STRIDE);
+#pragma unroll
+        for (int u = 0; u < 16; ++u) g = __fadd_rn(g, v[u]);
+    }
+    for (; c < aa.nparts; ++c) g = __fadd_rn(g, __ldcg(src + (size_t)c * STRIDE));
     g = __fmul_rn(g, aa.inv_batch);
     if (p == MLP_NPARAM) {
         if (aa.loss_out) aa.loss_out[aa.loss_slot_by_step ? step - aa.loss_base : 0] = g;

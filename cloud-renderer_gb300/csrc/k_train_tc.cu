@@ -2,8 +2,10 @@
 // fifth-generation tensor cores: forward, loss gradient, backward and the
 // per-CTA gradient partials that k_mlp_adam reduces in a fixed order.
 //
-// One CTA = 128 rows of the batch, 4 warps, thread = row.  The network has NL
-// = 1, 2 or 3 hidden layers (a template parameter).  Every GEMM is a
+// One CTA = 128 rows of the batch, 16 warps: four threads per row, each on 16
+// of the 64 columns of every epilogue (warps w, w + 4, w + 8, w + 12 share the
+// tensor-memory lanes 32 (w % 4) ..).  The network has NL = 1, 2 or 3 hidden
+// layers (a template parameter).  Every GEMM is a
 // tcgen05.mma (M = 128, FP16 operands from shared memory, FP32 accumulators
 // in tensor memory) issued by thread 0 and committed to one mbarrier:
 //   forward   z_l = A_l W_l^T + b_l          A_0 = x, A_l = h_l (K = 16, 64)
@@ -13,9 +15,10 @@
 //             the same product; K = the 128 batch rows)
 // Pre-activations are kept in FP16 (z_h) and SiLU is evaluated in FP32 on
 // them; activations and gradients enter the MMAs as FP16.  The output layer
-// (64 -> 1) and its gradients are FP32 per row (dW4 by deterministic
-// warp-shuffle trees).  Transposed operands (dz^T, h^T, x^T) are written by
-// the threads that own the rows.  Every mbarrier wait is bounded (ta.wait_ns
+// (64 -> 1) and its gradients are FP32: each thread's share of the output dot,
+// summed over the four parts in part order, and dW4 by deterministic
+// warp-shuffle trees.  Transposed operands (dz^T, h^T, x^T) are written by the
+// threads that own the rows and columns.  Every mbarrier wait is bounded (ta.wait_ns
 // of the global timer, 1 s in training); a timeout sets the status word (and
 // partial[NPARAM] to NaN), drains, frees tensor memory and returns: k_mlp_adam
 // then makes no update and the host reports CG_ERR_DEVICE_FAULT.
@@ -36,6 +39,12 @@
 namespace {
 
 constexpr uint32_t TT_COLS = 256;  // [0, 64) forward / dh, [64, 160) dW | db
+// four threads per batch row, each on 16 of the 64 columns of every epilogue
+// (16 warps: four per tensor-memory lane quarter)
+constexpr int TT_PARTS = 4;
+constexpr int TT_THREADS = 128 * TT_PARTS;
+constexpr int CW = 64 / TT_PARTS;
+static_assert(CW == 16, "ld_cols loads 16 columns");
 constexpr int ZS = 66;  // halves per row of the z stores (conflict-free rows)
 // shared memory map (bytes from the 1024-aligned base)
 constexpr int O_X = 0;             // 128 x 128 B SW128 (K = 16 used)
@@ -54,8 +63,9 @@ constexpr int O_WT3 = O_WT2 + 8192;
 constexpr int O_ONES = O_WT3 + 8192;  // one 8-row SW32 atom: rows (1, 1, 0, ...)
 constexpr int O_BIAS = O_ONES + 256;  // 3 x (64 x 32 B) SW32: (b_hi, b_lo, 0, ...)
 constexpr int O_Z = O_BIAS + 3 * 2048;           // 3 x 128 x ZS halves
-constexpr int O_F = O_Z + 3 * 128 * ZS * 2;      // floats: dy[128], w4[64], red[4][64], misc
-constexpr int O_BAR = O_F + (128 + 64 + 4 * 64 + 16) * 4;
+// floats: dy[128], w4[64], red[4][64], misc[16], output partials [TT_PARTS][128]
+constexpr int O_F = O_Z + 3 * 128 * ZS * 2;
+constexpr int O_BAR = O_F + (128 + 64 + 4 * 64 + 16 + TT_PARTS * 128) * 4;
 constexpr int TT_USED = O_BAR + 32;
 constexpr int TT_SMEM = TT_USED + 1024;
 static_assert(O_W2 % 1024 == 0 && O_W3 % 1024 == 0 && O_WT2 % 1024 == 0 && O_WT3 % 1024 == 0 &&
@@ -135,24 +145,24 @@ __device__ void fused_adam(const TrainArgs& ta, int step, int* flag) {
     }
     __syncthreads();
     const bool stopped = *flag != 0;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p <= MLP_NPARAM; p += gridDim.x * blockDim.x)
-        mlp::adam_param(ta.adam, p, step, stopped);
+    // 128 parameters per CTA (the first four warps), so that the slices spread
+    // over as many SMs as there are
+    if (threadIdx.x < 128)
+        for (int p = blockIdx.x * 128 + threadIdx.x; p <= MLP_NPARAM; p += gridDim.x * 128)
+            mlp::adam_param(ta.adam, p, step, stopped);
     if (blockIdx.x == 0 && threadIdx.x == 0 && !stopped) *ta.adam.step = step + 1;
 }
 
-// 64 FP32 columns of this thread's tensor-memory lane
-__device__ __forceinline__ void ld64(uint32_t taddr, float (&v)[64]) {
-    uint32_t r[32];
-    tc::tmem_ld32(taddr, r);
+// CW FP32 columns of this thread's tensor-memory lane
+__device__ __forceinline__ void ld_cols(uint32_t taddr, float (&v)[CW]) {
+    uint32_t r[16];
+    tc::tmem_ld16(taddr, r);
 #pragma unroll
-    for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
-    tc::tmem_ld32(taddr + 32u, r);
-#pragma unroll
-    for (int j = 0; j < 32; ++j) v[32 + j] = __uint_as_float(r[j]);
+    for (int j = 0; j < CW; ++j) v[j] = __uint_as_float(r[j]);
 }
 
 template <int NL>
-__global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
+__global__ void __launch_bounds__(TT_THREADS, 1) k_mlp_train_tc(TrainArgs ta) {
     extern __shared__ uint8_t smem_raw[];
     const uint32_t raw = tc::smem_addr(smem_raw);
     uint8_t* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
@@ -162,37 +172,41 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
     float* fw4 = fdy + 128;
     float* fred = fw4 + 64;
     float* fmisc = fred + 4 * 64;
+    float* fyp = fmisc + 16;  // [TT_PARTS][128] partial output dots
     uint64_t* bar = reinterpret_cast<uint64_t*>(base + O_BAR);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(base + O_BAR + 8);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // thread = (row, part): the row's tensor-memory lane is row (warp w reads
+    // lanes 32 (w % 4) ..), the part its CW columns c0 .. c0 + CW - 1
+    const int row = tid & 127, part = tid >> 7, wq = warp & 3;
+    const int c0 = part * CW;
 
     // ---- weights (FP16 image) of the NL hidden layers, the transposes of
     // layers 2 .. NL, biases, ones
-    for (int r = tid; r < 64; r += 128) {
-#pragma unroll
-        for (int c = 0; c < 2; ++c)
-            *reinterpret_cast<uint4*>(base + O_W1 + tc::sw32_offset(r, c)) =
-                *reinterpret_cast<const uint4*>(ta.w16 + MLP_H_W1 + r * 16 + 8 * c);
-#pragma unroll
-        for (int l = 1; l < NL; ++l) {
-            const int src = l == 1 ? MLP_H_W2 : MLP_H_W3;
-            uint8_t* w = base + (l == 1 ? O_W2 : O_W3);
-            uint8_t* wt = base + (l == 1 ? O_WT2 : O_WT3);
-#pragma unroll
-            for (int c = 0; c < 8; ++c) {
-                *reinterpret_cast<uint4*>(w + tc::sw128_offset(r, c)) =
-                    *reinterpret_cast<const uint4*>(ta.w16 + src + r * 64 + 8 * c);
-                // W^T row r (input r), K = outputs 8c .. 8c+7
-                __align__(16) __half t[8];
-#pragma unroll
-                for (int q = 0; q < 8; ++q) t[q] = ta.w16[src + (8 * c + q) * 64 + r];
-                *reinterpret_cast<uint4*>(wt + tc::sw128_offset(r, c)) =
-                    *reinterpret_cast<const uint4*>(t);
-            }
-        }
-        fw4[r] = __half2float(ta.w16[MLP_H_W4 + r]);
+    for (int i = tid; i < 64 * 2; i += TT_THREADS) {
+        const int r = i >> 1, c = i & 1;
+        *reinterpret_cast<uint4*>(base + O_W1 + tc::sw32_offset(r, c)) =
+            *reinterpret_cast<const uint4*>(ta.w16 + MLP_H_W1 + r * 16 + 8 * c);
     }
-    for (int i = tid; i < NL * 64; i += 128) {
+#pragma unroll
+    for (int l = 1; l < NL; ++l) {
+        const int src = l == 1 ? MLP_H_W2 : MLP_H_W3;
+        uint8_t* w = base + (l == 1 ? O_W2 : O_W3);
+        uint8_t* wt = base + (l == 1 ? O_WT2 : O_WT3);
+        for (int i = tid; i < 64 * 8; i += TT_THREADS) {
+            const int r = i >> 3, c = i & 7;
+            *reinterpret_cast<uint4*>(w + tc::sw128_offset(r, c)) =
+                *reinterpret_cast<const uint4*>(ta.w16 + src + r * 64 + 8 * c);
+            // W^T row r (input r), K = outputs 8c .. 8c+7
+            __align__(16) __half t[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) t[q] = ta.w16[src + (8 * c + q) * 64 + r];
+            *reinterpret_cast<uint4*>(wt + tc::sw128_offset(r, c)) =
+                *reinterpret_cast<const uint4*>(t);
+        }
+    }
+    for (int r = tid; r < 64; r += TT_THREADS) fw4[r] = __half2float(ta.w16[MLP_H_W4 + r]);
+    for (int i = tid; i < NL * 64; i += TT_THREADS) {
         const int l = i >> 6, n = i & 63;
         const int off = l == 0 ? MLP_B1 : (l == 1 ? MLP_B2 : MLP_B3);
         const float bv = ta.params[off + n];
@@ -212,12 +226,12 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
     // dz^T rows 64-127 stay zero; h^T rows 64-79: row 64 all ones, the rest zero
     {
         const uint32_t one2 = h2u(__floats2half2_rn(1.f, 1.f));
-        for (int i = tid; i < 2 * 64 * 8; i += 128) {
+        for (int i = tid; i < 2 * 64 * 8; i += TT_THREADS) {
             const int a = i >> 9, r = 64 + ((i >> 3) & 63), c = i & 7;
             *reinterpret_cast<uint4*>(base + O_DT + a * DT_ATOM + tc::sw128_offset(r, c)) =
                 make_uint4(0u, 0u, 0u, 0u);
         }
-        for (int i = tid; i < 2 * 16 * 8; i += 128) {
+        for (int i = tid; i < 2 * 16 * 8; i += TT_THREADS) {
             const int a = i >> 7, r = 64 + ((i >> 3) & 15), c = i & 7;
             const uint32_t v = r == 64 ? one2 : 0u;
             *reinterpret_cast<uint4*>(base + O_HT + a * HT_ATOM + tc::sw128_offset(r, c)) =
@@ -225,9 +239,9 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
         }
     }
 
-    // ---- this thread's row: features (normalised, FP16) into x and x^T
+    // ---- the row's features (normalised, FP16) into x (part 0)
     const int step0 = ta.step ? *ta.step : 0;
-    const long long r = (long long)blockIdx.x * 128 + tid;
+    const long long r = (long long)blockIdx.x * 128 + row;
     bool valid;
     long long idx;
     if (ta.sequential) {
@@ -243,17 +257,20 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
         idx = (long long)((lin * ta.perm_mul) % N);
         valid = true;
     }
-    __align__(16) __half xh[16];
+    float tau = -1.f;  // < 0: padding row
+    if (part == 0) {
+        __align__(16) __half xh[16];
 #pragma unroll
-    for (int j = 0; j < MLP_IN; ++j) {
-        const float f = valid ? ta.feat[(size_t)idx * MLP_IN + j] : 0.f;
-        xh[j] = __float2half_rn((f - ta.mu[j]) * ta.inv_sd[j]);
+        for (int j = 0; j < MLP_IN; ++j) {
+            const float f = valid ? ta.feat[(size_t)idx * MLP_IN + j] : 0.f;
+            xh[j] = __float2half_rn((f - ta.mu[j]) * ta.inv_sd[j]);
+        }
+        tau = valid ? ta.tau[idx] : -1.f;
+#pragma unroll
+        for (int c = 0; c < 2; ++c)
+            *reinterpret_cast<uint4*>(base + O_X + tc::sw128_offset(row, c)) =
+                *reinterpret_cast<const uint4*>(xh + 8 * c);
     }
-    const float tau = valid ? ta.tau[idx] : -1.f;  // < 0: padding row
-#pragma unroll
-    for (int c = 0; c < 2; ++c)
-        *reinterpret_cast<uint4*>(base + O_X + tc::sw128_offset(tid, c)) =
-            *reinterpret_cast<const uint4*>(xh + 8 * c);
 
     if (tid == 0) {
         tc::mbar_init(bar, 1);
@@ -265,7 +282,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
     }
     bool bad = tt_sync(false);
     const uint32_t tmem = *tslot;
-    const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+    const uint32_t lane_off = (uint32_t)(wq * 32) << 16;
     unsigned phase = 0;
     bool failed = false;
     auto wait = [&]() {
@@ -275,7 +292,6 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
     };
 
     // ---- forward
-    float y = 0.f;
     for (int l = 0; l < NL && !failed; ++l) {
         if (tt_sync(bad)) {
             failed = true;
@@ -293,121 +309,140 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
         }
         wait();
         if (!bad) {
-            float z[64];
-            ld64(tmem + lane_off, z);
-            __half* zrow = zs + (size_t)(l * 128 + tid) * ZS;
-            uint32_t hp[32];
+            float z[CW];
+            ld_cols(tmem + lane_off + (uint32_t)c0, z);
+            __half* zrow = zs + (size_t)(l * 128 + row) * ZS;
+            uint32_t hp[CW / 2];
 #pragma unroll
-            for (int j = 0; j < 32; ++j) {
+            for (int j = 0; j < CW / 2; ++j) {
                 const __half2 zh = __floats2half2_rn(z[2 * j], z[2 * j + 1]);
-                *reinterpret_cast<__half2*>(zrow + 2 * j) = zh;
+                *reinterpret_cast<__half2*>(zrow + c0 + 2 * j) = zh;
                 const float2 zf = __half22float2(zh);
                 hp[j] = h2u(__floats2half2_rn(silu_f(zf.x), silu_f(zf.y)));
             }
             if (l < NL - 1) {
                 uint8_t* ht = base + (l == 0 ? O_H1 : O_H2);
 #pragma unroll
-                for (int c = 0; c < 8; ++c)
-                    *reinterpret_cast<uint4*>(ht + tc::sw128_offset(tid, c)) =
+                for (int c = 0; c < CW / 8; ++c)
+                    *reinterpret_cast<uint4*>(ht + tc::sw128_offset(row, c0 / 8 + c)) =
                         make_uint4(hp[4 * c], hp[4 * c + 1], hp[4 * c + 2], hp[4 * c + 3]);
             } else {
-                float yy = ta.params[MLP_B4];
+                // the part's share of the 64 -> 1 output, summed in part order below
+                float yy = 0.f;
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
+                for (int j = 0; j < CW / 2; ++j) {
                     const float2 h = __half22float2(*reinterpret_cast<const __half2*>(&hp[j]));
-                    yy = fmaf(fw4[2 * j], h.x, yy);
-                    yy = fmaf(fw4[2 * j + 1], h.y, yy);
+                    yy = fmaf(fw4[c0 + 2 * j], h.x, yy);
+                    yy = fmaf(fw4[c0 + 2 * j + 1], h.y, yy);
                 }
-                y = yy;
+                fyp[part * 128 + row] = yy;
             }
         }
         tc::fence_before_sync();
     }
 
-    // ---- loss and its gradient (per row), the output layer's gradients
-    float dy = 0.f, loss = 0.f;
-    if (tau >= 0.f) {
-        const float k = ta.sigma * ta.tau_scale;
-        const float Th = __expf(-k * mlp::softplus(y)), T = __expf(-ta.sigma * tau);
-        const float diff = Th - T;
-        loss = diff * diff;
-        dy = 2.f * diff * (-k * mlp::sigmoid(y) * Th);
+    // ---- loss and its gradient (per row, part 0), the output layer's gradients
+    __syncthreads();  // the output partials of every part
+    float loss = 0.f;
+    if (part == 0) {
+        float y = ta.params[MLP_B4];
+#pragma unroll
+        for (int q = 0; q < TT_PARTS; ++q) y += fyp[q * 128 + row];
+        float dy = 0.f;
+        if (tau >= 0.f) {
+            const float k = ta.sigma * ta.tau_scale;
+            const float Th = __expf(-k * mlp::softplus(y)), T = __expf(-ta.sigma * tau);
+            const float diff = Th - T;
+            loss = diff * diff;
+            dy = 2.f * diff * (-k * mlp::sigmoid(y) * Th);
+        }
+        fdy[row] = dy;
     }
+    __syncthreads();  // dy of every row
+    const float dy = fdy[row];
     {
         // dW4[j] = sum_rows dy h[j] (h: the last hidden layer's activations)
-        // and db4 = sum_rows dy: shuffle trees per warp, then the four warps in
-        // order
-        const __half* zl = zs + (size_t)((NL - 1) * 128 + tid) * ZS;
-        for (int j = 0; j < 64; ++j) {
-            const float hl = __half2float(__float2half_rn(silu_f(__half2float(zl[j]))));
+        // and db4 = sum_rows dy: shuffle trees per warp, then the four row
+        // groups in order
+        const __half* zl = zs + (size_t)((NL - 1) * 128 + row) * ZS;
+        for (int j = 0; j < CW; ++j) {
+            const float hl = __half2float(__float2half_rn(silu_f(__half2float(zl[c0 + j]))));
             float v = dy * hl;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if (lane == 0) fred[warp * 64 + j] = v;
+            if (lane == 0) fred[wq * 64 + c0 + j] = v;
         }
-        float vb = dy, vl = loss;
+        if (part == 0) {
+            float vb = dy, vl = loss;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            vb += __shfl_xor_sync(0xffffffffu, vb, o);
-            vl += __shfl_xor_sync(0xffffffffu, vl, o);
-        }
-        if (lane == 0) {
-            fmisc[warp] = vb;
-            fmisc[4 + warp] = vl;
+            for (int o = 16; o > 0; o >>= 1) {
+                vb += __shfl_xor_sync(0xffffffffu, vb, o);
+                vl += __shfl_xor_sync(0xffffffffu, vl, o);
+            }
+            if (lane == 0) {
+                fmisc[wq] = vb;
+                fmisc[4 + wq] = vl;
+            }
         }
     }
 
-    float* part = ta.partial + (size_t)blockIdx.x * (MLP_NPARAM + 1);
-    // dz of the layer below from dh (tensor memory cols [0, 64)) or, for the
-    // last hidden layer, from dy w4: FP16 into the dz rows and dz^T
-    auto write_dz = [&](int l, const float (&dh)[64]) {
-        const __half* zrow = zs + (size_t)(l * 128 + tid) * ZS;
-        uint32_t dp[32];
+    float* part_out = ta.partial + (size_t)blockIdx.x * (MLP_NPARAM + 1);
+    // dz of the layer below from dh (the part's tensor-memory columns) or, for
+    // the last hidden layer, from dy w4: FP16 into the dz rows and dz^T
+    auto write_dz = [&](int l, const float (&dh)[CW]) {
+        const __half* zrow = zs + (size_t)(l * 128 + row) * ZS;
+        uint32_t dp[CW / 2];
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-            const float2 zf = __half22float2(*reinterpret_cast<const __half2*>(zrow + 2 * j));
+        for (int j = 0; j < CW / 2; ++j) {
+            const float2 zf =
+                __half22float2(*reinterpret_cast<const __half2*>(zrow + c0 + 2 * j));
             const __half2 d2 = __floats2half2_rn(dh[2 * j] * silu_grad_f(zf.x),
                                                  dh[2 * j + 1] * silu_grad_f(zf.y));
             dp[j] = h2u(d2);
-            *reinterpret_cast<__half*>(base + O_DT + kt_addr(2 * j, tid, DT_ATOM)) = __low2half(d2);
-            *reinterpret_cast<__half*>(base + O_DT + kt_addr(2 * j + 1, tid, DT_ATOM)) =
+            *reinterpret_cast<__half*>(base + O_DT + kt_addr(c0 + 2 * j, row, DT_ATOM)) =
+                __low2half(d2);
+            *reinterpret_cast<__half*>(base + O_DT + kt_addr(c0 + 2 * j + 1, row, DT_ATOM)) =
                 __high2half(d2);
         }
 #pragma unroll
-        for (int c = 0; c < 8; ++c)
-            *reinterpret_cast<uint4*>(base + O_D + tc::sw128_offset(tid, c)) =
+        for (int c = 0; c < CW / 8; ++c)
+            *reinterpret_cast<uint4*>(base + O_D + tc::sw128_offset(row, c0 / 8 + c)) =
                 make_uint4(dp[4 * c], dp[4 * c + 1], dp[4 * c + 2], dp[4 * c + 3]);
     };
-    // h^T (rows 0-63) from a row tile, or x^T (rows 0-15)
+    // h^T (rows 0-63) from a row tile, or x^T (rows 0-15): the part's features
     auto write_ht = [&](const uint8_t* rows, int nfeat) {
-        for (int c = 0; c < nfeat / 8; ++c) {
-            const uint4 q = *reinterpret_cast<const uint4*>(rows + tc::sw128_offset(tid, c));
+        for (int c = c0 / 8; c < (c0 + CW) / 8 && c < nfeat / 8; ++c) {
+            const uint4 q = *reinterpret_cast<const uint4*>(rows + tc::sw128_offset(row, c));
             const __half* h = reinterpret_cast<const __half*>(&q);
 #pragma unroll
             for (int e = 0; e < 8; ++e)
-                *reinterpret_cast<__half*>(base + O_HT + kt_addr(8 * c + e, tid, HT_ATOM)) = h[e];
+                *reinterpret_cast<__half*>(base + O_HT + kt_addr(8 * c + e, row, HT_ATOM)) = h[e];
         }
     };
-    // rows 0-63 (warps 0, 1) of tensor-memory cols [64, 160): dW[j][0..nin) and db[j]
+    // rows 0-63 (row groups 0, 1) of tensor-memory cols [64, 160): the part's
+    // columns of dW[j][0..nin), and db[j] (part 0)
     auto store_dw = [&](int wo, int bo, int nin) {
-        if (warp < 2) {
-            const int j = tid;
-            float v[64];
-            ld64(tmem + lane_off + 64u, v);
-            uint32_t rb[32];
-            tc::tmem_ld32(tmem + lane_off + 128u, rb);
-            for (int i = 0; i < nin; ++i) part[wo + j * nin + i] = v[i];
-            part[bo + j] = __uint_as_float(rb[0]);
+        if (wq < 2 && c0 < nin) {
+            const int j = row;
+            float v[CW];
+            ld_cols(tmem + lane_off + 64u + (uint32_t)c0, v);
+#pragma unroll
+            for (int i = 0; i < CW; ++i) part_out[wo + j * nin + c0 + i] = v[i];
+        }
+        if (wq < 2 && part == 0) {
+            uint32_t rb[16];
+            tc::tmem_ld16(tmem + lane_off + 128u, rb);
+            part_out[bo + row] = __uint_as_float(rb[0]);
         }
     };
 
-    // the input tile of hidden layer l (x, h1 or h2) and its width
+    // the input tile of hidden layer l (x, h1 or h2)
     auto input_of = [&](int l) { return base + (l == 0 ? O_X : (l == 1 ? O_H1 : O_H2)); };
     if (!failed && !bad) {
         // last hidden layer: dz = dy w4 * silu'(z)
-        float dh[64];
+        float dh[CW];
 #pragma unroll
-        for (int j = 0; j < 64; ++j) dh[j] = dy * fw4[j];
+        for (int j = 0; j < CW; ++j) dh[j] = dy * fw4[c0 + j];
         write_dz(NL - 1, dh);
         write_ht(input_of(NL - 1), NL - 1 == 0 ? 16 : 64);
     }
@@ -423,11 +458,11 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
             tc::mma_commit(bar);
         }
         wait();
-        float dh[64];
+        float dh[CW];
         if (!bad) {
             store_dw(l == 0 ? MLP_W1 : (l == 1 ? MLP_W2 : MLP_W3),
                      l == 0 ? MLP_B1 : (l == 1 ? MLP_B2 : MLP_B3), l == 0 ? 16 : 64);
-            if (l > 0) ld64(tmem + lane_off, dh);
+            if (l > 0) ld_cols(tmem + lane_off + (uint32_t)c0, dh);
         }
         tc::fence_before_sync();
         if (l > 0) {
@@ -450,18 +485,18 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train_tc(TrainArgs ta) {
         const bool drained = !bad || tc::mbar_wait(bar, phase, ta.wait_ns);
         const bool undrained = __syncthreads_or(!drained) != 0;
         if (tid == 0) {
-            part[MLP_NPARAM] = __int_as_float(0x7fc00000);  // NaN loss
+            part_out[MLP_NPARAM] = __int_as_float(0x7fc00000);  // NaN loss
             // bit 1: tensor memory is freed below with an MMA possibly still
             // in flight, so the host must treat the device as faulted
             atomicOr(ta.status, undrained ? 3ull : 1ull);
         }
     } else {
         if (tid < 64)
-            part[MLP_W4 + tid] =
+            part_out[MLP_W4 + tid] =
                 ((fred[tid] + fred[64 + tid]) + fred[128 + tid]) + fred[192 + tid];
         if (tid == 0) {
-            part[MLP_B4] = ((fmisc[0] + fmisc[1]) + fmisc[2]) + fmisc[3];
-            part[MLP_NPARAM] = ((fmisc[4] + fmisc[5]) + fmisc[6]) + fmisc[7];
+            part_out[MLP_B4] = ((fmisc[0] + fmisc[1]) + fmisc[2]) + fmisc[3];
+            part_out[MLP_NPARAM] = ((fmisc[4] + fmisc[5]) + fmisc[6]) + fmisc[7];
         }
     }
     tc::fence_before_sync();
@@ -493,7 +528,7 @@ int mlp_train_resident_ctas() {
     int per_sm = 1 << 30, sms = 0;
     for (TrainFn fn : kTrainFns) {
         int k = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, (const void*)fn, 128, TT_SMEM) !=
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, (const void*)fn, TT_THREADS, TT_SMEM) !=
             cudaSuccess)
             return 0;
         per_sm = std::min(per_sm, k);
@@ -510,7 +545,7 @@ cudaError_t launch_mlp_train(const TrainArgs& ta, int ctas, cudaStream_t st) {
     const int resident = mlp_train_resident_ctas();
     if (resident <= 0) return cudaErrorInvalidConfiguration;
     if (!ta.grid_bar) {
-        fn<<<ctas, 128, TT_SMEM, st>>>(ta);
+        fn<<<ctas, TT_THREADS, TT_SMEM, st>>>(ta);
         return cudaGetLastError();
     }
     // the fused optimiser's grid barrier needs every CTA resident: a
@@ -518,7 +553,7 @@ cudaError_t launch_mlp_train(const TrainArgs& ta, int ctas, cudaStream_t st) {
     if (ctas > resident) return cudaErrorCooperativeLaunchTooLarge;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)ctas);
-    cfg.blockDim = dim3(128);
+    cfg.blockDim = dim3(TT_THREADS);
     cfg.dynamicSmemBytes = TT_SMEM;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
