@@ -443,6 +443,51 @@ def test_output_destinations_agree(ctx, trained):
         pinned.free()
 
 
+def test_frame_replays_from_a_cuda_graph(ctx, trained):
+    """Voxelize + surrogate render captured into a CUDA graph on the caller's
+    stream (the shading and accumulate passes are programmatic dependent
+    launches) and replayed: the same bytes as the direct calls."""
+    import ctypes
+    torch = pytest.importorskip("torch")
+    mlp, _, _ = trained
+    cfg = configs.PLAIN_1080P
+    wl = workload.build(cfg, width=320, height=180)
+    vol, sun, _ = _pair(ctx, cfg, wl, cloudgb.FORMAT_BF16_FP16)
+    cam = workload.make_camera(wl.cameras[2])
+    shader = cloudgb.ConeTraceShader(useMlp=True, mlp=mlp, **wl.shader_kwargs())
+    out = cloudgb.DeviceBuffer(320 * 180 * 16)
+    stream = torch.cuda.Stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    vs = cloudgb.VoxelizeShader()
+    with torch.cuda.stream(stream):
+        for _ in range(2):  # buffers and textures in place before the capture
+            vs.voxelize(vol, sun, stream=sp)
+            shader.coneTrace(vol, cam, out=out, stream=sp)
+        stream.synchronize()
+        direct = out.download((180, 320, 4))
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream):
+            vs.voxelize(vol, sun, stream=sp)
+            shader.coneTrace(vol, cam, out=out, stream=sp)
+        out.upload(np.full((180, 320, 4), -3.0, np.float32))
+        g.replay()
+        stream.synchronize()
+    replayed = out.download((180, 320, 4))
+    assert np.array_equal(direct, replayed)
+    assert direct[..., 3].max() > 0.1
+
+
+def test_mlp_depth_is_checked(ctx):
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    for bad in (0, 4):
+        assert lib.cg_mlp_create_layers(ctx.handle, 1, bad, ctypes.byref(h)) == 2  # out of range
+    for good in (1, 2, 3):
+        m = surrogate.SunMLP(ctx, hidden_layers=good)
+        assert m.hidden_layers == good
+    assert surrogate.SunMLP(ctx).hidden_layers == 3
+
+
 def test_mlp_render_with_wind(ctx, trained):
     """The surrogate path's fBm volume follows the wind: renders at run times
     inside and past the noise domain's margin stay within RMSE 1e-2 of the
